@@ -1,0 +1,225 @@
+/*
+ * gbdic — GB300-native IC-GN digital image correlation, C ABI.
+ *
+ * This is the drop-in boundary for the live-dic native registration path.
+ * Every entry point takes plain pointers and sizes; no CUDA or framework type
+ * appears in a signature.  Each entry cites the reference interface it
+ * replaces (paths relative to DIC/LucasKanadeICGN/python/src/live_dic/).
+ *
+ * Return codes: GBDIC_OK, or a negative code; gbdic_last_error() returns the
+ * message of the last failed call on that handle (or, for a NULL handle, of
+ * the last failed create call on the calling thread).  Argument errors are
+ * reported before any device work and leave the handle's state unchanged.
+ *
+ * Threading: a handle owns one CUDA stream and is not thread-safe; callers
+ * serialise calls per handle (the Python layer holds a non-blocking lock, as
+ * the reference does, wgpu_backend.py:826-853).
+ *
+ * Layouts (identical to the reference's GPU buffers):
+ *   state       per subset 8 floats [tx, ux, uy, ty, vx, vy, status, iterations]
+ *               (affine / translation) or 16 floats [tx, ux, uy, ty, vx, vy,
+ *               uxx, uxy, uyy, vxx, vxy, vyy, status, iterations, 0, 0]
+ *               (quadratic), row-major over the subset grid.
+ *   plane       per pixel 4 floats [f, df/dx, df/dy, 0]
+ *   metadata    per subset 16 (n=6) or 28 (n=12) floats [sqrt(energy), valid,
+ *               J^T f (n), sum J (n), mean, sum of weights, padding]
+ *   inverse     per subset n*n floats, row-major inverse Hessian
+ *   roi_links   per subset 4 floats: UOD neighbour permission words
+ *               (bit (dy+1)*3+dx+1 for the 3x3 stencil, or the 9x9 lattice
+ *               packed in four 24-bit words for larger median filters)
+ */
+#ifndef GBDIC_H
+#define GBDIC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBDIC_ABI_VERSION 1
+
+enum {
+    GBDIC_OK = 0,
+    GBDIC_EINVAL = -1,   /* invalid argument (Python: ValueError) */
+    GBDIC_ESTATE = -2,   /* call out of order, e.g. before set_reference (ICGNError) */
+    GBDIC_ECUDA = -3,    /* CUDA / device error (ICGNError) */
+    GBDIC_ETIMEOUT = -4  /* a bounded device wait gave up (ICGNError) */
+};
+
+enum { GBDIC_MODEL_AFFINE = 0, GBDIC_MODEL_TRANSLATION = 1, GBDIC_MODEL_QUADRATIC = 2 };
+enum { GBDIC_INTERP_BSPLINE = 0, GBDIC_INTERP_LINEAR = 1, GBDIC_INTERP_KEYS = 2 };
+enum { GBDIC_OUTLIER_FLAG = 0, GBDIC_OUTLIER_REPLACE = 1, GBDIC_OUTLIER_DISABLED = 2,
+       GBDIC_OUTLIER_MEDIAN = 3 };
+enum { GBDIC_EXPORT_COEFFICIENTS = 0, GBDIC_EXPORT_PLANE = 1, GBDIC_EXPORT_METADATA = 2,
+       GBDIC_EXPORT_INVERSE = 3, GBDIC_EXPORT_RAW_STATE = 4, GBDIC_EXPORT_OUTPUT_STATE = 5,
+       GBDIC_EXPORT_WEIGHTS = 6, GBDIC_EXPORT_FRAME = 7, GBDIC_EXPORT_ADMISSIBLE = 8 };
+
+typedef struct gbdic_engine gbdic_engine;
+typedef struct gbdic_pyramid gbdic_pyramid;
+
+/* Construction options; mirrors ICGNWGPU.__init__ (wgpu_backend.py:889-906). */
+typedef struct {
+    int32_t device;                    /* CUDA device ordinal */
+    int32_t motion_model;              /* GBDIC_MODEL_* */
+    int32_t interpolation;             /* GBDIC_INTERP_* */
+    int32_t subset_size;               /* 4 .. 46340 */
+    int32_t subset_stride;             /* 1 .. subset_size */
+    int32_t spatial_weighting;         /* 0 uniform, 1 Gaussian */
+    float gaussian_sigma;              /* pixels, > 0 */
+    int32_t outlier_policy;            /* GBDIC_OUTLIER_* */
+    int32_t median_filter_size;        /* 3, 5, 7, 9 */
+    int32_t median_filter_scope;       /* 0 rejected only, 1 all */
+    int32_t threads_per_subset;        /* 16, 32, 64, 128 (lanes per subset) */
+    int32_t divergence_patience;       /* 0 disables the stagnation check */
+    int32_t divergence_min_iterations; /* >= 1 */
+    int32_t pipeline_slots;            /* frames that may be in flight, >= 1 */
+    int32_t persistent;                /* 1: one persistent launch over a work queue */
+} gbdic_options;
+
+/* Per-call solver controls; mirrors _validated_config (wgpu_backend.py:504-524). */
+typedef struct {
+    int32_t iterations;  /* 1 .. 30 */
+    float tolerance;     /* > 0, pixels of corner motion */
+    float zncc_min;      /* 0 .. 1 */
+} gbdic_solver_cfg;
+
+typedef struct {
+    int32_t width, height, grid_width, grid_height;
+    int32_t valid_count;  /* subsets whose reference is numerically admissible */
+    double device_ms;     /* CUDA-event time of the preparation kernels */
+} gbdic_ref_info;
+
+typedef struct {
+    double upload_ms;     /* host wall: staging + host->device copy issue */
+    double execute_ms;    /* host wall: submit to completion */
+    double readback_ms;   /* host wall: device->host copy into the caller's buffer */
+    double total_ms;      /* host wall of the whole call */
+    double device_ms;     /* CUDA-event time of the frame's kernels */
+} gbdic_timing;
+
+/* ---------------------------------------------------------- single scale */
+
+/* ICGNWGPU(...) construction (wgpu_backend.py:889-1179). */
+int gbdic_create(const gbdic_options *options, gbdic_engine **out);
+/* ICGNWGPU.close() (wgpu_backend.py:3078-3093); NULL is ignored. */
+void gbdic_destroy(gbdic_engine *engine);
+/* Message of the last failed call (ICGNError text). */
+const char *gbdic_last_error(const gbdic_engine *engine);
+/* Library ABI version (GBDIC_ABI_VERSION). */
+int gbdic_abi_version(void);
+
+/* ICGNWGPU.set_reference (wgpu_backend.py:2364-2560), GPU reference
+ * preparation: Gaussian, recursive B-spline, gradients, per-subset sums,
+ * Cholesky inverses.  roi_selected (grid bytes, 1 = selected) and roi_links
+ * may be NULL; excluded subsets get validity -3 (wgpu_backend.py:2433-2446). */
+int gbdic_set_reference(gbdic_engine *engine, const uint8_t *image, int32_t width, int32_t height,
+                        int64_t row_stride, const uint8_t *roi_selected, const float *roi_links,
+                        gbdic_ref_info *info);
+
+/* Upload of host-prepared reference arrays in the reference's own layout
+ * (_allocate_runtime, wgpu_backend.py:1569-1590), e.g. from _reference_arrays. */
+int gbdic_set_reference_arrays(gbdic_engine *engine, int32_t width, int32_t height,
+                               const float *plane, const float *metadata, const float *inverse,
+                               const float *roi_links, gbdic_ref_info *info);
+
+/* ICGNWGPU.register (wgpu_backend.py:2893-2944): upload, FIR prefilter,
+ * IC-GN, UOD, readback of the output state (UOD output unless disabled). */
+int gbdic_register(gbdic_engine *engine, const uint8_t *frame, int64_t row_stride,
+                   const gbdic_solver_cfg *cfg, float *out_state, gbdic_timing *timing);
+
+/* ICGNWGPU.register_seeded / _register_seeded_frame (wgpu_backend.py:
+ * 2774-2819, 1951-2036): solve active subsets from seed states (state
+ * layout); inactive subsets get status -1 (-3 when ROI-excluded). */
+int gbdic_register_seeded(gbdic_engine *engine, const uint8_t *frame, int64_t row_stride,
+                          const float *seed_state, const uint32_t *active,
+                          const gbdic_solver_cfg *cfg, float *out_state, gbdic_timing *timing);
+
+/* ICGNWGPU._retry_seeded (wgpu_backend.py:1893-1949): re-solve active
+ * subsets on the resident target, keeping inactive subsets' last raw state,
+ * then UOD. */
+int gbdic_retry_seeded(gbdic_engine *engine, const float *seed_state, const uint32_t *active,
+                       const gbdic_solver_cfg *cfg, float *out_state, gbdic_timing *timing);
+
+/* ICGNWGPU._final_affine_zncc (wgpu_backend.py:2843-2890, affine_zncc.wgsl):
+ * ZNCC of the last output state on the resident target; -2 = unavailable. */
+int gbdic_final_zncc(gbdic_engine *engine, float *out_zncc);
+
+/* ICGNWGPU._submit_slot / _retire_slot (wgpu_backend.py:2946-2994): the two
+ * halves of register() on one of `pipeline_slots` independent slots, so that
+ * register_stream can keep several frames in flight. */
+int gbdic_submit(gbdic_engine *engine, int32_t slot, const uint8_t *frame, int64_t row_stride,
+                 const gbdic_solver_cfg *cfg);
+int gbdic_retire(gbdic_engine *engine, int32_t slot, float *out_state, gbdic_timing *timing);
+
+/* Resident variant of register(): `device_frame` and `device_state` are
+ * device pointers (8-bit frame, dense rows; output state); `stream` is a
+ * cudaStream_t or NULL for the engine's stream.  No host synchronisation. */
+int gbdic_register_device(gbdic_engine *engine, const uint8_t *device_frame,
+                          const gbdic_solver_cfg *cfg, float *device_state, void *stream);
+
+/* Copies an internal buffer (GBDIC_EXPORT_*) to host memory. */
+int gbdic_export(gbdic_engine *engine, int32_t what, void *host_out, int64_t bytes);
+
+/* The engine's outlier pass (median_filter / median_filter_seed,
+ * icgn.wgsl:1325-1605) on a caller-supplied state field, with the prepared
+ * reference's validity and ROI links.  seed_mode selects the
+ * median_filter_seed entry (repaired windows become status 0). */
+int gbdic_apply_uod(gbdic_engine *engine, const float *state_in, int32_t seed_mode, float *state_out);
+
+/* --------------------------------------------------------- full pyramid */
+
+/* ICGNWGPUFullPyramid(...) (full_pyramid_backend.py:202-431). */
+typedef struct {
+    gbdic_options base;
+    int32_t levels;                 /* 1 .. 4 */
+    int32_t iterations[4];          /* per level, coarsest first */
+    float tolerance[4];             /* per level, coarsest first */
+    float zncc_min;
+    int32_t initialization;         /* 0 zero, 1 temporal, 2 ZNCC seed search */
+    uint32_t temporal_max_age;      /* 0xFFFFFFFE = never expire */
+    int32_t temporal_prediction;    /* 0 none, 1 velocity */
+    int32_t seed_search_radius;     /* integer search radius (pixels, coarsest level) */
+} gbdic_pyramid_options;
+
+/* Static per-level ROI tables produced by host-side planning (roi.py). */
+typedef struct {
+    const uint8_t *selected;        /* grid bytes, 1 = selected; NULL = all */
+    const float *links;             /* 4 floats per subset (UOD permissions) or NULL */
+    const uint32_t *seed_links;     /* finer levels: transfer permissions per subset, or NULL */
+} gbdic_level_roi;
+
+int gbdic_pyramid_create(const gbdic_pyramid_options *options, gbdic_pyramid **out);
+void gbdic_pyramid_destroy(gbdic_pyramid *pyramid);
+const char *gbdic_pyramid_last_error(const gbdic_pyramid *pyramid);
+/* ICGNWGPUFullPyramid.set_reference (full_pyramid_backend.py:1135-1368).
+ * `rois` has `levels` entries (finest first) or is NULL; temporal_links are
+ * the projection permissions of the coarsest grid (NULL = 31 everywhere). */
+int gbdic_pyramid_set_reference(gbdic_pyramid *pyramid, const uint8_t *image, int32_t width,
+                                int32_t height, int64_t row_stride, const gbdic_level_roi *rois,
+                                const uint32_t *temporal_links, gbdic_ref_info *info);
+/* Grid shape of one level (0 = finest). */
+int gbdic_pyramid_level_grid(gbdic_pyramid *pyramid, int32_t level, int32_t *grid_width,
+                             int32_t *grid_height);
+/* ICGNWGPUFullPyramid._submit_slot / _retire_slot / register
+ * (full_pyramid_backend.py:1693-1832).  counters receives the temporal
+ * counters [projected, accepted updates, velocity predicted, expired]. */
+int gbdic_pyramid_submit(gbdic_pyramid *pyramid, int32_t slot, const uint8_t *frame,
+                         int64_t row_stride);
+int gbdic_pyramid_retire(gbdic_pyramid *pyramid, int32_t slot, float *out_state,
+                         uint32_t *counters, gbdic_timing *timing);
+int gbdic_pyramid_register(gbdic_pyramid *pyramid, const uint8_t *frame, int64_t row_stride,
+                           float *out_state, uint32_t *counters, gbdic_timing *timing);
+/* Resident variant: device frame in, device state out, no host sync. */
+int gbdic_pyramid_register_device(gbdic_pyramid *pyramid, const uint8_t *device_frame,
+                                  float *device_state, void *stream);
+/* ICGNWGPUFullPyramid.reset_temporal_state (full_pyramid_backend.py:676-694). */
+int gbdic_pyramid_reset_temporal(gbdic_pyramid *pyramid);
+/* Copies one level's internal buffer (GBDIC_EXPORT_*). */
+int gbdic_pyramid_export(gbdic_pyramid *pyramid, int32_t level, int32_t what, void *host_out,
+                         int64_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBDIC_H */

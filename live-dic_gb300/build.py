@@ -1,0 +1,82 @@
+"""Build libgbdic.so (sm_103a) in-tree.
+
+    python live-dic_gb300/build.py            # incremental
+    python live-dic_gb300/build.py --force    # rebuild everything
+
+Each .cu translation unit is compiled by nvcc in parallel, then linked into
+live-dic_gb300/live_dic_gb300/libgbdic.so with the static CUDA runtime.
+--fmad=false is part of the numerical contract: a*b+c is fused only where
+the source writes fmaf().
+"""
+
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+CSRC = ROOT / "csrc"
+BUILD = ROOT / "_build"
+OUTPUT = ROOT / "live_dic_gb300" / "libgbdic.so"
+INCLUDE = ROOT.parent / "include"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "--fmad=false", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(INCLUDE)]
+
+
+def nvcc() -> str:
+    found = shutil.which("nvcc")
+    if found:
+        return found
+    candidate = Path("/usr/local/cuda/bin/nvcc")
+    if candidate.exists():
+        return str(candidate)
+    raise RuntimeError("nvcc not found; the CUDA toolkit is required to build libgbdic.so")
+
+
+def _stale(target: Path, sources: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(s.stat().st_mtime > t for s in sources)
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
+    units = sorted(CSRC.glob("*.cu"))
+    compiler = nvcc()
+    jobs = []
+    objects = []
+    for unit in units:
+        obj = BUILD / (unit.stem + ".o")
+        objects.append(obj)
+        if force or _stale(obj, [unit, *headers]):
+            jobs.append([compiler, *ARCH, *FLAGS, "-c", str(unit), "-o", str(obj)])
+
+    def run(cmd: list[str]) -> None:
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        result = subprocess.run(cmd, capture_output=True, text=True)
+        if result.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {cmd[-3]}:\n{result.stdout}\n{result.stderr}")
+
+    workers = max(1, min(len(jobs), os.cpu_count() or 4))
+    if jobs:
+        with ThreadPoolExecutor(max_workers=workers) as pool:
+            list(pool.map(run, jobs))
+    if force or jobs or _stale(OUTPUT, objects):
+        link = [compiler, *ARCH, "-shared", "-o", str(OUTPUT), *map(str, objects)]
+        run(link)
+    return OUTPUT
+
+
+if __name__ == "__main__":
+    parser = argparse.ArgumentParser(description=__doc__)
+    parser.add_argument("--force", action="store_true")
+    parser.add_argument("--verbose", action="store_true")
+    args = parser.parse_args()
+    print(build(force=args.force, verbose=args.verbose))

@@ -1,0 +1,411 @@
+// C ABI of the gbdic library (declarations and reference citations in
+// include/gbdic.h).  Every entry point converts exceptions into a return
+// code plus a message retrievable with gbdic_last_error().
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "engine.h"
+
+using gbdic::Failure;
+using gbdic::check_cuda;
+using gbdic::fail;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct SlotHost {
+    gbdic::HostBuffer in, out;
+    cudaEvent_t begin = nullptr, end = nullptr, done = nullptr;
+    bool pending = false;
+    std::chrono::steady_clock::time_point submitted;
+    double upload_ms = 0.0;
+    cudaGraphExec_t graph = nullptr;
+    void create() {
+        check_cuda(cudaEventCreate(&begin), "event");
+        check_cuda(cudaEventCreate(&end), "event");
+        check_cuda(cudaEventCreateWithFlags(&done, cudaEventDisableTiming), "event");
+    }
+    void destroy() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (begin) cudaEventDestroy(begin);
+        if (end) cudaEventDestroy(end);
+        if (done) cudaEventDestroy(done);
+        graph = nullptr;
+        begin = end = done = nullptr;
+    }
+};
+
+void fill_timing(gbdic_timing *t, const SlotHost &h, double execute_ms, double readback_ms) {
+    if (!t) return;
+    float dev = 0.0f;
+    cudaEventElapsedTime(&dev, h.begin, h.end);
+    t->upload_ms = h.upload_ms;
+    t->execute_ms = execute_ms;
+    t->readback_ms = readback_ms;
+    t->total_ms = gbdic::ms_since(h.submitted);
+    t->device_ms = dev;
+}
+
+template <typename Handle, typename F>
+int guarded(Handle *h, F &&f) {
+    if (h == nullptr) {
+        g_create_error = "null handle";
+        return GBDIC_EINVAL;
+    }
+    try {
+        check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+        f();
+        return GBDIC_OK;
+    } catch (const Failure &x) {
+        h->error = x.message;
+        return x.code;
+    } catch (const std::exception &x) {
+        h->error = x.what();
+        return GBDIC_ECUDA;
+    }
+}
+
+}  // namespace
+
+struct gbdic_engine {
+    std::unique_ptr<gbdic::Runtime> rt;
+    gbdic::Level level;
+    std::vector<SlotHost> host;
+    std::vector<gbdic_solver_cfg> slot_cfg;
+    bool ready = false;
+    std::string error;
+    int device = 0;
+    ~gbdic_engine() {
+        if (rt) {
+            cudaSetDevice(device);
+            cudaStreamSynchronize(rt->stream());
+        }
+        for (auto &h : host) h.destroy();
+        level.slots.clear();
+    }
+    void require_ready(const char *what) const {
+        if (!ready) fail(GBDIC_ESTATE, std::string("Call set_reference() before ") + what + "().");
+    }
+    void check_slot(int slot) const {
+        if (slot < 0 || slot >= (int)host.size()) fail(GBDIC_EINVAL, "slot index out of range");
+    }
+};
+
+extern "C" {
+
+int gbdic_abi_version(void) { return GBDIC_ABI_VERSION; }
+
+const char *gbdic_last_error(const gbdic_engine *engine) {
+    return engine ? engine->error.c_str() : g_create_error.c_str();
+}
+
+int gbdic_create(const gbdic_options *options, gbdic_engine **out) {
+    if (!options || !out) {
+        g_create_error = "options and output handle are required";
+        return GBDIC_EINVAL;
+    }
+    *out = nullptr;
+    auto *e = new gbdic_engine();
+    try {
+        gbdic::validate_options(*options);
+        e->device = options->device;
+        e->rt = std::make_unique<gbdic::Runtime>(*options);
+        e->host = std::vector<SlotHost>(options->pipeline_slots);
+        for (auto &h : e->host) h.create();
+        e->slot_cfg.resize(options->pipeline_slots);
+    } catch (const Failure &x) {
+        g_create_error = x.message;
+        delete e;
+        return x.code;
+    }
+    *out = e;
+    return GBDIC_OK;
+}
+
+void gbdic_destroy(gbdic_engine *engine) { delete engine; }
+
+int gbdic_set_reference(gbdic_engine *e, const uint8_t *image, int32_t width, int32_t height, int64_t row_stride,
+                        const uint8_t *roi_selected, const float *roi_links, gbdic_ref_info *info) {
+    return guarded(e, [&] {
+        const auto &o = e->rt->opts().o;
+        if (!image) fail(GBDIC_EINVAL, "image is required");
+        if (width < 16 || height < 16) fail(GBDIC_EINVAL, "Image dimensions must each be at least 16 pixels.");
+        if (row_stride < width) fail(GBDIC_EINVAL, "row_stride must be at least the width");
+        int gw, gh;
+        gbdic::grid_of(width, height, o.subset_size, o.subset_stride, gw, gh);
+        if (gw < 1 || gh < 1)
+            fail(GBDIC_EINVAL, "Reference dimensions must each be at least " + std::to_string(o.subset_size) + " pixels.");
+        e->ready = false;
+        e->rt->configure_level(e->level, width, height, (int)e->host.size());
+        auto &slot = *e->level.slots[0];
+        e->rt->upload_frame(e->level, slot, image, row_stride, e->host[0].in, e->rt->stream());
+        const double ms = e->rt->prepare_reference(e->level, slot.frame.as<uint8_t>(), roi_selected, roi_links);
+        for (auto &h : e->host) {
+            if (h.graph) cudaGraphExecDestroy(h.graph);
+            h.graph = nullptr;
+            h.pending = false;
+        }
+        e->ready = true;
+        if (info) {
+            info->width = width; info->height = height;
+            info->grid_width = gw; info->grid_height = gh;
+            info->valid_count = e->level.valid_count;
+            info->device_ms = ms;
+        }
+    });
+}
+
+int gbdic_set_reference_arrays(gbdic_engine *e, int32_t width, int32_t height, const float *plane,
+                               const float *metadata, const float *inverse, const float *roi_links,
+                               gbdic_ref_info *info) {
+    return guarded(e, [&] {
+        const auto &o = e->rt->opts().o;
+        if (!plane || !metadata || !inverse) fail(GBDIC_EINVAL, "plane, metadata and inverse are required");
+        int gw, gh;
+        gbdic::grid_of(width, height, o.subset_size, o.subset_stride, gw, gh);
+        if (width < 16 || height < 16 || gw < 1 || gh < 1) fail(GBDIC_EINVAL, "invalid reference dimensions");
+        e->ready = false;
+        e->rt->configure_level(e->level, width, height, (int)e->host.size());
+        e->rt->upload_reference_arrays(e->level, plane, metadata, inverse, roi_links);
+        e->ready = true;
+        if (info) {
+            info->width = width; info->height = height;
+            info->grid_width = gw; info->grid_height = gh;
+            info->valid_count = e->level.valid_count;
+            info->device_ms = 0.0;
+        }
+    });
+}
+
+namespace {
+
+// Frame stages of the single-scale engine on slot k (after the upload).
+void enqueue_frame(gbdic_engine *e, int k, const gbdic_solver_cfg &cfg, bool seeded, bool preserve, bool prefilter) {
+    auto &rt = *e->rt;
+    auto &lvl = e->level;
+    auto &slot = *lvl.slots[k];
+    auto &h = e->host[k];
+    cudaStream_t s = rt.stream();
+    check_cuda(cudaEventRecord(h.begin, s), "event");
+    if (prefilter) rt.enqueue_prefilter(lvl, slot, nullptr, s);
+    rt.enqueue_solve(lvl, slot, cfg, seeded, preserve, nullptr, nullptr, s);
+    rt.enqueue_uod(lvl, slot, false, nullptr, s);
+    check_cuda(cudaEventRecord(h.end, s), "event");
+}
+
+void readback(gbdic_engine *e, int k, float *out_state, gbdic_timing *timing, std::chrono::steady_clock::time_point t_exec) {
+    auto &rt = *e->rt;
+    auto &lvl = e->level;
+    auto &h = e->host[k];
+    const size_t bytes = (size_t)lvl.count * gbdic::state_stride(rt.opts().o.motion_model) * sizeof(float);
+    h.out.ensure(bytes);
+    check_cuda(cudaMemcpyAsync(h.out.as<float>(), rt.output_state(*lvl.slots[k]), bytes, cudaMemcpyDeviceToHost,
+                               rt.stream()), "state readback");
+    check_cuda(cudaEventRecord(h.done, rt.stream()), "event");
+    gbdic::wait_event(h.done, gbdic::kWaitMs);
+    const double exec_ms = gbdic::ms_since(t_exec);
+    const auto t_copy = std::chrono::steady_clock::now();
+    if (out_state) std::memcpy(out_state, h.out.as<float>(), bytes);
+    fill_timing(timing, h, exec_ms, gbdic::ms_since(t_copy));
+}
+
+}  // namespace
+
+int gbdic_register(gbdic_engine *e, const uint8_t *frame, int64_t row_stride, const gbdic_solver_cfg *cfg,
+                   float *out_state, gbdic_timing *timing) {
+    return guarded(e, [&] {
+        e->require_ready("register");
+        gbdic::validate_cfg(cfg);
+        if (!frame) fail(GBDIC_EINVAL, "frame is required");
+        if (row_stride < e->level.W) fail(GBDIC_EINVAL, "row_stride must be at least the width");
+        auto &h = e->host[0];
+        h.submitted = std::chrono::steady_clock::now();
+        e->rt->upload_frame(e->level, *e->level.slots[0], frame, row_stride, h.in, e->rt->stream());
+        h.upload_ms = gbdic::ms_since(h.submitted);
+        const auto t_exec = std::chrono::steady_clock::now();
+        enqueue_frame(e, 0, *cfg, false, false, true);
+        readback(e, 0, out_state, timing, t_exec);
+    });
+}
+
+int gbdic_register_seeded(gbdic_engine *e, const uint8_t *frame, int64_t row_stride, const float *seed_state,
+                          const uint32_t *active, const gbdic_solver_cfg *cfg, float *out_state,
+                          gbdic_timing *timing) {
+    return guarded(e, [&] {
+        e->require_ready("register_seeded");
+        gbdic::validate_cfg(cfg);
+        if (!frame || !seed_state || !active) fail(GBDIC_EINVAL, "frame, seed_state and active are required");
+        if (row_stride < e->level.W) fail(GBDIC_EINVAL, "row_stride must be at least the width");
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        auto &h = e->host[0];
+        const auto s = e->rt->stream();
+        h.submitted = std::chrono::steady_clock::now();
+        e->rt->upload_frame(lvl, slot, frame, row_stride, h.in, s);
+        const size_t sb = (size_t)lvl.count * gbdic::state_stride(e->rt->opts().o.motion_model) * sizeof(float);
+        check_cuda(cudaMemcpyAsync(slot.seed.get(), seed_state, sb, cudaMemcpyHostToDevice, s), "seed upload");
+        check_cuda(cudaMemcpyAsync(slot.active.get(), active, (size_t)lvl.count * sizeof(uint32_t), cudaMemcpyHostToDevice, s),
+                   "activity upload");
+        h.upload_ms = gbdic::ms_since(h.submitted);
+        const auto t_exec = std::chrono::steady_clock::now();
+        enqueue_frame(e, 0, *cfg, true, false, true);
+        readback(e, 0, out_state, timing, t_exec);
+    });
+}
+
+int gbdic_retry_seeded(gbdic_engine *e, const float *seed_state, const uint32_t *active, const gbdic_solver_cfg *cfg,
+                       float *out_state, gbdic_timing *timing) {
+    return guarded(e, [&] {
+        e->require_ready("retry_seeded");
+        gbdic::validate_cfg(cfg);
+        if (!seed_state || !active) fail(GBDIC_EINVAL, "seed_state and active are required");
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        auto &h = e->host[0];
+        const auto s = e->rt->stream();
+        h.submitted = std::chrono::steady_clock::now();
+        const size_t sb = (size_t)lvl.count * gbdic::state_stride(e->rt->opts().o.motion_model) * sizeof(float);
+        check_cuda(cudaMemcpyAsync(slot.seed.get(), seed_state, sb, cudaMemcpyHostToDevice, s), "seed upload");
+        check_cuda(cudaMemcpyAsync(slot.active.get(), active, (size_t)lvl.count * sizeof(uint32_t), cudaMemcpyHostToDevice, s),
+                   "activity upload");
+        h.upload_ms = gbdic::ms_since(h.submitted);
+        const auto t_exec = std::chrono::steady_clock::now();
+        enqueue_frame(e, 0, *cfg, true, true, false);
+        readback(e, 0, out_state, timing, t_exec);
+    });
+}
+
+int gbdic_final_zncc(gbdic_engine *e, float *out_zncc) {
+    return guarded(e, [&] {
+        e->require_ready("final_zncc");
+        if (!out_zncc) fail(GBDIC_EINVAL, "output is required");
+        if (e->rt->opts().o.motion_model != GBDIC_MODEL_AFFINE || e->rt->opts().o.spatial_weighting != 0)
+            fail(GBDIC_EINVAL, "include_zncc requires affine motion and uniform full windows");
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        gbdic::DeviceBuffer out;
+        out.ensure((size_t)lvl.count * sizeof(float));
+        gbdic::ZnccArgs z{};
+        z.coef = slot.coef.as<float>();
+        z.img = slot.frame.as<uint8_t>();
+        z.plane = lvl.plane.as<float4>();
+        z.state = e->rt->output_state(slot);
+        z.out = out.as<float>();
+        z.W = lvl.W; z.H = lvl.H; z.grid_w = lvl.gw; z.count = lvl.count;
+        z.S = e->rt->opts().o.subset_size; z.stride = e->rt->opts().o.subset_stride;
+        z.interp = e->rt->opts().o.interpolation;
+        check_cuda(gbdic::launch_final_zncc(z, e->rt->stream()), "final ZNCC launch");
+        check_cuda(cudaMemcpyAsync(out_zncc, out.get(), (size_t)lvl.count * sizeof(float), cudaMemcpyDeviceToHost,
+                                   e->rt->stream()), "ZNCC readback");
+        check_cuda(cudaStreamSynchronize(e->rt->stream()), "final ZNCC");
+    });
+}
+
+int gbdic_submit(gbdic_engine *e, int32_t slot_index, const uint8_t *frame, int64_t row_stride,
+                 const gbdic_solver_cfg *cfg) {
+    return guarded(e, [&] {
+        e->require_ready("register_stream");
+        gbdic::validate_cfg(cfg);
+        e->check_slot(slot_index);
+        if (!frame) fail(GBDIC_EINVAL, "frame is required");
+        if (row_stride < e->level.W) fail(GBDIC_EINVAL, "row_stride must be at least the width");
+        auto &h = e->host[slot_index];
+        if (h.pending) fail(GBDIC_ESTATE, "slot is still in flight; retire it first");
+        h.submitted = std::chrono::steady_clock::now();
+        e->rt->upload_frame(e->level, *e->level.slots[slot_index], frame, row_stride, h.in, e->rt->stream());
+        h.upload_ms = gbdic::ms_since(h.submitted);
+        enqueue_frame(e, slot_index, *cfg, false, false, true);
+        auto &lvl = e->level;
+        const size_t bytes = (size_t)lvl.count * gbdic::state_stride(e->rt->opts().o.motion_model) * sizeof(float);
+        h.out.ensure(bytes);
+        check_cuda(cudaMemcpyAsync(h.out.as<float>(), e->rt->output_state(*lvl.slots[slot_index]), bytes,
+                                   cudaMemcpyDeviceToHost, e->rt->stream()), "state readback");
+        check_cuda(cudaEventRecord(h.done, e->rt->stream()), "event");
+        h.pending = true;
+    });
+}
+
+int gbdic_retire(gbdic_engine *e, int32_t slot_index, float *out_state, gbdic_timing *timing) {
+    return guarded(e, [&] {
+        e->check_slot(slot_index);
+        auto &h = e->host[slot_index];
+        if (!h.pending) fail(GBDIC_ESTATE, "slot has no registration in flight");
+        const auto t_wait = std::chrono::steady_clock::now();
+        h.pending = false;
+        gbdic::wait_event(h.done, gbdic::kWaitMs);
+        const double wait_ms = gbdic::ms_since(t_wait);
+        const auto t_copy = std::chrono::steady_clock::now();
+        const size_t bytes = (size_t)e->level.count * gbdic::state_stride(e->rt->opts().o.motion_model) * sizeof(float);
+        if (out_state) std::memcpy(out_state, h.out.as<float>(), bytes);
+        fill_timing(timing, h, wait_ms, gbdic::ms_since(t_copy));
+    });
+}
+
+int gbdic_register_device(gbdic_engine *e, const uint8_t *device_frame, const gbdic_solver_cfg *cfg,
+                          float *device_state, void *stream) {
+    return guarded(e, [&] {
+        e->require_ready("register");
+        gbdic::validate_cfg(cfg);
+        if (!device_frame || !device_state) fail(GBDIC_EINVAL, "device_frame and device_state are required");
+        auto &rt = *e->rt;
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        cudaStream_t s = stream ? (cudaStream_t)stream : rt.stream();
+        rt.enqueue_prefilter(lvl, slot, device_frame, s);
+        const bool disabled = rt.opts().o.outlier_policy == GBDIC_OUTLIER_DISABLED;
+        rt.enqueue_solve(lvl, slot, *cfg, false, false, device_frame, disabled ? device_state : nullptr, s);
+        if (!disabled) rt.enqueue_uod(lvl, slot, false, device_state, s);
+    });
+}
+
+int gbdic_apply_uod(gbdic_engine *e, const float *state_in, int32_t seed_mode, float *state_out) {
+    return guarded(e, [&] {
+        e->require_ready("apply_uod");
+        if (!state_in || !state_out) fail(GBDIC_EINVAL, "state_in and state_out are required");
+        auto &rt = *e->rt;
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        const size_t bytes = (size_t)lvl.count * gbdic::state_stride(rt.opts().o.motion_model) * sizeof(float);
+        cudaStream_t s = rt.stream();
+        check_cuda(cudaMemcpyAsync(slot.state.get(), state_in, bytes, cudaMemcpyHostToDevice, s), "state upload");
+        if (rt.opts().o.outlier_policy == GBDIC_OUTLIER_DISABLED) {
+            check_cuda(cudaMemcpyAsync(slot.filtered.get(), slot.state.get(), bytes, cudaMemcpyDeviceToDevice, s), "copy");
+        } else {
+            rt.enqueue_uod(lvl, slot, seed_mode != 0, nullptr, s);
+        }
+        check_cuda(cudaMemcpyAsync(state_out, slot.filtered.get(), bytes, cudaMemcpyDeviceToHost, s), "state readback");
+        check_cuda(cudaStreamSynchronize(s), "UOD");
+    });
+}
+
+int gbdic_export(gbdic_engine *e, int32_t what, void *host_out, int64_t bytes) {
+    return guarded(e, [&] {
+        e->require_ready("export");
+        if (!host_out) fail(GBDIC_EINVAL, "output is required");
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        const int model = e->rt->opts().o.motion_model, n = gbdic::parameter_count(model);
+        const void *src = nullptr;
+        size_t size = 0;
+        switch (what) {
+        case GBDIC_EXPORT_COEFFICIENTS: src = slot.coef.get(); size = (size_t)lvl.W * lvl.H * sizeof(float); break;
+        case GBDIC_EXPORT_PLANE: src = lvl.plane.get(); size = (size_t)lvl.W * lvl.H * sizeof(float4); break;
+        case GBDIC_EXPORT_METADATA: src = lvl.meta.get(); size = (size_t)lvl.count * gbdic::meta_stride(model) * sizeof(float); break;
+        case GBDIC_EXPORT_INVERSE: src = lvl.inv.get(); size = (size_t)lvl.count * n * n * sizeof(float); break;
+        case GBDIC_EXPORT_RAW_STATE: src = slot.state.get(); size = (size_t)lvl.count * gbdic::state_stride(model) * sizeof(float); break;
+        case GBDIC_EXPORT_OUTPUT_STATE: src = e->rt->output_state(slot); size = (size_t)lvl.count * gbdic::state_stride(model) * sizeof(float); break;
+        case GBDIC_EXPORT_WEIGHTS: src = e->rt->weights().get(); size = e->rt->opts().weights.size() * sizeof(float); break;
+        case GBDIC_EXPORT_FRAME: src = slot.frame.get(); size = (size_t)lvl.W * lvl.H; break;
+        case GBDIC_EXPORT_ADMISSIBLE: src = lvl.admissible.get(); size = (size_t)lvl.count; break;
+        default: fail(GBDIC_EINVAL, "unknown export selector");
+        }
+        if (src == nullptr) fail(GBDIC_ESTATE, "buffer not available in this configuration");
+        if ((size_t)bytes < size) fail(GBDIC_EINVAL, "output buffer too small: need " + std::to_string(size) + " bytes");
+        check_cuda(cudaStreamSynchronize(e->rt->stream()), "pending work");
+        check_cuda(cudaMemcpy(host_out, src, size, cudaMemcpyDeviceToHost), "export");
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+// Host runtime of the gbdic library: device buffers, levels, slots.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/gbdic.h"
+#include "gbdic_kernels.h"
+
+namespace gbdic {
+
+// Failure carrying a gbdic return code and a message.
+struct Failure {
+    int code;
+    std::string message;
+};
+
+void check_cuda(cudaError_t err, const char *what);
+[[noreturn]] void fail(int code, const std::string &message);
+double ms_since(std::chrono::steady_clock::time_point t0);
+// Bounded host wait on an event (GBDIC_ETIMEOUT after `timeout_ms`).
+void wait_event(cudaEvent_t ev, double timeout_ms);
+void validate_options(const gbdic_options &o);
+void validate_cfg(const gbdic_solver_cfg *c);
+void grid_of(int W, int H, int S, int st, int &gw, int &gh);
+constexpr double kWaitMs = 120000.0;
+
+// Owning device allocation.
+class DeviceBuffer {
+  public:
+    DeviceBuffer() = default;
+    ~DeviceBuffer() { reset(); }
+    DeviceBuffer(const DeviceBuffer &) = delete;
+    DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+    void ensure(size_t bytes);  // (re)allocates when the size grows
+    void reset();
+    template <typename T> T *as() const { return static_cast<T *>(ptr_); }
+    size_t bytes() const { return bytes_; }
+    void *get() const { return ptr_; }
+
+  private:
+    void *ptr_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+// Owning pinned host allocation.
+class HostBuffer {
+  public:
+    HostBuffer() = default;
+    ~HostBuffer() { reset(); }
+    HostBuffer(const HostBuffer &) = delete;
+    HostBuffer &operator=(const HostBuffer &) = delete;
+    void ensure(size_t bytes);
+    void reset();
+    template <typename T> T *as() const { return static_cast<T *>(ptr_); }
+
+  private:
+    void *ptr_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+// Per-frame mutable buffers of one level.
+struct LevelSlot {
+    DeviceBuffer frame;     // W*H bytes
+    DeviceBuffer coef;      // W*H floats
+    DeviceBuffer state;     // raw solver state
+    DeviceBuffer filtered;  // UOD output
+    DeviceBuffer seed;      // seed states
+    DeviceBuffer active;    // seed activity
+    DeviceBuffer counter;   // persistent work-queue head
+};
+
+// One image scale: reference data plus its per-slot buffers.
+struct Level {
+    int W = 0, H = 0, gw = 0, gh = 0, count = 0;
+    bool roi = false;
+    DeviceBuffer plane, meta, inv, links, selected;
+    DeviceBuffer intensity, spline, scratch, valid;  // preparation scratch
+    DeviceBuffer admissible;                         // u8 per subset, ROI ignored
+    std::vector<std::unique_ptr<LevelSlot>> slots;
+    int valid_count = 0;
+};
+
+struct Options {
+    gbdic_options o;
+    int lanes = 32;
+    std::vector<float> weights;  // S*S integration weights
+    float weight_sum = 0.0f;
+};
+
+// Shared machinery of both engine kinds.
+class Runtime {
+  public:
+    explicit Runtime(const gbdic_options &options);
+    ~Runtime();
+    const Options &opts() const { return opt_; }
+    cudaStream_t stream() const { return stream_; }
+    int sm_count() const { return sm_count_; }
+
+    void configure_level(Level &level, int W, int H, int slots);
+    void ensure_slots(Level &level, int slots);
+    // GPU reference preparation from a device image (dense rows).
+    double prepare_reference(Level &level, const uint8_t *device_image, const uint8_t *roi_selected,
+                             const float *roi_links);
+    void upload_reference_arrays(Level &level, const float *plane, const float *meta,
+                                 const float *inverse, const float *links);
+    // Per-frame stages of one level on `stream`.
+    // `frame` (device bytes) and `state` / `out` override the slot's own
+    // buffers when non-null.
+    void enqueue_prefilter(Level &level, LevelSlot &slot, const uint8_t *frame, cudaStream_t stream);
+    void enqueue_solve(Level &level, LevelSlot &slot, const gbdic_solver_cfg &cfg, bool seeded,
+                       bool preserve, const uint8_t *frame, float *state, cudaStream_t stream);
+    void enqueue_uod(Level &level, LevelSlot &slot, bool seed_mode, float *out, cudaStream_t stream);
+    const float *output_state(LevelSlot &slot) const;
+    void upload_frame(Level &level, LevelSlot &slot, const uint8_t *frame, int64_t row_stride,
+                      HostBuffer &staging, cudaStream_t stream);
+    int persistent_grid(int lanes);
+    const DeviceBuffer &weights() const { return weights_; }
+
+  private:
+    Options opt_;
+    cudaStream_t stream_ = nullptr;
+    DeviceBuffer weights_;
+    int sm_count_ = 0;
+    int device_ = 0;
+    int persistent_grid_ = 0;
+    int persistent_lanes_ = 0;
+};
+
+}  // namespace gbdic

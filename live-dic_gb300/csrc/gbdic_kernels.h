@@ -1,0 +1,103 @@
+// Internal launcher declarations and argument blocks (host + device).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gbdic_common.cuh"
+
+namespace gbdic {
+
+// ------------------------------------------------------------ prefilter
+cudaError_t set_fir_taps(const float *taps25);
+cudaError_t launch_fir_prefilter(const uint8_t *img, int W, int H, int pitch, float *coef,
+                                 cudaStream_t stream);
+
+// ------------------------------------------------------------ solver
+template <int MODEL>
+cudaError_t launch_icgn_model(const SolveArgs &a, int interp, int lanes, bool gauss, int grid,
+                              cudaStream_t stream, int *occupancy_only);
+// Grid for a non-persistent launch of `count` subsets with `lanes` lanes.
+int icgn_grid(int count, int lanes);
+// Resident CTAs per SM of the solver variant (for persistent grids).
+int icgn_occupancy(int model, int interp, int lanes, bool gauss);
+cudaError_t launch_icgn(const SolveArgs &a, int model, int interp, int lanes, bool gauss,
+                        int persistent_grid, cudaStream_t stream);
+
+// ------------------------------------------------------------ UOD
+struct UodArgs {
+    const float *state;
+    float *out;
+    const float *meta;
+    const float *links;   // 4 floats per subset (ROI), or nullptr
+    int grid_w, grid_h, count;
+    int subset_stride;
+    int model, policy, median_size, scope_all, seed_mode, roi_enabled;
+};
+cudaError_t launch_uod(const UodArgs &a, cudaStream_t stream);
+
+// ------------------------------------------------------------ reference preparation
+struct PrepArgs {
+    const uint8_t *img;     // reference bytes, dense rows
+    int W, H, pitch;
+    int S, stride, grid_w, grid_h, count;
+    int model, interp, gaussian_weighting;
+    const float *weights;   // S*S integration weights (always provided)
+    float weight_sum;
+    const uint8_t *selected;  // ROI selection per subset, or nullptr
+    // outputs / scratch
+    float *intensity;       // H*W
+    float *spline;          // H*W (B-spline coefficients) and transposes
+    float *scratch;         // H*W
+    float4 *plane;          // H*W
+    float *meta;            // count * meta_stride
+    float *inv;             // count * n * n
+    unsigned *valid_count;
+    uint8_t *admissible;    // per subset numerical admissibility, ROI ignored
+};
+cudaError_t launch_reference_prep(const PrepArgs &a, cudaStream_t stream);
+
+// ------------------------------------------------------------ final ZNCC
+struct ZnccArgs {
+    const float *coef;
+    const uint8_t *img;
+    const float4 *plane;
+    const float *state;
+    float *out;
+    int W, H, grid_w, count, S, stride, interp;
+};
+cudaError_t launch_final_zncc(const ZnccArgs &a, cudaStream_t stream);
+
+// ------------------------------------------------------------ pyramid
+cudaError_t launch_reduce_half(const uint8_t *src, int W, int H, uint8_t *dst, cudaStream_t stream);
+
+struct SeedArgs {
+    const float *source;      // coarse (filtered) state
+    float *seed;              // destination seed state
+    uint32_t *active;         // destination activity
+    const uint32_t *links;    // per destination permissions, or nullptr (31)
+    int src_grid_w, src_grid_h, dst_grid_w, dst_count;
+    float src_scale, dst_scale, subset_size, subset_stride;
+    int model;
+    unsigned *projected;      // counter for temporal projection, or nullptr
+};
+cudaError_t launch_transfer_seed(const SeedArgs &a, cudaStream_t stream);
+
+struct TemporalArgs {
+    float *history;           // fine accepted history
+    uint32_t *ages;
+    const float *raw;         // fine raw state
+    const float *output;      // fine output (filtered) state
+    float *prev_history;      // velocity: previous accepted history
+    uint32_t *prev_ages;
+    float *prediction;        // velocity: predicted field
+    unsigned *counters;       // [projected, accepted updates, predicted, expired]
+    int count, model;
+    unsigned max_age;
+    int use_filtered;
+};
+cudaError_t launch_temporal_predict(const TemporalArgs &a, cudaStream_t stream);
+cudaError_t launch_temporal_save_previous(const TemporalArgs &a, cudaStream_t stream);
+cudaError_t launch_temporal_merge(const TemporalArgs &a, cudaStream_t stream);
+
+}  // namespace gbdic

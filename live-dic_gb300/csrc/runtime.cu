@@ -1,0 +1,370 @@
+// Host runtime of the gbdic library (see engine.h).
+//
+// Each level (image scale) keeps its prepared reference resident in HBM
+// (reference plane, metadata, inverse Hessians) and, per pipeline slot, its
+// own target, coefficient plane and solver states, so that several frames can
+// be in flight.  Frames are staged through pinned host buffers.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <thread>
+
+#include "engine.h"
+
+namespace gbdic {
+
+cudaError_t set_gauss_taps(const float *taps7);
+
+namespace {
+
+// Runtime taps of the target FIR: float32 values of the central 25 taps of
+// the Gaussian(sigma 1) * inverse cubic B-spline filter
+// (wgpu_backend.py:_fir_weights, 527-541), offsets -12..12.
+const uint32_t kFirBits[25] = {
+    0x318eddc4u, 0x3333f91eu, 0xb41a28f9u, 0x35101d98u, 0xb6067631u, 0x36fae8afu, 0xb7ea19e9u,
+    0x38da6b5eu, 0xb9cbc9bfu, 0x3abe2309u, 0x3cad8b0cu, 0x3e738da4u, 0x3ef59511u, 0x3e738da4u,
+    0x3cad8b0cu, 0x3abe2309u, 0xb9cbc9bfu, 0x38da6b5eu, 0xb7ea19e9u, 0x36fae8afu, 0xb6067631u,
+    0x35101d98u, 0xb41a28f9u, 0x3333f91eu, 0x318eddc4u};
+
+}  // namespace
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void fail(int code, const std::string &message) { throw Failure{code, message}; }
+
+// Bounded host wait on an event (GBDIC_ETIMEOUT after `timeout_ms`).
+void wait_event(cudaEvent_t ev, double timeout_ms) {
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t err = cudaEventQuery(ev);
+        if (err == cudaSuccess) return;
+        if (err != cudaErrorNotReady) check_cuda(err, "device execution");
+        if (ms_since(t0) > timeout_ms) fail(GBDIC_ETIMEOUT, "device work did not complete within the wait limit");
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
+void validate_options(const gbdic_options &o) {
+    if (o.motion_model < 0 || o.motion_model > 2) fail(GBDIC_EINVAL, "motion_model must be 'affine', 'translation', or 'quadratic'");
+    if (o.interpolation < 0 || o.interpolation > 2) fail(GBDIC_EINVAL, "interpolation must be 'bspline', 'linear', or 'cubic'");
+    if (o.subset_size < 4 || o.subset_size > 46340) fail(GBDIC_EINVAL, "subset_size must be an integer from 4 to 46340");
+    if (o.subset_stride < 1 || o.subset_stride > o.subset_size) fail(GBDIC_EINVAL, "subset_stride must be between 1 and subset_size");
+    if (o.spatial_weighting < 0 || o.spatial_weighting > 1) fail(GBDIC_EINVAL, "spatial_weighting must be 'uniform' or 'gaussian'");
+    if (o.spatial_weighting == 1 && !(std::isfinite(o.gaussian_sigma) && o.gaussian_sigma > 0.0f))
+        fail(GBDIC_EINVAL, "gaussian_sigma must be finite and greater than zero");
+    if (o.outlier_policy < 0 || o.outlier_policy > 3) fail(GBDIC_EINVAL, "outlier_policy must be 'replace', 'flag', 'disabled', or 'median'");
+    if (o.median_filter_size != 3 && o.median_filter_size != 5 && o.median_filter_size != 7 && o.median_filter_size != 9)
+        fail(GBDIC_EINVAL, "median_filter_size must be one of 3, 5, 7, or 9 subsets");
+    if (o.median_filter_scope < 0 || o.median_filter_scope > 1) fail(GBDIC_EINVAL, "median_filter_scope must be 'rejected' or 'all'");
+    if (o.threads_per_subset != 16 && o.threads_per_subset != 32 && o.threads_per_subset != 64 && o.threads_per_subset != 128)
+        fail(GBDIC_EINVAL, "threads_per_subset must be 16, 32, 64, or 128");
+    if (o.divergence_patience < 0 || o.divergence_patience > 30) fail(GBDIC_EINVAL, "divergence_patience must be an integer from 1 to 30");
+    if (o.divergence_min_iterations < 1 || o.divergence_min_iterations > 30)
+        fail(GBDIC_EINVAL, "divergence_min_iterations must be an integer from 1 to 30");
+    if (o.pipeline_slots < 1 || o.pipeline_slots > 64) fail(GBDIC_EINVAL, "pipeline_depth must be a positive integer");
+}
+
+void validate_cfg(const gbdic_solver_cfg *c) {
+    if (!c) fail(GBDIC_EINVAL, "solver configuration is required");
+    if (c->iterations < 1 || c->iterations > 30) fail(GBDIC_EINVAL, "iterations must be between 1 and 30");
+    if (!(std::isfinite(c->tolerance) && c->tolerance > 0.0f)) fail(GBDIC_EINVAL, "tolerance must be a finite positive number");
+    if (!(std::isfinite(c->zncc_min) && c->zncc_min >= 0.0f && c->zncc_min <= 1.0f)) fail(GBDIC_EINVAL, "zncc_min must be between 0 and 1");
+}
+
+void grid_of(int W, int H, int S, int st, int &gw, int &gh) {
+    if (W < S || H < S) { gw = gh = 0; return; }
+    gw = 1 + (W - S) / st;
+    gh = 1 + (H - S) / st;
+}
+
+void check_cuda(cudaError_t err, const char *what) {
+    if (err != cudaSuccess) throw Failure{GBDIC_ECUDA, std::string(what) + ": " + cudaGetErrorString(err)};
+}
+
+void DeviceBuffer::ensure(size_t bytes) {
+    if (ptr_ != nullptr && bytes <= bytes_) return;
+    reset();
+    if (bytes == 0) return;
+    check_cuda(cudaMalloc(&ptr_, bytes), "cudaMalloc");
+    bytes_ = bytes;
+}
+
+void DeviceBuffer::reset() {
+    if (ptr_ != nullptr) cudaFree(ptr_);
+    ptr_ = nullptr;
+    bytes_ = 0;
+}
+
+void HostBuffer::ensure(size_t bytes) {
+    if (ptr_ != nullptr && bytes <= bytes_) return;
+    reset();
+    if (bytes == 0) return;
+    check_cuda(cudaMallocHost(&ptr_, bytes), "cudaMallocHost");
+    bytes_ = bytes;
+}
+
+void HostBuffer::reset() {
+    if (ptr_ != nullptr) cudaFreeHost(ptr_);
+    ptr_ = nullptr;
+    bytes_ = 0;
+}
+
+Runtime::Runtime(const gbdic_options &options) {
+    validate_options(options);
+    opt_.o = options;
+    opt_.lanes = options.threads_per_subset;
+    device_ = options.device;
+    int count = 0;
+    check_cuda(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+    if (device_ < 0 || device_ >= count) fail(GBDIC_EINVAL, "CUDA device ordinal out of range");
+    check_cuda(cudaSetDevice(device_), "cudaSetDevice");
+    check_cuda(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_), "attribute");
+    check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    float taps[25];
+    std::memcpy(taps, kFirBits, sizeof taps);
+    check_cuda(set_fir_taps(taps), "FIR taps");
+    double g[7], gs = 0.0;
+    for (int k = 0; k < 7; ++k) { g[k] = std::exp(-0.5 * (k - 3) * (k - 3)); gs += g[k]; }
+    float gf[7];
+    for (int k = 0; k < 7; ++k) gf[k] = (float)(g[k] / gs);
+    check_cuda(set_gauss_taps(gf), "Gaussian taps");
+    const int S = options.subset_size;
+    opt_.weights.resize((size_t)S * S);
+    double wsum = 0.0;
+    const double half = 0.5 * (S - 1), sigma = options.gaussian_sigma;
+    for (int r = 0; r < S; ++r)
+        for (int c = 0; c < S; ++c) {
+            double w = 1.0;
+            if (options.spatial_weighting == 1) {
+                const double x = c - half, y = r - half;
+                w = std::exp(-0.5 * (x * x + y * y) / (sigma * sigma));
+            }
+            opt_.weights[(size_t)r * S + c] = (float)w;
+            wsum += w;
+        }
+    opt_.weight_sum = (float)wsum;
+    weights_.ensure(opt_.weights.size() * sizeof(float));
+    check_cuda(cudaMemcpy(weights_.get(), opt_.weights.data(), opt_.weights.size() * sizeof(float),
+                          cudaMemcpyHostToDevice), "weights upload");
+    if (options.persistent) persistent_grid(opt_.lanes);
+}
+
+Runtime::~Runtime() {
+    if (stream_ != nullptr) {
+        cudaSetDevice(device_);
+        cudaStreamSynchronize(stream_);
+        cudaStreamDestroy(stream_);
+    }
+}
+
+int Runtime::persistent_grid(int lanes) {
+    // Queried once per lane count outside any stream capture, then cached.
+    if (lanes != persistent_lanes_ || persistent_grid_ <= 0) {
+        const int per_sm = icgn_occupancy(opt_.o.motion_model, opt_.o.interpolation, lanes, opt_.o.spatial_weighting == 1);
+        persistent_grid_ = std::max(1, per_sm) * sm_count_;
+        persistent_lanes_ = lanes;
+    }
+    return persistent_grid_;
+}
+
+void Runtime::configure_level(Level &level, int W, int H, int slots) {
+    level.W = W;
+    level.H = H;
+    grid_of(W, H, opt_.o.subset_size, opt_.o.subset_stride, level.gw, level.gh);
+    level.count = level.gw * level.gh;
+    level.slots.clear();
+    ensure_slots(level, slots);
+}
+
+void Runtime::ensure_slots(Level &level, int slots) {
+    const size_t px = (size_t)level.W * level.H;
+    const size_t ss = (size_t)level.count * state_stride(opt_.o.motion_model) * sizeof(float);
+    while ((int)level.slots.size() < slots) {
+        auto s = std::make_unique<LevelSlot>();
+        s->frame.ensure(px);
+        if (opt_.o.interpolation == kInterpBspline) s->coef.ensure(px * sizeof(float));
+        s->state.ensure(ss);
+        s->filtered.ensure(ss);
+        s->seed.ensure(ss);
+        s->active.ensure((size_t)level.count * sizeof(uint32_t));
+        s->counter.ensure(sizeof(unsigned));
+        check_cuda(cudaMemsetAsync(s->state.get(), 0, ss, stream_), "clear state");
+        check_cuda(cudaMemsetAsync(s->filtered.get(), 0, ss, stream_), "clear state");
+        level.slots.push_back(std::move(s));
+    }
+}
+
+double Runtime::prepare_reference(Level &level, const uint8_t *device_image, const uint8_t *roi_selected,
+                                  const float *roi_links) {
+    const int model = opt_.o.motion_model, n = parameter_count(model);
+    const size_t px = (size_t)level.W * level.H;
+    level.plane.ensure(px * sizeof(float4));
+    level.meta.ensure((size_t)level.count * meta_stride(model) * sizeof(float));
+    level.inv.ensure((size_t)level.count * n * n * sizeof(float));
+    level.intensity.ensure(px * sizeof(float));
+    level.spline.ensure(px * sizeof(float));
+    level.scratch.ensure(px * sizeof(float));
+    level.valid.ensure(sizeof(unsigned));
+    level.admissible.ensure((size_t)level.count);
+    level.roi = roi_selected != nullptr;
+    if (roi_selected) {
+        level.selected.ensure(level.count);
+        check_cuda(cudaMemcpyAsync(level.selected.get(), roi_selected, level.count, cudaMemcpyHostToDevice, stream_), "ROI upload");
+    }
+    if (roi_links) {
+        level.links.ensure((size_t)level.count * 4 * sizeof(float));
+        check_cuda(cudaMemcpyAsync(level.links.get(), roi_links, (size_t)level.count * 4 * sizeof(float),
+                                   cudaMemcpyHostToDevice, stream_), "ROI links upload");
+    } else {
+        level.links.reset();
+    }
+    check_cuda(cudaMemsetAsync(level.valid.get(), 0, sizeof(unsigned), stream_), "clear counter");
+    PrepArgs a{};
+    a.img = device_image;
+    a.W = level.W; a.H = level.H; a.pitch = level.W;
+    a.S = opt_.o.subset_size; a.stride = opt_.o.subset_stride;
+    a.grid_w = level.gw; a.grid_h = level.gh; a.count = level.count;
+    a.model = model; a.interp = opt_.o.interpolation; a.gaussian_weighting = opt_.o.spatial_weighting;
+    a.weights = weights_.as<float>();
+    a.weight_sum = opt_.weight_sum;
+    a.selected = roi_selected ? level.selected.as<uint8_t>() : nullptr;
+    a.intensity = level.intensity.as<float>();
+    a.spline = level.spline.as<float>();
+    a.scratch = level.scratch.as<float>();
+    a.plane = level.plane.as<float4>();
+    a.meta = level.meta.as<float>();
+    a.inv = level.inv.as<float>();
+    a.valid_count = level.valid.as<unsigned>();
+    a.admissible = level.admissible.as<uint8_t>();
+    cudaEvent_t e0, e1;
+    check_cuda(cudaEventCreate(&e0), "event");
+    check_cuda(cudaEventCreate(&e1), "event");
+    cudaEventRecord(e0, stream_);
+    check_cuda(launch_reference_prep(a, stream_), "reference preparation launch");
+    cudaEventRecord(e1, stream_);
+    unsigned valid = 0;
+    check_cuda(cudaMemcpyAsync(&valid, level.valid.get(), sizeof(unsigned), cudaMemcpyDeviceToHost, stream_), "readback");
+    wait_event(e1, kWaitMs);
+    check_cuda(cudaStreamSynchronize(stream_), "reference preparation");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    level.valid_count = (int)valid;
+    return ms;
+}
+
+void Runtime::upload_reference_arrays(Level &level, const float *plane, const float *meta, const float *inverse,
+                                      const float *links) {
+    const int model = opt_.o.motion_model, n = parameter_count(model);
+    const size_t px = (size_t)level.W * level.H;
+    level.plane.ensure(px * sizeof(float4));
+    level.meta.ensure((size_t)level.count * meta_stride(model) * sizeof(float));
+    level.inv.ensure((size_t)level.count * n * n * sizeof(float));
+    check_cuda(cudaMemcpy(level.plane.get(), plane, px * sizeof(float4), cudaMemcpyHostToDevice), "plane upload");
+    check_cuda(cudaMemcpy(level.meta.get(), meta, (size_t)level.count * meta_stride(model) * sizeof(float),
+                          cudaMemcpyHostToDevice), "metadata upload");
+    check_cuda(cudaMemcpy(level.inv.get(), inverse, (size_t)level.count * n * n * sizeof(float),
+                          cudaMemcpyHostToDevice), "inverse upload");
+    level.roi = links != nullptr;
+    if (links) {
+        level.links.ensure((size_t)level.count * 4 * sizeof(float));
+        check_cuda(cudaMemcpy(level.links.get(), links, (size_t)level.count * 4 * sizeof(float),
+                              cudaMemcpyHostToDevice), "links upload");
+    } else {
+        level.links.reset();
+    }
+    int valid = 0;
+    std::vector<float> m((size_t)level.count * meta_stride(model));
+    std::memcpy(m.data(), meta, m.size() * sizeof(float));
+    std::vector<uint8_t> adm((size_t)level.count);
+    for (int i = 0; i < level.count; ++i) {
+        const float flag = m[(size_t)i * meta_stride(model) + 1];
+        valid += flag > 0.5f;
+        adm[(size_t)i] = (flag > 0.5f || flag == -4.0f) ? 1 : 0;
+    }
+    level.valid_count = valid;
+    level.admissible.ensure((size_t)level.count);
+    check_cuda(cudaMemcpy(level.admissible.get(), adm.data(), adm.size(), cudaMemcpyHostToDevice), "admissibility upload");
+}
+
+void Runtime::enqueue_prefilter(Level &level, LevelSlot &slot, const uint8_t *frame, cudaStream_t s) {
+    if (opt_.o.interpolation != kInterpBspline) return;
+    check_cuda(launch_fir_prefilter(frame ? frame : slot.frame.as<uint8_t>(), level.W, level.H, level.W,
+                                    slot.coef.as<float>(), s),
+               "prefilter launch");
+}
+
+void Runtime::enqueue_solve(Level &level, LevelSlot &slot, const gbdic_solver_cfg &cfg, bool seeded, bool preserve,
+                            const uint8_t *frame, float *state, cudaStream_t s) {
+    SolveArgs a{};
+    a.coef = slot.coef.as<float>();
+    a.img = frame ? frame : slot.frame.as<uint8_t>();
+    a.plane = level.plane.as<float4>();
+    a.meta = level.meta.as<float>();
+    a.inv = level.inv.as<float>();
+    a.weights = opt_.o.spatial_weighting == 1 ? weights_.as<float>() : nullptr;
+    a.seed = seeded ? slot.seed.as<float>() : nullptr;
+    a.active = seeded ? slot.active.as<uint32_t>() : nullptr;
+    a.state = state ? state : slot.state.as<float>();
+    a.work_counter = slot.counter.as<unsigned>();
+    a.W = level.W; a.H = level.H; a.grid_w = level.gw; a.count = level.count;
+    a.S = opt_.o.subset_size; a.stride = opt_.o.subset_stride;
+    a.iterations = cfg.iterations; a.tolerance = cfg.tolerance; a.zncc_min = cfg.zncc_min;
+    a.weight_sum = opt_.weight_sum;
+    a.roi_enabled = level.roi ? 1 : 0;
+    a.preserve_disabled = preserve ? 1 : 0;
+    a.use_mean = opt_.o.subset_stride != opt_.o.subset_size;
+    a.div_patience = opt_.o.divergence_patience;
+    a.div_min = opt_.o.divergence_min_iterations;
+    a.persistent = opt_.o.persistent;
+    int grid = 0;
+    if (a.persistent) {
+        grid = persistent_grid(opt_.lanes);
+        check_cuda(cudaMemsetAsync(slot.counter.get(), 0, sizeof(unsigned), s), "queue reset");
+    }
+    check_cuda(launch_icgn(a, opt_.o.motion_model, opt_.o.interpolation, opt_.lanes, opt_.o.spatial_weighting == 1,
+                           grid, s), "solver launch");
+}
+
+void Runtime::enqueue_uod(Level &level, LevelSlot &slot, bool seed_mode, float *out, cudaStream_t s) {
+    if (opt_.o.outlier_policy == GBDIC_OUTLIER_DISABLED) return;
+    UodArgs u{};
+    u.state = slot.state.as<float>();
+    u.out = out ? out : slot.filtered.as<float>();
+    u.meta = level.meta.as<float>();
+    u.links = level.links.get() ? level.links.as<float>() : nullptr;
+    u.grid_w = level.gw; u.grid_h = level.gh; u.count = level.count;
+    u.subset_stride = opt_.o.subset_stride;
+    u.model = opt_.o.motion_model;
+    u.policy = opt_.o.outlier_policy;
+    u.median_size = opt_.o.outlier_policy == GBDIC_OUTLIER_MEDIAN ? opt_.o.median_filter_size : 3;
+    u.scope_all = opt_.o.median_filter_scope;
+    u.seed_mode = seed_mode ? 1 : 0;
+    u.roi_enabled = (level.roi && u.links != nullptr) ? 1 : 0;
+    check_cuda(launch_uod(u, s), "UOD launch");
+}
+
+const float *Runtime::output_state(LevelSlot &slot) const {
+    return opt_.o.outlier_policy == GBDIC_OUTLIER_DISABLED ? slot.state.as<float>() : slot.filtered.as<float>();
+}
+
+void Runtime::upload_frame(Level &level, LevelSlot &slot, const uint8_t *frame, int64_t row_stride,
+                           HostBuffer &staging, cudaStream_t s) {
+    const size_t W = (size_t)level.W, H = (size_t)level.H;
+    staging.ensure(W * H);
+    uint8_t *dst = staging.as<uint8_t>();
+    if (row_stride == (int64_t)W) {
+        std::memcpy(dst, frame, W * H);
+    } else {
+        for (size_t r = 0; r < H; ++r) std::memcpy(dst + r * W, frame + (size_t)r * row_stride, W);
+    }
+    check_cuda(cudaMemcpyAsync(slot.frame.get(), dst, W * H, cudaMemcpyHostToDevice, s), "frame upload");
+}
+
+}  // namespace gbdic
+

@@ -1,0 +1,7 @@
+// IC-GN solver instantiations for the affine model (see solver_impl.cuh).
+#include "gbdic_kernels.h"
+#include "solver_impl.cuh"
+
+namespace gbdic {
+GBDIC_SOLVER_MODEL(kModelAffine)
+}  // namespace gbdic

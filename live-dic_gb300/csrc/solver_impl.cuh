@@ -1,0 +1,509 @@
+// IC-GN subset solver (reference: shaders/icgn.wgsl:595-1017).
+//
+// One group of LANES threads solves one subset.  Pixel p of the S x S subset
+// belongs to lane p % LANES; each lane accumulates its pixels in increasing p
+// order, and the lane partial sums are combined by the pairwise tree of
+// icgn.wgsl:782-799 (stride LANES/2 .. 1, lane i += lane i + stride).  For
+// LANES <= 32 the tree is a __shfl_down ladder inside a warp; for 64 and 128
+// the strides >= 32 go through shared memory first.  After the reduction the
+// totals are broadcast and every lane evaluates the same Gauss-Newton update
+// (identical operands, identical results), so the warp state never leaves
+// registers.
+//
+// Work distribution: a "unit" is a warp (LANES <= 32) or a 128-thread block
+// (LANES > 32) holding 128/LANES or 32/LANES groups.  Grid mode maps units to
+// the launch grid; persistent mode keeps one resident grid and lets every
+// unit pull the next batch of subsets from an atomic queue head, so subsets
+// with long iteration counts do not hold up a statically assigned tile.
+#pragma once
+
+#include "gbdic_common.cuh"
+
+namespace gbdic {
+
+template <int MODEL>
+struct SumCount {
+    static constexpr int value = MODEL == kModelQuadratic ? 15 : (MODEL == kModelTranslation ? 5 : 9);
+};
+
+// Tree reduction inside a warp segment of LANES lanes, then broadcast of the
+// segment's lane-0 totals to the whole segment.
+template <int LANES, int N>
+__device__ __forceinline__ void reduce_warp(float (&s)[N], int lane_in_warp) {
+#pragma unroll
+    for (int off = LANES / 2; off >= 1; off >>= 1) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) s[k] = s[k] + __shfl_down_sync(kFullMask, s[k], off, LANES);
+    }
+    const int src = lane_in_warp & ~(LANES - 1);
+#pragma unroll
+    for (int k = 0; k < N; ++k) s[k] = __shfl_sync(kFullMask, s[k], src);
+}
+
+// Same tree for 64 or 128 lanes: shared-memory strides down to 32, then the
+// shuffle ladder in the group's first warp; totals broadcast through `red`.
+template <int LANES, int N>
+__device__ __forceinline__ void reduce_block(float (&s)[N], float *red, int glane) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) red[k * LANES + glane] = s[k];
+    __syncthreads();
+#pragma unroll
+    for (int stride = LANES / 2; stride >= 32; stride >>= 1) {
+        if (glane < stride) {
+#pragma unroll
+            for (int k = 0; k < N; ++k)
+                red[k * LANES + glane] = red[k * LANES + glane] + red[k * LANES + glane + stride];
+        }
+        __syncthreads();
+    }
+    if (glane < 32) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            float v = red[k * LANES + glane];
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_down_sync(kFullMask, v, off);
+            if (glane == 0) red[k * LANES] = v;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; ++k) s[k] = red[k * LANES];
+    __syncthreads();
+}
+
+// Bounds check of icgn.wgsl:647-690: the warped corner (affine) or 3x3
+// control points (quadratic) must lie in [2, W-3] x [2, H-3].
+template <int MODEL>
+__device__ __forceinline__ bool warp_inside(const Warp &w, int px0, int py0, int S, float half,
+                                            int W, int H) {
+    const float xmax = (float)W - 3.0f, ymax = (float)H - 3.0f;
+    if (MODEL == kModelTranslation) {
+        float x0 = (float)px0 + w.t0, y0 = (float)py0 + w.t1;
+        float x1 = (float)(px0 + S - 1) + w.t0, y1 = (float)(py0 + S - 1) + w.t1;
+        return x0 >= 2.0f && y0 >= 2.0f && x1 <= xmax && y1 <= ymax;
+    }
+    bool inside = true;
+    constexpr int count = MODEL == kModelQuadratic ? 9 : 4;
+#pragma unroll
+    for (int p = 0; p < count; ++p) {
+        float lx, ly;
+        if (MODEL == kModelQuadratic) {
+            lx = (float)(p % 3 - 1) * half;
+            ly = (float)(p / 3 - 1) * half;
+        } else {
+            lx = (p == 1 || p == 3) ? half : -half;
+            ly = (p >= 2) ? half : -half;
+        }
+        float dx, dy;
+        displacement<MODEL>(w, lx, ly, 0.5f * lx * lx, lx * ly, 0.5f * ly * ly, dx, dy);
+        float px = ((float)px0 + (half + lx)) + dx;
+        float py = ((float)py0 + (half + ly)) + dy;
+        inside = inside && px >= 2.0f && py >= 2.0f && px <= xmax && py <= ymax;
+    }
+    return inside;
+}
+
+// Quadratic inverse composition (icgn.wgsl:393-513): lifted 6x6 warp matrix
+// of the increment, pivoted Gauss-Jordan in binary32; row swaps are done by
+// predicated selects so the augmented matrix stays in registers.
+__device__ __forceinline__ bool compose_quadratic(Warp &w, const float (&d)[12]) {
+    const float u = d[0], ux = d[1], uy = d[2], v = d[3], vx = d[4], vy = d[5];
+    const float uxx = d[6], uxy = d[7], uyy = d[8], vxx = d[9], vxy = d[10], vyy = d[11];
+    float m[6][12];
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int e = 0; e < 12; ++e) m[r][e] = (e == 6 + r) ? 1.0f : 0.0f;
+    m[0][0] = fmaf(u, uxx, fmaf(ux, ux, 1.0f + 2.0f * ux));
+    m[0][1] = fmaf(2.0f * (1.0f + ux), uy, 2.0f * u * uxy);
+    m[0][2] = fmaf(u, uyy, uy * uy);
+    m[0][3] = 2.0f * u * (1.0f + ux);
+    m[0][4] = 2.0f * u * uy;
+    m[0][5] = u * u;
+    m[1][0] = 0.5f * fmaf(u, vxx, fmaf(2.0f * (1.0f + ux), vx, v * uxx));
+    m[1][1] = (fmaf(u, vxy, fmaf(v, uxy, fmaf(ux, vy, fmaf(uy, vx, 1.0f)))) + vy) + ux;
+    m[1][2] = 0.5f * fmaf(u, vyy, fmaf(2.0f * uy, 1.0f + vy, v * uyy));
+    m[1][3] = fmaf(u, vx, fmaf(v, ux, v));
+    m[1][4] = fmaf(u, vy, fmaf(v, uy, u));
+    m[1][5] = u * v;
+    m[2][0] = fmaf(v, vxx, vx * vx);
+    m[2][1] = fmaf(2.0f * vx, 1.0f + vy, 2.0f * v * vxy);
+    m[2][2] = fmaf(v, vyy, fmaf(vy, vy, 1.0f + 2.0f * vy));
+    m[2][3] = 2.0f * v * vx;
+    m[2][4] = 2.0f * v * (1.0f + vy);
+    m[2][5] = v * v;
+    m[3][0] = 0.5f * uxx; m[3][1] = uxy; m[3][2] = 0.5f * uyy;
+    m[3][3] = 1.0f + ux;  m[3][4] = uy;  m[3][5] = u;
+    m[4][0] = 0.5f * vxx; m[4][1] = vxy; m[4][2] = 0.5f * vyy;
+    m[4][3] = vx;         m[4][4] = 1.0f + vy; m[4][5] = v;
+    m[5][0] = 0.0f; m[5][1] = 0.0f; m[5][2] = 0.0f; m[5][3] = 0.0f; m[5][4] = 0.0f; m[5][5] = 1.0f;
+#pragma unroll
+    for (int col = 0; col < 6; ++col) {
+        int prow = col;
+        float psize = fabsf(m[col][col]);
+#pragma unroll
+        for (int cand = col + 1; cand < 6; ++cand) {
+            float cs = fabsf(m[cand][col]);
+            if (cs > psize) { prow = cand; psize = cs; }
+        }
+        if (psize < 1e-8f) return false;
+#pragma unroll
+        for (int cand = col + 1; cand < 6; ++cand) {
+            if (cand == prow) {
+#pragma unroll
+                for (int e = 0; e < 12; ++e) {
+                    float tmp = m[col][e];
+                    m[col][e] = m[cand][e];
+                    m[cand][e] = tmp;
+                }
+            }
+        }
+        const float pivot = m[col][col];
+#pragma unroll
+        for (int e = 0; e < 12; ++e) m[col][e] = m[col][e] / pivot;
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            if (r == col) continue;
+            const float f = m[r][col];
+#pragma unroll
+            for (int e = 0; e < 12; ++e) m[r][e] = fmaf(-f, m[col][e], m[r][e]);
+        }
+    }
+    const float cu[6] = {0.5f * w.c0, w.c1, 0.5f * w.c2, 1.0f + w.l0, w.l1, w.t0};
+    const float cv[6] = {0.5f * w.c3, w.c4, 0.5f * w.c5, w.l2, 1.0f + w.l3, w.t1};
+    float nu[6], nv[6];
+#pragma unroll
+    for (int col = 0; col < 6; ++col) {
+        float au = 0.0f, av = 0.0f;
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+            au = fmaf(cu[e], m[e][6 + col], au);
+            av = fmaf(cv[e], m[e][6 + col], av);
+        }
+        nu[col] = au;
+        nv[col] = av;
+    }
+    w.c0 = 2.0f * nu[0]; w.c1 = nu[1]; w.c2 = 2.0f * nu[2];
+    w.c3 = 2.0f * nv[0]; w.c4 = nv[1]; w.c5 = 2.0f * nv[2];
+    w.t0 = nu[5];
+    w.t1 = nv[5];
+    w.l0 = nu[3] - 1.0f; w.l1 = nu[4];
+    w.l2 = nv[3];        w.l3 = nv[4] - 1.0f;
+    return true;
+}
+
+// icgn.wgsl:103-111 optional stagnation check (status 3 internal).
+__device__ __forceinline__ float divergence_status(const SolveArgs &a, float change, unsigned count,
+                                                   float status, float &previous, unsigned &stalled) {
+    if (a.div_patience == 0 || status != 0.0f) return status;
+    if (count >= (unsigned)a.div_min) stalled = (change >= previous) ? stalled + 1u : 0u;
+    previous = change;
+    return (stalled >= (unsigned)a.div_patience) ? 3.0f : status;
+}
+
+// Gauss-Newton update from the reduced totals (icgn.wgsl:801-921).  Returns
+// the new status; modifies the warp on a successful composition.
+template <int MODEL>
+__device__ __forceinline__ float gn_update(const SolveArgs &a, const float (&t)[SumCount<MODEL>::value],
+                                           const float *__restrict__ md, const float *__restrict__ hi,
+                                           float wsum, float half, unsigned it1, Warp &w,
+                                           float &prev_change, unsigned &stalled) {
+    constexpr int n = parameter_count(MODEL);
+    // Totals layout: 0 sum g, 1 sum g^2, 2 sum f g, then J^T g.
+    float jg[12];
+    if (MODEL == kModelTranslation) {
+        jg[0] = t[3]; jg[3] = t[4];
+        jg[1] = jg[2] = jg[4] = jg[5] = 0.0f;
+    } else {
+#pragma unroll
+        for (int k = 0; k < SumCount<MODEL>::value - 3; ++k) jg[k] = t[3 + k];
+    }
+    const float mean_g = t[0] / wsum;
+    const float norm_g = sqrtf(fmaxf(0.0f, fmaf(-t[0], mean_g, t[1])));
+    const float norm_f = __ldg(md + 0);
+    if (norm_g < 1e-9f || norm_f < 1e-9f) return -2.0f;
+    const float ratio = norm_f / norm_g;
+    const int sum_off = 2 + n;
+    float delta[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) delta[k] = 0.0f;
+    if (MODEL == kModelTranslation) {
+        float r0 = fmaf(-ratio, fmaf(-mean_g, __ldg(md + sum_off + 0), jg[0]), __ldg(md + 2));
+        float r3 = fmaf(-ratio, fmaf(-mean_g, __ldg(md + sum_off + 3), jg[3]), __ldg(md + 5));
+        float a0 = __ldg(hi + 0) * r0;
+        a0 = fmaf(__ldg(hi + 3), r3, a0);
+        float a3 = __ldg(hi + 18) * r0;
+        a3 = fmaf(__ldg(hi + 21), r3, a3);
+        delta[0] = -a0;
+        delta[3] = -a3;
+    } else {
+        float res[n];
+#pragma unroll
+        for (int k = 0; k < n; ++k)
+            res[k] = fmaf(-ratio, fmaf(-mean_g, __ldg(md + sum_off + k), jg[k]), __ldg(md + 2 + k));
+#pragma unroll
+        for (int r = 0; r < n; ++r) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int k = 0; k < n; ++k) acc = fmaf(__ldg(hi + r * n + k), res[k], acc);
+            delta[r] = -acc;
+        }
+    }
+    float change;
+    if (MODEL == kModelQuadratic) {
+        if (!compose_quadratic(w, delta)) return -1.0f;
+        change = 0.0f;
+#pragma unroll
+        for (int p = 0; p < 9; ++p) {
+            float x = (float)(p % 3 - 1) * half, y = (float)(p / 3 - 1) * half;
+            float hx2 = 0.5f * x * x, xy = x * y, hy2 = 0.5f * y * y;
+            float ca = fmaf(delta[2], y, fmaf(delta[1], x, delta[0]));
+            ca = ca + fmaf(delta[6], hx2, fmaf(delta[7], xy, delta[8] * hy2));
+            float cb = fmaf(delta[5], y, fmaf(delta[4], x, delta[3]));
+            cb = cb + fmaf(delta[9], hx2, fmaf(delta[10], xy, delta[11] * hy2));
+            change = fmaxf(change, length2(ca, cb));
+        }
+    } else if (MODEL == kModelTranslation) {
+        w.t0 = w.t0 - delta[0];
+        w.t1 = w.t1 - delta[3];
+        change = length2(delta[0], delta[3]);
+    } else {
+        const float det = fmaf(1.0f + delta[1], 1.0f + delta[5], -(delta[2] * delta[4]));
+        if (fabsf(det) < 1e-8f) return -1.0f;
+        const float i11 = (1.0f + delta[5]) / det, i12 = -delta[2] / det;
+        const float i21 = -delta[4] / det, i22 = (1.0f + delta[1]) / det;
+        const float w11 = 1.0f + w.l0, w12 = w.l1, w21 = w.l2, w22 = 1.0f + w.l3;
+        const float itx = -fmaf(i11, delta[0], i12 * delta[3]);
+        const float ity = -fmaf(i21, delta[0], i22 * delta[3]);
+        w.t0 = w.t0 + fmaf(w11, itx, w12 * ity);
+        w.t1 = w.t1 + fmaf(w21, itx, w22 * ity);
+        const float u11 = fmaf(w11, i11, w12 * i21), u12 = fmaf(w11, i12, w12 * i22);
+        const float u21 = fmaf(w21, i11, w22 * i21), u22 = fmaf(w21, i12, w22 * i22);
+        w.l0 = u11 - 1.0f; w.l1 = u12; w.l2 = u21; w.l3 = u22 - 1.0f;
+        change = 0.0f;
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            float x = (p == 1 || p == 3) ? half : -half;
+            float y = (p >= 2) ? half : -half;
+            float ca = fmaf(delta[2], y, fmaf(delta[1], x, delta[0]));
+            float cb = fmaf(delta[5], y, fmaf(delta[4], x, delta[3]));
+            change = fmaxf(change, length2(ca, cb));
+        }
+    }
+    const float zncc = t[2] / (norm_f * norm_g);
+    const float conv = (change >= a.tolerance) ? 0.0f : (zncc >= a.zncc_min ? 1.0f : -2.0f);
+    return divergence_status(a, change, it1, conv, prev_change, stalled);
+}
+
+template <int MODEL, int INTERP, int LANES, bool GAUSS>
+__device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int glane, int lane_in_warp,
+                                            float *red) {
+    constexpr int N = SumCount<MODEL>::value;
+    constexpr bool kBlock = LANES > 32;
+    constexpr bool kClamp = MODEL == kModelQuadratic;
+    const bool exists = idx < a.count;
+    const int sidx = exists ? idx : 0;
+    const float *md = a.meta + (size_t)sidx * meta_stride(MODEL);
+    const float *hi = a.inv + (size_t)sidx * parameter_count(MODEL) * parameter_count(MODEL);
+    Warp w = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    bool enabled = exists;
+    if (a.seed != nullptr && exists) {
+        const float4 *s = reinterpret_cast<const float4 *>(a.seed + (size_t)sidx * state_stride(MODEL));
+        float4 s0 = __ldg(s), s1 = __ldg(s + 1);
+        w.t0 = s0.x; w.l0 = s0.y; w.l1 = s0.z; w.t1 = s0.w;
+        w.l2 = s1.x; w.l3 = s1.y;
+        if (MODEL == kModelQuadratic) {
+            float4 s2 = __ldg(s + 2);
+            w.c0 = s1.z; w.c1 = s1.w; w.c2 = s2.x; w.c3 = s2.y; w.c4 = s2.z; w.c5 = s2.w;
+        }
+        enabled = __ldg(a.active + sidx) != 0u;
+    }
+    if (MODEL == kModelTranslation) { w.l0 = w.l1 = w.l2 = w.l3 = 0.0f; }
+    const float mvalid = __ldg(md + 1);
+    const bool valid = enabled && mvalid >= 0.5f;
+    const float rejected = a.roi_enabled ? fminf(-1.0f, mvalid) : -1.0f;
+    float status = valid ? 0.0f : rejected;
+    float iters = 0.0f;
+    bool done = !exists;
+    const int S = a.S;
+    const int gx = sidx % a.grid_w, gy = sidx / a.grid_w;
+    const int px0 = gx * a.stride, py0 = gy * a.stride;
+    const float half = 0.5f * ((float)S - 1.0f);
+    const float ref_mean = a.use_mean ? __ldg(md + (MODEL == kModelQuadratic ? 26 : 14)) : 0.0f;
+    const float wsum = GAUSS ? __ldg(md + 3 + 2 * parameter_count(MODEL)) : (float)(S * S);
+    float prev_change = 3.402823e38f;
+    unsigned stalled = 0u;
+    const int npix = S * S;
+    const int ldiv = LANES / S, lmod = LANES % S;
+    const int col0 = glane % S, row0 = glane / S;
+    const int W = a.W, H = a.H;
+
+    for (int it = 0; it < 30; ++it) {
+        if (!done) {
+            if (!(a.div_patience != 0 && status == 3.0f)) {
+                if (!warp_inside<MODEL>(w, px0, py0, S, half, W, H)) {
+                    if (!a.roi_enabled || status > -2.5f) status = -1.0f;
+                }
+            }
+            if (it >= a.iterations || fabsf(status) > 0.5f) done = true;
+        }
+        if (kBlock) {
+            if (!__syncthreads_or(!done)) break;
+        } else {
+            if (__all_sync(kFullMask, done)) break;
+        }
+        float s[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k) s[k] = 0.0f;
+        if (!done) {
+            int col = col0, row = row0;
+            for (int p = glane; p < npix; p += LANES) {
+                const float lx = (float)col - half, ly = (float)row - half;
+                float hx2 = 0.0f, xy = 0.0f, hy2 = 0.0f;
+                if (MODEL == kModelQuadratic) {
+                    hx2 = 0.5f * lx * lx;
+                    xy = lx * ly;
+                    hy2 = 0.5f * ly * ly;
+                }
+                float dx, dy;
+                displacement<MODEL>(w, lx, ly, hx2, xy, hy2, dx, dy);
+                const int pxi = px0 + col, pyi = py0 + row;
+                const float g = sample_target<INTERP, kClamp>(a.coef, a.img, W, H, (float)pxi + dx,
+                                                              (float)pyi + dy);
+                const float4 rv = __ldg(a.plane + (size_t)pyi * W + pxi);
+                const float f = rv.x - ref_mean;
+                float wc = g, wf = f;
+                if (GAUSS) {
+                    const float wt = __ldg(a.weights + p);
+                    wc = wt * g;
+                    wf = wt * f;
+                }
+                const float gxg = rv.y * wc, gyg = rv.z * wc;
+                s[0] = s[0] + wc;
+                s[1] = fmaf(wc, g, s[1]);
+                s[2] = fmaf(wf, g, s[2]);
+                if (MODEL == kModelTranslation) {
+                    s[3] = s[3] + gxg;
+                    s[4] = s[4] + gyg;
+                } else {
+                    s[3] = s[3] + gxg;
+                    s[4] = fmaf(gxg, lx, s[4]);
+                    s[5] = fmaf(gxg, ly, s[5]);
+                    s[6] = s[6] + gyg;
+                    s[7] = fmaf(gyg, lx, s[7]);
+                    s[8] = fmaf(gyg, ly, s[8]);
+                    if (MODEL == kModelQuadratic) {
+                        s[9] = fmaf(gxg, hx2, s[9]);
+                        s[10] = fmaf(gxg, xy, s[10]);
+                        s[11] = fmaf(gxg, hy2, s[11]);
+                        s[12] = fmaf(gyg, hx2, s[12]);
+                        s[13] = fmaf(gyg, xy, s[13]);
+                        s[14] = fmaf(gyg, hy2, s[14]);
+                    }
+                }
+                col += lmod;
+                row += ldiv;
+                if (col >= S) { col -= S; ++row; }
+            }
+        }
+        if (kBlock) reduce_block<LANES, N>(s, red, glane);
+        else reduce_warp<LANES, N>(s, lane_in_warp);
+        if (!done) {
+            iters = (float)(it + 1);
+            status = gn_update<MODEL>(a, s, md, hi, wsum, half, (unsigned)(it + 1), w, prev_change, stalled);
+        }
+    }
+    if (exists && (enabled || !a.preserve_disabled) && glane == 0) {
+        const float final_status = (a.div_patience != 0 && status == 3.0f) ? 0.0f : status;
+        float4 *o = reinterpret_cast<float4 *>(a.state + (size_t)idx * state_stride(MODEL));
+        o[0] = make_float4(w.t0, w.l0, w.l1, w.t1);
+        if (MODEL == kModelQuadratic) {
+            o[1] = make_float4(w.l2, w.l3, w.c0, w.c1);
+            o[2] = make_float4(w.c2, w.c3, w.c4, w.c5);
+            o[3] = make_float4(final_status, iters, 0.0f, 0.0f);
+        } else {
+            o[1] = make_float4(w.l2, w.l3, final_status, iters);
+        }
+    }
+}
+
+template <int MODEL, int INTERP, int LANES, bool GAUSS>
+__global__ void __launch_bounds__(128) icgn_kernel(SolveArgs a) {
+    constexpr bool kBlock = LANES > 32;
+    constexpr int kUnitThreads = kBlock ? 128 : 32;
+    constexpr int kGroups = kUnitThreads / LANES;
+    constexpr int N = SumCount<MODEL>::value;
+    __shared__ float red_smem[kBlock ? 128 * N : 1];
+    __shared__ int unit_base;
+    const int tid = threadIdx.x;
+    const int glane = tid % LANES;
+    const int group_in_unit = (tid % kUnitThreads) / LANES;
+    const int lane_in_warp = tid & 31;
+    const int units_per_block = 128 / kUnitThreads;
+    const long long unit = (long long)blockIdx.x * units_per_block + tid / kUnitThreads;
+    float *red = red_smem + (kBlock ? group_in_unit * LANES * N : 0);
+    for (;;) {
+        int base;
+        if (a.persistent) {
+            if (kBlock) {
+                if (tid == 0) unit_base = (int)atomicAdd(a.work_counter, (unsigned)kGroups);
+                __syncthreads();
+                base = unit_base;
+                __syncthreads();
+            } else {
+                int v = 0;
+                if (lane_in_warp == 0) v = (int)atomicAdd(a.work_counter, (unsigned)kGroups);
+                base = __shfl_sync(kFullMask, v, 0);
+            }
+        } else {
+            base = unit * kGroups < (long long)a.count ? (int)(unit * kGroups) : a.count;
+        }
+        if (base >= a.count) break;
+        solve_group<MODEL, INTERP, LANES, GAUSS>(a, base + group_in_unit, glane, lane_in_warp, red);
+        if (!a.persistent) break;
+    }
+}
+
+#define GBDIC_SOLVER_CASE(MODEL, INTERP, LANES)                                                   \
+    if (interp == INTERP && lanes == LANES) {                                                     \
+        if (occupancy_only) {                                                                      \
+            int blocks = 0;                                                                        \
+            if (gauss)                                                                             \
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(                                     \
+                    &blocks, icgn_kernel<MODEL, INTERP, LANES, true>, 128, 0);                     \
+            else                                                                                   \
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(                                     \
+                    &blocks, icgn_kernel<MODEL, INTERP, LANES, false>, 128, 0);                    \
+            *occupancy_only = blocks;                                                              \
+            return cudaSuccess;                                                                    \
+        }                                                                                          \
+        if (gauss)                                                                                 \
+            icgn_kernel<MODEL, INTERP, LANES, true><<<grid, 128, 0, stream>>>(a);                  \
+        else                                                                                       \
+            icgn_kernel<MODEL, INTERP, LANES, false><<<grid, 128, 0, stream>>>(a);                 \
+        return cudaGetLastError();                                                                 \
+    }
+
+// Launcher for one model (instantiated in solver_<model>.cu).  With
+// occupancy_only set, nothing is launched and the resident CTA count per SM
+// of the selected variant is stored there instead.
+#define GBDIC_SOLVER_MODEL(MODEL)                                                                 \
+    template <>                                                                                    \
+    cudaError_t launch_icgn_model<MODEL>(const SolveArgs &a, int interp, int lanes, bool gauss,    \
+                                         int grid, cudaStream_t stream, int *occupancy_only) {     \
+        GBDIC_SOLVER_CASE(MODEL, kInterpBspline, 16)                                               \
+        GBDIC_SOLVER_CASE(MODEL, kInterpBspline, 32)                                               \
+        GBDIC_SOLVER_CASE(MODEL, kInterpBspline, 64)                                               \
+        GBDIC_SOLVER_CASE(MODEL, kInterpBspline, 128)                                              \
+        GBDIC_SOLVER_CASE(MODEL, kInterpLinear, 16)                                                \
+        GBDIC_SOLVER_CASE(MODEL, kInterpLinear, 32)                                                \
+        GBDIC_SOLVER_CASE(MODEL, kInterpLinear, 64)                                                \
+        GBDIC_SOLVER_CASE(MODEL, kInterpLinear, 128)                                               \
+        GBDIC_SOLVER_CASE(MODEL, kInterpKeys, 16)                                                  \
+        GBDIC_SOLVER_CASE(MODEL, kInterpKeys, 32)                                                  \
+        GBDIC_SOLVER_CASE(MODEL, kInterpKeys, 64)                                                  \
+        GBDIC_SOLVER_CASE(MODEL, kInterpKeys, 128)                                                 \
+        return cudaErrorInvalidValue;                                                              \
+    }
+
+}  // namespace gbdic

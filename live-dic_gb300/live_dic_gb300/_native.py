@@ -1,0 +1,175 @@
+"""ctypes binding of libgbdic.so (include/gbdic.h).
+
+The library is built in-tree by live-dic_gb300/build.py.  Loading fails
+loudly with ICGNError when it is missing: there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import numpy as np
+
+from .engine import ICGNError
+
+LIBRARY_PATH = Path(__file__).resolve().parent / "libgbdic.so"
+
+OK, EINVAL, ESTATE, ECUDA, ETIMEOUT = 0, -1, -2, -3, -4
+EXPORT_COEFFICIENTS, EXPORT_PLANE, EXPORT_METADATA, EXPORT_INVERSE = 0, 1, 2, 3
+EXPORT_RAW_STATE, EXPORT_OUTPUT_STATE, EXPORT_WEIGHTS, EXPORT_FRAME = 4, 5, 6, 7
+EXPORT_ADMISSIBLE = 8
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("motion_model", C.c_int32),
+        ("interpolation", C.c_int32),
+        ("subset_size", C.c_int32),
+        ("subset_stride", C.c_int32),
+        ("spatial_weighting", C.c_int32),
+        ("gaussian_sigma", C.c_float),
+        ("outlier_policy", C.c_int32),
+        ("median_filter_size", C.c_int32),
+        ("median_filter_scope", C.c_int32),
+        ("threads_per_subset", C.c_int32),
+        ("divergence_patience", C.c_int32),
+        ("divergence_min_iterations", C.c_int32),
+        ("pipeline_slots", C.c_int32),
+        ("persistent", C.c_int32),
+    ]
+
+
+class SolverCfg(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("tolerance", C.c_float), ("zncc_min", C.c_float)]
+
+
+class RefInfo(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("grid_width", C.c_int32),
+        ("grid_height", C.c_int32),
+        ("valid_count", C.c_int32),
+        ("device_ms", C.c_double),
+    ]
+
+
+class Timing(C.Structure):
+    _fields_ = [
+        ("upload_ms", C.c_double),
+        ("execute_ms", C.c_double),
+        ("readback_ms", C.c_double),
+        ("total_ms", C.c_double),
+        ("device_ms", C.c_double),
+    ]
+
+
+class PyramidOptions(C.Structure):
+    _fields_ = [
+        ("base", Options),
+        ("levels", C.c_int32),
+        ("iterations", C.c_int32 * 4),
+        ("tolerance", C.c_float * 4),
+        ("zncc_min", C.c_float),
+        ("initialization", C.c_int32),
+        ("temporal_max_age", C.c_uint32),
+        ("temporal_prediction", C.c_int32),
+        ("seed_search_radius", C.c_int32),
+    ]
+
+
+class LevelRoi(C.Structure):
+    _fields_ = [
+        ("selected", C.POINTER(C.c_uint8)),
+        ("links", C.POINTER(C.c_float)),
+        ("seed_links", C.POINTER(C.c_uint32)),
+    ]
+
+
+P = C.c_void_p
+I32, I64 = C.c_int32, C.c_int64
+_SIGNATURES = {
+    "gbdic_abi_version": (C.c_int, []),
+    "gbdic_create": (C.c_int, [C.POINTER(Options), C.POINTER(P)]),
+    "gbdic_destroy": (None, [P]),
+    "gbdic_last_error": (C.c_char_p, [P]),
+    "gbdic_set_reference": (C.c_int, [P, P, I32, I32, I64, P, P, C.POINTER(RefInfo)]),
+    "gbdic_set_reference_arrays": (C.c_int, [P, I32, I32, P, P, P, P, C.POINTER(RefInfo)]),
+    "gbdic_register": (C.c_int, [P, P, I64, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),
+    "gbdic_register_seeded": (C.c_int, [P, P, I64, P, P, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),
+    "gbdic_retry_seeded": (C.c_int, [P, P, P, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),
+    "gbdic_final_zncc": (C.c_int, [P, P]),
+    "gbdic_submit": (C.c_int, [P, I32, P, I64, C.POINTER(SolverCfg)]),
+    "gbdic_retire": (C.c_int, [P, I32, P, C.POINTER(Timing)]),
+    "gbdic_register_device": (C.c_int, [P, P, C.POINTER(SolverCfg), P, P]),
+    "gbdic_export": (C.c_int, [P, I32, P, I64]),
+    "gbdic_apply_uod": (C.c_int, [P, P, I32, P]),
+    "gbdic_pyramid_create": (C.c_int, [C.POINTER(PyramidOptions), C.POINTER(P)]),
+    "gbdic_pyramid_destroy": (None, [P]),
+    "gbdic_pyramid_last_error": (C.c_char_p, [P]),
+    "gbdic_pyramid_set_reference": (C.c_int, [P, P, I32, I32, I64, P, P, C.POINTER(RefInfo)]),
+    "gbdic_pyramid_level_grid": (C.c_int, [P, I32, C.POINTER(I32), C.POINTER(I32)]),
+    "gbdic_pyramid_submit": (C.c_int, [P, I32, P, I64]),
+    "gbdic_pyramid_retire": (C.c_int, [P, I32, P, P, C.POINTER(Timing)]),
+    "gbdic_pyramid_register": (C.c_int, [P, P, I64, P, P, C.POINTER(Timing)]),
+    "gbdic_pyramid_register_device": (C.c_int, [P, P, P, P]),
+    "gbdic_pyramid_reset_temporal": (C.c_int, [P]),
+    "gbdic_pyramid_export": (C.c_int, [P, I32, I32, P, I64]),
+}
+EXPORTED_SYMBOLS = tuple(_SIGNATURES)
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load() -> C.CDLL:
+    """Load libgbdic.so (once).  Raises ICGNError when it has not been built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not LIBRARY_PATH.exists():
+                raise ICGNError(
+                    f"The CUDA library {LIBRARY_PATH} is missing; build it with "
+                    "`python live-dic_gb300/build.py` (nvcc for sm_103a is required)."
+                )
+            lib = C.CDLL(str(LIBRARY_PATH))
+            for name, (restype, argtypes) in _SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = restype
+                fn.argtypes = argtypes
+            _lib = lib
+    return _lib
+
+
+def ptr(array: np.ndarray | None) -> int | None:
+    return None if array is None else array.ctypes.data
+
+
+def check(code: int, message: bytes | None) -> None:
+    """Map a gbdic return code to the reference's exception types."""
+    if code == OK:
+        return
+    text = (message or b"").decode("utf-8", "replace") or f"gbdic error {code}"
+    if code == EINVAL:
+        raise ValueError(text)
+    raise ICGNError(text)
+
+
+def cuda_device_count() -> int:
+    """Number of visible CUDA devices (0 without a driver)."""
+    try:
+        rt = C.CDLL("libcudart.so")
+    except OSError:
+        try:
+            import torch  # PyTorch is only used to locate the runtime here
+
+            return int(torch.cuda.device_count())
+        except Exception:
+            return 0
+    count = C.c_int(0)
+    if rt.cudaGetDeviceCount(C.byref(count)) != 0:
+        return 0
+    return int(count.value)

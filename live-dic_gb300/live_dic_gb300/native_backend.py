@@ -1,0 +1,682 @@
+"""Single-scale IC-GN engine on the GB300 (drop-in for ICGNWGPU).
+
+Mirrors live_dic/wgpu_backend.py:ICGNWGPU (856-3099): same constructor
+arguments and validation messages, same methods and result types.  The GPU
+work (reference preparation, FIR prefilter, IC-GN, UOD, final ZNCC) runs in
+libgbdic.so through its C ABI; this module only validates, plans the static
+ROI geometry and packs results.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import operator
+import threading
+import time
+from collections import deque
+from collections.abc import Iterable, Iterator
+from functools import wraps
+from typing import Any
+
+import numpy as np
+
+from . import _native
+from .engine import ICGNError, ImageInput, ReferenceInfo, RegistrationResult, _as_uint8_gray, result_from_packed
+from .interpolation import INTERPOLATION_CODES, normalize_interpolation
+from .motion import MOTION_MODEL_CODES, normalize_motion_model, parameter_count, state_float_count
+from .outlier import (
+    MEDIAN_FILTER_SCOPE_CODES,
+    OUTLIER_POLICY_CODES,
+    normalize_median_filter_scope,
+    normalize_median_filter_size,
+    normalize_outlier_policy,
+)
+from .roi import RoiPlan, immutable, prepare_roi, validate_roi
+from .subset import DEFAULT_SUBSET_SIZE, normalize_subset_size, normalize_subset_stride, subset_grid_shape
+from .weighting import SPATIAL_WEIGHTING_CODES, normalize_gaussian_sigma, normalize_spatial_weighting
+
+MAX_ITERATIONS = 30
+DEFAULT_IN_FLIGHT_FRAMES = 2
+DEFAULT_PYRAMID_LEVELS = 1
+
+
+def _validated_config(iterations: int, tolerance: float, zncc_min: float) -> dict[str, float | int]:
+    """Solver controls (reference: wgpu_backend.py:504-524)."""
+    count, tol, zmin = int(iterations), float(tolerance), float(zncc_min)
+    if not 1 <= count <= MAX_ITERATIONS:
+        raise ValueError(f"iterations must be between 1 and {MAX_ITERATIONS}")
+    if not np.isfinite(tol) or tol <= 0.0:
+        raise ValueError("tolerance must be a finite positive number")
+    if not np.isfinite(zmin) or not 0.0 <= zmin <= 1.0:
+        raise ValueError("zncc_min must be between 0 and 1")
+    return {"iterations": count, "tolerance": tol, "znccMin": zmin}
+
+
+def _normalize_device_type(value: str) -> str:
+    if not isinstance(value, str) or value.strip().lower() not in ("auto", "gpu", "cpu"):
+        raise ValueError("device_type must be 'auto', 'gpu', or 'cpu'")
+    return value.strip().lower()
+
+
+def _normalize_solver_workgroup_size(value: int) -> int:
+    """Lanes per subset: the reference's 16, 32 or 128, plus 64 on this GPU."""
+    try:
+        size = operator.index(value)
+    except TypeError as error:
+        raise ValueError("solver_workgroup_size must be 16, 32, 64, or 128") from error
+    if isinstance(value, bool) or size not in (16, 32, 64, 128):
+        raise ValueError("solver_workgroup_size must be 16, 32, 64, or 128")
+    return size
+
+
+def _exclusive_call(method):
+    """One registration at a time per engine (wgpu_backend.py:826-838)."""
+
+    @wraps(method)
+    def guarded(self, *args, **kwargs):
+        if not self._registration_lock.acquire(blocking=False):
+            raise ICGNError("Another registration or registration stream is active.")
+        try:
+            return method(self, *args, **kwargs)
+        finally:
+            self._registration_lock.release()
+
+    return guarded
+
+
+def _exclusive_stream(method):
+    """Hold the lock until the generator is exhausted or closed (841-853)."""
+
+    @wraps(method)
+    def guarded(self, *args, **kwargs):
+        if not self._registration_lock.acquire(blocking=False):
+            raise ICGNError("Another registration or registration stream is active.")
+        try:
+            yield from method(self, *args, **kwargs)
+        finally:
+            self._registration_lock.release()
+
+    return guarded
+
+
+def native_options(
+    *,
+    device: int,
+    motion_model: str,
+    interpolation: str,
+    subset_size: int,
+    subset_stride: int,
+    spatial_weighting: str,
+    gaussian_sigma: float,
+    outlier_policy: str,
+    median_filter_size: int,
+    median_filter_scope: str,
+    lanes: int,
+    pipeline_slots: int,
+    persistent: bool,
+    divergence_patience: int = 0,
+    divergence_min_iterations: int = 4,
+) -> _native.Options:
+    o = _native.Options()
+    o.device = device
+    o.motion_model = MOTION_MODEL_CODES[motion_model]
+    o.interpolation = INTERPOLATION_CODES[interpolation]
+    o.subset_size = subset_size
+    o.subset_stride = subset_stride
+    o.spatial_weighting = SPATIAL_WEIGHTING_CODES[spatial_weighting]
+    o.gaussian_sigma = gaussian_sigma
+    o.outlier_policy = OUTLIER_POLICY_CODES[outlier_policy]
+    o.median_filter_size = median_filter_size
+    o.median_filter_scope = MEDIAN_FILTER_SCOPE_CODES[median_filter_scope]
+    o.threads_per_subset = lanes
+    o.divergence_patience = divergence_patience
+    o.divergence_min_iterations = divergence_min_iterations
+    o.pipeline_slots = pipeline_slots
+    o.persistent = int(persistent)
+    return o
+
+
+class ICGNWGPU:
+    """Persistent single-scale IC-GN engine on one CUDA device.
+
+    Construction validates every argument before any device work.  The
+    reference is prepared on the GPU by :meth:`set_reference` and stays
+    resident in HBM; each :meth:`register` uploads one 8-bit target, runs the
+    FIR prefilter, the IC-GN solve and the UOD pass, and returns the packed
+    field as zero-copy NumPy views.  ``solver_workgroup_size`` is the number
+    of CUDA lanes that share one subset (16, 32, 64 or 128); results at
+    different widths differ only by float reduction order.
+    ``device_type='cpu'`` is rejected: there is no CPU execution path.
+    """
+
+    roi: RoiPlan | None = None
+    reference_valid: np.ndarray | None = None
+
+    def __init__(
+        self,
+        *,
+        power_preference: str = "high-performance",
+        device_type: str = "auto",
+        prefer_subgroups: bool | None = None,
+        solver_workgroup_size: int = 32,
+        pyramid_levels: int = DEFAULT_PYRAMID_LEVELS,
+        interpolation: str = "bspline",
+        motion_model: str = "affine",
+        outlier_policy: str = "replace",
+        median_filter_size: int = 3,
+        median_filter_scope: str = "rejected",
+        subset_size: int = DEFAULT_SUBSET_SIZE,
+        subset_stride: int | None = None,
+        spatial_weighting: str = "uniform",
+        gaussian_sigma: float | None = None,
+        device: int = 0,
+        pipeline_slots: int = DEFAULT_IN_FLIGHT_FRAMES,
+        persistent: bool = False,
+    ) -> None:
+        self.device_type = _normalize_device_type(device_type)
+        if power_preference not in ("high-performance", "low-power"):
+            raise ValueError("power_preference must be 'high-performance' or 'low-power'")
+        self.interpolation = normalize_interpolation(interpolation)
+        self.motion_model = normalize_motion_model(motion_model)
+        self.outlier_policy = normalize_outlier_policy(outlier_policy)
+        self.median_filter_size = normalize_median_filter_size(median_filter_size)
+        self.median_filter_scope = normalize_median_filter_scope(median_filter_scope)
+        if self.median_filter_scope == "all" and self.outlier_policy != "median":
+            raise ValueError("median_filter_scope='all' requires outlier_policy='median'")
+        if self.median_filter_size > 3 and self.outlier_policy != "median":
+            raise ValueError("median_filter_size > 3 requires outlier_policy='median'")
+        self.subset_size = normalize_subset_size(subset_size)
+        self.subset_stride = normalize_subset_stride(subset_stride, subset_size=self.subset_size)
+        self.spatial_weighting = normalize_spatial_weighting(spatial_weighting)
+        self.gaussian_sigma = normalize_gaussian_sigma(gaussian_sigma, subset_size=self.subset_size)
+        self.solver_workgroup_size = _normalize_solver_workgroup_size(solver_workgroup_size)
+        if prefer_subgroups is True and (
+            self.subset_size != DEFAULT_SUBSET_SIZE or self.subset_stride != DEFAULT_SUBSET_SIZE
+        ):
+            raise ValueError("prefer_subgroups=True requires subset_size=16 and subset_stride=16")
+        if prefer_subgroups is True and (
+            self.interpolation != "bspline" or self.motion_model != "affine" or self.spatial_weighting != "uniform"
+        ):
+            raise ValueError(
+                "prefer_subgroups=True requires interpolation='bspline', "
+                "motion_model='affine', and spatial_weighting='uniform'"
+            )
+        try:
+            levels = operator.index(pyramid_levels)
+        except TypeError as error:
+            raise ValueError("pyramid_levels must be an integer from 1 to 3") from error
+        if isinstance(pyramid_levels, bool) or not 1 <= levels <= 3:
+            raise ValueError("pyramid_levels must be an integer from 1 to 3")
+        try:
+            slots = operator.index(pipeline_slots)
+        except TypeError as error:
+            raise ValueError("pipeline_depth must be a positive integer") from error
+        if slots < 1:
+            raise ValueError("pipeline_depth must be a positive integer")
+        if self.device_type == "cpu":
+            raise ICGNError("This engine executes on a CUDA GPU only; device_type='cpu' is not available.")
+        self.pyramid_levels = levels
+        self._pipeline_slots = slots
+        self._persistent = bool(persistent)
+        self._lib = _native.load()
+        self._registration_lock = threading.Lock()
+        self._closed = False
+        handle = C.c_void_p()
+        options = native_options(
+            device=int(device),
+            motion_model=self.motion_model,
+            interpolation=self.interpolation,
+            subset_size=self.subset_size,
+            subset_stride=self.subset_stride,
+            spatial_weighting=self.spatial_weighting,
+            gaussian_sigma=self.gaussian_sigma,
+            outlier_policy=self.outlier_policy,
+            median_filter_size=self.median_filter_size,
+            median_filter_scope=self.median_filter_scope,
+            lanes=self.solver_workgroup_size,
+            pipeline_slots=slots,
+            persistent=self._persistent,
+        )
+        code = self._lib.gbdic_create(C.byref(options), C.byref(handle))
+        _native.check(code, self._lib.gbdic_last_error(None))
+        self._handle = handle
+        self.device_index = int(device)
+        self.device_name = f"CUDA device {self.device_index} (gbdic sm_103a)"
+        self.solver = "persistent-queue" if self._persistent else "warp-per-subset"
+        self.execution_device_type = "gpu"
+        self.width = self.height = self.grid_width = self.grid_height = 0
+        self._reference_ready = False
+        self._config: dict[str, float | int] = {"iterations": 30, "tolerance": 1e-3, "znccMin": 0.8}
+        self.roi = None
+        self.reference_valid = None
+        self._pyramid_engines: list[ICGNWGPU] = []
+
+    # ------------------------------------------------------------ helpers
+    def _check(self, code: int) -> None:
+        if code != _native.OK:
+            _native.check(code, self._lib.gbdic_last_error(self._handle))
+
+    def _cfg(self, config: dict[str, float | int]) -> _native.SolverCfg:
+        return _native.SolverCfg(int(config["iterations"]), float(config["tolerance"]), float(config["znccMin"]))
+
+    def _resolve_config(self, iterations, tolerance, zncc_min) -> dict[str, float | int]:
+        return _validated_config(
+            int(self._config["iterations"]) if iterations is None else iterations,
+            float(self._config["tolerance"]) if tolerance is None else tolerance,
+            float(self._config["znccMin"]) if zncc_min is None else zncc_min,
+        )
+
+    def _prepare_target(self, target: ImageInput) -> np.ndarray:
+        frame = _as_uint8_gray(target)
+        if frame.shape != (self.height, self.width):
+            raise ValueError(
+                f"Target dimensions must be {self.width}x{self.height}; received {frame.shape[1]}x{frame.shape[0]}."
+            )
+        return frame
+
+    def _config_echo(self, config: dict[str, float | int]) -> dict[str, Any]:
+        echo: dict[str, Any] = {
+            **config,
+            "pyramidLevels": self.pyramid_levels,
+            "pyramidStrategy": "selective" if self.pyramid_levels > 1 else "single",
+            "width": self.width,
+            "height": self.height,
+            "subsetSize": self.subset_size,
+            "deviceType": self.device_type,
+            "executionDeviceType": self.execution_device_type,
+            "interpolation": self.interpolation,
+            "motionModel": self.motion_model,
+            "outlierPolicy": self.outlier_policy,
+            "medianFilterSize": self.median_filter_size,
+            "medianFilterScope": self.median_filter_scope,
+            "subsetStride": self.subset_stride,
+            "spatialWeighting": self.spatial_weighting,
+            "solverWorkgroupSize": self.solver_workgroup_size,
+            "gaussianSigma": self.gaussian_sigma,
+        }
+        if self.roi is not None:
+            echo["roi"] = self.roi.summary()
+        return echo
+
+    def _new_packed(self) -> np.ndarray:
+        return np.empty((self.grid_height, self.grid_width, state_float_count(self.motion_model)), dtype=np.float32)
+
+    def _result(self, packed: np.ndarray, timing: dict[str, float], config) -> RegistrationResult:
+        return result_from_packed(
+            packed,
+            motion_model=self.motion_model,
+            timing=timing,
+            config=self._config_echo(config),
+            width=self.width,
+            height=self.height,
+            subset_size=self.subset_size,
+            subset_stride=self.subset_stride,
+            roi=self.roi,
+            reference_valid=self.reference_valid,
+        )
+
+    @staticmethod
+    def _timing(t: _native.Timing) -> dict[str, float]:
+        return {
+            "uploadWallMs": t.upload_ms,
+            "executeReadbackWallMs": t.execute_ms + t.readback_ms,
+            "readbackCopyWallMs": t.readback_ms,
+            "deviceMs": t.device_ms,
+            "totalWallMs": t.total_ms,
+        }
+
+    # ------------------------------------------------------------ reference
+    def set_reference(
+        self,
+        image: ImageInput,
+        *,
+        iterations: int = 30,
+        tolerance: float = 1e-3,
+        zncc_min: float = 0.8,
+        roi_mask: np.ndarray | None = None,
+        roi_policy: str = "full",
+        roi_truncation: str = "none",
+    ) -> ReferenceInfo:
+        if self._closed:
+            raise ICGNError("This engine is closed; create a new engine before set_reference().")
+        started = time.perf_counter()
+        frame = _as_uint8_gray(image)
+        height, width = frame.shape
+        gw, gh = subset_grid_shape(width, height, subset_size=self.subset_size, subset_stride=self.subset_stride)
+        if gw < 1 or gh < 1:
+            raise ValueError(f"Reference dimensions must each be at least {self.subset_size} pixels.")
+        config = _validated_config(iterations, tolerance, zncc_min)
+        mask = validate_roi(roi_mask, roi_policy, frame.shape, self.motion_model, roi_truncation)
+        if roi_policy == "partial" and mask is not None:
+            raise ICGNError("roi_policy='partial' is not available in this build; use roi_policy='full'.")
+        roi = prepare_roi(mask, self.subset_size, self.subset_stride, median_filter_size=self.median_filter_size)
+        selected = links = None
+        if roi is not None and roi.effective:
+            selected = np.ascontiguousarray(roi.selected, dtype=np.uint8).ravel()
+            links = np.ascontiguousarray(roi.links_table(self.median_filter_size, self.outlier_policy))
+        self._reference_ready = False
+        info = _native.RefInfo()
+        prep_start = time.perf_counter()
+        self._check(
+            self._lib.gbdic_set_reference(
+                self._handle, _native.ptr(frame), width, height, frame.strides[0],
+                _native.ptr(selected), _native.ptr(links), C.byref(info),
+            )
+        )
+        prep_ms = (time.perf_counter() - prep_start) * 1e3
+        self.width, self.height, self.grid_width, self.grid_height = width, height, gw, gh
+        self._config = config
+        self.roi = roi
+        admissible = self._export(_native.EXPORT_ADMISSIBLE, np.uint8, (gh, gw))
+        self.reference_valid = immutable(admissible.astype(bool))
+        self._reference_ready = True
+        total_ms = (time.perf_counter() - started) * 1e3
+        return ReferenceInfo(
+            preparation_wall_ms=prep_ms,
+            runtime_build_wall_ms=prep_ms - info.device_ms,
+            reference_build_wall_ms=info.device_ms,
+            encoding_wall_ms=0.0,
+            total_wall_ms=total_ms,
+            config={k: v for k, v in self._config_echo(config).items() if k not in ("width", "height")},
+            device=self.device_name,
+            grid=(gw, gh),
+            width=width,
+            height=height,
+            subset_size=self.subset_size,
+            subset_stride=self.subset_stride,
+            roi=roi,
+            reference_valid=self.reference_valid,
+        )
+
+    def set_reference_arrays(
+        self,
+        width: int,
+        height: int,
+        plane: np.ndarray,
+        metadata: np.ndarray,
+        inverse: np.ndarray,
+        *,
+        iterations: int = 30,
+        tolerance: float = 1e-3,
+        zncc_min: float = 0.8,
+    ) -> None:
+        """Upload reference arrays prepared elsewhere, in the reference's own
+        layout (plane H*W*4, metadata grid*16|28, inverse grid*n*n)."""
+        gw, gh = subset_grid_shape(width, height, subset_size=self.subset_size, subset_stride=self.subset_stride)
+        n = parameter_count(self.motion_model)
+        stride = 28 if self.motion_model == "quadratic" else 16
+        plane = np.ascontiguousarray(plane, dtype=np.float32).ravel()
+        metadata = np.ascontiguousarray(metadata, dtype=np.float32).ravel()
+        inverse = np.ascontiguousarray(inverse, dtype=np.float32).ravel()
+        if plane.size != width * height * 4 or metadata.size != gw * gh * stride or inverse.size != gw * gh * n * n:
+            raise ValueError("reference arrays do not match the image and grid dimensions")
+        config = _validated_config(iterations, tolerance, zncc_min)
+        info = _native.RefInfo()
+        self._check(
+            self._lib.gbdic_set_reference_arrays(
+                self._handle, width, height, _native.ptr(plane), _native.ptr(metadata), _native.ptr(inverse),
+                None, C.byref(info),
+            )
+        )
+        self.width, self.height, self.grid_width, self.grid_height = width, height, gw, gh
+        self._config = config
+        self.roi = None
+        flags = metadata.reshape(-1, stride)[:, 1]
+        self.reference_valid = immutable(((flags > 0.5) | (flags == -4)).reshape(gh, gw))
+        self._reference_ready = True
+
+    # ------------------------------------------------------------ exports
+    def _export(self, what: int, dtype, shape) -> np.ndarray:
+        out = np.empty(shape, dtype=dtype)
+        self._check(self._lib.gbdic_export(self._handle, what, _native.ptr(out), out.nbytes))
+        return out
+
+    def export_metadata(self) -> np.ndarray:
+        stride = 28 if self.motion_model == "quadratic" else 16
+        return self._export(_native.EXPORT_METADATA, np.float32, (self.grid_width * self.grid_height, stride))
+
+    def export_reference(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(plane H*W*4, inverse grid*n*n, metadata grid*16|28) as prepared on the GPU."""
+        n = parameter_count(self.motion_model)
+        count = self.grid_width * self.grid_height
+        plane = self._export(_native.EXPORT_PLANE, np.float32, (self.height * self.width * 4,))
+        inverse = self._export(_native.EXPORT_INVERSE, np.float32, (count * n * n,))
+        metadata = self.export_metadata().ravel()
+        return plane, inverse, metadata
+
+    def export_coefficients(self) -> np.ndarray:
+        """B-spline coefficient plane of the last target (bspline mode)."""
+        return self._export(_native.EXPORT_COEFFICIENTS, np.float32, (self.height, self.width))
+
+    def export_weights(self) -> np.ndarray:
+        return self._export(_native.EXPORT_WEIGHTS, np.float32, (self.subset_size * self.subset_size,))
+
+    def export_raw_state(self) -> np.ndarray:
+        return self._export(_native.EXPORT_RAW_STATE, np.float32, (self.grid_height, self.grid_width, state_float_count(self.motion_model)))
+
+    def apply_outlier_filter(self, state: np.ndarray, *, seed_mode: bool = False) -> np.ndarray:
+        """Run this engine's outlier policy on a packed state field
+        (grid_height, grid_width, 8|16) on the GPU and return the result."""
+        stride = state_float_count(self.motion_model)
+        src = np.ascontiguousarray(state, dtype=np.float32)
+        if src.shape != (self.grid_height, self.grid_width, stride):
+            raise ValueError(f"state must have shape {(self.grid_height, self.grid_width, stride)}")
+        out = np.empty_like(src)
+        self._check(self._lib.gbdic_apply_uod(self._handle, _native.ptr(src), int(seed_mode), _native.ptr(out)))
+        return out
+
+    # ------------------------------------------------------------ solves
+    def _empty_roi_result(self, started: float, config) -> RegistrationResult:
+        packed = np.zeros((self.grid_height, self.grid_width, state_float_count(self.motion_model)), np.float32)
+        packed[..., parameter_count(self.motion_model)] = -3.0
+        elapsed = (time.perf_counter() - started) * 1e3
+        return self._result(packed, {"queueSubmissions": 0.0, "totalWallMs": elapsed, "resultAgeWallMs": elapsed}, config)
+
+    def _check_final_zncc(self) -> None:
+        if self.motion_model != "affine" or self.spatial_weighting != "uniform":
+            raise ValueError("include_zncc requires affine motion and uniform full windows")
+
+    def _attach_final_zncc(self, result: RegistrationResult) -> None:
+        start = time.perf_counter()
+        zncc = np.empty(self.grid_width * self.grid_height, np.float32)
+        self._check(self._lib.gbdic_final_zncc(self._handle, _native.ptr(zncc)))
+        zncc[zncc < -1.0] = np.nan
+        result._zncc = immutable(zncc.reshape(self.grid_height, self.grid_width))
+        elapsed = (time.perf_counter() - start) * 1e3
+        result.timing = {**result.timing, "finalZnccWallMs": elapsed, "totalWallMs": result.timing["totalWallMs"] + elapsed}
+
+    @_exclusive_call
+    def register(
+        self,
+        target: ImageInput,
+        *,
+        iterations: int | None = None,
+        tolerance: float | None = None,
+        zncc_min: float | None = None,
+        include_zncc: bool = False,
+    ) -> RegistrationResult:
+        if not self._reference_ready:
+            raise ICGNError("Call set_reference() before register().")
+        if include_zncc:
+            self._check_final_zncc()
+            if self.pyramid_levels != 1:
+                raise ValueError("include_zncc requires a single pyramid level")
+        started = time.perf_counter()
+        frame = self._prepare_target(target)
+        self._config = self._resolve_config(iterations, tolerance, zncc_min)
+        if self.roi is not None and self.roi.empty:
+            result = self._empty_roi_result(started, self._config)
+            if include_zncc:
+                result._zncc = immutable(np.full((self.grid_height, self.grid_width), np.nan, np.float32))
+            return result
+        packed = self._new_packed()
+        timing = _native.Timing()
+        self._check(
+            self._lib.gbdic_register(
+                self._handle, _native.ptr(frame), frame.strides[0], C.byref(self._cfg(self._config)),
+                _native.ptr(packed), C.byref(timing),
+            )
+        )
+        times = self._timing(timing)
+        times["totalWallMs"] = (time.perf_counter() - started) * 1e3
+        result = self._result(packed, times, self._config)
+        if include_zncc:
+            self._attach_final_zncc(result)
+        return result
+
+    @_exclusive_call
+    def register_seeded(
+        self,
+        target: ImageInput,
+        parameters: Any,
+        active: Any,
+        *,
+        iterations: int | None = None,
+        tolerance: float | None = None,
+        zncc_min: float | None = None,
+        include_zncc: bool = False,
+    ) -> RegistrationResult:
+        """Solve the active subsets from supplied initial warps
+        (reference: wgpu_backend.py:2774-2819).  ``parameters`` has shape
+        (grid_height, grid_width, 6) in result order; ``active`` is a Boolean
+        grid.  Inactive or ROI-excluded windows are not solved."""
+        if not self._reference_ready:
+            raise ICGNError("Call set_reference() before register_seeded().")
+        if self.motion_model != "affine":
+            raise ValueError("register_seeded currently requires motion_model='affine'")
+        if include_zncc:
+            self._check_final_zncc()
+        shape = (self.grid_height, self.grid_width)
+        values = np.asarray(parameters, dtype=np.float32)
+        mask = np.asarray(active)
+        if values.shape != (*shape, 6):
+            raise ValueError(f"parameters must have shape {(*shape, 6)}")
+        if mask.shape != shape or mask.dtype != np.bool_:
+            raise ValueError(f"active must be a Boolean array with shape {shape}")
+        if not np.isfinite(values[mask]).all():
+            raise ValueError("active parameters must be finite")
+        started = time.perf_counter()
+        frame = self._prepare_target(target)
+        self._config = self._resolve_config(iterations, tolerance, zncc_min)
+        seeds = np.zeros((*shape, 8), dtype=np.float32)
+        seeds[..., :6] = np.where(mask[..., None], values, 0)
+        act = mask.astype(np.uint32)
+        if self.roi is not None:
+            act = act * self.roi.selected.astype(np.uint32)
+        packed = self._new_packed()
+        timing = _native.Timing()
+        self._check(
+            self._lib.gbdic_register_seeded(
+                self._handle, _native.ptr(frame), frame.strides[0], _native.ptr(seeds), _native.ptr(np.ascontiguousarray(act)),
+                C.byref(self._cfg(self._config)), _native.ptr(packed), C.byref(timing),
+            )
+        )
+        times = self._timing(timing)
+        times["totalWallMs"] = (time.perf_counter() - started) * 1e3
+        result = self._result(packed, times, self._config)
+        if include_zncc:
+            self._attach_final_zncc(result)
+        return result
+
+    @_exclusive_stream
+    def register_stream(
+        self,
+        targets: Iterable[ImageInput],
+        *,
+        pipeline_depth: int = DEFAULT_IN_FLIGHT_FRAMES,
+        iterations: int | None = None,
+        tolerance: float | None = None,
+        zncc_min: float | None = None,
+    ) -> Iterator[RegistrationResult]:
+        """Register a sequence with up to ``pipeline_depth`` frames in flight;
+        results come back in input order (wgpu_backend.py:2997-3051)."""
+        if not self._reference_ready:
+            raise ICGNError("Call set_reference() before register_stream().")
+        try:
+            depth = operator.index(pipeline_depth)
+        except TypeError as error:
+            raise ValueError("pipeline_depth must be a positive integer") from error
+        if isinstance(pipeline_depth, bool) or depth < 1:
+            raise ValueError("pipeline_depth must be a positive integer")
+        if depth > self._pipeline_slots:
+            raise ValueError(f"pipeline_depth must be at most {self._pipeline_slots} for this engine")
+        self._config = self._resolve_config(iterations, tolerance, zncc_min)
+        if self.roi is not None and self.roi.empty:
+            for target in targets:
+                started = time.perf_counter()
+                self._prepare_target(target)
+                yield self._empty_roi_result(started, self._config)
+            return
+        cfg = self._cfg(self._config)
+        available = deque(range(depth))
+        pending: deque[tuple[int, float]] = deque()
+
+        def retire() -> RegistrationResult:
+            slot, started = pending.popleft()
+            packed = self._new_packed()
+            timing = _native.Timing()
+            self._check(self._lib.gbdic_retire(self._handle, slot, _native.ptr(packed), C.byref(timing)))
+            available.append(slot)
+            times = self._timing(timing)
+            times["pipelineLatencyWallMs"] = (time.perf_counter() - started) * 1e3
+            times["totalWallMs"] = times["pipelineLatencyWallMs"]
+            return self._result(packed, times, self._config)
+
+        try:
+            for target in targets:
+                if not available:
+                    yield retire()
+                slot = available.popleft()
+                started = time.perf_counter()
+                frame = self._prepare_target(target)
+                self._check(self._lib.gbdic_submit(self._handle, slot, _native.ptr(frame), frame.strides[0], C.byref(cfg)))
+                pending.append((slot, started))
+            while pending:
+                yield retire()
+        finally:
+            while pending:
+                slot, _ = pending.popleft()
+                self._lib.gbdic_retire(self._handle, slot, None, None)
+
+    def register_many(self, targets: Iterable[ImageInput], *, pipeline_depth: int = DEFAULT_IN_FLIGHT_FRAMES,
+                      iterations: int | None = None, tolerance: float | None = None,
+                      zncc_min: float | None = None) -> list[RegistrationResult]:
+        return list(
+            self.register_stream(targets, pipeline_depth=pipeline_depth, iterations=iterations,
+                                 tolerance=tolerance, zncc_min=zncc_min)
+        )
+
+    def register_device(self, device_frame: int, device_state: int, *, stream: int | None = None) -> None:
+        """Resident registration: ``device_frame`` (dense 8-bit rows) and
+        ``device_state`` are CUDA device addresses; no host synchronisation."""
+        if not self._reference_ready:
+            raise ICGNError("Call set_reference() before register().")
+        self._check(
+            self._lib.gbdic_register_device(
+                self._handle, C.c_void_p(device_frame), C.byref(self._cfg(self._config)),
+                C.c_void_p(device_state), C.c_void_p(stream or 0),
+            )
+        )
+
+    # ------------------------------------------------------------ lifetime
+    def close(self) -> None:
+        """Release GPU resources; repeated calls are harmless."""
+        if self._closed:
+            return
+        self._reference_ready = False
+        self._closed = True
+        handle, self._handle = self._handle, None
+        if handle:
+            self._lib.gbdic_destroy(handle)
+
+    def __enter__(self) -> ICGNWGPU:
+        return self
+
+    def __exit__(self, *_: object) -> None:
+        self.close()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,177 @@
+"""Generate golden vectors from the reference's own NumPy code.
+
+Run from the repository root, in a checkout where the reference sources are
+available (they are not needed afterwards):
+
+    python tests/golden/make_golden.py /root/reference
+
+The reference package imports Pillow and websockets at module level although
+none of the routines used here touch them, so both are replaced by empty
+stand-ins before the import.  Outputs: tests/golden/*.npz (small, seeded).
+"""
+
+from __future__ import annotations
+
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+
+
+def _import_reference(root: Path):
+    sys.modules.setdefault("websockets", types.ModuleType("websockets"))
+    pil = types.ModuleType("PIL")
+    image = types.ModuleType("PIL.Image")
+    image.Image = type("Image", (), {})
+    pil.Image = image
+    sys.modules.setdefault("PIL", pil)
+    sys.modules.setdefault("PIL.Image", image)
+    python_root = root / "DIC/LucasKanadeICGN/python"
+    sys.path.insert(0, str(python_root / "src"))
+    sys.path.insert(0, str(python_root / "tests"))
+    import live_dic.engine as engine
+    import live_dic.roi as roi
+    import live_dic.wgpu_backend as backend
+    import test_gpu_regressions as regressions
+
+    return backend, engine, roi, regressions
+
+
+def speckle(rng: np.random.Generator, height: int, width: int, dots: int) -> np.ndarray:
+    y, x = np.mgrid[:height, :width].astype(np.float64)
+    img = np.zeros((height, width))
+    cx = rng.uniform(0, width, dots)
+    cy = rng.uniform(0, height, dots)
+    sig = rng.uniform(1.5, 3.0, dots)
+    amp = rng.uniform(0.3, 1.0, dots)
+    for a, b, s, m in zip(cx, cy, sig, amp):
+        img += m * np.exp(-((x - a) ** 2 + (y - b) ** 2) / (2 * s * s))
+    img = 255.0 * (img - img.min()) / (img.max() - img.min())
+    return np.clip(np.rint(img + rng.normal(0, 0.5, img.shape)), 0, 255).astype(np.uint8)
+
+
+def main(reference_root: str) -> None:
+    backend, engine, roi, regressions = _import_reference(Path(reference_root))
+    rng = np.random.default_rng(20261203)
+    out: dict[str, np.ndarray] = {}
+
+    # FIR taps and the reference's own float32 FIR oracle (test_gpu_regressions._cpu_prefilter).
+    out["fir_weights"] = backend._fir_weights()
+    img = speckle(rng, 70, 83, 200)
+    out["prefilter_image"] = img
+    out["prefilter_expected"] = regressions._cpu_prefilter(img)
+
+    # Pyramid reduction: float separable (_reduce_half) and integer oracle.
+    for k, (h, w) in enumerate([(32, 48), (37, 53), (64, 64), (17, 16)]):
+        src = rng.integers(0, 256, size=(h, w), dtype=np.uint8)
+        out[f"reduce_{k}_in"] = src
+        out[f"reduce_{k}_half"] = backend._reduce_half(src)
+        out[f"reduce_{k}_int"] = regressions._integer_reduction(src)
+
+    # Reference preparation, every model x interpolation, overlapping and
+    # tiled grids, uniform and Gaussian weights, plus a flat image.
+    cases = []
+    ref_img = speckle(rng, 64, 72, 180)
+    out["prep_image"] = ref_img
+    for model in ("affine", "translation", "quadratic"):
+        for interp in ("bspline", "linear", "cubic"):
+            cases.append((model, interp, 21, 10, "uniform", None))
+    cases += [
+        ("affine", "bspline", 16, 16, "uniform", None),
+        ("affine", "bspline", 15, 5, "gaussian", 4.0),
+        ("quadratic", "bspline", 31, 31, "gaussian", 8.0),
+        ("translation", "linear", 8, 8, "uniform", None),
+        ("affine", "bspline", 24, 12, "uniform", None),
+    ]
+    for index, (model, interp, size, stride, weighting, sigma) in enumerate(cases):
+        plane, inverse, metadata = backend._reference_arrays(
+            ref_img,
+            interpolation=interp,
+            motion_model=model,
+            subset_size=size,
+            subset_stride=stride,
+            spatial_weighting=weighting,
+            gaussian_sigma=sigma,
+        )
+        out[f"prep_{index}_plane"] = plane
+        out[f"prep_{index}_inverse"] = inverse
+        out[f"prep_{index}_metadata"] = metadata
+    out["prep_cases"] = np.array(
+        [f"{m}|{i}|{s}|{t}|{w}|{'' if g is None else g}" for m, i, s, t, w, g in cases]
+    )
+    flat = np.full((40, 40), 91, dtype=np.uint8)
+    plane, inverse, metadata = backend._reference_arrays(flat, subset_size=13, subset_stride=13)
+    out["flat_inverse"] = inverse
+    out["flat_metadata"] = metadata
+
+    # Seed transfer on a synthetic coarse affine / quadratic field.
+    for model in ("affine", "quadratic"):
+        n = 12 if model == "quadratic" else 6
+        sh, sw = 7, 9
+        params = rng.normal(0, 0.5, size=(sh, sw, n)).astype(np.float32)
+        params[..., 1:3] *= 0.01
+        params[..., 4:6] *= 0.01
+        if n == 12:
+            params[..., 6:] *= 1e-4
+        status = rng.choice(np.array([1.0, 1.0, 1.0, 0.0, -1.0, 2.0], np.float32), size=(sh, sw))
+        available = rng.random((sh, sw)) > 0.1
+        requested = rng.random((13, 17)) > 0.2
+        result = types.SimpleNamespace(
+            parameters=params, status=status, config={"motionModel": model}
+        )
+        seeds, active = backend._transfer_pyramid_seed(
+            result,
+            source_available=available,
+            source_scale=2,
+            destination_scale=1,
+            destination_grid=(17, 13),
+            requested=requested,
+            subset_size=21,
+            subset_stride=10,
+        )
+        out[f"transfer_{model}_params"] = params
+        out[f"transfer_{model}_status"] = status
+        out[f"transfer_{model}_available"] = available
+        out[f"transfer_{model}_requested"] = requested
+        out[f"transfer_{model}_seeds"] = seeds
+        out[f"transfer_{model}_active"] = active
+
+    # ROI planning and pyramid seed permissions for a mask with a hole.
+    mask = np.ones((120, 150), dtype=bool)
+    yy, xx = np.mgrid[:120, :150]
+    mask[(xx - 70) ** 2 + (yy - 55) ** 2 < 23**2] = False
+    mask[:, 140:] = False
+    out["roi_mask"] = mask
+    plan = roi.prepare_roi(mask, 21, 10, policy="full", median_filter_size=3)
+    out["roi_selected"] = plan.selected
+    out["roi_neighbour_bits"] = plan.neighbour_bits
+    plan9 = roi.prepare_roi(mask, 21, 10, policy="full", median_filter_size=9)
+    out["roi_median_words"] = plan9.median_neighbour_words
+    coarse_mask = roi.reduce_mask(mask)
+    out["roi_reduced_mask"] = coarse_mask
+    coarse = roi.prepare_roi(coarse_mask, 21, 10, policy="full")
+    out["roi_coarse_selected"] = coarse.selected
+    out["roi_seed_permissions"] = roi.seed_permissions(
+        coarse, plan, source_scale=2, destination_scale=1, size=21, stride=10, reference_mask=mask
+    )
+    out["roi_temporal_permissions"] = roi.seed_permissions(
+        plan, coarse, source_scale=1, destination_scale=2, size=21, stride=10, reference_mask=mask
+    )
+
+    # Input normalisation.
+    floats = rng.random((20, 24)).astype(np.float32)
+    out["gray_float_in"] = floats
+    out["gray_float_out"] = engine._as_uint8_gray(floats)
+    wide = rng.uniform(0, 300, size=(20, 24))
+    out["gray_wide_in"] = wide
+    out["gray_wide_out"] = engine._as_uint8_gray(wide)
+
+    np.savez_compressed(HERE / "reference_vectors.npz", **out)
+    print(f"wrote {len(out)} arrays to {HERE / 'reference_vectors.npz'}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
