@@ -1,0 +1,431 @@
+#!/usr/bin/env python
+"""UHD DIC throughput benchmark (frames/s and subsets/s).
+
+Workload (one step = one target frame through the whole per-frame path):
+3840x2160 synthetic speckle reference, 60 targets deformed by the plane-strain
+Kirsch field of a circular hole (radius 300 px at the centre, masked out of
+the ROI), scaled to a 2 px peak and ramped linearly over the 60 frames;
+affine IC-GN with subset 31, step 8, B-spline interpolation, 3-level GPU
+pyramid, temporal seeding with velocity prediction, UOD replace.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`value` is measured with inputs resident in HBM (device frames through the
+resident C-ABI entry, CUDA events on the launching stream); `e2e` runs the
+public register_stream API on host NumPy frames (host->device upload and
+device->host readback inside the timed region).  With N > 1 (torchrun) every
+rank runs an independent replica on its own GPU and frame sequence.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for p in (ROOT / "live-dic_gb300", ROOT):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+METRIC = "UHD frames/s & subsets/s; learned- vs ZNCC-seeded IC-GN at equal RMSE"
+UNIT = "frames/s"
+
+
+def parse_args() -> argparse.Namespace:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--width", type=int, default=3840)
+    ap.add_argument("--height", type=int, default=2160)
+    ap.add_argument("--subset", type=int, default=31)
+    ap.add_argument("--stride", type=int, default=8)
+    ap.add_argument("--levels", type=int, default=3)
+    ap.add_argument("--frames", type=int, default=60)
+    ap.add_argument("--hole", type=float, default=300.0)
+    ap.add_argument("--peak", type=float, default=2.0)
+    ap.add_argument("--lanes", type=int, default=32)
+    ap.add_argument("--persistent", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env() -> tuple[int, int, int]:
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int) -> None:
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self) -> None:
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc) -> None:
+        if self.proc is not None:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_workload(args, rank: int, device: str):
+    from live_dic_gb300 import synthetic
+
+    seed = 1000 + 17 * rank
+    ref, sp = synthetic.reference_image(args.width, args.height, seed=seed, device=device)
+    field = synthetic.KirschField(args.width, args.height, args.hole, peak=args.peak)
+    mask = synthetic.hole_mask(args.width, args.height, args.hole)
+    return ref, sp, field, mask, seed
+
+
+def render_frames(args, sp, field, seed: int, count: int, device: str):
+    import torch
+
+    from live_dic_gb300 import synthetic
+
+    frames = []
+    for k in range(count):
+        load = (k + 1) / args.frames
+        img = synthetic.deformed_image(sp, field.torch_field(load), noise_seed=seed + 100 + k, device=device)
+        frames.append(torch.from_numpy(img))
+    return frames
+
+
+def cpu_sample_frame_time(args, frame: np.ndarray, plane, metadata, inverse, rows: int) -> tuple[float, dict]:
+    """Oracle port on the host cores: full-frame FIR prefilter plus the
+    finest-level IC-GN (zero seed) on `rows` subset rows; returns the
+    extrapolated seconds per frame."""
+    from oracle import oracle as oracle_c
+    from oracle import reference_prep as rp
+
+    S, st = args.subset, args.stride
+    gw = 1 + (args.width - S) // st
+    gh = 1 + (args.height - S) // st
+    rows = max(1, min(rows, gh))
+    start = (gh - rows) // 2
+    subsets = np.arange(start * gw, (start + rows) * gw, dtype=np.int32)
+    t0 = time.perf_counter()
+    coef = oracle_c.prefilter(frame, rp.runtime_fir_taps())
+    t1 = time.perf_counter()
+    state = np.zeros((gh * gw, 8), np.float32)
+    oracle_c.solve(frame, coef, plane, metadata, inverse, subset_size=S, subset_stride=st, lanes=32,
+                   iterations=16, tolerance=5e-3, subsets=subsets, state=state, roi_enabled=True)
+    t2 = time.perf_counter()
+    per_frame = (t1 - t0) + (t2 - t1) * gh / rows
+    return per_frame, {"prefilter_s": t1 - t0, "solve_s": t2 - t1, "rows": rows, "subsets": int(subsets.size)}
+
+
+def run_reference_arm(args) -> None:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import torch
+
+    from oracle import oracle as oracle_c
+    from oracle import reference_prep as rp
+
+    oracle_c.build()
+    device = "cuda" if torch.cuda.is_available() else "cpu"
+    ref, sp, field, mask, seed = make_workload(args, 0, device)
+    frames = [f.numpy() for f in render_frames(args, sp, field, seed, 4, device)]
+    plane, inverse, metadata = rp.reference_arrays(ref, subset_size=args.subset, subset_stride=args.stride)
+    from live_dic_gb300.roi import prepare_roi
+
+    plan = prepare_roi(mask, args.subset, args.stride)
+    meta = metadata.reshape(-1, 16).copy()
+    meta[~plan.selected.ravel(), 1] = -3.0
+    gh = 1 + (args.height - args.subset) // args.stride
+    rows = max(4, gh // 8)
+    for k in range(args.warmup if args.warmup < 2 else 1):
+        cpu_sample_frame_time(args, frames[k % len(frames)], plane, meta, inverse, rows)
+    times = []
+    for k in range(args.steps):
+        t, info = cpu_sample_frame_time(args, frames[k % len(frames)], plane, meta, inverse, rows)
+        times.append(t)
+    total = sum(times)
+    value = args.steps / total
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"oracle C port (OpenMP, {cores} threads): full-frame FIR prefilter + finest-level "
+                                   f"affine IC-GN from zero seed on {info['rows']} of {gh} subset rows per step, "
+                                   "extrapolated to the frame; the reference's own GPU path (WGSL via wgpu) cannot run "
+                                   "here: no graphics stack or software renderer on this box"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args) -> dict:
+    return {
+        "workload": f"{args.width}x{args.height} plate-with-hole (Kirsch, ROI hole r={args.hole:g} px, peak "
+                    f"{args.peak:g} px ramped over {args.frames} frames), affine IC-GN S{args.subset}/s{args.stride}, "
+                    f"bspline, {args.levels}-level GPU pyramid, temporal+velocity seeding, UOD replace",
+        "width": args.width,
+        "height": args.height,
+        "subset_size": args.subset,
+        "subset_stride": args.stride,
+        "pyramid_levels": args.levels,
+        "lanes_per_subset": args.lanes,
+        "persistent": bool(args.persistent),
+        "parallelism": "replicas",
+        "l2": "no flush: per-step working set (finest reference plane 133 MB + coefficient planes + states) exceeds "
+              "the 129 MB L2",
+    }
+
+
+def main() -> None:
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+    import torch
+
+    rank, world, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    device = f"cuda:{local}"
+
+    from live_dic_gb300 import ICGNWGPUFullPyramid, _native
+
+    if args.warmup + args.steps > args.frames:
+        args.frames = args.warmup + args.steps
+    ref, sp, field, mask, seed = make_workload(args, rank, device)
+    frames = render_frames(args, sp, field, seed, args.frames, device)
+    dev_frames = torch.stack(frames).to(device).contiguous()
+    engine = ICGNWGPUFullPyramid(
+        pyramid_levels=args.levels, subset_size=args.subset, subset_stride=args.stride,
+        initialization="temporal", temporal_prediction="velocity", solver_workgroup_size=args.lanes,
+        device=local, pipeline_slots=2, persistent=args.persistent,
+    )
+    info = engine.set_reference(ref, roi_mask=mask)
+    gw, gh = info.grid
+    state = torch.zeros(gw * gh * 8, dtype=torch.float32, device=device)
+    stream = torch.cuda.Stream(device=device)
+
+    # ---------------- resident throughput (value)
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup):
+            engine.register_device(dev_frames[k].data_ptr(), state.data_ptr(), stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    engine.set_profiling(True)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            for k in range(args.warmup, args.warmup + args.steps):
+                engine.register_device(dev_frames[k].data_ptr(), state.data_ptr(), stream=stream.cuda_stream)
+            end.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = start.elapsed_time(end)
+    profile = engine.read_profile()
+    engine.set_profiling(False)
+    final_state = state.view(gh, gw, 8).cpu().numpy()
+    ms_max = ms
+    if dist:
+        t = torch.tensor([ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * args.steps / (ms_max / 1e3)
+
+    # ---------------- accuracy of the last timed frame against the FP64 field
+    from live_dic_gb300 import synthetic
+
+    cx, cy = synthetic.subset_centres(args.width, args.height, args.subset, args.stride)
+    last = args.warmup + args.steps - 1
+    truth = field.truth(cx, cy, load=(last + 1) / args.frames)
+    ok = final_state[..., 6] >= 1.0
+    err = final_state[..., [0, 3]][ok] - truth[ok]
+    rmse = float(np.sqrt(np.mean(np.sum(err * err, axis=1)))) if ok.any() else None
+    selected = int(info.roi.selected.sum()) if info.roi is not None else gw * gh
+
+    # ---------------- end to end through the public API (host frames)
+    e2e = None
+    if not args.no_e2e:
+        host_frames = [f.numpy() for f in frames]
+        engine.reset_temporal_state()
+        for k in range(args.warmup):
+            engine.register(host_frames[k])
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        results = list(engine.register_stream(host_frames[args.warmup: args.warmup + args.steps], pipeline_depth=2))
+        t1 = time.perf_counter()
+        e2e_s = t1 - t0
+        if dist:
+            t = torch.tensor([e2e_s], device=device)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        age = [r.timing["resultAgeWallMs"] for r in results]
+        e2e = {
+            "value": world * args.steps / e2e_s,
+            "unit": UNIT,
+            "h2d_bytes_per_step": args.width * args.height,
+            "d2h_bytes_per_step": gw * gh * 8 * 4 + 16,
+            "api": "ICGNWGPUFullPyramid.register_stream(pipeline_depth=2), host NumPy uint8 frames",
+            "result_age_ms_p50": float(np.percentile(age, 50)),
+            "result_age_ms_p95": float(np.percentile(age, 95)),
+        }
+
+    if rank != 0:
+        engine.close()
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # ---------------- roofline of the dominant kernel (IC-GN solver, FP32 pipe)
+    lib = _native.load()
+    import ctypes
+
+    peak = ctypes.c_double()
+    _native.check(lib.gbdic_fp32_peak_probe(local, ctypes.byref(peak)), b"FP32 probe failed")
+    S = args.subset
+    flops = (90.0 * S * S + 150.0) * profile["iterations"]
+    solver_s = profile["solver_ms"] / 1e3
+    achieved = flops / solver_s / 1e12 if solver_s > 0 else None
+    launches = max(1, profile["timed_launches"])
+    traffic = None
+    traffic_file = ROOT / "profiles" / "traffic_per_launch.json"
+    if traffic_file.exists():
+        traffic = json.loads(traffic_file.read_text()).get("icgn_solver_dram_bytes_per_launch")
+    roofline = {
+        "bound": "fp32",
+        "kernel": "icgn_kernel<affine,bspline,32 lanes> (all pyramid levels)",
+        "achieved": achieved,
+        "peak": peak.value,
+        "unit": "TFLOP/s",
+        "frac": achieved / peak.value if achieved else None,
+        "peak_source": "measured in this run by gbdic_fp32_peak_probe (FMA chains on every SM); "
+                       "MEASURED_PEAKS.json has no FP32 figure",
+        "traffic": traffic,
+        "flops_per_launch": flops / launches,
+        "avg_launch_ms": profile["solver_ms"] / launches,
+        "solver_share_of_step": profile["solver_ms"] / ms if ms > 0 else None,
+        "iterations_per_subset_frame": profile["iterations"] / (args.steps * selected),
+    }
+
+    cpu_baseline = None
+    if world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as oracle_c
+
+        oracle_c.build()
+        plane = engine.export_level(0, _native.EXPORT_PLANE, np.float32, (args.height * args.width * 4,))
+        meta = engine.export_level(0, _native.EXPORT_METADATA, np.float32, (gw * gh * 16,))
+        inv = engine.export_level(0, _native.EXPORT_INVERSE, np.float32, (gw * gh * 36,))
+        frame = frames[last].numpy()
+        rows = max(4, gh // 4)
+        per_frame, sample = cpu_sample_frame_time(args, frame, plane, meta, inv, rows)
+        cores = os.cpu_count()
+        cpu_baseline = {
+            "value": 1.0 / per_frame,
+            "unit": UNIT,
+            "cores": cores,
+            "kind": "port",
+            "sample": f"oracle C port with {cores} OpenMP threads: full-frame FIR prefilter ({sample['prefilter_s']:.2f} s) "
+                      f"+ finest-level affine IC-GN on {sample['rows']} of {gh} subset rows ({sample['subsets']} subsets, "
+                      f"{sample['solve_s']:.2f} s), extrapolated to one frame; GPU-prepared reference arrays",
+        }
+
+    summary = clocks.summary()
+    kernels_per_frame = (args.levels - 1) + 2 + 3 + 4 * (args.levels - 1) + 2
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": workload_config(args),
+        "subsets_per_s": value * selected,
+        "subsets_per_frame": selected,
+        "displacement_rmse_px": rmse,
+        "accepted_fraction": float(ok.sum() / max(1, selected)),
+        "clocks": {"sm_mhz": summary["sm_mhz"], "sm_max_mhz": summary["sm_max_mhz"], "reasons": summary["reasons"]},
+        "gpu_launches": kernels_per_frame * args.steps,
+        "roofline": roofline,
+        "cpu_baseline": cpu_baseline,
+        "e2e": e2e,
+    }
+    print(json.dumps(line), flush=True)
+    engine.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

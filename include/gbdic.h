@@ -219,6 +219,22 @@ int gbdic_pyramid_reset_temporal(gbdic_pyramid *pyramid);
 int gbdic_pyramid_export(gbdic_pyramid *pyramid, int32_t level, int32_t what, void *host_out,
                          int64_t bytes);
 
+/* ------------------------------------------------------------ profiling */
+
+/* Solver profiling (no reference counterpart; the reference reports wall-clock
+ * timing dicts only): CUDA events around every IC-GN launch issued outside
+ * graph capture, and a device counter of executed Gauss-Newton iterations.
+ * Enabling resets the counters; read waits for the recorded launches. */
+int gbdic_profile(gbdic_engine *engine, int32_t enable);
+int gbdic_profile_read(gbdic_engine *engine, double *solver_ms, int64_t *launches,
+                       int64_t *timed_launches, uint64_t *iterations);
+int gbdic_pyramid_profile(gbdic_pyramid *pyramid, int32_t enable);
+int gbdic_pyramid_profile_read(gbdic_pyramid *pyramid, double *solver_ms, int64_t *launches,
+                               int64_t *timed_launches, uint64_t *iterations);
+/* Measured FP32 fused multiply-add throughput of `device` (TFLOP/s), the
+ * denominator of the solver's FP32 roofline. */
+int gbdic_fp32_peak_probe(int32_t device, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

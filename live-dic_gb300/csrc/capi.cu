@@ -409,3 +409,28 @@ int gbdic_export(gbdic_engine *e, int32_t what, void *host_out, int64_t bytes) {
 }
 
 }  // extern "C"
+
+extern "C" {
+
+int gbdic_profile(gbdic_engine *e, int32_t enable) {
+    return guarded(e, [&] {
+        check_cuda(cudaStreamSynchronize(e->rt->stream()), "pending work");
+        e->rt->set_profiling(enable != 0);
+    });
+}
+
+int gbdic_profile_read(gbdic_engine *e, double *solver_ms, int64_t *launches, int64_t *timed_launches,
+                       uint64_t *iterations) {
+    return guarded(e, [&] {
+        double ms = 0.0;
+        long long n = 0, t = 0;
+        unsigned long long it = 0;
+        e->rt->profile_read(ms, n, t, it);
+        if (solver_ms) *solver_ms = ms;
+        if (launches) *launches = n;
+        if (timed_launches) *timed_launches = t;
+        if (iterations) *iterations = it;
+    });
+}
+
+}  // extern "C"

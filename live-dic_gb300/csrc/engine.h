@@ -121,6 +121,12 @@ class Runtime {
                       HostBuffer &staging, cudaStream_t stream);
     int persistent_grid(int lanes);
     const DeviceBuffer &weights() const { return weights_; }
+    // Solver profiling: CUDA events around every solver launch (outside graph
+    // capture) and a device counter of executed Gauss-Newton iterations.
+    void set_profiling(bool enable);
+    void profile_reset();
+    void profile_read(double &solver_ms, long long &launches, long long &timed, unsigned long long &iterations);
+    bool profiling() const { return profiling_; }
 
   private:
     Options opt_;
@@ -130,6 +136,11 @@ class Runtime {
     int device_ = 0;
     int persistent_grid_ = 0;
     int persistent_lanes_ = 0;
+    bool profiling_ = false;
+    std::vector<cudaEvent_t> profile_begin_, profile_end_;
+    int profile_used_ = 0;
+    long long profile_launches_ = 0;
+    DeviceBuffer profile_iterations_;
 };
 
 }  // namespace gbdic

@@ -152,6 +152,7 @@ struct SolveArgs {
     int roi_enabled, preserve_disabled, use_mean;
     int div_patience, div_min;
     int persistent;
+    unsigned long long *iteration_total;  // profiling: sum of executed iterations, or nullptr
 };
 
 }  // namespace gbdic

@@ -477,3 +477,28 @@ int gbdic_pyramid_export(gbdic_pyramid *p, int32_t level, int32_t what, void *ho
 }
 
 }  // extern "C"
+
+extern "C" {
+
+int gbdic_pyramid_profile(gbdic_pyramid *p, int32_t enable) {
+    return pguarded(p, [&] {
+        check_cuda(cudaStreamSynchronize(p->rt->stream()), "pending work");
+        p->rt->set_profiling(enable != 0);
+    });
+}
+
+int gbdic_pyramid_profile_read(gbdic_pyramid *p, double *solver_ms, int64_t *launches, int64_t *timed_launches,
+                               uint64_t *iterations) {
+    return pguarded(p, [&] {
+        double ms = 0.0;
+        long long n = 0, t = 0;
+        unsigned long long it = 0;
+        p->rt->profile_read(ms, n, t, it);
+        if (solver_ms) *solver_ms = ms;
+        if (launches) *launches = n;
+        if (timed_launches) *timed_launches = t;
+        if (iterations) *iterations = it;
+    });
+}
+
+}  // extern "C"

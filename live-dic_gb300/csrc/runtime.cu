@@ -159,6 +159,8 @@ Runtime::~Runtime() {
         cudaStreamSynchronize(stream_);
         cudaStreamDestroy(stream_);
     }
+    for (auto ev : profile_begin_) cudaEventDestroy(ev);
+    for (auto ev : profile_end_) cudaEventDestroy(ev);
 }
 
 int Runtime::persistent_grid(int lanes) {
@@ -322,13 +324,58 @@ void Runtime::enqueue_solve(Level &level, LevelSlot &slot, const gbdic_solver_cf
     a.div_patience = opt_.o.divergence_patience;
     a.div_min = opt_.o.divergence_min_iterations;
     a.persistent = opt_.o.persistent;
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    check_cuda(cudaStreamIsCapturing(s, &capture), "capture query");
+    const bool timed = profiling_ && capture == cudaStreamCaptureStatusNone &&
+                       profile_used_ < (int)profile_begin_.size();
+    if (profiling_) a.iteration_total = profile_iterations_.as<unsigned long long>();
     int grid = 0;
     if (a.persistent) {
         grid = persistent_grid(opt_.lanes);
         check_cuda(cudaMemsetAsync(slot.counter.get(), 0, sizeof(unsigned), s), "queue reset");
     }
+    if (timed) check_cuda(cudaEventRecord(profile_begin_[profile_used_], s), "profile event");
     check_cuda(launch_icgn(a, opt_.o.motion_model, opt_.o.interpolation, opt_.lanes, opt_.o.spatial_weighting == 1,
                            grid, s), "solver launch");
+    if (timed) check_cuda(cudaEventRecord(profile_end_[profile_used_++], s), "profile event");
+    if (profiling_) ++profile_launches_;
+}
+
+void Runtime::set_profiling(bool enable) {
+    if (enable && profile_begin_.empty()) {
+        profile_begin_.resize(4096);
+        profile_end_.resize(4096);
+        for (size_t i = 0; i < profile_begin_.size(); ++i) {
+            check_cuda(cudaEventCreate(&profile_begin_[i]), "event");
+            check_cuda(cudaEventCreate(&profile_end_[i]), "event");
+        }
+        profile_iterations_.ensure(sizeof(unsigned long long));
+    }
+    profiling_ = enable;
+    profile_reset();
+}
+
+void Runtime::profile_reset() {
+    profile_used_ = 0;
+    profile_launches_ = 0;
+    if (profile_iterations_.get())
+        check_cuda(cudaMemset(profile_iterations_.get(), 0, sizeof(unsigned long long)), "profile reset");
+}
+
+void Runtime::profile_read(double &solver_ms, long long &launches, long long &timed, unsigned long long &iterations) {
+    solver_ms = 0.0;
+    for (int i = 0; i < profile_used_; ++i) {
+        check_cuda(cudaEventSynchronize(profile_end_[i]), "profile sync");
+        float ms = 0.0f;
+        check_cuda(cudaEventElapsedTime(&ms, profile_begin_[i], profile_end_[i]), "profile elapsed");
+        solver_ms += ms;
+    }
+    launches = profile_launches_;
+    timed = profile_used_;
+    iterations = 0;
+    if (profile_iterations_.get())
+        check_cuda(cudaMemcpy(&iterations, profile_iterations_.get(), sizeof(iterations), cudaMemcpyDeviceToHost),
+                   "profile readback");
 }
 
 void Runtime::enqueue_uod(Level &level, LevelSlot &slot, bool seed_mode, float *out, cudaStream_t s) {

@@ -413,6 +413,8 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int gla
             status = gn_update<MODEL>(a, s, md, hi, wsum, half, (unsigned)(it + 1), w, prev_change, stalled);
         }
     }
+    if (a.iteration_total != nullptr && exists && glane == 0 && iters > 0.0f)
+        atomicAdd(a.iteration_total, (unsigned long long)iters);
     if (exists && (enabled || !a.preserve_disabled) && glane == 0) {
         const float final_status = (a.div_patience != 0 && status == 3.0f) ? 0.0f : status;
         float4 *o = reinterpret_cast<float4 *>(a.state + (size_t)idx * state_stride(MODEL));

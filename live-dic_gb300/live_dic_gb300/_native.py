@@ -118,6 +118,11 @@ _SIGNATURES = {
     "gbdic_pyramid_register_device": (C.c_int, [P, P, P, P]),
     "gbdic_pyramid_reset_temporal": (C.c_int, [P]),
     "gbdic_pyramid_export": (C.c_int, [P, I32, I32, P, I64]),
+    "gbdic_profile": (C.c_int, [P, I32]),
+    "gbdic_profile_read": (C.c_int, [P, P, P, P, P]),
+    "gbdic_pyramid_profile": (C.c_int, [P, I32]),
+    "gbdic_pyramid_profile_read": (C.c_int, [P, P, P, P, P]),
+    "gbdic_fp32_peak_probe": (C.c_int, [I32, P]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 

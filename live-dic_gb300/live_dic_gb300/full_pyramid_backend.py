@@ -542,6 +542,18 @@ class ICGNWGPUFullPyramid:
         self._check(self._lib.gbdic_pyramid_register_device(
             self._handle, C.c_void_p(device_frame), C.c_void_p(device_state), C.c_void_p(stream or 0)))
 
+    def set_profiling(self, enable: bool) -> None:
+        """Time every solver launch of the resident path with CUDA events and
+        count executed Gauss-Newton iterations (resets the counters)."""
+        self._check(self._lib.gbdic_pyramid_profile(self._handle, int(bool(enable))))
+
+    def read_profile(self) -> dict[str, float]:
+        ms, launches, timed, iters = C.c_double(), C.c_int64(), C.c_int64(), C.c_uint64()
+        self._check(self._lib.gbdic_pyramid_profile_read(
+            self._handle, C.byref(ms), C.byref(launches), C.byref(timed), C.byref(iters)))
+        return {"solver_ms": ms.value, "launches": launches.value, "timed_launches": timed.value,
+                "iterations": iters.value}
+
     def reset_temporal_state(self) -> None:
         """Forget the temporal history (676-694); no-op before set_reference."""
         if self._handle is not None:
