@@ -161,6 +161,33 @@ int gbdic_register_device(gbdic_engine *engine, const uint8_t *device_frame,
 /* Copies an internal buffer (GBDIC_EXPORT_*) to host memory. */
 int gbdic_export(gbdic_engine *engine, int32_t what, void *host_out, int64_t bytes);
 
+/* One registration (FIR prefilter + IC-GN, no outlier pass) for callers that
+ * cannot allocate GPU memory: code running inside a stream capture, real-time
+ * loops that forbid allocator calls, plug-ins whose host framework owns every
+ * device allocation.  No counterpart in the reference.  Every pointer is a
+ * device pointer supplied by the caller (reference arrays in the layout of
+ * gbdic_set_reference_arrays, state as in gbdic_register); `weights` is NULL
+ * for uniform integration or S*S Gaussian weights.  The coefficient scratch is
+ * a fixed 8 MiB array in the library (frames up to 2,097,152 pixels, larger
+ * ones return GBDIC_EINVAL), held by every GPU that loads the library until
+ * exit and shared by all calls: calls that overlap on the GPU race.  The first
+ * call on a device sets that device up and should come before any stream
+ * capture.  Errors: message in gbdic_last_error(NULL). */
+typedef struct {
+    const uint8_t *frame;      /* width*height target bytes, dense rows */
+    const float *plane;        /* width*height*4 floats */
+    const float *metadata;     /* 16 (n=6) or 28 (n=12) floats per subset */
+    const float *inverse;      /* n*n floats per subset */
+    const float *weights;      /* S*S Gaussian weights, or NULL */
+    int32_t width, height;
+    int32_t motion_model, interpolation;
+    int32_t subset_size, subset_stride;
+    int32_t threads_per_subset;
+    int32_t roi_enabled;       /* propagate validity -3 of ROI-excluded windows */
+    gbdic_solver_cfg cfg;
+} gbdic_noalloc_frame;
+int gbdic_register_noalloc(const gbdic_noalloc_frame *frame, float *device_state, void *stream);
+
 /* The engine's outlier pass (median_filter / median_filter_seed,
  * icgn.wgsl:1325-1605) on a caller-supplied state field, with the prepared
  * reference's validity and ROI links.  seed_mode selects the

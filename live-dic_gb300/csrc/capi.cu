@@ -97,6 +97,12 @@ extern "C" {
 
 int gbdic_abi_version(void) { return GBDIC_ABI_VERSION; }
 
+}  // extern "C"
+
+void gbdic::set_thread_error(const std::string &message) { g_create_error = message; }
+
+extern "C" {
+
 const char *gbdic_last_error(const gbdic_engine *engine) {
     return engine ? engine->error.c_str() : g_create_error.c_str();
 }

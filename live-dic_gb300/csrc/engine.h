@@ -28,6 +28,10 @@ void wait_event(cudaEvent_t ev, double timeout_ms);
 void validate_options(const gbdic_options &o);
 void validate_cfg(const gbdic_solver_cfg *c);
 void grid_of(int W, int H, int S, int st, int &gw, int &gh);
+// The 25 float32 runtime taps of the target FIR (offsets -12..12).
+void fir_taps(float out[25]);
+// Message returned by gbdic_last_error(NULL) on the calling thread.
+void set_thread_error(const std::string &message);
 constexpr double kWaitMs = 120000.0;
 
 // Owning device allocation.

@@ -81,6 +81,8 @@ void grid_of(int W, int H, int S, int st, int &gw, int &gh) {
     gh = 1 + (H - S) / st;
 }
 
+void fir_taps(float out[25]) { std::memcpy(out, kFirBits, sizeof kFirBits); }
+
 void check_cuda(cudaError_t err, const char *what) {
     if (err != cudaSuccess) throw Failure{GBDIC_ECUDA, std::string(what) + ": " + cudaGetErrorString(err)};
 }

@@ -67,6 +67,27 @@ class Timing(C.Structure):
     ]
 
 
+class NoAllocFrame(C.Structure):
+    """Arguments of gbdic_register_noalloc (all pointers are device pointers)."""
+
+    _fields_ = [
+        ("frame", C.c_void_p),
+        ("plane", C.c_void_p),
+        ("metadata", C.c_void_p),
+        ("inverse", C.c_void_p),
+        ("weights", C.c_void_p),
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("motion_model", C.c_int32),
+        ("interpolation", C.c_int32),
+        ("subset_size", C.c_int32),
+        ("subset_stride", C.c_int32),
+        ("threads_per_subset", C.c_int32),
+        ("roi_enabled", C.c_int32),
+        ("cfg", SolverCfg),
+    ]
+
+
 class PyramidOptions(C.Structure):
     _fields_ = [
         ("base", Options),
@@ -123,6 +144,7 @@ _SIGNATURES = {
     "gbdic_pyramid_profile": (C.c_int, [P, I32]),
     "gbdic_pyramid_profile_read": (C.c_int, [P, P, P, P, P]),
     "gbdic_fp32_peak_probe": (C.c_int, [I32, P]),
+    "gbdic_register_noalloc": (C.c_int, [C.POINTER(NoAllocFrame), P, P]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 
