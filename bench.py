@@ -66,6 +66,23 @@ def dist_env() -> tuple[int, int, int]:
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def slowest_ms(local_ms: float, world: int, dist, device) -> float:
+    """Maximum of a per-rank duration over all ranks (the job's clock)."""
+    if dist is None or world <= 1:
+        return local_ms
+    import torch
+
+    t = torch.tensor([local_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(*, steps: int, local_ms: float, world: int, dist, device) -> float:
+    """Whole-job frames/s: every replica processed `steps` frames; the job
+    took as long as its slowest rank."""
+    return world * steps / (slowest_ms(local_ms, world, dist, device) / 1e3)
+
+
 class ClockSampler:
     """nvidia-smi samples (200 ms) during the timed region."""
 
@@ -289,12 +306,8 @@ def main() -> None:
     profile = engine.read_profile()
     engine.set_profiling(False)
     final_state = state.view(gh, gw, 8).cpu().numpy()
-    ms_max = ms
-    if dist:
-        t = torch.tensor([ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * args.steps / (ms_max / 1e3)
+    ms_max = slowest_ms(ms, world, dist, device)
+    value = job_throughput(steps=args.steps, local_ms=ms, world=world, dist=dist, device=device)
 
     # ---------------- accuracy of the last timed frame against the FP64 field
     from live_dic_gb300 import synthetic
@@ -320,11 +333,7 @@ def main() -> None:
         t0 = time.perf_counter()
         results = list(engine.register_stream(host_frames[args.warmup: args.warmup + args.steps], pipeline_depth=2))
         t1 = time.perf_counter()
-        e2e_s = t1 - t0
-        if dist:
-            t = torch.tensor([e2e_s], device=device)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = slowest_ms((t1 - t0) * 1e3, world, dist, device) / 1e3
         age = [r.timing["resultAgeWallMs"] for r in results]
         e2e = {
             "value": world * args.steps / e2e_s,

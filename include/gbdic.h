@@ -53,7 +53,8 @@ enum { GBDIC_OUTLIER_FLAG = 0, GBDIC_OUTLIER_REPLACE = 1, GBDIC_OUTLIER_DISABLED
        GBDIC_OUTLIER_MEDIAN = 3 };
 enum { GBDIC_EXPORT_COEFFICIENTS = 0, GBDIC_EXPORT_PLANE = 1, GBDIC_EXPORT_METADATA = 2,
        GBDIC_EXPORT_INVERSE = 3, GBDIC_EXPORT_RAW_STATE = 4, GBDIC_EXPORT_OUTPUT_STATE = 5,
-       GBDIC_EXPORT_WEIGHTS = 6, GBDIC_EXPORT_FRAME = 7, GBDIC_EXPORT_ADMISSIBLE = 8 };
+       GBDIC_EXPORT_WEIGHTS = 6, GBDIC_EXPORT_FRAME = 7, GBDIC_EXPORT_ADMISSIBLE = 8,
+       GBDIC_EXPORT_SEED = 9, GBDIC_EXPORT_ACTIVE = 10 };
 
 typedef struct gbdic_engine gbdic_engine;
 typedef struct gbdic_pyramid gbdic_pyramid;

@@ -405,6 +405,8 @@ int gbdic_export(gbdic_engine *e, int32_t what, void *host_out, int64_t bytes) {
         case GBDIC_EXPORT_WEIGHTS: src = e->rt->weights().get(); size = e->rt->opts().weights.size() * sizeof(float); break;
         case GBDIC_EXPORT_FRAME: src = slot.frame.get(); size = (size_t)lvl.W * lvl.H; break;
         case GBDIC_EXPORT_ADMISSIBLE: src = lvl.admissible.get(); size = (size_t)lvl.count; break;
+        case GBDIC_EXPORT_SEED: src = slot.seed.get(); size = (size_t)lvl.count * gbdic::state_stride(model) * sizeof(float); break;
+        case GBDIC_EXPORT_ACTIVE: src = slot.active.get(); size = (size_t)lvl.count * sizeof(uint32_t); break;
         default: fail(GBDIC_EINVAL, "unknown export selector");
         }
         if (src == nullptr) fail(GBDIC_ESTATE, "buffer not available in this configuration");

@@ -86,6 +86,7 @@ struct Level {
     DeviceBuffer plane, meta, inv, links, selected;
     DeviceBuffer intensity, spline, scratch, valid;  // preparation scratch
     DeviceBuffer admissible;                         // u8 per subset, ROI ignored
+    DeviceBuffer ref_image;                          // reference bytes (seed search)
     std::vector<std::unique_ptr<LevelSlot>> slots;
     int valid_count = 0;
 };

@@ -80,8 +80,24 @@ struct SeedArgs {
     float src_scale, dst_scale, subset_size, subset_stride;
     int model;
     unsigned *projected;      // counter for temporal projection, or nullptr
+    int mark_missing;         // write status -1 into seeds that received no estimate
 };
 cudaError_t launch_transfer_seed(const SeedArgs &a, cudaStream_t stream);
+
+// ------------------------------------------------------------ ZNCC seed search
+struct SearchArgs {
+    const uint8_t *ref;       // level reference bytes (W*H)
+    const uint8_t *tgt;       // level target bytes (W*H)
+    float *seed;              // seed states (written)
+    uint32_t *active;         // activity (written)
+    float *score;             // best ZNCC per subset, or nullptr
+    const uint8_t *selected;  // ROI selection, or nullptr
+    unsigned *searched;       // count of searched subsets, or nullptr
+    int W, H, grid_w, count, S, stride, radius, model;
+    int only_missing;         // search only seeds whose status slot is -1
+};
+size_t zncc_search_smem(int S, int radius);
+cudaError_t launch_zncc_search(const SearchArgs &a, cudaStream_t stream);
 
 struct TemporalArgs {
     float *history;           // fine accepted history

@@ -67,6 +67,9 @@ struct gbdic_pyramid {
     }
     int L() const { return (int)levels.size(); }
     bool temporal() const { return po.initialization == 1; }
+    // ZNCC integer seed search at the coarsest level: initialization 2, or
+    // temporal initialization with a search radius (subsets without history).
+    bool search() const { return po.seed_search_radius > 0 && (po.initialization == 2 || po.initialization == 1); }
     bool velocity() const { return po.temporal_prediction == 1; }
     gbdic_solver_cfg cfg_of(int level) const {
         const int schedule = L() - 1 - level;  // options are coarsest first
@@ -157,7 +160,26 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
         a.subset_size = (float)p->po.base.subset_size; a.subset_stride = (float)p->po.base.subset_stride;
         a.model = model;
         a.projected = ps.counters.as<unsigned>();
+        a.mark_missing = p->search() ? 1 : 0;
         check_cuda(gbdic::launch_transfer_seed(a, s), "projection launch");
+        seeded = true;
+    }
+    if (p->search()) {
+        // ZNCC integer search at the coarsest level: every subset (zncc
+        // initialization) or only those without a temporal seed.
+        gbdic::SearchArgs q{};
+        q.ref = coarse.ref_image.as<uint8_t>();
+        q.tgt = cframe ? cframe : cslot.frame.as<uint8_t>();
+        q.seed = cslot.seed.as<float>();
+        q.active = cslot.active.as<uint32_t>();
+        q.selected = coarse.roi ? coarse.selected.as<uint8_t>() : nullptr;
+        q.searched = nullptr;
+        q.W = coarse.W; q.H = coarse.H; q.grid_w = coarse.gw; q.count = coarse.count;
+        q.S = p->po.base.subset_size; q.stride = p->po.base.subset_stride;
+        q.radius = p->po.seed_search_radius;
+        q.model = model;
+        q.only_missing = p->temporal() ? 1 : 0;
+        check_cuda(gbdic::launch_zncc_search(q, s), "seed search launch");
         seeded = true;
     }
     rt.enqueue_prefilter(coarse, cslot, cframe, s);
@@ -263,7 +285,13 @@ int gbdic_pyramid_create(const gbdic_pyramid_options *options, gbdic_pyramid **o
             gbdic_solver_cfg c{po.iterations[i], po.tolerance[i], po.zncc_min};
             gbdic::validate_cfg(&c);
         }
-        if (po.initialization < 0 || po.initialization > 1) fail(GBDIC_EINVAL, "unsupported initialization");
+        if (po.initialization < 0 || po.initialization > 2) fail(GBDIC_EINVAL, "unsupported initialization");
+        if (po.seed_search_radius < 0 || po.seed_search_radius > 64)
+            fail(GBDIC_EINVAL, "seed_search_radius must be an integer from 1 to 64");
+        if (po.initialization == 2 && po.seed_search_radius < 1)
+            fail(GBDIC_EINVAL, "initialization='zncc' requires seed_search_radius >= 1");
+        if (po.seed_search_radius > 0 && gbdic::zncc_search_smem(po.base.subset_size, po.seed_search_radius) > 48 * 1024)
+            fail(GBDIC_EINVAL, "subset_size + 2 * seed_search_radius is too large for the seed search tile");
         if (po.temporal_prediction != 0 && po.initialization != 1)
             fail(GBDIC_EINVAL, "temporal_prediction requires temporal initialization");
         gbdic::validate_options(po.base);
@@ -467,6 +495,8 @@ int gbdic_pyramid_export(gbdic_pyramid *p, int32_t level, int32_t what, void *ho
         case GBDIC_EXPORT_WEIGHTS: src = p->rt->weights().get(); size = p->rt->opts().weights.size() * sizeof(float); break;
         case GBDIC_EXPORT_FRAME: src = slot.frame.get(); size = (size_t)lvl.W * lvl.H; break;
         case GBDIC_EXPORT_ADMISSIBLE: src = lvl.admissible.get(); size = (size_t)lvl.count; break;
+        case GBDIC_EXPORT_SEED: src = slot.seed.get(); size = p->state_bytes(level); break;
+        case GBDIC_EXPORT_ACTIVE: src = slot.active.get(); size = (size_t)lvl.count * sizeof(uint32_t); break;
         default: fail(GBDIC_EINVAL, "unknown export selector");
         }
         if (src == nullptr) fail(GBDIC_ESTATE, "buffer not available in this configuration");

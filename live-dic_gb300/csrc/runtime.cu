@@ -214,6 +214,9 @@ double Runtime::prepare_reference(Level &level, const uint8_t *device_image, con
     level.scratch.ensure(px * sizeof(float));
     level.valid.ensure(sizeof(unsigned));
     level.admissible.ensure((size_t)level.count);
+    level.ref_image.ensure(px);
+    check_cuda(cudaMemcpyAsync(level.ref_image.get(), device_image, px, cudaMemcpyDeviceToDevice, stream_),
+               "reference bytes");
     level.roi = roi_selected != nullptr;
     if (roi_selected) {
         level.selected.ensure(level.count);

@@ -186,6 +186,7 @@ __global__ void transfer_seed_kernel(SeedArgs a) {
         } else {
             d[1] = make_float4(acc[4], acc[5], 0.0f, 0.0f);
         }
+        if (a.mark_missing && wsum == 0.0f) a.seed[(size_t)i * state_stride(a.model) + status_slot(a.model)] = -1.0f;
         a.active[i] = (perm >> 4) & 1u;
         projected = wsum > 0.0f && (perm & 16u) != 0u;
     }

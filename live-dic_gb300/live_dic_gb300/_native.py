@@ -19,7 +19,7 @@ LIBRARY_PATH = Path(__file__).resolve().parent / "libgbdic.so"
 OK, EINVAL, ESTATE, ECUDA, ETIMEOUT = 0, -1, -2, -3, -4
 EXPORT_COEFFICIENTS, EXPORT_PLANE, EXPORT_METADATA, EXPORT_INVERSE = 0, 1, 2, 3
 EXPORT_RAW_STATE, EXPORT_OUTPUT_STATE, EXPORT_WEIGHTS, EXPORT_FRAME = 4, 5, 6, 7
-EXPORT_ADMISSIBLE = 8
+EXPORT_ADMISSIBLE, EXPORT_SEED, EXPORT_ACTIVE = 8, 9, 10
 
 
 class Options(C.Structure):

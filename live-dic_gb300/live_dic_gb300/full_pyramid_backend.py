@@ -37,7 +37,7 @@ DEFAULT_FULL_PYRAMID_LEVELS = 2
 _DEFAULT_ITERATION_SCHEDULES = {1: (30,), 2: (8, 16), 3: (6, 8, 16), 4: (12, 8, 8, 16)}
 _DEFAULT_TOLERANCES = (1e-2, 5e-3, 5e-3)
 _FOUR_LEVEL_TOLERANCES = (1e-2, *_DEFAULT_TOLERANCES)
-_INITIALIZATIONS = ("zero", "temporal", "fourier", "wgpu-matching")
+_INITIALIZATIONS = ("zero", "temporal", "fourier", "wgpu-matching", "zncc")
 
 
 def _level_count(value: int) -> int:
@@ -107,6 +107,7 @@ class ICGNWGPUFullPyramid:
         device: int = 0,
         pipeline_slots: int = DEFAULT_IN_FLIGHT_FRAMES,
         persistent: bool = False,
+        seed_search_radius: int | None = None,
     ) -> None:
         if not isinstance(pyramid_policy, str) or pyramid_policy not in ("fixed", "adaptive"):
             raise ValueError("pyramid_policy must be 'fixed' or 'adaptive'")
@@ -132,7 +133,20 @@ class ICGNWGPUFullPyramid:
         if temporal_fine_correction and (initialization != "temporal" or pyramid_levels != 2):
             raise ValueError("temporal_fine_correction requires temporal initialization and two levels")
         if not isinstance(initialization, str) or initialization not in _INITIALIZATIONS:
-            raise ValueError("initialization must be 'zero', 'temporal', 'fourier' or 'wgpu-matching'")
+            raise ValueError("initialization must be 'zero', 'temporal', 'fourier', 'wgpu-matching' or 'zncc'")
+        if seed_search_radius is not None:
+            try:
+                radius = operator.index(seed_search_radius)
+            except TypeError as error:
+                raise ValueError("seed_search_radius must be an integer from 1 to 64") from error
+            if isinstance(seed_search_radius, bool) or not 1 <= radius <= 64:
+                raise ValueError("seed_search_radius must be an integer from 1 to 64")
+            if initialization not in ("zncc", "temporal"):
+                raise ValueError("seed_search_radius requires initialization='zncc' or 'temporal'")
+            seed_search_radius = radius
+        elif initialization == "zncc":
+            seed_search_radius = 8
+        self.seed_search_radius = seed_search_radius
         if matching_options is not None and initialization != "wgpu-matching":
             raise ValueError("matching_options requires initialization='wgpu-matching'")
         if temporal_max_age is not None:
@@ -242,7 +256,8 @@ class ICGNWGPUFullPyramid:
             po.iterations[i] = self.iterations_per_level[i]
             po.tolerance[i] = self.tolerance_per_level[i]
         po.zncc_min = self._zncc_min
-        po.initialization = 1 if self.initialization == "temporal" else 0
+        po.initialization = {"zero": 0, "temporal": 1, "zncc": 2}[self.initialization]
+        po.seed_search_radius = self.seed_search_radius or 0
         po.temporal_max_age = 0xFFFFFFFE if self.temporal_max_age is None else int(self.temporal_max_age)
         po.temporal_prediction = 1 if self.temporal_prediction == "velocity" else 0
         handle = C.c_void_p()
@@ -398,6 +413,11 @@ class ICGNWGPUFullPyramid:
             )
             if self.temporal_prediction == "velocity":
                 echo["temporalPrediction"] = "velocity"
+        if self.initialization == "zncc":
+            echo["initialization"] = "zncc"
+        if self.seed_search_radius:
+            echo.update(seedSearch="zncc-integer", seedSearchRadius=self.seed_search_radius,
+                        seedSearchLevel="coarsest")
         if self.roi is not None:
             echo["roi"] = {**self.roi.summary(), "selectedPerLevel": self._roi_level_counts}
         return echo

@@ -921,6 +921,73 @@ void oracle_temporal_save_previous(int count, int model, const float *history, c
     }
 }
 
+/* ------------------------------------------------------- ZNCC seed search */
+
+/* Exhaustive integer-shift ZNCC search (the CUDA seed search restated):
+ * for every subset (or, with only_missing, every subset whose seed status
+ * slot is -1), the shift (dx, dy) in [-R, R]^2 maximising
+ *   (n Sfg - Sf Sg) / sqrt((n Sff - Sf^2)(n Sgg - Sg^2))
+ * over exact integer sums of the 8-bit windows, lowest row-major index on
+ * ties; windows leaving the image are skipped.  Writes a translation seed
+ * and activity 1 (ROI-excluded subsets: zero seed, activity 0). */
+void oracle_seed_search(const uint8_t *ref, const uint8_t *tgt, int W, int H, int grid_w, int grid_h, int S,
+                        int stride, int R, int model, int only_missing, const uint8_t *selected, float *seed,
+                        uint32_t *active, float *score) {
+    const int ss = state_stride(model), sat = model == MODEL_QUADRATIC ? 12 : 6;
+    const int count = grid_w * grid_h, side = 2 * R + 1;
+    #pragma omp parallel for schedule(dynamic, 4)
+    for (int idx = 0; idx < count; ++idx) {
+        float *sd = seed + (size_t)idx * ss;
+        if (only_missing && sd[sat] != -1.0f) continue;
+        const int px0 = (idx % grid_w) * stride, py0 = (idx / grid_w) * stride;
+        if (selected && !selected[idx]) {
+            if (!only_missing) {
+                for (int k = 0; k < ss; ++k) sd[k] = 0.0f;
+                active[idx] = 0u;
+                if (score) score[idx] = -2.0f;
+            }
+            continue;
+        }
+        long long sf = 0, sff = 0;
+        for (int r = 0; r < S; ++r)
+            for (int c = 0; c < S; ++c) {
+                const long long f = ref[(size_t)(py0 + r) * W + px0 + c];
+                sf += f;
+                sff += f * f;
+            }
+        const long long n = (long long)S * S, vf = n * sff - sf * sf;
+        double best = -3.0;
+        int best_cand = -1;
+        for (int cand = 0; cand < side * side; ++cand) {
+            const int dy = cand / side - R, dx = cand % side - R;
+            if (px0 + dx < 0 || py0 + dy < 0 || px0 + dx + S - 1 > W - 1 || py0 + dy + S - 1 > H - 1) continue;
+            long long sg = 0, sgg = 0, sfg = 0;
+            for (int r = 0; r < S; ++r)
+                for (int c = 0; c < S; ++c) {
+                    const long long g = tgt[(size_t)(py0 + dy + r) * W + px0 + dx + c];
+                    const long long f = ref[(size_t)(py0 + r) * W + px0 + c];
+                    sg += g;
+                    sgg += g * g;
+                    sfg += f * g;
+                }
+            const long long vg = n * sgg - sg * sg;
+            double s = -2.0;
+            if (vf > 0 && vg > 0) s = (double)(n * sfg - sf * sg) / sqrt((double)vf * (double)vg);
+            if (s > best) {
+                best = s;
+                best_cand = cand;
+            }
+        }
+        for (int k = 0; k < ss; ++k) sd[k] = 0.0f;
+        if (best_cand >= 0 && best > -1.5) {
+            sd[0] = (float)(best_cand % side - R);
+            sd[3] = (float)(best_cand / side - R);
+        }
+        active[idx] = 1u;
+        if (score) score[idx] = (float)best;
+    }
+}
+
 /* ------------------------------------------------------------ final ZNCC */
 
 /* affine_zncc.wgsl:57-99 with `lanes` lanes; -2 marks unavailable. */

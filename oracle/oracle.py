@@ -224,6 +224,27 @@ def transfer_seed(
     return seeds, active
 
 
+def seed_search(reference: np.ndarray, target: np.ndarray, *, subset_size: int, subset_stride: int, radius: int,
+                model: str = "affine", seed: np.ndarray | None = None, only_missing: bool = False,
+                selected: np.ndarray | None = None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Exhaustive integer ZNCC search; returns (seed states, activity, best scores)."""
+    ref = np.ascontiguousarray(reference, dtype=np.uint8)
+    tgt = np.ascontiguousarray(target, dtype=np.uint8)
+    h, w = ref.shape
+    gw = 1 + (w - subset_size) // subset_stride
+    gh = 1 + (h - subset_size) // subset_stride
+    stride = 16 if model == "quadratic" else 8
+    seeds = np.zeros((gh * gw, stride), np.float32) if seed is None else np.ascontiguousarray(seed, np.float32).copy()
+    active = np.ones(gh * gw, np.uint32)
+    score = np.full(gh * gw, -3.0, np.float32)
+    sel = None if selected is None else np.ascontiguousarray(selected, dtype=np.uint8).ravel()
+    lib().oracle_seed_search(
+        _p(ref, C.c_uint8), _p(tgt, C.c_uint8), w, h, gw, gh, subset_size, subset_stride, radius, MODELS[model],
+        int(only_missing), _p(sel, C.c_uint8), _p(seeds), _p(active, C.c_uint32), _p(score),
+    )
+    return seeds, active, score
+
+
 def final_zncc(image, coef, plane, state, *, subset_size, subset_stride, interpolation="bspline", lanes=64):
     img = np.ascontiguousarray(image, dtype=np.uint8)
     h, w = img.shape

@@ -1,0 +1,169 @@
+"""Host-side behaviour that needs no GPU: the C ABI surface, argument
+validation before any device work (as the reference's portable tests pin,
+DIC/LucasKanadeICGN/python/tests/test_wgpu_backend.py:57-231), input
+normalisation and ROI planning against the reference's golden vectors,
+result views, and the multi-process replica aggregation of bench.py."""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from live_dic_gb300 import ICGNWGPU, ICGNWGPUFullPyramid, _native, roi
+from live_dic_gb300.engine import _as_uint8_gray, result_from_packed
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_library_exports_every_declared_symbol():
+    header = (ROOT / "include" / "gbdic.h").read_text()
+    declared = set(re.findall(r"^(?:int|void|const char \*)\s*\**\s*(gbdic_\w+)\(", header, flags=re.M))
+    assert len(declared) >= 30
+    lib = ctypes.CDLL(str(_native.LIBRARY_PATH))
+    for name in sorted(declared):
+        assert hasattr(lib, name), name
+    assert declared == set(_native.EXPORTED_SYMBOLS)
+    assert _native.load().gbdic_abi_version() == 1
+
+
+@pytest.mark.parametrize(
+    "kwargs,message",
+    [
+        ({"motion_model": "spline"}, "motion_model"),
+        ({"interpolation": "nearest"}, "interpolation"),
+        ({"outlier_policy": "drop"}, "outlier_policy"),
+        ({"median_filter_size": 4}, "median_filter_size"),
+        ({"median_filter_scope": "all"}, "median_filter_scope"),
+        ({"median_filter_size": 5}, "median_filter_size"),
+        ({"subset_size": 3}, "subset_size"),
+        ({"subset_size": 46341}, "subset_size"),
+        ({"subset_size": 16, "subset_stride": 17}, "subset_stride"),
+        ({"subset_stride": True}, "subset_stride"),
+        ({"spatial_weighting": "triangle"}, "spatial_weighting"),
+        ({"spatial_weighting": "gaussian", "gaussian_sigma": 0.0}, "gaussian_sigma"),
+        ({"solver_workgroup_size": 48}, "solver_workgroup_size"),
+        ({"pyramid_levels": 4}, "pyramid_levels"),
+        ({"pyramid_levels": True}, "pyramid_levels"),
+        ({"device_type": "tpu"}, "device_type"),
+        ({"power_preference": "max"}, "power_preference"),
+        ({"prefer_subgroups": True, "subset_size": 32}, "prefer_subgroups"),
+    ],
+)
+def test_engine_validation_before_device_work(kwargs, message):
+    with pytest.raises(ValueError, match=message):
+        ICGNWGPU(**kwargs)
+
+
+@pytest.mark.parametrize(
+    "kwargs,message",
+    [
+        ({"pyramid_levels": 5}, "pyramid_levels"),
+        ({"iterations_per_level": (8,)}, "iterations_per_level"),
+        ({"iterations_per_level": (0, 16)}, "iterations"),
+        ({"tolerance_per_level": (1e-2, -1.0)}, "tolerance"),
+        ({"initialization": "random"}, "initialization"),
+        ({"temporal_prediction": "velocity"}, "temporal_prediction"),
+        ({"temporal_max_age": -1}, "temporal_max_age"),
+        ({"pyramid_policy": "adaptive"}, "adaptive"),
+        ({"adaptive_acceptance": 1.5}, "adaptive_acceptance"),
+        ({"seed_search_radius": 0, "initialization": "zncc"}, "seed_search_radius"),
+        ({"seed_search_radius": 4}, "seed_search_radius"),
+        ({"divergence_patience": 31}, "divergence_patience"),
+    ],
+)
+def test_full_pyramid_validation_before_device_work(kwargs, message):
+    with pytest.raises(ValueError, match=message):
+        ICGNWGPUFullPyramid(**kwargs)
+
+
+def test_input_normalisation_matches_reference(golden):
+    np.testing.assert_array_equal(_as_uint8_gray(golden["gray_float_in"]), golden["gray_float_out"])
+    np.testing.assert_array_equal(_as_uint8_gray(golden["gray_wide_in"]), golden["gray_wide_out"])
+    with pytest.raises(ValueError, match="at least 16"):
+        _as_uint8_gray(np.zeros((8, 32), np.uint8))
+    with pytest.raises(ValueError, match=r"\[0, 255\]"):
+        _as_uint8_gray(np.full((20, 20), 300, np.int32))
+    rgb = np.random.default_rng(0).integers(0, 256, (20, 20, 3), dtype=np.uint8)
+    luma = _as_uint8_gray(rgb)
+    assert luma.shape == (20, 20) and luma.dtype == np.uint8
+
+
+def test_roi_planning_matches_reference(golden):
+    mask = golden["roi_mask"]
+    plan = roi.prepare_roi(mask, 21, 10)
+    np.testing.assert_array_equal(plan.selected, golden["roi_selected"])
+    np.testing.assert_array_equal(plan.neighbour_bits, golden["roi_neighbour_bits"])
+    np.testing.assert_array_equal(roi.prepare_roi(mask, 21, 10, median_filter_size=9).median_neighbour_words,
+                                  golden["roi_median_words"])
+    coarse_mask = roi.reduce_mask(mask)
+    np.testing.assert_array_equal(coarse_mask, golden["roi_reduced_mask"])
+    coarse = roi.prepare_roi(coarse_mask, 21, 10)
+    np.testing.assert_array_equal(coarse.selected, golden["roi_coarse_selected"])
+    np.testing.assert_array_equal(
+        roi.seed_permissions(coarse, plan, source_scale=2, destination_scale=1, size=21, stride=10,
+                             reference_mask=mask),
+        golden["roi_seed_permissions"],
+    )
+    np.testing.assert_array_equal(
+        roi.seed_permissions(plan, coarse, source_scale=1, destination_scale=2, size=21, stride=10,
+                             reference_mask=mask),
+        golden["roi_temporal_permissions"],
+    )
+    with pytest.raises(TypeError):
+        roi.validate_roi(mask.astype(np.uint8), "full", mask.shape, "affine")
+    with pytest.raises(ValueError, match="translation and affine"):
+        roi.validate_roi(mask, "full", mask.shape, "quadratic")
+
+
+def test_result_views_statistics_and_archive(tmp_path):
+    packed = np.zeros((3, 4, 8), np.float32)
+    packed[..., 0] = 0.5
+    packed[..., 3] = -0.25
+    packed[..., 6] = 1.0
+    packed[..., 7] = 3.0
+    packed[0, 0, 6] = 2.0
+    packed[2, 3, 6] = -1.0
+    result = result_from_packed(packed, motion_model="affine", timing={"totalWallMs": 1.0},
+                                config={"motionModel": "affine"}, width=64, height=48, subset_size=16,
+                                subset_stride=16)
+    assert result.accepted == 11 and result.replaced == 1
+    assert result.mean_translation == (0.5, -0.25)
+    result.displacement[1, 1, 0] = 7.0  # zero-copy view of the packed field
+    assert packed[1, 1, 0] == 7.0
+    assert result.rmse((0.5, -0.25)) > 0
+    assert result.populations["accepted"] == 11
+    path = tmp_path / "field.npz"
+    result.save_npz(path)
+    with np.load(path) as archive:
+        assert archive["parameters"].shape == (3, 4, 6)
+        assert tuple(archive["parameter_order"]) == result.parameter_order
+
+
+def _replica_worker(rank, world, port, out):
+    import torch
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+
+    value = bench.job_throughput(steps=10, local_ms=100.0 * (rank + 1), world=world, dist=dist, device="cpu")
+    out[rank] = value
+    dist.destroy_process_group()
+    del torch
+
+
+def test_bench_replica_throughput_two_gloo_ranks():
+    import torch.multiprocessing as mp
+
+    manager = mp.Manager()
+    out = manager.dict()
+    port = 29500 + (os.getpid() % 1000)
+    mp.spawn(_replica_worker, args=(2, port, out), nprocs=2, join=True)
+    # both ranks see the slowest rank's time: 2 replicas x 10 frames / 0.2 s
+    assert out[0] == pytest.approx(100.0) and out[1] == pytest.approx(100.0)

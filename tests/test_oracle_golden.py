@@ -148,6 +148,19 @@ def test_oracle_quadratic_gate():
     assert np.sqrt(np.mean(curv * curv)) < 2e-4
 
 
+def test_oracle_seed_search_finds_integer_shift():
+    rng = np.random.default_rng(3)
+    ref = rng.integers(0, 256, size=(90, 100), dtype=np.uint8)
+    tgt = np.roll(ref, shift=(-2, 3), axis=(0, 1))  # target(x) = ref(x - 3, y + 2)
+    seeds, active, score = oracle_c.seed_search(ref, tgt, subset_size=21, subset_stride=10, radius=5)
+    gw = 1 + (100 - 21) // 10
+    interior = score > 0.999
+    assert interior.sum() > 10 and active.all()
+    np.testing.assert_array_equal(seeds[interior][:, 0], 3.0)
+    np.testing.assert_array_equal(seeds[interior][:, 3], -2.0)
+    assert seeds.shape == (gw * (1 + (90 - 21) // 10), 8)
+
+
 def test_oracle_uod_flags_a_planted_outlier():
     """A planted translation spike in a smooth field is flagged (status 2)
     and, under 'replace', takes the neighbour medians (icgn.wgsl:1484-1592)."""
