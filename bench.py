@@ -57,6 +57,7 @@ def parse_args() -> argparse.Namespace:
     ap.add_argument("--peak", type=float, default=2.0)
     ap.add_argument("--lanes", type=int, default=32)
     ap.add_argument("--persistent", action="store_true")
+    ap.add_argument("--autotune", action="store_true", help="pick lanes/persistence with the solver autotuner")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -276,9 +277,10 @@ def main() -> None:
     engine = ICGNWGPUFullPyramid(
         pyramid_levels=args.levels, subset_size=args.subset, subset_stride=args.stride,
         initialization="temporal", temporal_prediction="velocity", solver_workgroup_size=args.lanes,
-        device=local, pipeline_slots=2, persistent=args.persistent,
+        device=local, pipeline_slots=2, persistent=args.persistent, autotune=args.autotune,
     )
     info = engine.set_reference(ref, roi_mask=mask)
+    args.lanes, args.persistent = engine.solver_workgroup_size, engine._persistent
     gw, gh = info.grid
     state = torch.zeros(gw * gh * 8, dtype=torch.float32, device=device)
     stream = torch.cuda.Stream(device=device)
@@ -368,7 +370,7 @@ def main() -> None:
         traffic = json.loads(traffic_file.read_text()).get("icgn_solver_dram_bytes_per_launch")
     roofline = {
         "bound": "fp32",
-        "kernel": "icgn_kernel<affine,bspline,32 lanes> (all pyramid levels)",
+        "kernel": f"icgn_kernel<affine,bspline,{args.lanes} lanes> (all pyramid levels)",
         "achieved": achieved,
         "peak": peak.value,
         "unit": "TFLOP/s",
@@ -420,6 +422,8 @@ def main() -> None:
         "dtype": "f32",
         "data": "synthetic",
         "config": workload_config(args),
+        "solver_variant": engine.solver,
+        "solver_tuning_ms": engine.solver_tuning_ms or None,
         "subsets_per_s": value * selected,
         "subsets_per_frame": selected,
         "displacement_rmse_px": rmse,

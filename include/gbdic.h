@@ -263,6 +263,13 @@ int gbdic_pyramid_profile_read(gbdic_pyramid *pyramid, double *solver_ms, int64_
  * denominator of the solver's FP32 roofline. */
 int gbdic_fp32_peak_probe(int32_t device, double *tflops);
 
+/* Switch the IC-GN solver variant (lanes per subset 16/32/64/128, persistent
+ * work queue on/off) of a prepared handle without re-preparing the reference;
+ * the autotuner's actuator (reference: ICGNWGPU._autotune_solver,
+ * wgpu_backend.py:2213-2296, which switches between solver pipelines). */
+int gbdic_set_solver_variant(gbdic_engine *engine, int32_t threads_per_subset, int32_t persistent);
+int gbdic_pyramid_set_solver_variant(gbdic_pyramid *pyramid, int32_t threads_per_subset, int32_t persistent);
+
 #ifdef __cplusplus
 }
 #endif

@@ -420,6 +420,17 @@ int gbdic_export(gbdic_engine *e, int32_t what, void *host_out, int64_t bytes) {
 
 extern "C" {
 
+int gbdic_set_solver_variant(gbdic_engine *e, int32_t threads_per_subset, int32_t persistent) {
+    return guarded(e, [&] {
+        check_cuda(cudaStreamSynchronize(e->rt->stream()), "pending work");
+        e->rt->set_variant(threads_per_subset, persistent != 0);
+        for (auto &h : e->host) {
+            if (h.graph) cudaGraphExecDestroy(h.graph);
+            h.graph = nullptr;
+        }
+    });
+}
+
 int gbdic_profile(gbdic_engine *e, int32_t enable) {
     return guarded(e, [&] {
         check_cuda(cudaStreamSynchronize(e->rt->stream()), "pending work");

@@ -125,6 +125,8 @@ class Runtime {
     void upload_frame(Level &level, LevelSlot &slot, const uint8_t *frame, int64_t row_stride,
                       HostBuffer &staging, cudaStream_t stream);
     int persistent_grid(int lanes);
+    // Switch the solver variant (lanes per subset, persistent queue).
+    void set_variant(int lanes, bool persistent);
     const DeviceBuffer &weights() const { return weights_; }
     // Solver profiling: CUDA events around every solver launch (outside graph
     // capture) and a device counter of executed Gauss-Newton iterations.

@@ -510,6 +510,19 @@ int gbdic_pyramid_export(gbdic_pyramid *p, int32_t level, int32_t what, void *ho
 
 extern "C" {
 
+int gbdic_pyramid_set_solver_variant(gbdic_pyramid *p, int32_t threads_per_subset, int32_t persistent) {
+    return pguarded(p, [&] {
+        for (auto &s : p->slots)
+            if (s.pending) fail(GBDIC_ESTATE, "retire every slot before switching the solver variant");
+        check_cuda(cudaStreamSynchronize(p->rt->stream()), "pending work");
+        p->rt->set_variant(threads_per_subset, persistent != 0);
+        for (auto &s : p->slots) {
+            if (s.graph) cudaGraphExecDestroy(s.graph);
+            s.graph = nullptr;
+        }
+    });
+}
+
 int gbdic_pyramid_profile(gbdic_pyramid *p, int32_t enable) {
     return pguarded(p, [&] {
         check_cuda(cudaStreamSynchronize(p->rt->stream()), "pending work");

@@ -165,6 +165,15 @@ Runtime::~Runtime() {
     for (auto ev : profile_end_) cudaEventDestroy(ev);
 }
 
+void Runtime::set_variant(int lanes, bool persistent) {
+    if (lanes != 16 && lanes != 32 && lanes != 64 && lanes != 128)
+        fail(GBDIC_EINVAL, "threads_per_subset must be 16, 32, 64, or 128");
+    opt_.lanes = lanes;
+    opt_.o.threads_per_subset = lanes;
+    opt_.o.persistent = persistent ? 1 : 0;
+    if (persistent) persistent_grid(lanes);
+}
+
 int Runtime::persistent_grid(int lanes) {
     // Queried once per lane count outside any stream capture, then cached.
     if (lanes != persistent_lanes_ || persistent_grid_ <= 0) {

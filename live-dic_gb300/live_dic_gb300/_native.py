@@ -145,6 +145,8 @@ _SIGNATURES = {
     "gbdic_pyramid_profile_read": (C.c_int, [P, P, P, P, P]),
     "gbdic_fp32_peak_probe": (C.c_int, [I32, P]),
     "gbdic_register_noalloc": (C.c_int, [C.POINTER(NoAllocFrame), P, P]),
+    "gbdic_set_solver_variant": (C.c_int, [P, I32, I32]),
+    "gbdic_pyramid_set_solver_variant": (C.c_int, [P, I32, I32]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 

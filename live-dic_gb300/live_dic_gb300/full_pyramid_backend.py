@@ -22,6 +22,7 @@ from typing import Any
 import numpy as np
 
 from . import _native
+from . import autotune as _tuning
 from .engine import ICGNError, ImageInput, ReferenceInfo, RegistrationResult, _as_uint8_gray, result_from_packed
 from .interpolation import normalize_interpolation
 from .motion import normalize_motion_model, parameter_count, state_float_count
@@ -108,7 +109,11 @@ class ICGNWGPUFullPyramid:
         pipeline_slots: int = DEFAULT_IN_FLIGHT_FRAMES,
         persistent: bool = False,
         seed_search_radius: int | None = None,
+        autotune: bool = False,
     ) -> None:
+        self._autotune = bool(autotune)
+        self.solver_tuning_ms: dict[str, float] = {}
+        self.solver_validation: dict[str, dict] = {}
         if not isinstance(pyramid_policy, str) or pyramid_policy not in ("fixed", "adaptive"):
             raise ValueError("pyramid_policy must be 'fixed' or 'adaptive'")
         if pyramid_policy == "adaptive" and (initialization != "temporal" or pyramid_levels != 2):
@@ -226,6 +231,7 @@ class ICGNWGPUFullPyramid:
         self._handle = self._create(device)
         self.device_index = int(device)
         self.device_name = f"CUDA device {self.device_index} (gbdic sm_103a)"
+        self.solver = _tuning.variant_name(self.solver_workgroup_size, self._persistent)
         self.execution_device_type = "gpu"
         self._reference_ready = False
         self.roi = None
@@ -362,6 +368,9 @@ class ICGNWGPUFullPyramid:
             int(p.selected.sum()) if p is not None else d[2] * d[3] for p, d in zip(plans, dims, strict=True)
         ]
         self._reference_ready = True
+        usable = self.reference_valid if self.roi is None else self.reference_valid & self.roi.selected
+        if self._autotune and usable.any():
+            self._autotune_solver(reference)
         total = (time.perf_counter() - started) * 1e3
         return ReferenceInfo(
             preparation_wall_ms=total,
@@ -561,6 +570,29 @@ class ICGNWGPUFullPyramid:
             raise ICGNError("Call set_reference() before register().")
         self._check(self._lib.gbdic_pyramid_register_device(
             self._handle, C.c_void_p(device_frame), C.c_void_p(device_state), C.c_void_p(stream or 0)))
+
+    def set_solver_variant(self, lanes: int, persistent: bool = False) -> None:
+        """Select the solver variant of every level (lanes per subset, grid or persistent queue)."""
+        self._check(self._lib.gbdic_pyramid_set_solver_variant(
+            self._handle, _normalize_solver_workgroup_size(lanes), int(bool(persistent))))
+        self.solver_workgroup_size = int(lanes)
+        self._persistent = bool(persistent)
+        self.solver = _tuning.variant_name(int(lanes), bool(persistent))
+
+    def _autotune_solver(self, reference: np.ndarray) -> None:
+        """Fastest validated variant on the reference shifted by (-1, +2) px;
+        the temporal history is reset afterwards."""
+        target = np.ascontiguousarray(np.roll(reference, shift=(-1, 2), axis=(0, 1)))
+
+        def run():
+            self.reset_temporal_state()
+            r = self.register(target)
+            packed = np.concatenate([r.parameters, r.status[..., None], r.iterations[..., None]], -1)
+            return packed, float(r.timing["deviceMs"])
+
+        best, self.solver_tuning_ms, self.solver_validation = _tuning.autotune(self.set_solver_variant, run)
+        self.set_solver_variant(*best)
+        self.reset_temporal_state()
 
     def set_profiling(self, enable: bool) -> None:
         """Time every solver launch of the resident path with CUDA events and

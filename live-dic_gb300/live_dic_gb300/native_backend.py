@@ -21,6 +21,7 @@ from typing import Any
 import numpy as np
 
 from . import _native
+from . import autotune as _tuning
 from .engine import ICGNError, ImageInput, ReferenceInfo, RegistrationResult, _as_uint8_gray, result_from_packed
 from .interpolation import INTERPOLATION_CODES, normalize_interpolation
 from .motion import MOTION_MODEL_CODES, normalize_motion_model, parameter_count, state_float_count
@@ -172,6 +173,7 @@ class ICGNWGPU:
         device: int = 0,
         pipeline_slots: int = DEFAULT_IN_FLIGHT_FRAMES,
         persistent: bool = False,
+        autotune: bool = False,
     ) -> None:
         self.device_type = _normalize_device_type(device_type)
         if power_preference not in ("high-performance", "low-power"):
@@ -218,6 +220,9 @@ class ICGNWGPU:
         self.pyramid_levels = levels
         self._pipeline_slots = slots
         self._persistent = bool(persistent)
+        self._autotune = bool(autotune)
+        self.solver_tuning_ms: dict[str, float] = {}
+        self.solver_validation: dict[str, dict] = {}
         self._lib = _native.load()
         self._registration_lock = threading.Lock()
         self._closed = False
@@ -242,7 +247,7 @@ class ICGNWGPU:
         self._handle = handle
         self.device_index = int(device)
         self.device_name = f"CUDA device {self.device_index} (gbdic sm_103a)"
-        self.solver = "persistent-queue" if self._persistent else "warp-per-subset"
+        self.solver = _tuning.variant_name(self.solver_workgroup_size, self._persistent)
         self.execution_device_type = "gpu"
         self.width = self.height = self.grid_width = self.grid_height = 0
         self._reference_ready = False
@@ -255,6 +260,27 @@ class ICGNWGPU:
     def _check(self, code: int) -> None:
         if code != _native.OK:
             _native.check(code, self._lib.gbdic_last_error(self._handle))
+
+    def set_solver_variant(self, lanes: int, persistent: bool = False) -> None:
+        """Select the solver variant: lanes per subset and grid or persistent queue."""
+        self._check(self._lib.gbdic_set_solver_variant(self._handle, _normalize_solver_workgroup_size(lanes),
+                                                       int(bool(persistent))))
+        self.solver_workgroup_size = int(lanes)
+        self._persistent = bool(persistent)
+        self.solver = _tuning.variant_name(int(lanes), bool(persistent))
+
+    def _autotune_solver(self, reference: np.ndarray) -> None:
+        """Choose the fastest validated variant on the reference shifted by
+        (-1, +2) pixels (wgpu_backend.py:2213-2296)."""
+        target = np.ascontiguousarray(np.roll(reference, shift=(-1, 2), axis=(0, 1)))
+
+        def run():
+            r = self.register(target)
+            packed = np.concatenate([r.parameters, r.status[..., None], r.iterations[..., None]], -1)
+            return packed, float(r.timing["deviceMs"])
+
+        best, self.solver_tuning_ms, self.solver_validation = _tuning.autotune(self.set_solver_variant, run)
+        self.set_solver_variant(*best)
 
     def _cfg(self, config: dict[str, float | int]) -> _native.SolverCfg:
         return _native.SolverCfg(int(config["iterations"]), float(config["tolerance"]), float(config["znccMin"]))
@@ -370,6 +396,9 @@ class ICGNWGPU:
         admissible = self._export(_native.EXPORT_ADMISSIBLE, np.uint8, (gh, gw))
         self.reference_valid = immutable(admissible.astype(bool))
         self._reference_ready = True
+        usable = self.reference_valid if roi is None else self.reference_valid & roi.selected
+        if self._autotune and usable.any():
+            self._autotune_solver(frame)
         total_ms = (time.perf_counter() - started) * 1e3
         return ReferenceInfo(
             preparation_wall_ms=prep_ms,

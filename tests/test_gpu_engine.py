@@ -58,6 +58,18 @@ def test_c0_parity_with_oracle_and_truth(c0_pair):
     assert (status == 1).mean() > 0.9
 
 
+def test_autotuner_selects_a_validated_variant(c0_pair):
+    ref, tgt = c0_pair
+    with ICGNWGPU(subset_size=21, subset_stride=10, autotune=True) as engine:
+        engine.set_reference(ref)
+        chosen = engine.solver
+        result = engine.register(tgt)
+    assert chosen in engine.solver_tuning_ms
+    assert engine.solver_validation[chosen]["valid"]
+    assert len(engine.solver_validation) == 8
+    assert (result.status == 1).mean() > 0.9
+
+
 def test_stream_matches_register(c0_pair):
     ref, tgt = c0_pair
     with ICGNWGPU(subset_size=21, subset_stride=10, pipeline_slots=3) as engine:

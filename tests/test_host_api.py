@@ -144,6 +144,26 @@ def test_result_views_statistics_and_archive(tmp_path):
         assert tuple(archive["parameter_order"]) == result.parameter_order
 
 
+def test_autotune_acceptance_rule():
+    from live_dic_gb300.autotune import compare_solver_outputs
+
+    rng = np.random.default_rng(1)
+    base = np.zeros((20, 30, 8), np.float32)
+    base[..., :6] = rng.normal(0, 0.1, (20, 30, 6))
+    base[..., 6] = 1.0
+    ok = compare_solver_outputs(base, base + np.float32(1e-5) * (np.arange(8) < 6))
+    assert ok["valid"] and ok["parameter_max_abs"] < 2e-5
+    far = base.copy()
+    far[..., 0] += 0.05
+    assert compare_solver_outputs(base, far)["reason"] == "parameters disagree"
+    flipped = base.copy()
+    flipped[:5, :, 6] = 0.0
+    assert compare_solver_outputs(base, flipped)["reason"] == "accepted subset masks disagree"
+    nan = base.copy()
+    nan[0, 0, 0] = np.nan
+    assert compare_solver_outputs(base, nan)["reason"] == "non-finite solver output"
+
+
 def _replica_worker(rank, world, port, out):
     import torch
     import torch.distributed as dist
