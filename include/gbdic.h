@@ -270,6 +270,60 @@ int gbdic_fp32_peak_probe(int32_t device, double *tflops);
 int gbdic_set_solver_variant(gbdic_engine *engine, int32_t threads_per_subset, int32_t persistent);
 int gbdic_pyramid_set_solver_variant(gbdic_pyramid *pyramid, int32_t threads_per_subset, int32_t persistent);
 
+/* ------------------------------------------------------------ batch */
+
+/* Batched registration of many fixed-reference jobs of uneven image size,
+ * subset size and shape function in one step (no reference counterpart: the
+ * reference runs one ICGNWGPU engine per image size and registers pairs one
+ * call at a time, wgpu_backend.py:2893-2944).  Each job carries its own
+ * GPU-prepared reference (B-spline interpolation, uniform weighting) and is
+ * solved from a zero seed exactly like gbdic_register, followed by its own
+ * outlier pass.  A step is one CUDA graph: prefilter of every target, one
+ * persistent IC-GN launch per shape-function class over a device work queue
+ * (affine/translation jobs, quadratic jobs), then the outlier passes. */
+typedef struct gbdic_batch gbdic_batch;
+
+typedef struct {
+    int32_t motion_model;        /* GBDIC_MODEL_* */
+    int32_t subset_size;
+    int32_t subset_stride;
+    int32_t outlier_policy;      /* GBDIC_OUTLIER_DISABLED / REPLACE / FLAG */
+    gbdic_solver_cfg cfg;
+} gbdic_batch_job;
+
+/* Step modes: one persistent launch per class over the shared work queue, or
+ * one grid launch per job in job order (the per-pair baseline). */
+enum { GBDIC_BATCH_PERSISTENT = 0, GBDIC_BATCH_PER_JOB = 1 };
+
+int gbdic_batch_create(int32_t device, gbdic_batch **out);
+int gbdic_batch_destroy(gbdic_batch *batch);
+const char *gbdic_batch_last_error(const gbdic_batch *batch);
+/* Add a job: its reference image (dense or strided rows) is prepared on the
+ * GPU.  roi_selected / roi_links as for gbdic_set_reference (affine and
+ * translation only).  Writes the job index. */
+int gbdic_batch_add(gbdic_batch *batch, const gbdic_batch_job *job, const uint8_t *reference, int32_t width,
+                    int32_t height, int64_t row_stride, const uint8_t *roi_selected, const float *roi_links,
+                    gbdic_ref_info *info, int32_t *job_index);
+/* Lanes per subset (32, 64, 128), step mode, and persistent CTAs per SM
+ * (0 = as many as are resident). */
+int gbdic_batch_set_variant(gbdic_batch *batch, int32_t threads_per_subset, int32_t mode, int32_t ctas_per_sm);
+/* One step from host frames: frames[j] is job j's target (rows of its own
+ * width, row_strides[j] bytes apart); out_states[j] receives its output
+ * state grid (grid_h * grid_w * 8 or 16 floats). */
+int gbdic_batch_register(gbdic_batch *batch, const uint8_t *const *frames, const int64_t *row_strides,
+                         float *const *out_states, gbdic_timing *timing);
+/* Resident path: copy a device frame into job j's target buffer ... */
+int gbdic_batch_load_device(gbdic_batch *batch, int32_t job, const uint8_t *device_frame, int64_t row_stride,
+                            void *stream);
+/* ... then run one step on `stream` (NULL: the batch's stream) from the
+ * loaded targets; outputs stay on the device (gbdic_batch_export).  With
+ * `profile` set the stages are launched directly rather than as the graph,
+ * and timing->device_ms is the solver launches' time alone. */
+int gbdic_batch_run_device(gbdic_batch *batch, void *stream, int32_t profile, gbdic_timing *timing);
+/* Copy job j's GBDIC_EXPORT_* array to host memory (OUTPUT_STATE, RAW_STATE,
+ * METADATA, ADMISSIBLE). */
+int gbdic_batch_export(gbdic_batch *batch, int32_t job, int32_t what, void *host_out, int64_t bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,6 +120,10 @@ class Runtime {
     void enqueue_prefilter(Level &level, LevelSlot &slot, const uint8_t *frame, cudaStream_t stream);
     void enqueue_solve(Level &level, LevelSlot &slot, const gbdic_solver_cfg &cfg, bool seeded,
                        bool preserve, const uint8_t *frame, float *state, cudaStream_t stream);
+    // The solver arguments enqueue_solve launches with (work_counter = the
+    // slot's queue head; the persistent flag of the current variant).
+    SolveArgs solve_args(Level &level, LevelSlot &slot, const gbdic_solver_cfg &cfg, bool seeded,
+                         bool preserve, const uint8_t *frame, float *state) const;
     void enqueue_uod(Level &level, LevelSlot &slot, bool seed_mode, float *out, cudaStream_t stream);
     const float *output_state(LevelSlot &slot) const;
     void upload_frame(Level &level, LevelSlot &slot, const uint8_t *frame, int64_t row_stride,

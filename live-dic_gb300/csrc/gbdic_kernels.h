@@ -24,6 +24,21 @@ int icgn_occupancy(int model, int interp, int lanes, bool gauss);
 cudaError_t launch_icgn(const SolveArgs &a, int model, int interp, int lanes, bool gauss,
                         int persistent_grid, cudaStream_t stream);
 
+// One persistent launch over many jobs (B-spline, uniform weighting).
+constexpr int kMaxBatchJobs = 256;
+struct BatchSolveArgs {
+    const SolveArgs *args;   // per job, in queue order (device)
+    const int *models;       // per job, in queue order (device); one shape-function class
+    const int *first;        // jobs + 1 queue offsets, each a multiple of batch_units (device)
+    unsigned *work_counter;  // queue head, zeroed before the launch
+    int jobs;
+};
+// Subsets one scheduling unit (warp or 128-thread block) claims at a time.
+int batch_units(int lanes);
+// Launches of the affine/translation class or of the quadratic class.
+int icgn_batch_occupancy(int lanes, bool quadratic);
+cudaError_t launch_icgn_batch(const BatchSolveArgs &b, int lanes, bool quadratic, int grid, cudaStream_t stream);
+
 // ------------------------------------------------------------ UOD
 struct UodArgs {
     const float *state;

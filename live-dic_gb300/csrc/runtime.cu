@@ -315,8 +315,8 @@ void Runtime::enqueue_prefilter(Level &level, LevelSlot &slot, const uint8_t *fr
                "prefilter launch");
 }
 
-void Runtime::enqueue_solve(Level &level, LevelSlot &slot, const gbdic_solver_cfg &cfg, bool seeded, bool preserve,
-                            const uint8_t *frame, float *state, cudaStream_t s) {
+SolveArgs Runtime::solve_args(Level &level, LevelSlot &slot, const gbdic_solver_cfg &cfg, bool seeded, bool preserve,
+                              const uint8_t *frame, float *state) const {
     SolveArgs a{};
     a.coef = slot.coef.as<float>();
     a.img = frame ? frame : slot.frame.as<uint8_t>();
@@ -338,6 +338,12 @@ void Runtime::enqueue_solve(Level &level, LevelSlot &slot, const gbdic_solver_cf
     a.div_patience = opt_.o.divergence_patience;
     a.div_min = opt_.o.divergence_min_iterations;
     a.persistent = opt_.o.persistent;
+    return a;
+}
+
+void Runtime::enqueue_solve(Level &level, LevelSlot &slot, const gbdic_solver_cfg &cfg, bool seeded, bool preserve,
+                            const uint8_t *frame, float *state, cudaStream_t s) {
+    SolveArgs a = solve_args(level, slot, cfg, seeded, preserve, frame, state);
     cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
     check_cuda(cudaStreamIsCapturing(s, &capture), "capture query");
     const bool timed = profiling_ && capture == cudaStreamCaptureStatusNone &&

@@ -5,6 +5,7 @@ The public names follow live_dic/__init__.py (21-41).  All GPU work runs in
 libgbdic.so (hand-written sm_103a CUDA) through its C ABI.
 """
 
+from .batch import ICGNBatch
 from .engine import PARAMETER_ORDER, ICGNError, ImageInput, ReferenceInfo, RegistrationResult
 from .full_pyramid_backend import DEFAULT_FULL_PYRAMID_LEVELS, ICGNWGPUFullPyramid
 from .motion import AFFINE_PARAMETER_ORDER, MOTION_MODELS, QUADRATIC_PARAMETER_ORDER
@@ -12,7 +13,7 @@ from .native_backend import DEFAULT_IN_FLIGHT_FRAMES, DEFAULT_PYRAMID_LEVELS, IC
 from .outlier import OUTLIER_POLICIES
 
 SEEDED_SOLVE_API_VERSION = 1
-# GB300 names for the same engines.
+# GB300 names for the same engines (ICGNBatch has no reference counterpart).
 ICGNCUDA = ICGNWGPU
 ICGNCUDAFullPyramid = ICGNWGPUFullPyramid
 
@@ -21,6 +22,7 @@ __all__ = [
     "DEFAULT_FULL_PYRAMID_LEVELS",
     "DEFAULT_IN_FLIGHT_FRAMES",
     "DEFAULT_PYRAMID_LEVELS",
+    "ICGNBatch",
     "ICGNCUDA",
     "ICGNCUDAFullPyramid",
     "ICGNError",

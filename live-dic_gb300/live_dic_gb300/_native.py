@@ -110,6 +110,18 @@ class LevelRoi(C.Structure):
     ]
 
 
+class BatchJob(C.Structure):
+    _fields_ = [
+        ("motion_model", C.c_int32),
+        ("subset_size", C.c_int32),
+        ("subset_stride", C.c_int32),
+        ("outlier_policy", C.c_int32),
+        ("cfg", SolverCfg),
+    ]
+
+
+BATCH_PERSISTENT, BATCH_PER_JOB = 0, 1
+
 P = C.c_void_p
 I32, I64 = C.c_int32, C.c_int64
 _SIGNATURES = {
@@ -147,6 +159,15 @@ _SIGNATURES = {
     "gbdic_register_noalloc": (C.c_int, [C.POINTER(NoAllocFrame), P, P]),
     "gbdic_set_solver_variant": (C.c_int, [P, I32, I32]),
     "gbdic_pyramid_set_solver_variant": (C.c_int, [P, I32, I32]),
+    "gbdic_batch_create": (C.c_int, [I32, C.POINTER(P)]),
+    "gbdic_batch_destroy": (C.c_int, [P]),
+    "gbdic_batch_last_error": (C.c_char_p, [P]),
+    "gbdic_batch_add": (C.c_int, [P, C.POINTER(BatchJob), P, I32, I32, I64, P, P, C.POINTER(RefInfo), C.POINTER(I32)]),
+    "gbdic_batch_set_variant": (C.c_int, [P, I32, I32, I32]),
+    "gbdic_batch_register": (C.c_int, [P, P, P, P, C.POINTER(Timing)]),
+    "gbdic_batch_load_device": (C.c_int, [P, I32, P, I64, P]),
+    "gbdic_batch_run_device": (C.c_int, [P, P, I32, C.POINTER(Timing)]),
+    "gbdic_batch_export": (C.c_int, [P, I32, I32, P, I64]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 

@@ -230,6 +230,75 @@ class KirschField:
         return field
 
 
+def smooth_field(rng: np.random.Generator, width: int, height: int, peak: float):
+    """Random affine-plus-sinusoid field whose largest |(u, v)| over the
+    image is `peak` px.  Returns (field, params) with field usable on numpy
+    arrays and torch tensors."""
+    a = [float(x) for x in rng.uniform(-1.0, 1.0, 6)]
+    wavelengths = [float(x) for x in rng.uniform(0.6, 1.5, 4) * max(width, height)]
+    phases = [float(x) for x in rng.uniform(0.0, 2 * math.pi, 4)]
+    amps = [float(x) for x in rng.uniform(0.3, 1.0, 2)]
+
+    def raw(X, Y):
+        lib = torch if torch is not None and isinstance(X, torch.Tensor) else np
+        xn, yn = X / width - 0.5, Y / height - 0.5
+        u = a[0] + a[1] * xn + a[2] * yn + amps[0] * lib.sin(2 * math.pi * X / wavelengths[0] + phases[0]) * lib.cos(
+            2 * math.pi * Y / wavelengths[1] + phases[1])
+        v = a[3] + a[4] * xn + a[5] * yn + amps[1] * lib.cos(2 * math.pi * X / wavelengths[2] + phases[2]) * lib.sin(
+            2 * math.pi * Y / wavelengths[3] + phases[3])
+        return u, v
+
+    gy, gx = np.mgrid[0:height:8, 0:width:8].astype(np.float64)
+    u, v = raw(gx, gy)
+    scale = peak / float(np.sqrt(u * u + v * v).max())
+
+    def field(X, Y):
+        u, v = raw(X, Y)
+        return scale * u, scale * v
+
+    return field, {"affine": a, "wavelengths": wavelengths, "phases": phases, "amplitudes": amps,
+                   "scale": scale, "peak": peak}
+
+
+def rectangle_roi(rng: np.random.Generator, width: int, height: int, holes: int,
+                  radius: tuple[float, float] = (40.0, 200.0)) -> np.ndarray:
+    """A rectangle inset 3-10 % from each edge with `holes` circular holes
+    (radius drawn from `radius`, capped to an eighth of the smaller side)."""
+    x0, x1 = (rng.uniform(0.03, 0.10, 2) * width).astype(int)
+    y0, y1 = (rng.uniform(0.03, 0.10, 2) * height).astype(int)
+    mask = np.zeros((height, width), dtype=bool)
+    mask[y0:height - y1, x0:width - x1] = True
+    yy, xx = np.ogrid[:height, :width]
+    cap = min(width, height) / 8.0
+    for _ in range(holes):
+        r = min(rng.uniform(*radius), cap)
+        cx = rng.uniform(x0 + r, width - x1 - r)
+        cy = rng.uniform(y0 + r, height - y1 - r)
+        mask &= (xx - cx) ** 2 + (yy - cy) ** 2 >= r * r
+    return mask
+
+
+def uneven_workload(seed: int, count: int = 16, *, sizes=((640, 480), (1280, 720), (1920, 1080), (3840, 2160)),
+                    subsets=(15, 21, 31, 41), quadratic_fraction: float = 0.5, peak=(0.5, 3.0),
+                    device: str | None = None) -> list[dict]:
+    """Image pairs of uneven size, subset size and shape function: each with
+    a rectangle ROI holding 0-3 holes (affine jobs; the quadratic model takes
+    no ROI mask) and a random smooth affine-plus-sinusoid field."""
+    rng = np.random.default_rng(seed)
+    pairs = []
+    for k in range(count):
+        width, height = sizes[int(rng.integers(len(sizes)))]
+        size = int(subsets[int(rng.integers(len(subsets)))])
+        model = "quadratic" if rng.uniform() < quadratic_fraction else "affine"
+        field, params = smooth_field(rng, width, height, float(rng.uniform(*peak)))
+        mask = None if model == "quadratic" else rectangle_roi(rng, width, height, int(rng.integers(0, 4)))
+        ref, sp = reference_image(width, height, seed=seed * 1000 + 2 * k, device=device)
+        tgt = deformed_image(sp, field, noise_seed=seed * 1000 + 2 * k + 1, device=device)
+        pairs.append({"reference": ref, "target": tgt, "motion_model": model, "subset_size": size,
+                      "subset_stride": size // 3, "roi_mask": mask, "field": field, "field_params": params})
+    return pairs
+
+
 def hole_mask(width: int, height: int, radius: float) -> np.ndarray:
     y, x = np.ogrid[:height, :width]
     return (x - 0.5 * width) ** 2 + (y - 0.5 * height) ** 2 >= radius**2

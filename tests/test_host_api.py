@@ -187,3 +187,35 @@ def test_bench_replica_throughput_two_gloo_ranks():
     mp.spawn(_replica_worker, args=(2, port, out), nprocs=2, join=True)
     # both ranks see the slowest rank's time: 2 replicas x 10 frames / 0.2 s
     assert out[0] == pytest.approx(100.0) and out[1] == pytest.approx(100.0)
+
+
+@pytest.mark.parametrize(
+    "kwargs,message",
+    [
+        ({"solver_workgroup_size": 16}, "solver_workgroup_size"),
+        ({"solver_workgroup_size": True}, "solver_workgroup_size"),
+        ({"mode": "sequential"}, "mode"),
+        ({"ctas_per_sm": 33}, "ctas_per_sm"),
+    ],
+)
+def test_batch_validation_before_device_work(kwargs, message):
+    from live_dic_gb300 import ICGNBatch
+
+    with pytest.raises(ValueError, match=message):
+        ICGNBatch(**kwargs)
+
+
+def test_uneven_workload_generator():
+    from live_dic_gb300 import synthetic
+
+    pairs = synthetic.uneven_workload(4, count=5, sizes=((96, 80), (128, 96)), subsets=(15, 21), device="cpu")
+    assert len(pairs) == 5
+    for p in pairs:
+        h, w = p["reference"].shape
+        assert p["target"].shape == (h, w) and p["target"].dtype == np.uint8
+        assert p["subset_stride"] == p["subset_size"] // 3
+        assert (p["roi_mask"] is None) == (p["motion_model"] == "quadratic")
+        gy, gx = np.mgrid[0:h:8, 0:w:8].astype(np.float64)
+        u, v = p["field"](gx, gy)
+        assert np.sqrt(u * u + v * v).max() == pytest.approx(p["field_params"]["peak"], rel=1e-9)
+        assert 0.5 <= p["field_params"]["peak"] <= 3.0
