@@ -104,84 +104,99 @@ __device__ __forceinline__ bool warp_inside(const Warp &w, int px0, int py0, int
 }
 
 // Quadratic inverse composition (icgn.wgsl:393-513): lifted 6x6 warp matrix
-// of the increment, pivoted Gauss-Jordan in binary32; row swaps are done by
-// predicated selects so the augmented matrix stays in registers.
-__device__ __forceinline__ bool compose_quadratic(Warp &w, const float (&d)[12]) {
+// of the increment, pivoted Gauss-Jordan in binary32 on the augmented 6x12
+// matrix [M | I].  The matrix is spread over a 16-lane segment of the warp,
+// lane e (< 12) holding column e, so no lane keeps more than six of its
+// entries: the pivot column is broadcast by shuffles, every lane applies
+// the row swap, the pivot-row division and the eliminations
+// m[r][e] = fma(-m[r][col], m[col][e], m[r][e]) to its own column.  Each
+// entry sees exactly the operations of the row-by-row elimination, so the
+// result is bitwise that of a single-thread elimination.  `sl` is the lane
+// index within the segment; `mask` names the lanes executing the call.
+__device__ __forceinline__ bool compose_quadratic(Warp &w, const float (&d)[12], int sl, unsigned mask) {
     const float u = d[0], ux = d[1], uy = d[2], v = d[3], vx = d[4], vy = d[5];
     const float uxx = d[6], uxy = d[7], uyy = d[8], vxx = d[9], vxy = d[10], vyy = d[11];
-    float m[6][12];
+    float L[6][6];
+    L[0][0] = fmaf(u, uxx, fmaf(ux, ux, 1.0f + 2.0f * ux));
+    L[0][1] = fmaf(2.0f * (1.0f + ux), uy, 2.0f * u * uxy);
+    L[0][2] = fmaf(u, uyy, uy * uy);
+    L[0][3] = 2.0f * u * (1.0f + ux);
+    L[0][4] = 2.0f * u * uy;
+    L[0][5] = u * u;
+    L[1][0] = 0.5f * fmaf(u, vxx, fmaf(2.0f * (1.0f + ux), vx, v * uxx));
+    L[1][1] = (fmaf(u, vxy, fmaf(v, uxy, fmaf(ux, vy, fmaf(uy, vx, 1.0f)))) + vy) + ux;
+    L[1][2] = 0.5f * fmaf(u, vyy, fmaf(2.0f * uy, 1.0f + vy, v * uyy));
+    L[1][3] = fmaf(u, vx, fmaf(v, ux, v));
+    L[1][4] = fmaf(u, vy, fmaf(v, uy, u));
+    L[1][5] = u * v;
+    L[2][0] = fmaf(v, vxx, vx * vx);
+    L[2][1] = fmaf(2.0f * vx, 1.0f + vy, 2.0f * v * vxy);
+    L[2][2] = fmaf(v, vyy, fmaf(vy, vy, 1.0f + 2.0f * vy));
+    L[2][3] = 2.0f * v * vx;
+    L[2][4] = 2.0f * v * (1.0f + vy);
+    L[2][5] = v * v;
+    L[3][0] = 0.5f * uxx; L[3][1] = uxy; L[3][2] = 0.5f * uyy;
+    L[3][3] = 1.0f + ux;  L[3][4] = uy;  L[3][5] = u;
+    L[4][0] = 0.5f * vxx; L[4][1] = vxy; L[4][2] = 0.5f * vyy;
+    L[4][3] = vx;         L[4][4] = 1.0f + vy; L[4][5] = v;
+    L[5][0] = 0.0f; L[5][1] = 0.0f; L[5][2] = 0.0f; L[5][3] = 0.0f; L[5][4] = 0.0f; L[5][5] = 1.0f;
+    const int e = sl < 12 ? sl : 11;  // lanes 12-15 shadow column 11
+    float c[6];
 #pragma unroll
-    for (int r = 0; r < 6; ++r)
+    for (int r = 0; r < 6; ++r) {
+        float x = (e - 6 == r) ? 1.0f : 0.0f;
 #pragma unroll
-        for (int e = 0; e < 12; ++e) m[r][e] = (e == 6 + r) ? 1.0f : 0.0f;
-    m[0][0] = fmaf(u, uxx, fmaf(ux, ux, 1.0f + 2.0f * ux));
-    m[0][1] = fmaf(2.0f * (1.0f + ux), uy, 2.0f * u * uxy);
-    m[0][2] = fmaf(u, uyy, uy * uy);
-    m[0][3] = 2.0f * u * (1.0f + ux);
-    m[0][4] = 2.0f * u * uy;
-    m[0][5] = u * u;
-    m[1][0] = 0.5f * fmaf(u, vxx, fmaf(2.0f * (1.0f + ux), vx, v * uxx));
-    m[1][1] = (fmaf(u, vxy, fmaf(v, uxy, fmaf(ux, vy, fmaf(uy, vx, 1.0f)))) + vy) + ux;
-    m[1][2] = 0.5f * fmaf(u, vyy, fmaf(2.0f * uy, 1.0f + vy, v * uyy));
-    m[1][3] = fmaf(u, vx, fmaf(v, ux, v));
-    m[1][4] = fmaf(u, vy, fmaf(v, uy, u));
-    m[1][5] = u * v;
-    m[2][0] = fmaf(v, vxx, vx * vx);
-    m[2][1] = fmaf(2.0f * vx, 1.0f + vy, 2.0f * v * vxy);
-    m[2][2] = fmaf(v, vyy, fmaf(vy, vy, 1.0f + 2.0f * vy));
-    m[2][3] = 2.0f * v * vx;
-    m[2][4] = 2.0f * v * (1.0f + vy);
-    m[2][5] = v * v;
-    m[3][0] = 0.5f * uxx; m[3][1] = uxy; m[3][2] = 0.5f * uyy;
-    m[3][3] = 1.0f + ux;  m[3][4] = uy;  m[3][5] = u;
-    m[4][0] = 0.5f * vxx; m[4][1] = vxy; m[4][2] = 0.5f * vyy;
-    m[4][3] = vx;         m[4][4] = 1.0f + vy; m[4][5] = v;
-    m[5][0] = 0.0f; m[5][1] = 0.0f; m[5][2] = 0.0f; m[5][3] = 0.0f; m[5][4] = 0.0f; m[5][5] = 1.0f;
+        for (int k = 0; k < 6; ++k)
+            if (e == k) x = L[r][k];
+        c[r] = x;
+    }
 #pragma unroll
     for (int col = 0; col < 6; ++col) {
+        float pc[6];  // pivot column before the swap
+#pragma unroll
+        for (int r = 0; r < 6; ++r) pc[r] = __shfl_sync(mask, c[r], col, 16);
         int prow = col;
-        float psize = fabsf(m[col][col]);
+        float psize = fabsf(pc[col]);
 #pragma unroll
         for (int cand = col + 1; cand < 6; ++cand) {
-            float cs = fabsf(m[cand][col]);
+            const float cs = fabsf(pc[cand]);
             if (cs > psize) { prow = cand; psize = cs; }
         }
         if (psize < 1e-8f) return false;
+        float pivot = pc[col];
 #pragma unroll
         for (int cand = col + 1; cand < 6; ++cand) {
             if (cand == prow) {
-#pragma unroll
-                for (int e = 0; e < 12; ++e) {
-                    float tmp = m[col][e];
-                    m[col][e] = m[cand][e];
-                    m[cand][e] = tmp;
-                }
+                const float t = c[col];
+                c[col] = c[cand];
+                c[cand] = t;
+                const float tp = pc[col];
+                pc[col] = pc[cand];
+                pc[cand] = tp;
+                pivot = pc[col];
             }
         }
-        const float pivot = m[col][col];
-#pragma unroll
-        for (int e = 0; e < 12; ++e) m[col][e] = m[col][e] / pivot;
+        c[col] = c[col] / pivot;
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
             if (r == col) continue;
-            const float f = m[r][col];
-#pragma unroll
-            for (int e = 0; e < 12; ++e) m[r][e] = fmaf(-f, m[col][e], m[r][e]);
+            c[r] = fmaf(-pc[r], c[col], c[r]);
         }
     }
+    // nu[k] = sum_e cu[e] m[e][6 + k] (ascending e), on lane 6 + k.
     const float cu[6] = {0.5f * w.c0, w.c1, 0.5f * w.c2, 1.0f + w.l0, w.l1, w.t0};
     const float cv[6] = {0.5f * w.c3, w.c4, 0.5f * w.c5, w.l2, 1.0f + w.l3, w.t1};
+    float au = 0.0f, av = 0.0f;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        au = fmaf(cu[r], c[r], au);
+        av = fmaf(cv[r], c[r], av);
+    }
     float nu[6], nv[6];
 #pragma unroll
-    for (int col = 0; col < 6; ++col) {
-        float au = 0.0f, av = 0.0f;
-#pragma unroll
-        for (int e = 0; e < 6; ++e) {
-            au = fmaf(cu[e], m[e][6 + col], au);
-            av = fmaf(cv[e], m[e][6 + col], av);
-        }
-        nu[col] = au;
-        nv[col] = av;
+    for (int k = 0; k < 6; ++k) {
+        nu[k] = __shfl_sync(mask, au, 6 + k, 16);
+        nv[k] = __shfl_sync(mask, av, 6 + k, 16);
     }
     w.c0 = 2.0f * nu[0]; w.c1 = nu[1]; w.c2 = 2.0f * nu[2];
     w.c3 = 2.0f * nv[0]; w.c4 = nv[1]; w.c5 = 2.0f * nv[2];
@@ -203,11 +218,13 @@ __device__ __forceinline__ float divergence_status(const SolveArgs &a, float cha
 
 // Gauss-Newton update from the reduced totals (icgn.wgsl:801-921).  Returns
 // the new status; modifies the warp on a successful composition.
+// Quadratic: `sl` / `mask` as for compose_quadratic; lane r of each 16-lane
+// segment forms row r of H^-1 r and the rows are exchanged by shuffles.
 template <int MODEL>
 __device__ __forceinline__ float gn_update(const SolveArgs &a, const float (&t)[SumCount<MODEL>::value],
                                            const float *__restrict__ md, const float *__restrict__ hi,
                                            float wsum, float half, unsigned it1, Warp &w,
-                                           float &prev_change, unsigned &stalled) {
+                                           float &prev_change, unsigned &stalled, int sl, unsigned mask) {
     constexpr int n = parameter_count(MODEL);
     // Totals layout: 0 sum g, 1 sum g^2, 2 sum f g, then J^T g.
     float jg[12];
@@ -241,17 +258,26 @@ __device__ __forceinline__ float gn_update(const SolveArgs &a, const float (&t)[
 #pragma unroll
         for (int k = 0; k < n; ++k)
             res[k] = fmaf(-ratio, fmaf(-mean_g, __ldg(md + sum_off + k), jg[k]), __ldg(md + 2 + k));
-#pragma unroll
-        for (int r = 0; r < n; ++r) {
+        if (MODEL == kModelQuadratic) {
+            const int row = sl < n ? sl : 0;
             float acc = 0.0f;
 #pragma unroll
-            for (int k = 0; k < n; ++k) acc = fmaf(__ldg(hi + r * n + k), res[k], acc);
-            delta[r] = -acc;
+            for (int k = 0; k < n; ++k) acc = fmaf(__ldg(hi + row * n + k), res[k], acc);
+#pragma unroll
+            for (int r = 0; r < n; ++r) delta[r] = -__shfl_sync(mask, acc, r, 16);
+        } else {
+#pragma unroll
+            for (int r = 0; r < n; ++r) {
+                float acc = 0.0f;
+#pragma unroll
+                for (int k = 0; k < n; ++k) acc = fmaf(__ldg(hi + r * n + k), res[k], acc);
+                delta[r] = -acc;
+            }
         }
     }
     float change;
     if (MODEL == kModelQuadratic) {
-        if (!compose_quadratic(w, delta)) return -1.0f;
+        if (!compose_quadratic(w, delta, sl, mask)) return -1.0f;
         change = 0.0f;
 #pragma unroll
         for (int p = 0; p < 9; ++p) {
@@ -337,6 +363,9 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int gla
     const int ldiv = LANES / S, lmod = LANES % S;
     const int col0 = glane % S, row0 = glane / S;
     const int W = a.W, H = a.H;
+    // Lanes that run the update together: the group's half warp for 16-lane
+    // groups (groups are uniform in `done`), else the whole warp.
+    const unsigned seg_mask = LANES == 16 ? (0xffffu << (lane_in_warp & 16)) : kFullMask;
 
     for (int it = 0; it < 30; ++it) {
         if (!done) {
@@ -410,7 +439,8 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int gla
         else reduce_warp<LANES, N>(s, lane_in_warp);
         if (!done) {
             iters = (float)(it + 1);
-            status = gn_update<MODEL>(a, s, md, hi, wsum, half, (unsigned)(it + 1), w, prev_change, stalled);
+            status = gn_update<MODEL>(a, s, md, hi, wsum, half, (unsigned)(it + 1), w, prev_change, stalled,
+                                      lane_in_warp & 15, seg_mask);
         }
     }
     if (a.iteration_total != nullptr && exists && glane == 0 && iters > 0.0f)
@@ -430,7 +460,7 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int gla
 }
 
 template <int MODEL, int INTERP, int LANES, bool GAUSS>
-__global__ void __launch_bounds__(128) icgn_kernel(SolveArgs a) {
+__global__ void __launch_bounds__(128, MODEL == kModelQuadratic ? 5 : 1) icgn_kernel(SolveArgs a) {
     constexpr bool kBlock = LANES > 32;
     constexpr int kUnitThreads = kBlock ? 128 : 32;
     constexpr int kGroups = kUnitThreads / LANES;
