@@ -195,6 +195,33 @@ int gbdic_register_noalloc(const gbdic_noalloc_frame *frame, float *device_state
  * median_filter_seed entry (repaired windows become status 0). */
 int gbdic_apply_uod(gbdic_engine *engine, const float *state_in, int32_t seed_mode, float *state_out);
 
+/* ICGNWGPU.affine_frontier_seeds (wgpu_backend.py:2671-2771,
+ * spatial_seed.wgsl:268-309): for every permitted, not yet accepted subset,
+ * the component-wise median of its accepted 3x3 neighbours' first-order
+ * affine transports.  `states` holds grid*8 floats ([tx,ux,uy,ty],[vx,vy,
+ * accepted 0/1, 0]); `permissions` one word per subset (bits 0-8 = 3x3
+ * neighbourhood, bit 4 = the subset itself usable).  Writes grid*8 seed
+ * floats (zero where no seed) and grid activity bytes. */
+int gbdic_affine_frontier(gbdic_engine *engine, const float *states, const uint32_t *permissions,
+                          float *out_seeds, uint8_t *out_active);
+
+typedef struct {
+    int32_t sample_step;        /* every k-th pixel of the window in x and y */
+    float min_gain;             /* best ZNCC must beat the own hypothesis by this */
+    float min_displacement;     /* ... and move the seed by more than this (px) */
+    int32_t failed_only;        /* score only subsets whose status < 0.5 */
+    int32_t candidate_mode;     /* 0 neighbours, 1 neighbour median only, 2 both */
+} gbdic_choose_cfg;
+
+/* Translation seed selection (spatial_seed.wgsl:65-190, `choose`): ZNCC of
+ * up to 11 hypotheses (own, prior, 8 neighbours, neighbour median) on the
+ * last registered target.  `states` / `prior` (NULL: zero hypothesis) as for
+ * gbdic_affine_frontier.  Writes grid*8 seed floats for improved subsets,
+ * grid*4 score floats (own rho, best rho, improved, 0) and activity bytes. */
+int gbdic_spatial_choose(gbdic_engine *engine, const float *states, const float *prior,
+                         const uint32_t *permissions, const gbdic_choose_cfg *cfg, float *out_seeds,
+                         float *out_scores, uint8_t *out_active);
+
 /* --------------------------------------------------------- full pyramid */
 
 /* ICGNWGPUFullPyramid(...) (full_pyramid_backend.py:202-431). */

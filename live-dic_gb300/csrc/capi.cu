@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "engine.h"
 
@@ -383,6 +384,107 @@ int gbdic_apply_uod(gbdic_engine *e, const float *state_in, int32_t seed_mode, f
         }
         check_cuda(cudaMemcpyAsync(state_out, slot.filtered.get(), bytes, cudaMemcpyDeviceToHost, s), "state readback");
         check_cuda(cudaStreamSynchronize(s), "UOD");
+    });
+}
+
+namespace {
+
+// Device copies of a host snapshot / permission table for the spatial seed
+// kernels, and the activity readback.
+struct SpatialBuffers {
+    gbdic::DeviceBuffer snapshot, prior, permissions, seeds, scores, active;
+    void load(int count, const float *states, const float *prior_states, const uint32_t *perms, cudaStream_t s) {
+        snapshot.ensure((size_t)count * 8 * sizeof(float));
+        permissions.ensure((size_t)count * sizeof(uint32_t));
+        seeds.ensure((size_t)count * 8 * sizeof(float));
+        scores.ensure((size_t)count * 4 * sizeof(float));
+        active.ensure((size_t)count * sizeof(uint32_t));
+        check_cuda(cudaMemcpyAsync(snapshot.get(), states, (size_t)count * 8 * sizeof(float), cudaMemcpyHostToDevice, s),
+                   "snapshot upload");
+        check_cuda(cudaMemcpyAsync(permissions.get(), perms, (size_t)count * sizeof(uint32_t), cudaMemcpyHostToDevice, s),
+                   "permission upload");
+        if (prior_states) {
+            prior.ensure((size_t)count * 8 * sizeof(float));
+            check_cuda(cudaMemcpyAsync(prior.get(), prior_states, (size_t)count * 8 * sizeof(float),
+                                       cudaMemcpyHostToDevice, s), "prior upload");
+        }
+        check_cuda(cudaMemsetAsync(seeds.get(), 0, (size_t)count * 8 * sizeof(float), s), "clear");
+        check_cuda(cudaMemsetAsync(scores.get(), 0, (size_t)count * 4 * sizeof(float), s), "clear");
+        check_cuda(cudaMemsetAsync(active.get(), 0, (size_t)count * sizeof(uint32_t), s), "clear");
+    }
+    void read(int count, float *out_seeds, float *out_scores, uint8_t *out_active, cudaStream_t s) {
+        std::vector<uint32_t> act((size_t)count);
+        if (out_seeds)
+            check_cuda(cudaMemcpyAsync(out_seeds, seeds.get(), (size_t)count * 8 * sizeof(float), cudaMemcpyDeviceToHost, s),
+                       "seed readback");
+        if (out_scores)
+            check_cuda(cudaMemcpyAsync(out_scores, scores.get(), (size_t)count * 4 * sizeof(float), cudaMemcpyDeviceToHost,
+                                       s), "score readback");
+        check_cuda(cudaMemcpyAsync(act.data(), active.get(), (size_t)count * sizeof(uint32_t), cudaMemcpyDeviceToHost, s),
+                   "activity readback");
+        check_cuda(cudaStreamSynchronize(s), "spatial seeds");
+        if (out_active)
+            for (int i = 0; i < count; ++i) out_active[i] = act[(size_t)i] ? 1 : 0;
+    }
+};
+
+}  // namespace
+
+int gbdic_affine_frontier(gbdic_engine *e, const float *states, const uint32_t *permissions, float *out_seeds,
+                          uint8_t *out_active) {
+    return guarded(e, [&] {
+        e->require_ready("affine_frontier_seeds");
+        if (!states || !permissions) fail(GBDIC_EINVAL, "states and permissions are required");
+        if (e->rt->opts().o.motion_model != GBDIC_MODEL_AFFINE)
+            fail(GBDIC_EINVAL, "affine_frontier_seeds requires motion_model='affine'");
+        auto &lvl = e->level;
+        cudaStream_t s = e->rt->stream();
+        SpatialBuffers b;
+        b.load(lvl.count, states, nullptr, permissions, s);
+        gbdic::FrontierArgs a{};
+        a.snapshot = b.snapshot.as<float>();
+        a.permissions = b.permissions.as<uint32_t>();
+        a.seeds = b.seeds.as<float>();
+        a.active = b.active.as<uint32_t>();
+        a.count = lvl.count; a.grid_w = lvl.gw; a.stride = e->rt->opts().o.subset_stride;
+        check_cuda(gbdic::launch_affine_frontier(a, s), "affine frontier launch");
+        b.read(lvl.count, out_seeds, nullptr, out_active, s);
+    });
+}
+
+int gbdic_spatial_choose(gbdic_engine *e, const float *states, const float *prior, const uint32_t *permissions,
+                         const gbdic_choose_cfg *cfg, float *out_seeds, float *out_scores, uint8_t *out_active) {
+    return guarded(e, [&] {
+        e->require_ready("spatial seed selection");
+        if (!states || !permissions || !cfg) fail(GBDIC_EINVAL, "states, permissions and cfg are required");
+        if (cfg->sample_step < 1 || cfg->sample_step > e->rt->opts().o.subset_size)
+            fail(GBDIC_EINVAL, "sample_step must be in [1, subset_size]");
+        if (cfg->candidate_mode < 0 || cfg->candidate_mode > 2) fail(GBDIC_EINVAL, "candidate_mode must be 0, 1 or 2");
+        if (!(cfg->min_gain >= 0.0f) || !(cfg->min_displacement >= 0.0f))
+            fail(GBDIC_EINVAL, "min_gain and min_displacement must be non-negative");
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        if (!lvl.ref_image.get())
+            fail(GBDIC_ESTATE, "spatial seed selection needs a reference prepared by set_reference()");
+        cudaStream_t s = e->rt->stream();
+        SpatialBuffers b;
+        b.load(lvl.count, states, prior, permissions, s);
+        gbdic::ChooseArgs a{};
+        a.ref = lvl.ref_image.as<uint8_t>();
+        a.tgt = slot.frame.as<uint8_t>();
+        a.snapshot = b.snapshot.as<float>();
+        a.prior = prior ? b.prior.as<float>() : nullptr;
+        a.permissions = b.permissions.as<uint32_t>();
+        a.seeds = b.seeds.as<float>();
+        a.scores = b.scores.as<float>();
+        a.active = b.active.as<uint32_t>();
+        a.W = lvl.W; a.H = lvl.H; a.grid_w = lvl.gw; a.count = lvl.count;
+        a.S = e->rt->opts().o.subset_size; a.stride = e->rt->opts().o.subset_stride;
+        a.sample_step = cfg->sample_step;
+        a.min_gain = cfg->min_gain; a.min_displacement = cfg->min_displacement;
+        a.failed_only = cfg->failed_only ? 1 : 0; a.candidate_mode = cfg->candidate_mode;
+        check_cuda(gbdic::launch_spatial_choose(a, s), "spatial choose launch");
+        b.read(lvl.count, out_seeds, out_scores, out_active, s);
     });
 }
 

@@ -114,6 +114,30 @@ struct SearchArgs {
 size_t zncc_search_smem(int S, int radius);
 cudaError_t launch_zncc_search(const SearchArgs &a, cudaStream_t stream);
 
+// ------------------------------------------------------------ spatial seeds
+struct FrontierArgs {
+    const float *snapshot;        // states, 8 floats per subset
+    const uint32_t *permissions;  // 3x3 bits, bit 4 = own
+    float *seeds;                 // written for new frontier subsets
+    uint32_t *active;             // set to 1 for new frontier subsets
+    int count, grid_w, stride;
+};
+cudaError_t launch_affine_frontier(const FrontierArgs &a, cudaStream_t stream);
+
+struct ChooseArgs {
+    const uint8_t *ref, *tgt;     // reference and target bytes (W*H)
+    const float *snapshot;        // states, 8 floats per subset
+    const float *prior;           // prior states, or nullptr (zero hypothesis)
+    const uint32_t *permissions;
+    float *seeds;                 // written for improved subsets
+    float *scores;                // (own rho, best rho, improved, 0) per permitted subset
+    uint32_t *active;             // set to 1 for improved subsets
+    int W, H, grid_w, count, S, stride, sample_step;
+    float min_gain, min_displacement;
+    int failed_only, candidate_mode;  // candidate_mode 0 neighbours, 1 median only, 2 both
+};
+cudaError_t launch_spatial_choose(const ChooseArgs &a, cudaStream_t stream);
+
 struct TemporalArgs {
     float *history;           // fine accepted history
     uint32_t *ages;

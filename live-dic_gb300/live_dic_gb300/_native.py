@@ -122,6 +122,16 @@ class BatchJob(C.Structure):
 
 BATCH_PERSISTENT, BATCH_PER_JOB = 0, 1
 
+
+class ChooseCfg(C.Structure):
+    _fields_ = [
+        ("sample_step", C.c_int32),
+        ("min_gain", C.c_float),
+        ("min_displacement", C.c_float),
+        ("failed_only", C.c_int32),
+        ("candidate_mode", C.c_int32),
+    ]
+
 P = C.c_void_p
 I32, I64 = C.c_int32, C.c_int64
 _SIGNATURES = {
@@ -168,6 +178,8 @@ _SIGNATURES = {
     "gbdic_batch_load_device": (C.c_int, [P, I32, P, I64, P]),
     "gbdic_batch_run_device": (C.c_int, [P, P, I32, C.POINTER(Timing)]),
     "gbdic_batch_export": (C.c_int, [P, I32, I32, P, I64]),
+    "gbdic_affine_frontier": (C.c_int, [P, P, P, P, P]),
+    "gbdic_spatial_choose": (C.c_int, [P, P, P, P, C.POINTER(ChooseCfg), P, P, P]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 

@@ -251,6 +251,7 @@ class ICGNWGPU:
         self.execution_device_type = "gpu"
         self.width = self.height = self.grid_width = self.grid_height = 0
         self._reference_ready = False
+        self._target_ready = False
         self._config: dict[str, float | int] = {"iterations": 30, "tolerance": 1e-3, "znccMin": 0.8}
         self.roi = None
         self.reference_valid = None
@@ -381,6 +382,7 @@ class ICGNWGPU:
             selected = np.ascontiguousarray(roi.selected, dtype=np.uint8).ravel()
             links = np.ascontiguousarray(roi.links_table(self.median_filter_size, self.outlier_policy))
         self._reference_ready = False
+        self._target_ready = False
         info = _native.RefInfo()
         prep_start = time.perf_counter()
         self._check(
@@ -546,12 +548,118 @@ class ICGNWGPU:
                 _native.ptr(packed), C.byref(timing),
             )
         )
+        self._target_ready = True
         times = self._timing(timing)
         times["totalWallMs"] = (time.perf_counter() - started) * 1e3
         result = self._result(packed, times, self._config)
         if include_zncc:
             self._attach_final_zncc(result)
         return result
+
+    # ------------------------------------------------------------ spatial seeds
+    def _spatial_permissions(self) -> tuple[np.ndarray, np.ndarray]:
+        """(usable windows, 3x3 permission words) as the reference builds them
+        for its spatial-seed passes (wgpu_backend.py:2696-2711)."""
+        shape = (self.grid_height, self.grid_width)
+        valid = np.asarray(self.reference_valid, dtype=bool).copy()
+        if self.roi is not None:
+            valid &= self.roi.selected
+        permissions = np.zeros(shape, dtype=np.uint32)
+        padded = np.pad(valid, 1)
+        for dy in range(-1, 2):
+            for dx in range(-1, 2):
+                neighbour = padded[1 + dy: 1 + dy + shape[0], 1 + dx: 1 + dx + shape[1]]
+                permissions |= (valid & neighbour).astype(np.uint32) << ((dy + 1) * 3 + dx + 1)
+        if self.roi is not None:
+            permissions &= np.asarray(self.roi.neighbour_bits, dtype=np.uint32)
+        return valid, permissions
+
+    def _spatial_inputs(self, parameters: Any, accepted: Any, what: str) -> tuple[np.ndarray, np.ndarray]:
+        if not self._reference_ready:
+            raise ICGNError(f"Call set_reference() before {what}().")
+        shape = (self.grid_height, self.grid_width)
+        values = np.asarray(parameters, dtype=np.float32)
+        mask = np.asarray(accepted)
+        if values.shape != (*shape, 6):
+            raise ValueError(f"parameters must have shape {(*shape, 6)}")
+        if mask.shape != shape or mask.dtype != np.bool_:
+            raise ValueError(f"accepted must be a Boolean array with shape {shape}")
+        if not np.isfinite(values[mask]).all():
+            raise ValueError("accepted parameters must be finite")
+        return values, mask
+
+    def affine_frontier_seeds(self, parameters: Any, accepted: Any) -> tuple[np.ndarray, np.ndarray]:
+        """Median first-order transports of accepted affine neighbours onto
+        the next frontier (wgpu_backend.py:2671-2771).  Returns seeds
+        (grid_h, grid_w, 6) and the Boolean frontier; these are guesses for
+        register_seeded, not accepted results."""
+        values, mask = self._spatial_inputs(parameters, accepted, "affine_frontier_seeds")
+        if self.motion_model != "affine":
+            raise ValueError("affine_frontier_seeds requires motion_model='affine'")
+        shape = (self.grid_height, self.grid_width)
+        valid, permissions = self._spatial_permissions()
+        accepted_valid = mask & valid
+        packed = np.zeros((*shape, 8), dtype=np.float32)
+        packed[..., :6] = np.where(accepted_valid[..., None], values, 0)
+        packed[..., 6] = accepted_valid
+        seeds = np.zeros((*shape, 8), dtype=np.float32)
+        active = np.zeros(shape, dtype=np.uint8)
+        permissions = np.ascontiguousarray(permissions)
+        self._check(self._lib.gbdic_affine_frontier(self._handle, _native.ptr(packed), _native.ptr(permissions),
+                                                    _native.ptr(seeds), _native.ptr(active)))
+        return seeds[..., :6].copy(), active.astype(bool)
+
+    _CANDIDATE_MODES = {"neighbours": 0, "median": 1, "neighbours+median": 2}
+
+    def spatial_seed_candidates(
+        self,
+        parameters: Any,
+        accepted: Any,
+        *,
+        prior: Any = None,
+        sample_step: int = 1,
+        min_gain: float = 0.0,
+        min_displacement: float = 0.0,
+        failed_only: bool = False,
+        candidate_mode: str = "neighbours",
+    ) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """Translation seed selection on the target of the last register()
+        (spatial_seed.wgsl:65-190, `choose`): ZNCC of the own translation, the
+        prior's, the 3x3 neighbours' and/or their median, every
+        `sample_step`-th pixel, bilinear target.  Returns (seeds (gh, gw, 6)
+        for improved subsets, the Boolean improved mask, scores (gh, gw, 2):
+        own and best ZNCC, 0 where not scored)."""
+        values, mask = self._spatial_inputs(parameters, accepted, "spatial_seed_candidates")
+        if not self._target_ready:
+            raise ICGNError("Call register() before spatial_seed_candidates().")
+        if candidate_mode not in self._CANDIDATE_MODES:
+            raise ValueError(f"candidate_mode must be one of {tuple(self._CANDIDATE_MODES)}")
+        if isinstance(sample_step, bool) or not 1 <= int(sample_step) <= self.subset_size:
+            raise ValueError("sample_step must be an integer in [1, subset_size]")
+        if not (float(min_gain) >= 0.0 and float(min_displacement) >= 0.0):
+            raise ValueError("min_gain and min_displacement must be non-negative")
+        shape = (self.grid_height, self.grid_width)
+        _, permissions = self._spatial_permissions()
+        packed = np.zeros((*shape, 8), dtype=np.float32)
+        packed[..., :6] = np.nan_to_num(values, nan=0.0, posinf=0.0, neginf=0.0)
+        packed[..., 6] = mask
+        prior_packed = None
+        if prior is not None:
+            pv = np.asarray(prior, dtype=np.float32)
+            if pv.shape != (*shape, 6):
+                raise ValueError(f"prior must have shape {(*shape, 6)}")
+            prior_packed = np.zeros((*shape, 8), dtype=np.float32)
+            prior_packed[..., :6] = pv
+        cfg = _native.ChooseCfg(int(sample_step), float(min_gain), float(min_displacement), int(bool(failed_only)),
+                                self._CANDIDATE_MODES[candidate_mode])
+        seeds = np.zeros((*shape, 8), dtype=np.float32)
+        scores = np.zeros((*shape, 4), dtype=np.float32)
+        active = np.zeros(shape, dtype=np.uint8)
+        permissions = np.ascontiguousarray(permissions)
+        self._check(self._lib.gbdic_spatial_choose(self._handle, _native.ptr(packed), _native.ptr(prior_packed),
+                                                   _native.ptr(permissions), C.byref(cfg), _native.ptr(seeds),
+                                                   _native.ptr(scores), _native.ptr(active)))
+        return seeds[..., :6].copy(), active.astype(bool), scores[..., :2].copy()
 
     @_exclusive_call
     def register_seeded(
@@ -600,6 +708,7 @@ class ICGNWGPU:
                 C.byref(self._cfg(self._config)), _native.ptr(packed), C.byref(timing),
             )
         )
+        self._target_ready = True
         times = self._timing(timing)
         times["totalWallMs"] = (time.perf_counter() - started) * 1e3
         result = self._result(packed, times, self._config)

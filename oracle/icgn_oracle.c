@@ -15,6 +15,8 @@
  *   - full_pyramid.wgsl:251-435 coarse-to-fine seed transfer
  *   - full_pyramid.wgsl:83-148,437-575 temporal projection / merge / velocity
  *   - affine_zncc.wgsl:57-99 final ZNCC of a converged affine warp
+ *   - spatial_seed.wgsl:40-52,65-190,268-309 translation hypothesis scoring
+ *     (choose) and the affine frontier transport
  *
  * Rounding contract (shared with the CUDA kernels, which are written
  * independently to the same contract): every float operation is a single
@@ -1036,6 +1038,161 @@ void oracle_final_zncc(int W, int H, int grid_w, int grid_h, int S, int st, int 
             out[index] = fminf(fmaxf(r, -1.0f), 1.0f);
         } else {
             out[index] = -2.0f;
+        }
+    }
+}
+
+/* ------------------------------------------------------------ spatial seeds */
+
+/* spatial_seed.wgsl:40-52: insertion sort, mean of the two middle values. */
+static float spatial_median(float *v, int n) {
+    for (int i = 1; i < n; ++i) {
+        float value = v[i];
+        int j = i;
+        while (j > 0 && !(v[j - 1] <= value)) {
+            v[j] = v[j - 1];
+            --j;
+        }
+        v[j] = value;
+    }
+    return 0.5f * (v[(n - 1) / 2] + v[n / 2]);
+}
+
+/* spatial_seed.wgsl:268-309 affine_frontier.  states / seeds: 8 floats per
+ * subset; active receives 1 for every new frontier subset. */
+void oracle_affine_frontier(int count, int grid_w, int stride, const float *snap, const uint32_t *perms,
+                            float *seeds, uint32_t *active) {
+    const int gh = count / grid_w;
+    for (int index = 0; index < count; ++index) {
+        if ((perms[index] & 16u) == 0u) continue;
+        if (snap[8 * index + 6] >= 0.5f) continue;
+        int gx = index % grid_w, gy = index / grid_w;
+        float t0[9], g0[9], g1[9], t1[9], g2[9], g3[9];
+        int n = 0;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                if (dx == 0 && dy == 0) continue;
+                int x = gx + dx, y = gy + dy, bit = (dy + 1) * 3 + dx + 1;
+                if (x < 0 || y < 0 || x >= grid_w || y >= gh || (perms[index] & (1u << bit)) == 0u) continue;
+                int nb = y * grid_w + x;
+                const float *p = snap + 8 * nb;
+                if ((perms[nb] & 16u) == 0u || p[6] != 1.0f) continue;
+                float ddx = (float)(-dx) * (float)stride, ddy = (float)(-dy) * (float)stride;
+                t0[n] = p[0] + (p[1] * ddx + p[2] * ddy);
+                t1[n] = p[3] + (p[4] * ddx + p[5] * ddy);
+                g0[n] = p[1]; g1[n] = p[2]; g2[n] = p[4]; g3[n] = p[5];
+                ++n;
+            }
+        if (n == 0) continue;
+        float *d = seeds + 8 * index;
+        d[0] = spatial_median(t0, n); d[1] = spatial_median(g0, n);
+        d[2] = spatial_median(g1, n); d[3] = spatial_median(t1, n);
+        d[4] = spatial_median(g2, n); d[5] = spatial_median(g3, n);
+        d[6] = 0.0f; d[7] = 0.0f;
+        active[index] = 1u;
+    }
+}
+
+static float unorm8(uint8_t b) { return (float)b / 255.0f; }
+
+static float spatial_linear(const uint8_t *img, int W, float x, float y) {
+    float fx = floorf(x), fy = floorf(y);
+    int ix = (int)fx, iy = (int)fy;
+    float tx = x - fx, ty = y - fy;
+    const uint8_t *r0 = img + (size_t)iy * W + ix, *r1 = r0 + W;
+    float a = unorm8(r0[0]), b = unorm8(r0[1]), c = unorm8(r1[0]), e = unorm8(r1[1]);
+    float top = a * (1.0f - tx) + b * tx;
+    float bottom = c * (1.0f - tx) + e * tx;
+    return 255.0f * (top * (1.0f - ty) + bottom * ty) - 128.0f;
+}
+
+/* spatial_seed.wgsl:65-190 choose (no score cache): 64 lane-strided partial
+ * sums per hypothesis and the halving pairwise tree. */
+void oracle_spatial_choose(const uint8_t *ref, const uint8_t *tgt, int W, int H, int grid_w, int count, int S,
+                           int stride, int sample_step, float min_gain, float min_displacement, int failed_only,
+                           int candidate_mode, const float *snap, const float *prior, const uint32_t *perms,
+                           float *seeds, float *scores, uint32_t *active) {
+    const int gh = count / grid_w;
+    #pragma omp parallel for schedule(dynamic, 16)
+    for (int index = 0; index < count; ++index) {
+        uint32_t perm = perms[index];
+        if ((perm & 16u) == 0u) continue;
+        if (failed_only && snap[8 * index + 6] >= 0.5f) continue;
+        int gx = index % grid_w, gy = index / grid_w;
+        float ownx = snap[8 * index + 0], owny = snap[8 * index + 3];
+        float cand[11][3];
+        for (int k = 0; k < 11; ++k) cand[k][0] = cand[k][1] = cand[k][2] = 0.0f;
+        cand[0][0] = ownx; cand[0][1] = owny; cand[0][2] = 1.0f;
+        cand[1][0] = prior ? prior[8 * index + 0] : 0.0f;
+        cand[1][1] = prior ? prior[8 * index + 3] : 0.0f;
+        cand[1][2] = 1.0f;
+        float us[9], vs[9];
+        int n = 0, slot = 2;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                int bit = (dy + 1) * 3 + dx + 1, x = gx + dx, y = gy + dy;
+                int inside = x >= 0 && y >= 0 && x < grid_w && y < gh;
+                if (inside && (perm & (1u << bit)) != 0u) {
+                    int nb = y * grid_w + x;
+                    if ((perms[nb] & 16u) != 0u) {
+                        float px = snap[8 * nb + 0], py = snap[8 * nb + 3];
+                        if ((dx != 0 || dy != 0) && candidate_mode != 1) {
+                            cand[slot][0] = px; cand[slot][1] = py; cand[slot][2] = 1.0f;
+                        }
+                        if (snap[8 * nb + 6] >= 0.5f) { us[n] = px; vs[n] = py; ++n; }
+                    }
+                }
+                if (dx != 0 || dy != 0) ++slot;
+            }
+        if (candidate_mode != 0 && n > 0) {
+            cand[10][0] = spatial_median(us, n); cand[10][1] = spatial_median(vs, n); cand[10][2] = 1.0f;
+        }
+        float bx = ownx, by = owny, brho = -2.0f, bown = -2.0f;
+        float ox = (float)(gx * stride), oy = (float)(gy * stride);
+        int side = (S + sample_step - 1) / sample_step, total = side * side;
+        float ftotal = (float)total;
+        for (int k = 0; k < 11; ++k) {
+            float cx = cand[k][0], cy = cand[k][1];
+            float minx = ox + cx, miny = oy + cy;
+            float maxx = minx + (float)(S - 1), maxy = miny + (float)(S - 1);
+            if (cand[k][2] == 0.0f || !(fabsf(cx) <= 1e12f && fabsf(cy) <= 1e12f) || minx < 2.0f || miny < 2.0f ||
+                maxx > (float)(W - 3) || maxy > (float)(H - 3))
+                continue;
+            float sx[64], sy[64], sz[64], sw[64], sg[64];
+            for (int lane = 0; lane < 64; ++lane) {
+                float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f, g2 = 0.0f;
+                for (int pixel = lane; pixel < total; pixel += 64) {
+                    float offx = (float)(pixel % side) * (float)sample_step;
+                    float offy = (float)(pixel / side) * (float)sample_step;
+                    int rx = (int)(ox + offx), ry = (int)(oy + offy);
+                    float f = 255.0f * unorm8(ref[(size_t)ry * W + rx]) - 128.0f;
+                    float g = spatial_linear(tgt, W, (ox + offx) + cx, (oy + offy) + cy);
+                    a0 = a0 + f; a1 = a1 + g; a2 = a2 + f * g; a3 = a3 + f * f; g2 = g2 + g * g;
+                }
+                sx[lane] = a0; sy[lane] = a1; sz[lane] = a2; sw[lane] = a3; sg[lane] = g2;
+            }
+            for (int off = 32; off > 0; off >>= 1)
+                for (int lane = 0; lane < off; ++lane) {
+                    sx[lane] = sx[lane] + sx[lane + off]; sy[lane] = sy[lane] + sy[lane + off];
+                    sz[lane] = sz[lane] + sz[lane + off]; sw[lane] = sw[lane] + sw[lane + off];
+                    sg[lane] = sg[lane] + sg[lane + off];
+                }
+            float vf = fmaxf(0.0f, sw[0] - sx[0] * sx[0] / ftotal);
+            float vg = fmaxf(0.0f, sg[0] - sy[0] * sy[0] / ftotal);
+            float rho = -2.0f;
+            if (vf > 1e-9f && vg > 1e-9f) rho = (sz[0] - sx[0] * sy[0] / ftotal) / sqrtf(vf * vg);
+            if (k == 0) bown = rho;
+            if (rho > brho) { bx = cx; by = cy; brho = rho; }
+        }
+        float ddx = bx - ownx, ddy = by - owny;
+        int improved = brho > bown + min_gain && sqrtf(ddx * ddx + ddy * ddy) > min_displacement;
+        scores[4 * index + 0] = bown; scores[4 * index + 1] = brho;
+        scores[4 * index + 2] = improved ? 1.0f : 0.0f; scores[4 * index + 3] = 0.0f;
+        if (improved) {
+            float *d = seeds + 8 * index;
+            d[0] = bx; d[1] = 0.0f; d[2] = 0.0f; d[3] = by;
+            d[4] = d[5] = d[6] = d[7] = 0.0f;
+            active[index] = 1u;
         }
     }
 }

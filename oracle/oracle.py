@@ -258,3 +258,38 @@ def final_zncc(image, coef, plane, state, *, subset_size, subset_stride, interpo
         _p(np.ascontiguousarray(state, dtype=np.float32)), _p(out),
     )
     return out
+
+
+def affine_frontier(states: np.ndarray, permissions: np.ndarray, *, subset_stride: int) -> tuple[np.ndarray, np.ndarray]:
+    """spatial_seed.wgsl affine_frontier on a (gh, gw, 8) snapshot; returns
+    (seeds (gh, gw, 8), activity (gh, gw) bool)."""
+    snap = np.ascontiguousarray(states, dtype=np.float32)
+    gh, gw = snap.shape[:2]
+    perms = np.ascontiguousarray(permissions, dtype=np.uint32)
+    seeds = np.zeros((gh, gw, 8), np.float32)
+    active = np.zeros((gh, gw), np.uint32)
+    lib().oracle_affine_frontier(gh * gw, gw, subset_stride, _p(snap), _p(perms, C.c_uint32), _p(seeds),
+                                 _p(active, C.c_uint32))
+    return seeds, active.astype(bool)
+
+
+def spatial_choose(reference: np.ndarray, target: np.ndarray, states: np.ndarray, permissions: np.ndarray, *,
+                   subset_size: int, subset_stride: int, prior: np.ndarray | None = None, sample_step: int = 1,
+                   min_gain: float = 0.0, min_displacement: float = 0.0, failed_only: bool = False,
+                   candidate_mode: int = 0) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """spatial_seed.wgsl choose; returns (seeds (gh, gw, 8), activity, scores (gh, gw, 4))."""
+    ref = np.ascontiguousarray(reference, dtype=np.uint8)
+    tgt = np.ascontiguousarray(target, dtype=np.uint8)
+    h, w = ref.shape
+    snap = np.ascontiguousarray(states, dtype=np.float32)
+    gh, gw = snap.shape[:2]
+    perms = np.ascontiguousarray(permissions, dtype=np.uint32)
+    pri = None if prior is None else np.ascontiguousarray(prior, dtype=np.float32)
+    seeds = np.zeros((gh, gw, 8), np.float32)
+    scores = np.zeros((gh, gw, 4), np.float32)
+    active = np.zeros((gh, gw), np.uint32)
+    lib().oracle_spatial_choose(
+        _p(ref, C.c_uint8), _p(tgt, C.c_uint8), w, h, gw, gh * gw, subset_size, subset_stride, sample_step,
+        C.c_float(min_gain), C.c_float(min_displacement), int(failed_only), candidate_mode, _p(snap), _p(pri),
+        _p(perms, C.c_uint32), _p(seeds), _p(scores), _p(active, C.c_uint32))
+    return seeds, active.astype(bool), scores
