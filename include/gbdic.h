@@ -137,9 +137,10 @@ int gbdic_register_seeded(gbdic_engine *engine, const uint8_t *frame, int64_t ro
                           const gbdic_solver_cfg *cfg, float *out_state, gbdic_timing *timing);
 
 /* ICGNWGPU._retry_seeded (wgpu_backend.py:1893-1949): re-solve active
- * subsets on the resident target, keeping inactive subsets' last raw state,
- * then UOD. */
-int gbdic_retry_seeded(gbdic_engine *engine, const float *seed_state, const uint32_t *active,
+ * subsets on the target resident in `slot` (0 after gbdic_register; a
+ * retired stream slot before its next submit), keeping inactive subsets'
+ * last raw state, then UOD. */
+int gbdic_retry_seeded(gbdic_engine *engine, int32_t slot, const float *seed_state, const uint32_t *active,
                        const gbdic_solver_cfg *cfg, float *out_state, gbdic_timing *timing);
 
 /* ICGNWGPU._final_affine_zncc (wgpu_backend.py:2843-2890, affine_zncc.wgsl):

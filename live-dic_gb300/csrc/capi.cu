@@ -262,15 +262,17 @@ int gbdic_register_seeded(gbdic_engine *e, const uint8_t *frame, int64_t row_str
     });
 }
 
-int gbdic_retry_seeded(gbdic_engine *e, const float *seed_state, const uint32_t *active, const gbdic_solver_cfg *cfg,
-                       float *out_state, gbdic_timing *timing) {
+int gbdic_retry_seeded(gbdic_engine *e, int32_t slot_index, const float *seed_state, const uint32_t *active,
+                       const gbdic_solver_cfg *cfg, float *out_state, gbdic_timing *timing) {
     return guarded(e, [&] {
         e->require_ready("retry_seeded");
         gbdic::validate_cfg(cfg);
+        e->check_slot(slot_index);
         if (!seed_state || !active) fail(GBDIC_EINVAL, "seed_state and active are required");
+        if (e->host[slot_index].pending) fail(GBDIC_ESTATE, "slot is still in flight; retire it first");
         auto &lvl = e->level;
-        auto &slot = *lvl.slots[0];
-        auto &h = e->host[0];
+        auto &slot = *lvl.slots[slot_index];
+        auto &h = e->host[slot_index];
         const auto s = e->rt->stream();
         h.submitted = std::chrono::steady_clock::now();
         const size_t sb = (size_t)lvl.count * gbdic::state_stride(e->rt->opts().o.motion_model) * sizeof(float);
@@ -279,8 +281,8 @@ int gbdic_retry_seeded(gbdic_engine *e, const float *seed_state, const uint32_t 
                    "activity upload");
         h.upload_ms = gbdic::ms_since(h.submitted);
         const auto t_exec = std::chrono::steady_clock::now();
-        enqueue_frame(e, 0, *cfg, true, true, false);
-        readback(e, 0, out_state, timing, t_exec);
+        enqueue_frame(e, slot_index, *cfg, true, true, false);
+        readback(e, slot_index, out_state, timing, t_exec);
     });
 }
 

@@ -143,7 +143,7 @@ _SIGNATURES = {
     "gbdic_set_reference_arrays": (C.c_int, [P, I32, I32, P, P, P, P, C.POINTER(RefInfo)]),
     "gbdic_register": (C.c_int, [P, P, I64, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),
     "gbdic_register_seeded": (C.c_int, [P, P, I64, P, P, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),
-    "gbdic_retry_seeded": (C.c_int, [P, P, P, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),
+    "gbdic_retry_seeded": (C.c_int, [P, I32, P, P, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),
     "gbdic_final_zncc": (C.c_int, [P, P]),
     "gbdic_submit": (C.c_int, [P, I32, P, I64, C.POINTER(SolverCfg)]),
     "gbdic_retire": (C.c_int, [P, I32, P, C.POINTER(Timing)]),

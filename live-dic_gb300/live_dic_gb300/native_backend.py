@@ -32,7 +32,8 @@ from .outlier import (
     normalize_median_filter_size,
     normalize_outlier_policy,
 )
-from .roi import RoiPlan, immutable, prepare_roi, validate_roi
+from .pyramid_recovery import pyramid_dependency_mask, reduce_half, transfer_pyramid_seed
+from .roi import RoiPlan, immutable, integral, prepare_roi, reduce_mask, seed_permissions, validate_roi
 from .subset import DEFAULT_SUBSET_SIZE, normalize_subset_size, normalize_subset_stride, subset_grid_shape
 from .weighting import SPATIAL_WEIGHTING_CODES, normalize_gaussian_sigma, normalize_spatial_weighting
 
@@ -256,6 +257,7 @@ class ICGNWGPU:
         self.roi = None
         self.reference_valid = None
         self._pyramid_engines: list[ICGNWGPU] = []
+        self._roi_seed_permissions: np.ndarray | None = None
 
     # ------------------------------------------------------------ helpers
     def _check(self, code: int) -> None:
@@ -383,6 +385,7 @@ class ICGNWGPU:
             links = np.ascontiguousarray(roi.links_table(self.median_filter_size, self.outlier_policy))
         self._reference_ready = False
         self._target_ready = False
+        self._close_pyramid_engines()
         info = _native.RefInfo()
         prep_start = time.perf_counter()
         self._check(
@@ -398,6 +401,8 @@ class ICGNWGPU:
         admissible = self._export(_native.EXPORT_ADMISSIBLE, np.uint8, (gh, gw))
         self.reference_valid = immutable(admissible.astype(bool))
         self._reference_ready = True
+        if self.pyramid_levels > 1:
+            self._prepare_pyramid(frame, zncc_min=config["znccMin"])
         usable = self.reference_valid if roi is None else self.reference_valid & roi.selected
         if self._autotune and usable.any():
             self._autotune_solver(frame)
@@ -552,9 +557,143 @@ class ICGNWGPU:
         times = self._timing(timing)
         times["totalWallMs"] = (time.perf_counter() - started) * 1e3
         result = self._result(packed, times, self._config)
+        if self._pyramid_engines:
+            result = self._recover_pyramid(0, frame, packed, result)
         if include_zncc:
             self._attach_final_zncc(result)
         return result
+
+    # ------------------------------------------------------------ selective pyramid recovery
+    def _close_pyramid_engines(self) -> None:
+        engines = getattr(self, "_pyramid_engines", [])
+        for engine in engines:
+            engine.close()
+        engines.clear()
+        self._roi_seed_permissions = None
+
+    def _prepare_pyramid(self, reference: np.ndarray, *, zncc_min: float) -> None:
+        """Coarse references of the selective recovery (wgpu_backend.py:2303-2362):
+        one single-scale engine per coarser level on the reduced reference
+        (12 iterations, tolerance 1e-2), reduced ROI masks and coarse-to-fine
+        seed permissions."""
+        self._close_pyramid_engines()
+        reduced = reference
+        mask = None if self.roi is None else self.roi.mask
+        for _ in range(1, self.pyramid_levels):
+            reduced = reduce_half(reduced)
+            mask = None if mask is None else reduce_mask(mask)
+            engine = ICGNWGPU(
+                solver_workgroup_size=self.solver_workgroup_size, pyramid_levels=1,
+                interpolation=self.interpolation, motion_model=self.motion_model,
+                outlier_policy=self.outlier_policy, median_filter_size=self.median_filter_size,
+                subset_size=self.subset_size, subset_stride=self.subset_stride,
+                spatial_weighting=self.spatial_weighting, gaussian_sigma=self.gaussian_sigma,
+                device=self.device_index, pipeline_slots=1,
+            )
+            try:
+                engine.set_reference(reduced, iterations=12, tolerance=1e-2, zncc_min=zncc_min, roi_mask=mask)
+            except Exception:
+                engine.close()
+                self._close_pyramid_engines()
+                raise
+            self._pyramid_engines.append(engine)
+        levels = [self, *self._pyramid_engines]
+        for level in levels:
+            level._roi_seed_permissions = None
+        if self.roi is not None and self.roi.effective:
+            prefix = integral(self.roi.mask)
+            for index, (destination, source) in enumerate(zip(levels[:-1], levels[1:], strict=True)):
+                destination._roi_seed_permissions = seed_permissions(
+                    source.roi, destination.roi, source_scale=1 << (index + 1), destination_scale=1 << index,
+                    size=self.subset_size, stride=self.subset_stride, reference_mask=self.roi.mask,
+                    reference_prefix=prefix)
+
+    def _register_seeded_states(self, frame: np.ndarray, seeds: np.ndarray, active: np.ndarray) -> np.ndarray:
+        """Seeded solve from full seed states (the reference's
+        _register_seeded_frame, wgpu_backend.py:1951-2036); returns the packed field."""
+        packed = self._new_packed()
+        timing = _native.Timing()
+        act = np.ascontiguousarray(active, dtype=np.uint32)
+        if self.roi is not None:
+            act = act * self.roi.selected.astype(np.uint32)
+        self._check(self._lib.gbdic_register_seeded(
+            self._handle, _native.ptr(frame), frame.strides[0], _native.ptr(np.ascontiguousarray(seeds)),
+            _native.ptr(np.ascontiguousarray(act)), C.byref(self._cfg(self._config)), _native.ptr(packed),
+            C.byref(timing)))
+        self._target_ready = True
+        return packed
+
+    def _recover_pyramid(self, slot: int, frame: np.ndarray, fine_packed: np.ndarray,
+                         fine_result: RegistrationResult) -> RegistrationResult:
+        """Re-solve failed fine subsets from coarse-to-fine seeds
+        (wgpu_backend.py:2038-2197)."""
+        recoverable = np.zeros(fine_result.status.shape, dtype=np.bool_)
+        if self.grid_width > 2 and self.grid_height > 2:
+            recoverable[1:-1, 1:-1] = True
+        failed = (np.asarray(fine_result.status) < 0.5) & recoverable
+        if self.roi is not None:
+            failed &= self.roi.selected
+        failed_count = int(np.count_nonzero(failed))
+        if failed_count == 0:
+            return fine_result
+        started = time.perf_counter()
+        reduced_targets = []
+        reduced = frame
+        for _ in self._pyramid_engines:
+            reduced = reduce_half(reduced)
+            reduced_targets.append(reduced)
+        requested_by_level = []
+        requested = failed
+        destination_scale = 1
+        for level_index, engine in enumerate(self._pyramid_engines):
+            level_scale = 1 << (level_index + 1)
+            requested = pyramid_dependency_mask(
+                source_grid=(engine.grid_width, engine.grid_height), source_scale=level_scale,
+                destination_scale=destination_scale, requested=requested, subset_size=self.subset_size,
+                subset_stride=self.subset_stride)
+            requested_by_level.append(requested)
+            if engine.roi is not None:
+                requested &= engine.roi.selected
+            destination_scale = level_scale
+        n = parameter_count(self.motion_model)
+        source = None  # (parameters, status, available, scale)
+        for level_index in range(len(self._pyramid_engines) - 1, -1, -1):
+            engine = self._pyramid_engines[level_index]
+            level_scale = 1 << (level_index + 1)
+            level_requested = requested_by_level[level_index]
+            if source is None:
+                seeds = np.zeros((engine.grid_height, engine.grid_width, state_float_count(self.motion_model)),
+                                 np.float32)
+                active = level_requested.astype(np.uint32)
+            else:
+                seeds, active = transfer_pyramid_seed(
+                    source[0], source[1], motion_model=self.motion_model, source_available=source[2],
+                    source_scale=source[3], destination_scale=level_scale,
+                    destination_grid=(engine.grid_width, engine.grid_height), requested=level_requested,
+                    subset_size=self.subset_size, subset_stride=self.subset_stride,
+                    permissions=engine._roi_seed_permissions)
+            level_packed = engine._register_seeded_states(reduced_targets[level_index], seeds, active)
+            source = (level_packed[..., :n], level_packed[..., n], level_requested, level_scale)
+        seeds, active = transfer_pyramid_seed(
+            source[0], source[1], motion_model=self.motion_model, source_available=source[2],
+            source_scale=source[3], destination_scale=1, destination_grid=(self.grid_width, self.grid_height),
+            requested=failed, subset_size=self.subset_size, subset_stride=self.subset_stride,
+            permissions=self._roi_seed_permissions)
+        recovered = self._new_packed()
+        timing = _native.Timing()
+        self._check(self._lib.gbdic_retry_seeded(
+            self._handle, int(slot), _native.ptr(np.ascontiguousarray(seeds)), _native.ptr(np.ascontiguousarray(active)),
+            C.byref(self._cfg(self._config)), _native.ptr(recovered), C.byref(timing)))
+        recovered_count = int(np.count_nonzero(failed & (recovered[..., n] >= 0.5)))
+        preserved = np.asarray(fine_result.status) >= 0.5
+        recovered[preserved] = fine_packed[preserved]
+        times = dict(fine_result.timing)
+        times.update(self._timing(timing))
+        pyramid_ms = (time.perf_counter() - started) * 1e3
+        times.update({"pyramidFailedBefore": float(failed_count), "pyramidRecovered": float(recovered_count),
+                      "pyramidLevels": float(self.pyramid_levels), "pyramidWallMs": pyramid_ms,
+                      "totalWallMs": fine_result.timing["totalWallMs"] + pyramid_ms})
+        return self._result(recovered, times, self._config)
 
     # ------------------------------------------------------------ spatial seeds
     def _spatial_permissions(self) -> tuple[np.ndarray, np.ndarray]:
@@ -750,15 +889,18 @@ class ICGNWGPU:
         pending: deque[tuple[int, float]] = deque()
 
         def retire() -> RegistrationResult:
-            slot, started = pending.popleft()
+            slot, started, frame = pending.popleft()
             packed = self._new_packed()
             timing = _native.Timing()
             self._check(self._lib.gbdic_retire(self._handle, slot, _native.ptr(packed), C.byref(timing)))
-            available.append(slot)
             times = self._timing(timing)
             times["pipelineLatencyWallMs"] = (time.perf_counter() - started) * 1e3
             times["totalWallMs"] = times["pipelineLatencyWallMs"]
-            return self._result(packed, times, self._config)
+            result = self._result(packed, times, self._config)
+            if self._pyramid_engines:
+                result = self._recover_pyramid(slot, frame, packed, result)
+            available.append(slot)
+            return result
 
         try:
             for target in targets:
@@ -768,12 +910,12 @@ class ICGNWGPU:
                 started = time.perf_counter()
                 frame = self._prepare_target(target)
                 self._check(self._lib.gbdic_submit(self._handle, slot, _native.ptr(frame), frame.strides[0], C.byref(cfg)))
-                pending.append((slot, started))
+                pending.append((slot, started, frame))
             while pending:
                 yield retire()
         finally:
             while pending:
-                slot, _ = pending.popleft()
+                slot, _, _ = pending.popleft()
                 self._lib.gbdic_retire(self._handle, slot, None, None)
 
     def register_many(self, targets: Iterable[ImageInput], *, pipeline_depth: int = DEFAULT_IN_FLIGHT_FRAMES,
@@ -803,6 +945,7 @@ class ICGNWGPU:
             return
         self._reference_ready = False
         self._closed = True
+        self._close_pyramid_engines()
         handle, self._handle = self._handle, None
         if handle:
             self._lib.gbdic_destroy(handle)

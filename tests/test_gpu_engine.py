@@ -165,3 +165,30 @@ def test_temporal_stream_tracks_ramp_and_counts():
     assert results[1].timing["temporallySeededCoarseSubsets"] > 0
     assert results[2].timing["velocityPredictedSubsets"] > 0
     assert again.timing["temporallySeededCoarseSubsets"] == 0
+
+
+def test_selective_pyramid_recovery_of_failed_subsets():
+    ref, sp = synthetic.reference_image(384, 320, seed=71, device="cpu")
+    tgt = synthetic.deformed_image(sp, synthetic.affine_field(6.3, 0.0, 0.0, -5.2, 0.0, 0.0), noise_seed=72,
+                                   device="cpu")
+    mask = synthetic.hole_mask(384, 320, 50.0)
+    with ICGNWGPU(subset_size=31, subset_stride=8) as single:
+        single.set_reference(ref, roi_mask=mask)
+        plain = single.register(tgt)
+    with ICGNWGPU(subset_size=31, subset_stride=8, pyramid_levels=3) as engine:
+        info = engine.set_reference(ref, roi_mask=mask)
+        result = engine.register(tgt)
+        streamed = list(engine.register_stream([tgt, tgt], pipeline_depth=2))
+    inside = info.roi.selected
+    assert (result.status[~inside] == -3).all()
+    assert result.timing["pyramidFailedBefore"] > 0 and result.timing["pyramidRecovered"] > 0
+    ok, ok_plain = result.status >= 1, plain.status >= 1
+    assert ok[inside].mean() > ok_plain[inside].mean() + 0.3
+    assert ok[inside].mean() > 0.75  # the outer ring and windows pushed off the image stay unrecoverable
+    np.testing.assert_allclose(np.median(result.displacement[ok], axis=0), [6.3, -5.2], atol=0.02)
+    # subsets the fine level solved are kept as they were
+    kept = ok_plain
+    np.testing.assert_array_equal(result.parameters[kept], plain.parameters[kept])
+    for r in streamed:
+        np.testing.assert_array_equal(r.status, result.status)
+        np.testing.assert_array_equal(r.parameters, result.parameters)

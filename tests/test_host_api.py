@@ -219,3 +219,27 @@ def test_uneven_workload_generator():
         u, v = p["field"](gx, gy)
         assert np.sqrt(u * u + v * v).max() == pytest.approx(p["field_params"]["peak"], rel=1e-9)
         assert 0.5 <= p["field_params"]["peak"] <= 3.0
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_recovery_reduction_matches_reference(golden, k):
+    from live_dic_gb300.pyramid_recovery import reduce_half
+
+    np.testing.assert_array_equal(reduce_half(golden[f"reduce_{k}_in"]), golden[f"reduce_{k}_half"])
+
+
+@pytest.mark.parametrize("model", ["affine", "quadratic"])
+def test_recovery_seed_transfer_matches_reference(golden, model):
+    from live_dic_gb300.pyramid_recovery import pyramid_dependency_mask, transfer_pyramid_seed
+
+    requested = golden[f"transfer_{model}_requested"]
+    seeds, active = transfer_pyramid_seed(
+        golden[f"transfer_{model}_params"], golden[f"transfer_{model}_status"], motion_model=model,
+        source_available=golden[f"transfer_{model}_available"], source_scale=2, destination_scale=1,
+        destination_grid=(17, 13), requested=requested, subset_size=21, subset_stride=10)
+    np.testing.assert_allclose(seeds, golden[f"transfer_{model}_seeds"], rtol=1e-6, atol=1e-7)
+    np.testing.assert_array_equal(active, golden[f"transfer_{model}_active"])
+    status = golden[f"transfer_{model}_status"]
+    closure = pyramid_dependency_mask(source_grid=(status.shape[1], status.shape[0]), source_scale=2,
+                                      destination_scale=1, requested=requested, subset_size=21, subset_stride=10)
+    assert closure.shape == status.shape and closure.any()
