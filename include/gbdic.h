@@ -352,6 +352,73 @@ int gbdic_batch_run_device(gbdic_batch *batch, void *stream, int32_t profile, gb
  * METADATA, ADMISSIBLE). */
 int gbdic_batch_export(gbdic_batch *batch, int32_t job, int32_t what, void *host_out, int64_t bytes);
 
+/* ------------------------------------------------- learned seed network */
+
+/* Building blocks of the learned seed-proposal network (no counterpart in the
+ * reference, whose large-motion initialisers are the pyramid, the Fourier
+ * phase correlation and wgpu-matching).  All pointers are device pointers;
+ * `stream` is a cudaStream_t or NULL.  Errors: message in
+ * gbdic_last_error(NULL).
+ *
+ * BF16 tensor-core GEMM (tcgen05, FP32 accumulation in tensor memory):
+ *   D[m][n] (+)= sum_k A[m][k] B[n][k] (+ bias[n]) (ReLU)
+ * A: M x K, B: N x K, both BF16 row-major with K contiguous; M % 128 == 0,
+ * N % 16 == 0, K % (64 * k_split) == 0.  Split s writes its partial at
+ * D + s * split_stride (bias must be NULL when k_split > 1).  A pipeline wait
+ * that expires sets *device_error to 1 (device_error may be NULL). */
+typedef struct {
+    const void *a, *b;
+    int32_t M, N, K, k_split;
+    float *d_f32;          /* FP32 output, or NULL */
+    void *d_bf16;          /* BF16 output, or NULL */
+    int32_t ldd;           /* output row stride in elements, multiple of 4 */
+    int64_t split_stride;
+    const float *bias;
+    int32_t relu, accumulate;
+} gbdic_nn_gemm_desc;
+int gbdic_nn_gemm(const gbdic_nn_gemm_desc *desc, int32_t *device_error, void *stream);
+
+/* 64x64 reference/target patch pairs around `centres` ((x, y) per patch,
+ * image pixels) of uint8 images W x H: refs / tgts are device arrays of
+ * device image pointers, image_index (or NULL) selects the image of each
+ * patch.  Output [count][64][64][2] BF16, each channel at zero mean and unit
+ * variance; coordinates outside the image are clamped. */
+int gbdic_nn_patches(const uint8_t *const *refs, const uint8_t *const *tgts, const int32_t *image_index,
+                     const float *centres, int32_t count, int32_t width, int32_t height, void *out, void *stream);
+
+/* 3x3, stride-2, pad-1 convolution shapes (NHWC BF16 activations). */
+typedef struct {
+    int32_t B, H, W, C, OH, OW, Cout, Kp;
+} gbdic_nn_conv_shape;
+/* Forward GEMM operand A[(b, oy, ox)][(ky, kx, ci)] (zero beyond 9 C). */
+int gbdic_nn_im2col(const gbdic_nn_conv_shape *shape, const void *x, void *a, void *stream);
+/* Data-gradient operand G[(b, iy, ix)][(ky, kx, co)] from output gradients. */
+int gbdic_nn_dgrad_gather(const gbdic_nn_conv_shape *shape, const void *dz, void *g, void *stream);
+/* dst (Cp x Rp) = src (R x C, row stride ld_src) transposed, zero padded. */
+int gbdic_nn_transpose(const void *src, int32_t rows, int32_t cols, int32_t ld_src, void *dst, int32_t rows_padded,
+                       int32_t cols_padded, void *stream);
+/* dZ (BF16, rows x C) = dY (FP32, row stride ld) where Y > 0, else 0. */
+int gbdic_nn_relu_backward(const float *dy, int32_t ld, const void *y, void *dz, int64_t rows, int32_t cols,
+                           void *stream);
+/* db[c] = sum_r dY[r][c] (masked by Y > 0 when y != NULL). */
+int gbdic_nn_bias_grad(const float *dy, int32_t ld, const void *y, int64_t rows, int32_t cols, float *db,
+                       void *stream);
+/* out[n][k] = sum_s partial[s][k][n] for k < Kp (partials Kp_rows x N). */
+int gbdic_nn_splitk_reduce(const float *partial, int32_t splits, int32_t kp_rows, int32_t n, int32_t kp, float *out,
+                           void *stream);
+/* Adam step on `count` FP32 parameters; hyper = {lr, beta1, beta2, eps,
+ * 1 - beta1^t, 1 - beta2^t, weight_decay}. */
+int gbdic_nn_adam(float *param, const float *grad, float *m, float *v, int64_t count, const float *hyper,
+                  void *stream);
+/* BF16 copy of W [Cout][Kp] and, when wt != NULL, the data-gradient operand
+ * Wt[ci][(ky, kx, co)] (row length kt). */
+int gbdic_nn_pack_weights(const float *w, int32_t cout, int32_t cin, int32_t kp, void *wb, void *wt, int32_t kt,
+                          void *stream);
+/* Mean squared-error loss over the first `outputs` columns and its gradient
+ * (BF16 [B][ldg], zero beyond `outputs`). */
+int gbdic_nn_regression_loss(const float *pred, int32_t ldp, const float *target, int32_t outputs, int32_t batch,
+                             void *grad, int32_t ldg, float *loss, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

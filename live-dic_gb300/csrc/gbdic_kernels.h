@@ -138,6 +138,59 @@ struct ChooseArgs {
 };
 cudaError_t launch_spatial_choose(const ChooseArgs &a, cudaStream_t stream);
 
+// ------------------------------------------------------------ learned seeds
+// D (+)= A B^T on the tensor cores: A M x K, B N x K, BF16 row-major (K
+// contiguous); M % 128 == 0, N % 16 == 0, K % (64 k_split) == 0.
+struct TcGemmArgs {
+    const void *a, *b;        // BF16
+    int M, N, K, k_split;     // split s writes its partial at d + s * split_stride
+    float *d_f32;             // FP32 output or nullptr
+    void *d_bf16;             // BF16 output or nullptr
+    int ldd;                  // output row stride (elements, % 4 == 0)
+    long long split_stride;
+    const float *bias;        // per column, or nullptr
+    int relu, accumulate;     // accumulate: D_f32 += result
+    int *error;               // set to 1 when a pipeline wait expired
+};
+int tc_gemm_tile_n(int N);
+cudaError_t launch_tc_gemm(const TcGemmArgs &a, cudaStream_t stream);
+
+struct NnPatchArgs {
+    const uint8_t *const *refs;   // device array of device image pointers
+    const uint8_t *const *tgts;
+    const int *image_index;       // per patch, or nullptr (image 0)
+    const float *centres;         // per patch (x, y), image pixels
+    int count, W, H;
+    void *out;                    // [count][64][64][2] BF16
+};
+struct NnConvShape {
+    int B, H, W, C;       // input NHWC
+    int OH, OW, Cout;     // 3x3 stride-2 pad-1 output
+    int Kp;               // padded reduction length of the forward GEMM (>= 9 C)
+};
+struct NnAdamArgs {
+    float *param;
+    const float *grad;
+    float *m, *v;
+    long long count;
+    float lr, beta1, beta2, eps, bias1, bias2, weight_decay;
+};
+cudaError_t launch_nn_patches(const NnPatchArgs &a, cudaStream_t s);
+cudaError_t launch_nn_im2col(const NnConvShape &sh, const void *x, void *A, cudaStream_t s);
+cudaError_t launch_nn_dgrad_gather(const NnConvShape &sh, const void *dz, void *G, cudaStream_t s);
+cudaError_t launch_nn_transpose(const void *src, int R, int C, int ld_src, void *dst, int Rp, int Cp, cudaStream_t s);
+cudaError_t launch_nn_relu_backward(const float *dy, int ld, const void *y, void *dz, long long rows, int C,
+                                    cudaStream_t s);
+cudaError_t launch_nn_bias_grad(const float *dy, int ld, const void *y, long long rows, int C, float *db,
+                                cudaStream_t s);
+cudaError_t launch_nn_splitk_reduce(const float *partial, int splits, int Kp_rows, int N, int Kp, float *out,
+                                    cudaStream_t s);
+cudaError_t launch_nn_adam(const NnAdamArgs &a, cudaStream_t s);
+cudaError_t launch_nn_pack_weights(const float *w, int Cout, int Cin, int Kp, void *wb, void *wt, int Kt,
+                                   cudaStream_t s);
+cudaError_t launch_nn_regression_loss(const float *pred, int ldp, const float *target, int outputs, int B, void *grad,
+                                      int ldg, float *loss, cudaStream_t s);
+
 struct TemporalArgs {
     float *history;           // fine accepted history
     uint32_t *ages;

@@ -1,0 +1,114 @@
+// C ABI of the learned seed network's kernels (declarations in
+// include/gbdic.h).  Thin argument checks, then the launchers of tc_gemm.cu
+// and nn_ops.cu; errors go to gbdic_last_error(NULL).
+#include <string>
+
+#include "engine.h"
+
+namespace {
+
+int rc(cudaError_t err, const char *what) {
+    if (err == cudaSuccess) return GBDIC_OK;
+    gbdic::set_thread_error(std::string(what) + ": " + cudaGetErrorString(err));
+    return err == cudaErrorInvalidValue ? GBDIC_EINVAL : GBDIC_ECUDA;
+}
+
+int invalid(const char *message) {
+    gbdic::set_thread_error(message);
+    return GBDIC_EINVAL;
+}
+
+cudaStream_t as_stream(void *s) { return static_cast<cudaStream_t>(s); }
+
+bool valid_shape(const gbdic_nn_conv_shape *s) {
+    return s && s->B > 0 && s->H > 0 && s->W > 0 && s->C > 0 && s->Cout > 0 && s->OH == (s->H + 1) / 2 &&
+           s->OW == (s->W + 1) / 2 && s->Kp >= 9 * s->C;
+}
+
+gbdic::NnConvShape shape_of(const gbdic_nn_conv_shape *s) {
+    return {s->B, s->H, s->W, s->C, s->OH, s->OW, s->Cout, s->Kp};
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbdic_nn_gemm(const gbdic_nn_gemm_desc *d, int32_t *device_error, void *stream) {
+    if (!d) return invalid("gemm descriptor is required");
+    gbdic::TcGemmArgs a{};
+    a.a = d->a; a.b = d->b;
+    a.M = d->M; a.N = d->N; a.K = d->K; a.k_split = d->k_split;
+    a.d_f32 = d->d_f32; a.d_bf16 = d->d_bf16; a.ldd = d->ldd; a.split_stride = d->split_stride;
+    a.bias = d->bias; a.relu = d->relu; a.accumulate = d->accumulate;
+    a.error = device_error;
+    return rc(gbdic::launch_tc_gemm(a, as_stream(stream)),
+              "tensor-core GEMM (M % 128, N % 16, K % (64 k_split), 16-byte aligned operands, ldd % 4)");
+}
+
+int gbdic_nn_patches(const uint8_t *const *refs, const uint8_t *const *tgts, const int32_t *image_index,
+                     const float *centres, int32_t count, int32_t width, int32_t height, void *out, void *stream) {
+    if (!refs || !tgts || !centres || !out || count < 0 || width < 1 || height < 1)
+        return invalid("patch arguments are incomplete");
+    gbdic::NnPatchArgs a{refs, tgts, image_index, centres, count, width, height, out};
+    return rc(gbdic::launch_nn_patches(a, as_stream(stream)), "patch extraction");
+}
+
+int gbdic_nn_im2col(const gbdic_nn_conv_shape *s, const void *x, void *a, void *stream) {
+    if (!valid_shape(s) || !x || !a) return invalid("invalid convolution shape or pointers");
+    return rc(gbdic::launch_nn_im2col(shape_of(s), x, a, as_stream(stream)), "im2col");
+}
+
+int gbdic_nn_dgrad_gather(const gbdic_nn_conv_shape *s, const void *dz, void *g, void *stream) {
+    if (!valid_shape(s) || !dz || !g) return invalid("invalid convolution shape or pointers");
+    return rc(gbdic::launch_nn_dgrad_gather(shape_of(s), dz, g, as_stream(stream)), "gradient gather");
+}
+
+int gbdic_nn_transpose(const void *src, int32_t rows, int32_t cols, int32_t ld_src, void *dst, int32_t rows_padded,
+                       int32_t cols_padded, void *stream) {
+    if (!src || !dst || rows < 0 || cols < 0 || ld_src < cols || rows_padded < rows || cols_padded < cols)
+        return invalid("invalid transpose arguments");
+    return rc(gbdic::launch_nn_transpose(src, rows, cols, ld_src, dst, rows_padded, cols_padded, as_stream(stream)),
+              "transpose");
+}
+
+int gbdic_nn_relu_backward(const float *dy, int32_t ld, const void *y, void *dz, int64_t rows, int32_t cols,
+                           void *stream) {
+    if (!dy || !y || !dz || ld < cols || rows < 0 || cols <= 0) return invalid("invalid ReLU backward arguments");
+    return rc(gbdic::launch_nn_relu_backward(dy, ld, y, dz, rows, cols, as_stream(stream)), "ReLU backward");
+}
+
+int gbdic_nn_bias_grad(const float *dy, int32_t ld, const void *y, int64_t rows, int32_t cols, float *db,
+                       void *stream) {
+    if (!dy || !db || ld < cols || rows < 0 || cols <= 0) return invalid("invalid bias gradient arguments");
+    return rc(gbdic::launch_nn_bias_grad(dy, ld, y, rows, cols, db, as_stream(stream)), "bias gradient");
+}
+
+int gbdic_nn_splitk_reduce(const float *partial, int32_t splits, int32_t kp_rows, int32_t n, int32_t kp, float *out,
+                           void *stream) {
+    if (!partial || !out || splits < 1 || kp > kp_rows || n <= 0 || kp <= 0) return invalid("invalid split-K reduction");
+    return rc(gbdic::launch_nn_splitk_reduce(partial, splits, kp_rows, n, kp, out, as_stream(stream)), "split-K reduce");
+}
+
+int gbdic_nn_adam(float *param, const float *grad, float *m, float *v, int64_t count, const float *hyper,
+                  void *stream) {
+    if (!param || !grad || !m || !v || !hyper || count < 0) return invalid("invalid Adam arguments");
+    gbdic::NnAdamArgs a{param, grad, m, v, count, hyper[0], hyper[1], hyper[2], hyper[3], hyper[4], hyper[5], hyper[6]};
+    return rc(gbdic::launch_nn_adam(a, as_stream(stream)), "Adam");
+}
+
+int gbdic_nn_pack_weights(const float *w, int32_t cout, int32_t cin, int32_t kp, void *wb, void *wt, int32_t kt,
+                          void *stream) {
+    if (!w || !wb || cout <= 0 || cin <= 0 || kp < 9 * cin || (wt && kt < 9 * cout))
+        return invalid("invalid weight packing arguments");
+    return rc(gbdic::launch_nn_pack_weights(w, cout, cin, kp, wb, wt, kt, as_stream(stream)), "weight packing");
+}
+
+int gbdic_nn_regression_loss(const float *pred, int32_t ldp, const float *target, int32_t outputs, int32_t batch,
+                             void *grad, int32_t ldg, float *loss, void *stream) {
+    if (!pred || !target || !grad || !loss || outputs <= 0 || ldp < outputs || ldg < outputs || batch <= 0)
+        return invalid("invalid loss arguments");
+    return rc(gbdic::launch_nn_regression_loss(pred, ldp, target, outputs, batch, grad, ldg, loss, as_stream(stream)),
+              "regression loss");
+}
+
+}  // extern "C"

@@ -1,0 +1,281 @@
+// Data-movement and element-wise kernels of the learned seed network.  The
+// contractions (convolutions as implicit GEMMs, the final linear layer and
+// all their gradients) run on the tensor cores in tc_gemm.cu; everything here
+// is HBM-bound glue around them:
+//   patch extraction and normalisation, 3x3 stride-2 im2col, the gather of
+//   output gradients for the data gradient, BF16 transposes, ReLU backward,
+//   bias gradients, split-K reduction of weight gradients, Adam, weight
+//   packing and the regression loss.
+// Activations are NHWC BF16 (rows = pixels, channels contiguous); weights are
+// [Cout][(ky, kx, ci)] with the reduction index padded to the GEMM tile.
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "gbdic_kernels.h"
+
+namespace gbdic {
+namespace {
+
+__device__ __forceinline__ float bf(const __nv_bfloat16 v) { return __bfloat162float(v); }
+
+// One CTA (256 threads) per patch: 64 x 64 pixels of the reference and target
+// level images around (cx, cy), each channel normalised to zero mean and unit
+// variance, written as [64][64][2] BF16.
+__global__ void __launch_bounds__(256) patch_kernel(NnPatchArgs a) {
+    const int b = blockIdx.x;
+    if (b >= a.count) return;
+    const int img = a.image_index ? a.image_index[b] : 0;
+    const uint8_t *ref = a.refs[img], *tgt = a.tgts[img];
+    const int x0 = (int)floorf(a.centres[2 * b] + 0.5f) - 32, y0 = (int)floorf(a.centres[2 * b + 1] + 0.5f) - 32;
+    float vr[16], vt[16];
+    float sr = 0.0f, st = 0.0f, qr = 0.0f, qt = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int p = threadIdx.x + 256 * i;
+        const int x = min(max(x0 + (p & 63), 0), a.W - 1), y = min(max(y0 + (p >> 6), 0), a.H - 1);
+        vr[i] = (float)ref[(size_t)y * a.W + x];
+        vt[i] = (float)tgt[(size_t)y * a.W + x];
+        sr += vr[i]; st += vt[i]; qr += vr[i] * vr[i]; qt += vt[i] * vt[i];
+    }
+    __shared__ float red[4][8];
+    float v4[4] = {sr, st, qr, qt};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float v = v4[k];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    float tot[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float v = 0.0f;
+        for (int w = 0; w < 8; ++w) v += red[k][w];
+        tot[k] = v;
+    }
+    const float mr = tot[0] / 4096.0f, mt = tot[1] / 4096.0f;
+    const float ir = rsqrtf(fmaxf(tot[2] / 4096.0f - mr * mr, 1e-2f));
+    const float it = rsqrtf(fmaxf(tot[3] / 4096.0f - mt * mt, 1e-2f));
+    __nv_bfloat162 *out = reinterpret_cast<__nv_bfloat162 *>(a.out) + (size_t)b * 4096;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int p = threadIdx.x + 256 * i;
+        out[p] = __floats2bfloat162_rn((vr[i] - mr) * ir, (vt[i] - mt) * it);
+    }
+}
+
+// A[m][k] for m = (b, oy, ox), k = (ky, kx, ci) < 9 C; zero for k >= 9 C.
+__global__ void im2col_kernel(NnConvShape s, const __nv_bfloat16 *x, __nv_bfloat16 *A) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long rows = (long long)s.B * s.OH * s.OW;
+    if (idx >= rows * s.Kp) return;
+    const int k = (int)(idx % s.Kp);
+    const long long m = idx / s.Kp;
+    __nv_bfloat16 v = __float2bfloat16(0.0f);
+    if (k < 9 * s.C) {
+        const int tap = k / s.C, ci = k % s.C, ky = tap / 3, kx = tap % 3;
+        const int ox = (int)(m % s.OW), oy = (int)((m / s.OW) % s.OH), b = (int)(m / ((long long)s.OW * s.OH));
+        const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
+        if (iy >= 0 && iy < s.H && ix >= 0 && ix < s.W) v = x[(((size_t)b * s.H + iy) * s.W + ix) * s.C + ci];
+    }
+    A[idx] = v;
+}
+
+// G[m][k] for input pixel m = (b, iy, ix) and k = (ky, kx, co) < 9 Cout: the
+// output gradient at (oy, ox) = ((iy + 1 - ky) / 2, (ix + 1 - kx) / 2) when
+// both are integral and inside the output, else zero.
+__global__ void dgrad_gather_kernel(NnConvShape s, const __nv_bfloat16 *dz, __nv_bfloat16 *G) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long rows = (long long)s.B * s.H * s.W;
+    const int kg = 9 * s.Cout;
+    if (idx >= rows * kg) return;
+    const int k = (int)(idx % kg);
+    const long long m = idx / kg;
+    const int tap = k / s.Cout, co = k % s.Cout, ky = tap / 3, kx = tap % 3;
+    const int ix = (int)(m % s.W), iy = (int)((m / s.W) % s.H), b = (int)(m / ((long long)s.W * s.H));
+    const int ty = iy + 1 - ky, tx = ix + 1 - kx;
+    __nv_bfloat16 v = __float2bfloat16(0.0f);
+    if (ty >= 0 && tx >= 0 && !(ty & 1) && !(tx & 1) && (ty >> 1) < s.OH && (tx >> 1) < s.OW)
+        v = dz[(((size_t)b * s.OH + (ty >> 1)) * s.OW + (tx >> 1)) * s.Cout + co];
+    G[idx] = v;
+}
+
+// dst[c][r] = src[r][c] for r < R, c < C; zero in the padding up to Rp x Cp.
+__global__ void transpose_kernel(const __nv_bfloat16 *src, int R, int C, int ld_src, __nv_bfloat16 *dst, int Rp,
+                                 int Cp) {
+    __shared__ __nv_bfloat16 tile[32][33];
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int r = r0 + i, c = c0 + threadIdx.x;
+        tile[i][threadIdx.x] = (r < R && c < C) ? src[(size_t)r * ld_src + c] : __float2bfloat16(0.0f);
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int c = c0 + i, r = r0 + threadIdx.x;
+        if (c < Cp && r < Rp) dst[(size_t)c * Rp + r] = tile[threadIdx.x][i];
+    }
+}
+
+// dZ = dY * (Y > 0) as BF16; rows x C, dY with row stride ld.
+__global__ void relu_backward_kernel(const float *dy, int ld, const __nv_bfloat16 *y, __nv_bfloat16 *dz, long long rows,
+                                     int C) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= rows * C) return;
+    const long long r = idx / C;
+    const int c = (int)(idx % C);
+    const float g = bf(y[idx]) > 0.0f ? dy[r * ld + c] : 0.0f;
+    dz[idx] = __float2bfloat16(g);
+}
+
+// db[c] = sum over rows of dY[r][c] * (Y[r][c] > 0) (Y == nullptr: no mask),
+// one CTA per column, fixed summation order.
+__global__ void __launch_bounds__(256) bias_grad_kernel(const float *dy, int ld, const __nv_bfloat16 *y, long long rows,
+                                                        int C, float *db) {
+    const int c = blockIdx.x;
+    float acc = 0.0f;
+    for (long long r = threadIdx.x; r < rows; r += 256) {
+        const float g = dy[r * ld + c];
+        acc += (y == nullptr || bf(y[r * C + c]) > 0.0f) ? g : 0.0f;
+    }
+    __shared__ float red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int off = 128; off > 0; off >>= 1) {
+        if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[c] = red[0];
+}
+
+// out[n][k] = sum_s partial[s][k][n] (s ascending) for k < Kp, n < N.
+__global__ void splitk_reduce_kernel(const float *partial, int splits, int Kp_rows, int N, int Kp, float *out) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= N * Kp) return;
+    const int n = idx / Kp, k = idx % Kp;
+    float acc = 0.0f;
+    for (int s = 0; s < splits; ++s) acc += partial[((size_t)s * Kp_rows + k) * N + n];
+    out[idx] = acc;
+}
+
+__global__ void adam_kernel(NnAdamArgs a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.count) return;
+    const float g = a.grad[i] + a.weight_decay * a.param[i];
+    const float m = a.beta1 * a.m[i] + (1.0f - a.beta1) * g;
+    const float v = a.beta2 * a.v[i] + (1.0f - a.beta2) * g * g;
+    a.m[i] = m;
+    a.v[i] = v;
+    a.param[i] -= a.lr * (m / a.bias1) / (sqrtf(v / a.bias2) + a.eps);
+}
+
+// W [Cout][Kp] FP32 -> BF16 copy, and the data-gradient operand
+// Wt[ci][(ky, kx, co)] = W[co][(ky, kx, ci)] (when wt != nullptr).
+__global__ void pack_weights_kernel(const float *w, int Cout, int Cin, int Kp, __nv_bfloat16 *wb, __nv_bfloat16 *wt,
+                                    int Kt) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= Cout * Kp) return;
+    const int co = idx / Kp, k = idx % Kp;
+    const __nv_bfloat16 v = __float2bfloat16(w[idx]);
+    wb[idx] = v;
+    if (wt != nullptr && k < 9 * Cin) {
+        const int tap = k / Cin, ci = k % Cin;
+        wt[(size_t)ci * Kt + tap * Cout + co] = v;
+    }
+}
+
+// Loss 0.5 / B sum (pred - target)^2 over the first `outputs` columns and
+// its gradient (pred - target) / B as BF16 [B][ldg] (zero elsewhere); one CTA.
+__global__ void __launch_bounds__(256) regression_loss_kernel(const float *pred, int ldp, const float *target,
+                                                              int outputs, int B, __nv_bfloat16 *grad, int ldg,
+                                                              float *loss) {
+    float acc = 0.0f;
+    for (int i = threadIdx.x; i < B * ldg; i += 256) {
+        const int b = i / ldg, j = i % ldg;
+        float g = 0.0f;
+        if (j < outputs) {
+            const float d = pred[(size_t)b * ldp + j] - target[(size_t)b * outputs + j];
+            acc += 0.5f * d * d;
+            g = d / (float)B;
+        }
+        grad[i] = __float2bfloat16(g);
+    }
+    __shared__ float red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int off = 128; off > 0; off >>= 1) {
+        if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *loss = red[0] / (float)B;
+}
+
+unsigned blocks(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+cudaError_t launch_nn_patches(const NnPatchArgs &a, cudaStream_t s) {
+    if (a.count <= 0) return cudaSuccess;
+    patch_kernel<<<a.count, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_im2col(const NnConvShape &sh, const void *x, void *A, cudaStream_t s) {
+    const long long n = (long long)sh.B * sh.OH * sh.OW * sh.Kp;
+    im2col_kernel<<<blocks(n, 256), 256, 0, s>>>(sh, static_cast<const __nv_bfloat16 *>(x), static_cast<__nv_bfloat16 *>(A));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_dgrad_gather(const NnConvShape &sh, const void *dz, void *G, cudaStream_t s) {
+    const long long n = (long long)sh.B * sh.H * sh.W * 9 * sh.Cout;
+    dgrad_gather_kernel<<<blocks(n, 256), 256, 0, s>>>(sh, static_cast<const __nv_bfloat16 *>(dz),
+                                                      static_cast<__nv_bfloat16 *>(G));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_transpose(const void *src, int R, int C, int ld_src, void *dst, int Rp, int Cp, cudaStream_t s) {
+    dim3 grid((Rp + 31) / 32, (Cp + 31) / 32), block(32, 8);
+    transpose_kernel<<<grid, block, 0, s>>>(static_cast<const __nv_bfloat16 *>(src), R, C, ld_src,
+                                            static_cast<__nv_bfloat16 *>(dst), Rp, Cp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_relu_backward(const float *dy, int ld, const void *y, void *dz, long long rows, int C,
+                                    cudaStream_t s) {
+    relu_backward_kernel<<<blocks(rows * C, 256), 256, 0, s>>>(dy, ld, static_cast<const __nv_bfloat16 *>(y),
+                                                               static_cast<__nv_bfloat16 *>(dz), rows, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_bias_grad(const float *dy, int ld, const void *y, long long rows, int C, float *db,
+                                cudaStream_t s) {
+    bias_grad_kernel<<<C, 256, 0, s>>>(dy, ld, static_cast<const __nv_bfloat16 *>(y), rows, C, db);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_splitk_reduce(const float *partial, int splits, int Kp_rows, int N, int Kp, float *out,
+                                    cudaStream_t s) {
+    splitk_reduce_kernel<<<blocks((long long)N * Kp, 256), 256, 0, s>>>(partial, splits, Kp_rows, N, Kp, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_adam(const NnAdamArgs &a, cudaStream_t s) {
+    adam_kernel<<<blocks(a.count, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_pack_weights(const float *w, int Cout, int Cin, int Kp, void *wb, void *wt, int Kt,
+                                   cudaStream_t s) {
+    pack_weights_kernel<<<blocks((long long)Cout * Kp, 256), 256, 0, s>>>(
+        w, Cout, Cin, Kp, static_cast<__nv_bfloat16 *>(wb), static_cast<__nv_bfloat16 *>(wt), Kt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_regression_loss(const float *pred, int ldp, const float *target, int outputs, int B, void *grad,
+                                      int ldg, float *loss, cudaStream_t s) {
+    regression_loss_kernel<<<1, 256, 0, s>>>(pred, ldp, target, outputs, B, static_cast<__nv_bfloat16 *>(grad), ldg,
+                                             loss);
+    return cudaGetLastError();
+}
+
+}  // namespace gbdic

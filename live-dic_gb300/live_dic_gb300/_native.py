@@ -132,6 +132,20 @@ class ChooseCfg(C.Structure):
         ("candidate_mode", C.c_int32),
     ]
 
+class NnGemmDesc(C.Structure):
+    _fields_ = [
+        ("a", C.c_void_p), ("b", C.c_void_p),
+        ("M", C.c_int32), ("N", C.c_int32), ("K", C.c_int32), ("k_split", C.c_int32),
+        ("d_f32", C.c_void_p), ("d_bf16", C.c_void_p),
+        ("ldd", C.c_int32), ("split_stride", C.c_int64),
+        ("bias", C.c_void_p), ("relu", C.c_int32), ("accumulate", C.c_int32),
+    ]
+
+
+class NnConvShape(C.Structure):
+    _fields_ = [(name, C.c_int32) for name in ("B", "H", "W", "C", "OH", "OW", "Cout", "Kp")]
+
+
 P = C.c_void_p
 I32, I64 = C.c_int32, C.c_int64
 _SIGNATURES = {
@@ -180,6 +194,17 @@ _SIGNATURES = {
     "gbdic_batch_export": (C.c_int, [P, I32, I32, P, I64]),
     "gbdic_affine_frontier": (C.c_int, [P, P, P, P, P]),
     "gbdic_spatial_choose": (C.c_int, [P, P, P, P, C.POINTER(ChooseCfg), P, P, P]),
+    "gbdic_nn_gemm": (C.c_int, [C.POINTER(NnGemmDesc), P, P]),
+    "gbdic_nn_patches": (C.c_int, [P, P, P, P, I32, I32, I32, P, P]),
+    "gbdic_nn_im2col": (C.c_int, [C.POINTER(NnConvShape), P, P, P]),
+    "gbdic_nn_dgrad_gather": (C.c_int, [C.POINTER(NnConvShape), P, P, P]),
+    "gbdic_nn_transpose": (C.c_int, [P, I32, I32, I32, P, I32, I32, P]),
+    "gbdic_nn_relu_backward": (C.c_int, [P, I32, P, P, I64, I32, P]),
+    "gbdic_nn_bias_grad": (C.c_int, [P, I32, P, I64, I32, P, P]),
+    "gbdic_nn_splitk_reduce": (C.c_int, [P, I32, I32, I32, I32, P, P]),
+    "gbdic_nn_adam": (C.c_int, [P, P, P, P, I64, P, P]),
+    "gbdic_nn_pack_weights": (C.c_int, [P, I32, I32, I32, P, P, I32, P]),
+    "gbdic_nn_regression_loss": (C.c_int, [P, I32, P, I32, I32, P, I32, P, P]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 
