@@ -160,6 +160,22 @@ int gbdic_retire(gbdic_engine *engine, int32_t slot, float *out_state, gbdic_tim
 int gbdic_register_device(gbdic_engine *engine, const uint8_t *device_frame,
                           const gbdic_solver_cfg *cfg, float *device_state, void *stream);
 
+/* Resident variant of register_seeded(): device frame, seed states (state
+ * layout), activity words and output state; `stream` as for
+ * gbdic_register_device.  Inactive subsets get status -1 (-3 ROI-excluded). */
+int gbdic_register_seeded_device(gbdic_engine *engine, const uint8_t *device_frame, const float *device_seed,
+                                 const uint32_t *device_active, const gbdic_solver_cfg *cfg, float *device_state,
+                                 void *stream);
+
+/* Integer ZNCC search (new here; nearest reference component
+ * spatial_seed.wgsl:65-190) of the device target against the prepared
+ * reference for the subsets whose device_mask byte is non-zero (all when
+ * NULL): shifts within +-radius, around the rounded seed translation when
+ * `centered`; writes translation seeds and activity in place. */
+int gbdic_search_seeds_device(gbdic_engine *engine, const uint8_t *device_frame, float *device_seed,
+                              uint32_t *device_active, const uint8_t *device_mask, int32_t radius, int32_t centered,
+                              void *stream);
+
 /* Copies an internal buffer (GBDIC_EXPORT_*) to host memory. */
 int gbdic_export(gbdic_engine *engine, int32_t what, void *host_out, int64_t bytes);
 
@@ -415,9 +431,22 @@ int gbdic_nn_adam(float *param, const float *grad, float *m, float *v, int64_t c
 int gbdic_nn_pack_weights(const float *w, int32_t cout, int32_t cin, int32_t kp, void *wb, void *wt, int32_t kt,
                           void *stream);
 /* Mean squared-error loss over the first `outputs` columns and its gradient
- * (BF16 [B][ldg], zero beyond `outputs`). */
+ * (BF16 [B][ldg] and, when grad_f32 != NULL, FP32 [B][ldg]; zero beyond
+ * `outputs`). */
 int gbdic_nn_regression_loss(const float *pred, int32_t ldp, const float *target, int32_t outputs, int32_t batch,
-                             void *grad, int32_t ldg, float *loss, void *stream);
+                             void *grad, float *grad_f32, int32_t ldg, float *loss, void *stream);
+/* Half-resolution pyramid level of a device uint8 image (exact integer
+ * [1 4 6 4 1]^2 / 256 with reflection, full_pyramid.wgsl:218-249). */
+int gbdic_reduce_half(const uint8_t *src, int32_t width, int32_t height, uint8_t *dst, void *stream);
+/* Seeds of every subset of a grid_w x grid_h grid from network outputs on a
+ * lattice of every `step`-th subset in x and y (lattice_w x lattice_h rows of
+ * `pred`, row stride ldp, normalised [tx/ts, ux*gs, uy*gs, ty/ts, vx*gs,
+ * vy*gs]): bilinear blend of the four surrounding lattice warps, each
+ * Taylor-recentred to the subset centre.  Writes affine seed states (8
+ * floats) and activity 1. */
+int gbdic_nn_lattice_seeds(const float *pred, int32_t ldp, int32_t lattice_w, int32_t lattice_h, int32_t step,
+                           int32_t grid_w, int32_t grid_h, int32_t subset_stride, float translation_scale,
+                           float gradient_scale, float *seeds, uint32_t *active, void *stream);
 
 #ifdef __cplusplus
 }

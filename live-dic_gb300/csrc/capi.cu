@@ -369,6 +369,55 @@ int gbdic_register_device(gbdic_engine *e, const uint8_t *device_frame, const gb
     });
 }
 
+int gbdic_register_seeded_device(gbdic_engine *e, const uint8_t *device_frame, const float *device_seed,
+                                 const uint32_t *device_active, const gbdic_solver_cfg *cfg, float *device_state,
+                                 void *stream) {
+    return guarded(e, [&] {
+        e->require_ready("register_seeded");
+        gbdic::validate_cfg(cfg);
+        if (!device_frame || !device_seed || !device_active || !device_state)
+            fail(GBDIC_EINVAL, "device frame, seed, activity and state are required");
+        auto &rt = *e->rt;
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        cudaStream_t s = stream ? (cudaStream_t)stream : rt.stream();
+        const size_t sb = (size_t)lvl.count * gbdic::state_stride(rt.opts().o.motion_model) * sizeof(float);
+        check_cuda(cudaMemcpyAsync(slot.seed.get(), device_seed, sb, cudaMemcpyDeviceToDevice, s), "seed copy");
+        check_cuda(cudaMemcpyAsync(slot.active.get(), device_active, (size_t)lvl.count * sizeof(uint32_t),
+                                   cudaMemcpyDeviceToDevice, s), "activity copy");
+        rt.enqueue_prefilter(lvl, slot, device_frame, s);
+        const bool disabled = rt.opts().o.outlier_policy == GBDIC_OUTLIER_DISABLED;
+        rt.enqueue_solve(lvl, slot, *cfg, true, false, device_frame, disabled ? device_state : nullptr, s);
+        if (!disabled) rt.enqueue_uod(lvl, slot, false, device_state, s);
+    });
+}
+
+int gbdic_search_seeds_device(gbdic_engine *e, const uint8_t *device_frame, float *device_seed,
+                              uint32_t *device_active, const uint8_t *device_mask, int32_t radius, int32_t centered,
+                              void *stream) {
+    return guarded(e, [&] {
+        e->require_ready("seed search");
+        auto &lvl = e->level;
+        if (!device_frame || !device_seed || !device_active) fail(GBDIC_EINVAL, "device frame, seed and activity are required");
+        if (!lvl.ref_image.get()) fail(GBDIC_ESTATE, "seed search needs a reference prepared by set_reference()");
+        const auto &o = e->rt->opts().o;
+        if (radius < 1 || gbdic::zncc_search_smem(o.subset_size, radius) > 48 * 1024)
+            fail(GBDIC_EINVAL, "radius must be >= 1 and its search tile must fit 48 KB of shared memory");
+        gbdic::SearchArgs q{};
+        q.ref = lvl.ref_image.as<uint8_t>();
+        q.tgt = device_frame;
+        q.seed = device_seed;
+        q.active = device_active;
+        q.selected = lvl.roi && lvl.selected.get() ? lvl.selected.as<uint8_t>() : nullptr;
+        q.W = lvl.W; q.H = lvl.H; q.grid_w = lvl.gw; q.count = lvl.count;
+        q.S = o.subset_size; q.stride = o.subset_stride; q.radius = radius; q.model = o.motion_model;
+        q.centered = centered ? 1 : 0;
+        q.subset_mask = device_mask;
+        cudaStream_t s = stream ? (cudaStream_t)stream : e->rt->stream();
+        check_cuda(gbdic::launch_zncc_search(q, s), "seed search launch");
+    });
+}
+
 int gbdic_apply_uod(gbdic_engine *e, const float *state_in, int32_t seed_mode, float *state_out) {
     return guarded(e, [&] {
         e->require_ready("apply_uod");

@@ -110,6 +110,8 @@ struct SearchArgs {
     unsigned *searched;       // count of searched subsets, or nullptr
     int W, H, grid_w, count, S, stride, radius, model;
     int only_missing;         // search only seeds whose status slot is -1
+    int centered;             // shifts around the rounded seed translation
+    const uint8_t *subset_mask;  // search only where non-zero, or nullptr
 };
 size_t zncc_search_smem(int S, int radius);
 cudaError_t launch_zncc_search(const SearchArgs &a, cudaStream_t stream);
@@ -189,7 +191,15 @@ cudaError_t launch_nn_adam(const NnAdamArgs &a, cudaStream_t s);
 cudaError_t launch_nn_pack_weights(const float *w, int Cout, int Cin, int Kp, void *wb, void *wt, int Kt,
                                    cudaStream_t s);
 cudaError_t launch_nn_regression_loss(const float *pred, int ldp, const float *target, int outputs, int B, void *grad,
-                                      int ldg, float *loss, cudaStream_t s);
+                                      float *grad_f32, int ldg, float *loss, cudaStream_t s);
+struct NnLatticeArgs {
+    const float *pred;    // lattice_w * lattice_h rows, stride ldp, normalised outputs
+    int ldp, lattice_w, lattice_h, step, grid_w, grid_h, stride;
+    float translation_scale, gradient_scale;
+    float *seeds;         // grid_w * grid_h * 8
+    uint32_t *active;
+};
+cudaError_t launch_nn_lattice_seeds(const NnLatticeArgs &a, cudaStream_t s);
 
 struct TemporalArgs {
     float *history;           // fine accepted history

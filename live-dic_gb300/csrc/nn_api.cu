@@ -104,11 +104,29 @@ int gbdic_nn_pack_weights(const float *w, int32_t cout, int32_t cin, int32_t kp,
 }
 
 int gbdic_nn_regression_loss(const float *pred, int32_t ldp, const float *target, int32_t outputs, int32_t batch,
-                             void *grad, int32_t ldg, float *loss, void *stream) {
+                             void *grad, float *grad_f32, int32_t ldg, float *loss, void *stream) {
     if (!pred || !target || !grad || !loss || outputs <= 0 || ldp < outputs || ldg < outputs || batch <= 0)
         return invalid("invalid loss arguments");
-    return rc(gbdic::launch_nn_regression_loss(pred, ldp, target, outputs, batch, grad, ldg, loss, as_stream(stream)),
+    return rc(gbdic::launch_nn_regression_loss(pred, ldp, target, outputs, batch, grad, grad_f32, ldg, loss,
+                                               as_stream(stream)),
               "regression loss");
+}
+
+int gbdic_reduce_half(const uint8_t *src, int32_t width, int32_t height, uint8_t *dst, void *stream) {
+    if (!src || !dst || width < 2 || height < 2) return invalid("invalid reduction arguments");
+    return rc(gbdic::launch_reduce_half(src, width, height, dst, as_stream(stream)), "pyramid reduction");
+}
+
+int gbdic_nn_lattice_seeds(const float *pred, int32_t ldp, int32_t lattice_w, int32_t lattice_h, int32_t step,
+                           int32_t grid_w, int32_t grid_h, int32_t subset_stride, float translation_scale,
+                           float gradient_scale, float *seeds, uint32_t *active, void *stream) {
+    if (!pred || !seeds || !active || ldp < 6 || lattice_w < 1 || lattice_h < 1 || step < 1 || grid_w < 1 ||
+        grid_h < 1 || subset_stride < 1 || (lattice_w - 1) * step < grid_w - step || (lattice_h - 1) * step < grid_h - step ||
+        !(gradient_scale != 0.0f))
+        return invalid("invalid lattice seed arguments");
+    gbdic::NnLatticeArgs a{pred, ldp, lattice_w, lattice_h, step, grid_w, grid_h, subset_stride, translation_scale,
+                           gradient_scale, seeds, active};
+    return rc(gbdic::launch_nn_lattice_seeds(a, as_stream(stream)), "lattice seeds");
 }
 
 }  // extern "C"

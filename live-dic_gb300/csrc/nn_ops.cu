@@ -187,8 +187,8 @@ __global__ void pack_weights_kernel(const float *w, int Cout, int Cin, int Kp, _
 // Loss 0.5 / B sum (pred - target)^2 over the first `outputs` columns and
 // its gradient (pred - target) / B as BF16 [B][ldg] (zero elsewhere); one CTA.
 __global__ void __launch_bounds__(256) regression_loss_kernel(const float *pred, int ldp, const float *target,
-                                                              int outputs, int B, __nv_bfloat16 *grad, int ldg,
-                                                              float *loss) {
+                                                              int outputs, int B, __nv_bfloat16 *grad,
+                                                              float *grad_f32, int ldg, float *loss) {
     float acc = 0.0f;
     for (int i = threadIdx.x; i < B * ldg; i += 256) {
         const int b = i / ldg, j = i % ldg;
@@ -199,6 +199,7 @@ __global__ void __launch_bounds__(256) regression_loss_kernel(const float *pred,
             g = d / (float)B;
         }
         grad[i] = __float2bfloat16(g);
+        if (grad_f32) grad_f32[i] = g;
     }
     __shared__ float red[256];
     red[threadIdx.x] = acc;
@@ -208,6 +209,39 @@ __global__ void __launch_bounds__(256) regression_loss_kernel(const float *pred,
         __syncthreads();
     }
     if (threadIdx.x == 0) *loss = red[0] / (float)B;
+}
+
+// Seeds of every subset from a lattice of every `step`-th subset: bilinear
+// weights over the four surrounding lattice nodes, each node's affine warp
+// Taylor-recentred to the subset centre (offset (gx - lx step) stride).
+__global__ void lattice_seed_kernel(NnLatticeArgs a) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.grid_w * a.grid_h) return;
+    const int gx = idx % a.grid_w, gy = idx / a.grid_w;
+    const float u = (float)gx / (float)a.step, v = (float)gy / (float)a.step;
+    const int lx = a.lattice_w > 1 ? min(max((int)floorf(u), 0), a.lattice_w - 2) : 0;
+    const int ly = a.lattice_h > 1 ? min(max((int)floorf(v), 0), a.lattice_h - 2) : 0;
+    const float fx = a.lattice_w > 1 ? fminf(fmaxf(u - (float)lx, 0.0f), 1.0f) : 0.0f;
+    const float fy = a.lattice_h > 1 ? fminf(fmaxf(v - (float)ly, 0.0f), 1.0f) : 0.0f;
+    float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    for (int corner = 0; corner < 4; ++corner) {
+        const int cx = min(lx + (corner & 1), a.lattice_w - 1), cy = min(ly + (corner >> 1), a.lattice_h - 1);
+        const float w = ((corner & 1) ? fx : 1.0f - fx) * ((corner & 2) ? fy : 1.0f - fy);
+        const float *p = a.pred + (size_t)(cy * a.lattice_w + cx) * a.ldp;
+        const float tx = p[0] * a.translation_scale, ux = p[1] / a.gradient_scale, uy = p[2] / a.gradient_scale;
+        const float ty = p[3] * a.translation_scale, vx = p[4] / a.gradient_scale, vy = p[5] / a.gradient_scale;
+        const float dx = (float)(gx - cx * a.step) * (float)a.stride, dy = (float)(gy - cy * a.step) * (float)a.stride;
+        acc[0] += w * (tx + ux * dx + uy * dy);
+        acc[1] += w * ux;
+        acc[2] += w * uy;
+        acc[3] += w * (ty + vx * dx + vy * dy);
+        acc[4] += w * vx;
+        acc[5] += w * vy;
+    }
+    float4 *s = reinterpret_cast<float4 *>(a.seeds + (size_t)idx * 8);
+    s[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    s[1] = make_float4(acc[4], acc[5], 0.0f, 0.0f);
+    a.active[idx] = 1u;
 }
 
 unsigned blocks(long long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -272,9 +306,16 @@ cudaError_t launch_nn_pack_weights(const float *w, int Cout, int Cin, int Kp, vo
 }
 
 cudaError_t launch_nn_regression_loss(const float *pred, int ldp, const float *target, int outputs, int B, void *grad,
-                                      int ldg, float *loss, cudaStream_t s) {
-    regression_loss_kernel<<<1, 256, 0, s>>>(pred, ldp, target, outputs, B, static_cast<__nv_bfloat16 *>(grad), ldg,
-                                             loss);
+                                      float *grad_f32, int ldg, float *loss, cudaStream_t s) {
+    regression_loss_kernel<<<1, 256, 0, s>>>(pred, ldp, target, outputs, B, static_cast<__nv_bfloat16 *>(grad),
+                                             grad_f32, ldg, loss);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_lattice_seeds(const NnLatticeArgs &a, cudaStream_t s) {
+    const long long n = (long long)a.grid_w * a.grid_h;
+    if (n <= 0) return cudaSuccess;
+    lattice_seed_kernel<<<blocks(n, 256), 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -12,7 +12,10 @@
 // is evaluated in binary64 from the exact sums,
 //   (n Sfg - Sf Sg) / sqrt((n Sff - Sf^2) (n Sgg - Sg^2)),
 // and the best candidate (lowest index on ties) becomes a translation seed.
-// Candidates whose window leaves the image are skipped.
+// Candidates whose window leaves the image are skipped.  In centred mode the
+// shifts are taken around the rounded translation already in the seed (the
+// reseeding of a failed learned proposal), and a subset mask can restrict the
+// search to chosen subsets.
 #include "gbdic_common.cuh"
 #include "gbdic_kernels.h"
 
@@ -27,9 +30,18 @@ __global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
     const int ss = state_stride(a.model), sat = status_slot(a.model);
     float *seed = a.seed + (size_t)idx * ss;
     if (a.only_missing && seed[sat] != -1.0f) return;  // block-uniform
+    if (a.subset_mask != nullptr && a.subset_mask[idx] == 0) return;
     const bool selected = a.selected == nullptr || a.selected[idx] != 0;
     const int S = a.S, R = a.radius, T = S + 2 * R, side = 2 * R + 1, C = side * side;
-    const int px0 = (idx % a.grid_w) * a.stride, py0 = (idx / a.grid_w) * a.stride;
+    // Centred mode: candidates around the rounded current translation seed.
+    int cx0 = 0, cy0 = 0;
+    if (a.centered) {
+        const float sx = seed[0], sy = seed[3];
+        cx0 = (fabsf(sx) <= (float)a.W) ? (int)rintf(sx) : 0;
+        cy0 = (fabsf(sy) <= (float)a.H) ? (int)rintf(sy) : 0;
+    }
+    const int px0 = (idx % a.grid_w) * a.stride + cx0, py0 = (idx / a.grid_w) * a.stride + cy0;
+    const int rx0 = (idx % a.grid_w) * a.stride, ry0 = (idx / a.grid_w) * a.stride;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     __shared__ double s_best[4];
     __shared__ int s_cand[4];
@@ -45,7 +57,7 @@ __global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
     uint8_t *tile = smem + S * S;
     for (int i = tid; i < S * S; i += blockDim.x) {
         const int col = i % S, row = i / S;
-        ref[i] = a.ref[(size_t)(py0 + row) * a.W + px0 + col];
+        ref[i] = a.ref[(size_t)(ry0 + row) * a.W + rx0 + col];
     }
     for (int i = tid; i < T * T; i += blockDim.x) {
         const int col = i % T, row = i / T;
@@ -113,8 +125,8 @@ __global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
         }
         for (int k = 0; k < ss; ++k) seed[k] = 0.0f;
         if (c >= 0 && b > -1.5) {
-            seed[0] = (float)(c % side - R);
-            seed[3] = (float)(c / side - R);
+            seed[0] = (float)(cx0 + c % side - R);
+            seed[3] = (float)(cy0 + c / side - R);
         }
         a.active[idx] = 1u;
         if (a.score) a.score[idx] = (float)b;

@@ -204,7 +204,11 @@ _SIGNATURES = {
     "gbdic_nn_splitk_reduce": (C.c_int, [P, I32, I32, I32, I32, P, P]),
     "gbdic_nn_adam": (C.c_int, [P, P, P, P, I64, P, P]),
     "gbdic_nn_pack_weights": (C.c_int, [P, I32, I32, I32, P, P, I32, P]),
-    "gbdic_nn_regression_loss": (C.c_int, [P, I32, P, I32, I32, P, I32, P, P]),
+    "gbdic_nn_regression_loss": (C.c_int, [P, I32, P, I32, I32, P, P, I32, P, P]),
+    "gbdic_reduce_half": (C.c_int, [P, I32, I32, P, P]),
+    "gbdic_nn_lattice_seeds": (C.c_int, [P, I32, I32, I32, I32, I32, I32, I32, C.c_float, C.c_float, P, P, P]),
+    "gbdic_register_seeded_device": (C.c_int, [P, P, P, P, C.POINTER(SolverCfg), P, P]),
+    "gbdic_search_seeds_device": (C.c_int, [P, P, P, P, P, I32, I32, P]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 

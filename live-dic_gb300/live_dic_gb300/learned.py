@@ -1,0 +1,513 @@
+"""Learned seed proposal: a small CNN that maps a reference/target patch pair
+to an initial affine warp for IC-GN.
+
+No counterpart in the reference (its large-motion initialisers are the image
+pyramid, the Fourier phase correlation of fourier.py and the optional
+wgpu-matching package).  The network, its training and its use are built on
+the library's own kernels:
+
+* ``SeedNet`` -- five 3x3 stride-2 convolutions with ReLU (channels 32, 64,
+  128, 128, 64) and a linear layer to 6 outputs (315,878 parameters) on
+  64 x 64 x 2 patches.  Forward and backward run as implicit GEMMs on the
+  tcgen05 tensor cores (BF16 operands, FP32 accumulation in tensor memory):
+  im2col -> GEMM(+bias, ReLU) forward; gathered output gradients x
+  transposed weights for data gradients; transposed im2col x transposed
+  output gradients (split-K, fixed-order reduction) for weight gradients.
+  FP32 master weights, Adam.  PyTorch only allocates the device buffers and
+  owns the stream.
+* ``training_pairs`` -- subset pairs the engine generates itself: seeded
+  speckle under random affine warps (translation +-20 px, strain +-5 %,
+  rotation +-3 deg), labelled by IC-GN converged from the imposed warp.
+* ``LearnedSeeder`` -- per frame: half-resolution pyramid level, the network
+  on a lattice of every `step`-th subset, lattice -> per-subset seeds
+  (bilinear blend of Taylor-recentred warps), seeded IC-GN; subsets that
+  fail or whose ZNCC falls below the threshold are reseeded by the integer
+  ZNCC search around their proposal and solved again.
+
+Outputs are normalised as [tx / 16, ux * 20, uy * 20, ty / 16, vx * 20,
+vy * 20] (translations in full-resolution pixels).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native
+from .engine import ICGNError
+
+CONV_CHANNELS = ((2, 32), (32, 64), (64, 128), (128, 128), (128, 64))
+PATCH = 64
+OUTPUTS = 6
+OUT_PAD = 16          # linear-layer output columns (GEMM tile)
+LOSS_PAD = 64         # K padding of the output gradient
+TRANSLATION_SCALE = 16.0
+GRADIENT_SCALE = 20.0
+NORMALISATION = np.array([1 / TRANSLATION_SCALE, GRADIENT_SCALE, GRADIENT_SCALE, 1 / TRANSLATION_SCALE,
+                          GRADIENT_SCALE, GRADIENT_SCALE], np.float32)
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _pad(x: int, m: int) -> int:
+    return (x + m - 1) // m * m
+
+
+def _ptr(t) -> C.c_void_p | None:
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _call(lib, name: str, *args) -> None:
+    code = getattr(lib, name)(*args)
+    _native.check(code, lib.gbdic_last_error(None))
+
+
+@dataclass
+class _Conv:
+    cin: int
+    cout: int
+    H: int            # input side
+    OH: int           # output side
+    kp: int           # forward reduction length (padded 9 cin)
+    kp_rows: int      # kp padded to 128 (rows of the weight-gradient GEMM)
+    kt: int           # data-gradient reduction length (9 cout)
+    M: int            # output rows (B OH^2)
+    Min: int          # input rows (B H^2)
+
+
+class SeedNet:
+    """The proposal network and its optimiser state on one CUDA device.
+    ``batch`` (a multiple of 128) fixes the buffer shapes."""
+
+    def __init__(self, batch: int = 512, *, device: int = 0, seed: int = 0) -> None:
+        torch = _torch()
+        if batch <= 0 or batch % 128:
+            raise ValueError("batch must be a positive multiple of 128")
+        self.lib = _native.load()
+        self.B = batch
+        self.device = torch.device("cuda", device)
+        dev = self.device
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        self.convs: list[_Conv] = []
+        H = PATCH
+        for cin, cout in CONV_CHANNELS:
+            oh = (H + 1) // 2
+            kp = _pad(9 * cin, 64)
+            self.convs.append(_Conv(cin, cout, H, oh, kp, _pad(kp, 128), 9 * cout, batch * oh * oh, batch * H * H))
+            H = oh
+        self.features = CONV_CHANNELS[-1][1] * H * H  # 64 x 2 x 2 = 256
+        bf16, f32 = torch.bfloat16, torch.float32
+        self.params: list = []
+        # conv weights [Cout][kp] (zero beyond 9 cin), He initialisation
+        self.w, self.b = [], []
+        for c in self.convs:
+            w = torch.zeros(c.cout, c.kp)
+            w[:, :9 * c.cin] = torch.randn(c.cout, 9 * c.cin, generator=g) * math.sqrt(2.0 / (9 * c.cin))
+            self.w.append(w.to(dev))
+            self.b.append(torch.zeros(c.cout, device=dev))
+        w6 = torch.zeros(OUT_PAD, self.features)
+        w6[:OUTPUTS] = torch.randn(OUTPUTS, self.features, generator=g) * math.sqrt(1.0 / self.features)
+        self.w6 = w6.to(dev)
+        self.b6 = torch.zeros(OUT_PAD, device=dev)
+        self.params = [*self.w, *self.b, self.w6, self.b6]
+        self.grads = [torch.zeros_like(p) for p in self.params]
+        self.m = [torch.zeros_like(p) for p in self.params]
+        self.v = [torch.zeros_like(p) for p in self.params]
+        self.steps = 0
+        # BF16 operands
+        self.wb = [torch.zeros(c.cout, c.kp, dtype=bf16, device=dev) for c in self.convs]
+        self.wt = [torch.zeros(c.cin, c.kt, dtype=bf16, device=dev) for c in self.convs]
+        self.w6b = torch.zeros(OUT_PAD, self.features, dtype=bf16, device=dev)
+        self.w6t = torch.zeros(self.features, LOSS_PAD, dtype=bf16, device=dev)
+        # activations
+        self.x0 = torch.zeros(batch, PATCH, PATCH, 2, dtype=bf16, device=dev)
+        self.a = [torch.zeros(c.M, c.kp, dtype=bf16, device=dev) for c in self.convs]
+        self.y = [torch.zeros(c.M, c.cout, dtype=bf16, device=dev) for c in self.convs]
+        self.out = torch.zeros(batch, OUT_PAD, dtype=f32, device=dev)
+        # backward buffers (allocated on first backward)
+        self._bwd = None
+        self.err = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.loss = torch.zeros(1, dtype=f32, device=dev)
+        self.pack()
+
+    # ------------------------------------------------------------ kernels
+    def _gemm(self, a, b, M, N, K, *, d_f32=None, d_bf16=None, ldd=None, bias=None, relu=False, k_split=1,
+              split_stride=0, stream=None):
+        desc = _native.NnGemmDesc(a.data_ptr(), b.data_ptr(), M, N, K, k_split,
+                                  d_f32.data_ptr() if d_f32 is not None else None,
+                                  d_bf16.data_ptr() if d_bf16 is not None else None, ldd or N, split_stride,
+                                  bias.data_ptr() if bias is not None else None, int(relu), 0)
+        _call(self.lib, "gbdic_nn_gemm", C.byref(desc), _ptr(self.err), stream)
+
+    def _shape(self, i: int) -> _native.NnConvShape:
+        c = self.convs[i]
+        return _native.NnConvShape(self.B, c.H, c.H, c.cin, c.OH, c.OH, c.cout, c.kp)
+
+    def pack(self, stream=None) -> None:
+        """BF16 operands from the FP32 master weights."""
+        for i, c in enumerate(self.convs):
+            _call(self.lib, "gbdic_nn_pack_weights", _ptr(self.w[i]), c.cout, c.cin, c.kp, _ptr(self.wb[i]),
+                  _ptr(self.wt[i]), c.kt, stream)
+        _call(self.lib, "gbdic_nn_pack_weights", _ptr(self.w6), OUT_PAD, 1, self.features, _ptr(self.w6b), None, 0,
+              stream)
+        _call(self.lib, "gbdic_nn_transpose", _ptr(self.w6b), OUT_PAD, self.features, self.features, _ptr(self.w6t),
+              LOSS_PAD, self.features, stream)
+
+    # ------------------------------------------------------------ forward
+    def forward(self, stream=None):
+        """self.x0 (B x 64 x 64 x 2 BF16) -> self.out (B x 16 FP32, first 6 used)."""
+        x = self.x0
+        for i, c in enumerate(self.convs):
+            _call(self.lib, "gbdic_nn_im2col", C.byref(self._shape(i)), _ptr(x), _ptr(self.a[i]), stream)
+            self._gemm(self.a[i], self.wb[i], c.M, c.cout, c.kp, d_bf16=self.y[i], bias=self.b[i], relu=True,
+                       stream=stream)
+            x = self.y[i]
+        self._gemm(self.y[-1], self.w6b, self.B, OUT_PAD, self.features, d_f32=self.out, bias=self.b6, stream=stream)
+        return self.out
+
+    # ------------------------------------------------------------ backward
+    def _backward_buffers(self):
+        torch = _torch()
+        dev, bf16, f32 = self.device, torch.bfloat16, torch.float32
+        B = self.B
+        bufs = {
+            "dout": torch.zeros(B, LOSS_PAD, dtype=bf16, device=dev),
+            "dout_f32": torch.zeros(B, LOSS_PAD, dtype=f32, device=dev),
+            "doutT": torch.zeros(OUT_PAD, B, dtype=bf16, device=dev),
+            "y5T": torch.zeros(self.features, B, dtype=bf16, device=dev),
+            "dw6T": torch.zeros(self.features, OUT_PAD, dtype=f32, device=dev),
+            "dy": [torch.zeros(c.M, c.cout, dtype=f32, device=dev) for c in self.convs],
+            "dz": [torch.zeros(c.M, c.cout, dtype=bf16, device=dev) for c in self.convs],
+            "dzT": [torch.zeros(c.cout, c.M, dtype=bf16, device=dev) for c in self.convs],
+            "aT": [torch.zeros(c.kp_rows, c.M, dtype=bf16, device=dev) for c in self.convs],
+            "g": [None] + [torch.zeros(c.Min, c.kt, dtype=bf16, device=dev) for c in self.convs[1:]],
+        }
+        bufs["splits"] = [self._splits(c) for c in self.convs]
+        bufs["partial"] = [torch.zeros(s, c.kp_rows, c.cout, dtype=f32, device=dev)
+                           for s, c in zip(bufs["splits"], self.convs, strict=True)]
+        return bufs
+
+    @staticmethod
+    def _splits(c: _Conv) -> int:
+        tiles = (c.kp_rows // 128) * max(1, c.cout // 128)
+        want = max(1, 304 // tiles)
+        s = 1
+        while s * 2 <= want and c.M % (64 * s * 2) == 0 and c.M // (s * 2) >= 256:
+            s *= 2
+        return s
+
+    def loss_and_grad(self, target, stream=None) -> None:
+        """Loss of self.out against `target` (B x 6 FP32, normalised) into
+        self.loss and the output gradient."""
+        if self._bwd is None:
+            self._bwd = self._backward_buffers()
+        b = self._bwd
+        _call(self.lib, "gbdic_nn_regression_loss", _ptr(self.out), OUT_PAD, _ptr(target), OUTPUTS, self.B,
+              _ptr(b["dout"]), _ptr(b["dout_f32"]), LOSS_PAD, _ptr(self.loss), stream)
+
+    def backward(self, stream=None) -> None:
+        """Gradients of every parameter into self.grads (after loss_and_grad)."""
+        b = self._bwd
+        lib, B, F = self.lib, self.B, self.features
+        nconv = len(self.convs)
+        # linear layer: dW6^T = Y5^T dOut, db6 = sum dOut, dY5 = dOut W6
+        _call(lib, "gbdic_nn_transpose", _ptr(self.y[-1]), B, F, F, _ptr(b["y5T"]), B, F, stream)
+        _call(lib, "gbdic_nn_transpose", _ptr(b["dout"]), B, OUT_PAD, LOSS_PAD, _ptr(b["doutT"]), B, OUT_PAD, stream)
+        self._gemm(b["y5T"], b["doutT"], F, OUT_PAD, B, d_f32=b["dw6T"], stream=stream)
+        _call(lib, "gbdic_nn_splitk_reduce", _ptr(b["dw6T"]), 1, F, OUT_PAD, F, _ptr(self.grads[2 * nconv]), stream)
+        _call(lib, "gbdic_nn_bias_grad", _ptr(b["dout_f32"]), LOSS_PAD, None, B, OUT_PAD,
+              _ptr(self.grads[2 * nconv + 1]), stream)
+        self._gemm(b["dout"], self.w6t, B, F, LOSS_PAD, d_f32=b["dy"][-1].view(B, F), stream=stream)
+        for i in range(nconv - 1, -1, -1):
+            c = self.convs[i]
+            dy, dz = b["dy"][i], b["dz"][i]
+            _call(lib, "gbdic_nn_relu_backward", _ptr(dy), c.cout, _ptr(self.y[i]), _ptr(dz), c.M, c.cout, stream)
+            _call(lib, "gbdic_nn_bias_grad", _ptr(dy), c.cout, _ptr(self.y[i]), c.M, c.cout,
+                  _ptr(self.grads[nconv + i]), stream)
+            # weight gradient: dW^T[k][co] = sum_m A[m][k] dZ[m][co]
+            _call(lib, "gbdic_nn_transpose", _ptr(self.a[i]), c.M, c.kp, c.kp, _ptr(b["aT"][i]), c.M, c.kp_rows,
+                  stream)
+            _call(lib, "gbdic_nn_transpose", _ptr(dz), c.M, c.cout, c.cout, _ptr(b["dzT"][i]), c.M, c.cout, stream)
+            splits = b["splits"][i]
+            self._gemm(b["aT"][i], b["dzT"][i], c.kp_rows, c.cout, c.M, d_f32=b["partial"][i], k_split=splits,
+                       split_stride=c.kp_rows * c.cout, stream=stream)
+            _call(lib, "gbdic_nn_splitk_reduce", _ptr(b["partial"][i]), splits, c.kp_rows, c.cout, c.kp,
+                  _ptr(self.grads[i]), stream)
+            if i > 0:
+                # data gradient: dY_{i-1}[m][ci] = sum_(ky,kx,co) G[m][.] Wt[ci][.]
+                _call(lib, "gbdic_nn_dgrad_gather", C.byref(self._shape(i)), _ptr(dz), _ptr(b["g"][i]), stream)
+                self._gemm(b["g"][i], self.wt[i], c.Min, c.cin, c.kt, d_f32=b["dy"][i - 1], stream=stream)
+
+    def adam_step(self, lr: float = 1e-3, *, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
+                  weight_decay: float = 0.0, stream=None) -> None:
+        self.steps += 1
+        t = self.steps
+        hyper = (C.c_float * 7)(lr, beta1, beta2, eps, 1 - beta1 ** t, 1 - beta2 ** t, weight_decay)
+        for p, g, m, v in zip(self.params, self.grads, self.m, self.v, strict=True):
+            _call(self.lib, "gbdic_nn_adam", _ptr(p), _ptr(g), _ptr(m), _ptr(v), p.numel(), hyper, stream)
+        self.pack(stream)
+
+    def check_device_errors(self) -> None:
+        if int(self.err.item()) != 0:
+            raise ICGNError("a tensor-core GEMM pipeline wait expired")
+
+    # ------------------------------------------------------------ patches
+    def load_patches(self, refs, tgts, image_index, centres, count: int, width: int, height: int, stream=None):
+        """Patches into self.x0 (rows beyond `count` keep their contents)."""
+        _call(self.lib, "gbdic_nn_patches", _ptr(refs), _ptr(tgts), _ptr(image_index), _ptr(centres), count, width,
+              height, _ptr(self.x0), stream)
+
+    def state_dict(self) -> dict[str, np.ndarray]:
+        names = [f"w{i}" for i in range(len(self.w))] + [f"b{i}" for i in range(len(self.b))] + ["w6", "b6"]
+        return {n: p.detach().cpu().numpy() for n, p in zip(names, self.params, strict=True)}
+
+    def load_state_dict(self, state: dict[str, np.ndarray]) -> None:
+        torch = _torch()
+        names = [f"w{i}" for i in range(len(self.w))] + [f"b{i}" for i in range(len(self.b))] + ["w6", "b6"]
+        for n, p in zip(names, self.params, strict=True):
+            p.copy_(torch.as_tensor(state[n], device=self.device))
+        self.pack()
+
+
+# ---------------------------------------------------------------- training data
+def random_warp(rng: np.random.Generator, *, translation: float = 20.0, strain: float = 0.05,
+                rotation_deg: float = 3.0) -> tuple[np.ndarray, np.ndarray]:
+    """(t, G): translation and displacement gradient R (I + E) - I."""
+    t = rng.uniform(-translation, translation, 2)
+    exx, eyy, exy = rng.uniform(-strain, strain, 3)
+    th = math.radians(rng.uniform(-rotation_deg, rotation_deg))
+    R = np.array([[math.cos(th), -math.sin(th)], [math.sin(th), math.cos(th)]])
+    G = R @ (np.eye(2) + np.array([[exx, exy], [exy, eyy]])) - np.eye(2)
+    return t, G
+
+
+@dataclass
+class TrainingSet:
+    """Level-1 images on the device and labelled patch centres."""
+
+    refs: object          # torch uint8 [n, h, w]
+    tgts: object
+    ref_ptrs: object      # torch int64 [n] device pointers
+    tgt_ptrs: object
+    image_index: object   # torch int32 [P]
+    centres: object       # torch float32 [P, 2] level-1 pixels
+    labels: object        # torch float32 [P, 6] normalised
+    width: int
+    height: int
+
+    @property
+    def size(self) -> int:
+        return int(self.labels.shape[0])
+
+
+def training_pairs(images: int, *, size: int = 512, subset_size: int = 31, subset_stride: int = 8, seed: int = 0,
+                   device: int = 0, translation: float = 20.0, strain: float = 0.05,
+                   rotation_deg: float = 3.0) -> TrainingSet:
+    """Subset pairs generated by the engine: speckle under random affine
+    warps, labelled by IC-GN converged from the imposed warp (status 1 only)."""
+    torch = _torch()
+    from . import synthetic
+    from .native_backend import ICGNWGPU
+
+    lib = _native.load()
+    rng = np.random.default_rng(seed)
+    dev = torch.device("cuda", device)
+    half = size // 2
+    refs = torch.empty(images, half, half, dtype=torch.uint8, device=dev)
+    tgts = torch.empty_like(refs)
+    idx_all, cen_all, lab_all = [], [], []
+    with ICGNWGPU(subset_size=subset_size, subset_stride=subset_stride, outlier_policy="disabled",
+                  device=device) as engine:
+        for k in range(images):
+            ref, sp = synthetic.reference_image(size, size, seed=seed * 100003 + 2 * k, device=f"cuda:{device}")
+            t, G = random_warp(rng, translation=translation, strain=strain, rotation_deg=rotation_deg)
+            c = 0.5 * (size - 1)
+
+            def field(X, Y, t=t, G=G, c=c):
+                return (t[0] + G[0, 0] * (X - c) + G[0, 1] * (Y - c), t[1] + G[1, 0] * (X - c) + G[1, 1] * (Y - c))
+
+            tgt = synthetic.deformed_image(sp, field, noise_seed=seed * 100003 + 2 * k + 1, device=f"cuda:{device}")
+            engine.set_reference(ref)
+            gh, gw = engine.grid_height, engine.grid_width
+            cx, cy = synthetic.subset_centres(size, size, subset_size, subset_stride)
+            truth = np.zeros((gh, gw, 6), np.float32)
+            u, v = field(cx, cy)
+            truth[..., 0], truth[..., 3] = u, v
+            truth[..., 1], truth[..., 2], truth[..., 4], truth[..., 5] = G[0, 0], G[0, 1], G[1, 0], G[1, 1]
+            result = engine.register_seeded(tgt, truth, np.ones((gh, gw), bool))
+            ok = np.asarray(result.status) == 1
+            r_dev = torch.from_numpy(ref).to(dev)
+            t_dev = torch.from_numpy(tgt).to(dev)
+            _call(lib, "gbdic_reduce_half", _ptr(r_dev), size, size, _ptr(refs[k]), None)
+            _call(lib, "gbdic_reduce_half", _ptr(t_dev), size, size, _ptr(tgts[k]), None)
+            idx_all.append(np.full(int(ok.sum()), k, np.int32))
+            cen_all.append(np.stack([cx[ok] / 2.0, cy[ok] / 2.0], -1).astype(np.float32))
+            lab_all.append((np.asarray(result.parameters)[ok] * NORMALISATION).astype(np.float32))
+    torch.cuda.synchronize(dev)
+    ptr = lambda t: torch.tensor([t[i].data_ptr() for i in range(images)], dtype=torch.int64, device=dev)  # noqa: E731
+    return TrainingSet(refs, tgts, ptr(refs), ptr(tgts), torch.from_numpy(np.concatenate(idx_all)).to(dev),
+                       torch.from_numpy(np.concatenate(cen_all)).to(dev), torch.from_numpy(np.concatenate(lab_all)).to(dev),
+                       half, half)
+
+
+def train(net: SeedNet, data: TrainingSet, *, steps: int, lr: float = 2e-3, seed: int = 0,
+          log_every: int = 0) -> list[float]:
+    """Adam on shuffled mini-batches of `data`; returns the loss of every step."""
+    torch = _torch()
+    g = torch.Generator(device=net.device).manual_seed(seed)
+    B = net.B
+    losses = []
+    target = torch.zeros(B, OUTPUTS, device=net.device)
+    idx = torch.empty(B, dtype=torch.int32, device=net.device)
+    cen = torch.empty(B, 2, device=net.device)
+    order = torch.randperm(data.size, generator=g, device=net.device)
+    cursor = 0
+    for step in range(steps):
+        if cursor + B > data.size:
+            order = torch.randperm(data.size, generator=g, device=net.device)
+            cursor = 0
+        pick = order[cursor:cursor + B]
+        cursor += B
+        idx.copy_(data.image_index[pick])
+        cen.copy_(data.centres[pick])
+        target.copy_(data.labels[pick])
+        net.load_patches(data.ref_ptrs, data.tgt_ptrs, idx, cen, B, data.width, data.height)
+        # cosine decay
+        rate = lr * 0.5 * (1 + math.cos(math.pi * step / max(1, steps)))
+        net.forward()
+        net.loss_and_grad(target)
+        net.backward()
+        net.adam_step(rate)
+        if log_every and (step % log_every == 0 or step == steps - 1):
+            losses.append(float(net.loss.item()))
+    torch.cuda.synchronize(net.device)
+    net.check_device_errors()
+    return losses
+
+
+def predict(net: SeedNet, refs_ptrs, tgts_ptrs, image_index, centres, width: int, height: int):
+    """Normalised predictions (P x 6, numpy) for P patch centres."""
+    torch = _torch()
+    P = int(centres.shape[0])
+    out = np.empty((P, OUTPUTS), np.float32)
+    for s in range(0, P, net.B):
+        n = min(net.B, P - s)
+        net.load_patches(refs_ptrs, tgts_ptrs, None if image_index is None else image_index[s:s + n],
+                         centres[s:s + n], n, width, height)
+        net.forward()
+        out[s:s + n] = net.out[:n, :OUTPUTS].cpu().numpy()
+    torch.cuda.synchronize(net.device)
+    return out
+
+
+# ---------------------------------------------------------------- inference
+class LearnedSeeder:
+    """Learned-seed registration for one fixed reference on the single-scale
+    engine: network proposals on a subset lattice, seeded IC-GN, and ZNCC
+    reseeding of failed or low-ZNCC subsets."""
+
+    def __init__(self, engine, net: SeedNet, *, step: int = 4, reseed_radius: int = 6) -> None:
+        torch = _torch()
+        if not engine._reference_ready or engine.motion_model != "affine":
+            raise ValueError("LearnedSeeder needs an affine engine with a prepared reference")
+        self.engine, self.net, self.step, self.radius = engine, net, int(step), int(reseed_radius)
+        self.lib = _native.load()
+        dev = net.device
+        W, H = engine.width, engine.height
+        self.W, self.H, self.gw, self.gh = W, H, engine.grid_width, engine.grid_height
+        self.lw, self.lh = (self.gw + self.step - 1) // self.step, (self.gh + self.step - 1) // self.step
+        self.lattice = self.lw * self.lh
+        S, s = engine.subset_size, engine.subset_stride
+        gy, gx = np.mgrid[0:self.lh, 0:self.lw] * self.step
+        cx = gx * s + 0.5 * (S - 1)
+        cy = gy * s + 0.5 * (S - 1)
+        self.centres = torch.from_numpy(np.stack([cx.ravel() / 2.0, cy.ravel() / 2.0], -1).astype(np.float32)).to(dev)
+        self.ref_half = torch.empty(H // 2, W // 2, dtype=torch.uint8, device=dev)
+        self.tgt_half = torch.empty_like(self.ref_half)
+        self.ref_ptrs = torch.tensor([self.ref_half.data_ptr()], dtype=torch.int64, device=dev)
+        self.tgt_ptrs = torch.tensor([self.tgt_half.data_ptr()], dtype=torch.int64, device=dev)
+        self._ref_full = torch.empty(H, W, dtype=torch.uint8, device=dev)
+        usable = np.asarray(engine.reference_valid, dtype=bool)
+        if engine.roi is not None:
+            usable = usable & np.asarray(engine.roi.selected, dtype=bool)
+        self.usable = torch.from_numpy(np.ascontiguousarray(usable).ravel()).to(dev)
+        self.pred = torch.zeros(self.lattice, OUT_PAD, device=dev)
+        self.seeds = torch.zeros(self.gh * self.gw * 8, device=dev)
+        self.active = torch.zeros(self.gh * self.gw, dtype=torch.int32, device=dev)
+        self.state = torch.zeros(self.gh * self.gw * 8, device=dev)
+        self.mask = torch.zeros(self.gh * self.gw, dtype=torch.uint8, device=dev)
+        self.batches = (self.lattice + net.B - 1) // net.B
+
+    def set_reference_image(self, reference: np.ndarray) -> None:
+        """Half-resolution reference for the network (the engine keeps its own)."""
+        torch = _torch()
+        self._ref_full.copy_(torch.from_numpy(np.ascontiguousarray(reference, dtype=np.uint8)))
+        _call(self.lib, "gbdic_reduce_half", _ptr(self._ref_full), self.W, self.H, _ptr(self.ref_half), None)
+
+    def propose(self, frame, stream=None) -> None:
+        """Network proposals for device frame `frame` (uint8 H x W) -> self.seeds."""
+        net = self.net
+        _call(self.lib, "gbdic_reduce_half", _ptr(frame), self.W, self.H, _ptr(self.tgt_half), stream)
+        for b in range(self.batches):
+            s0 = b * net.B
+            n = min(net.B, self.lattice - s0)
+            _call(self.lib, "gbdic_nn_patches", _ptr(self.ref_ptrs), _ptr(self.tgt_ptrs), None,
+                  C.c_void_p(self.centres.data_ptr() + 8 * s0), n, self.W // 2, self.H // 2, _ptr(net.x0), stream)
+            net.forward(stream)
+            _native_copy(self.pred, s0, net.out, n)
+        _call(self.lib, "gbdic_nn_lattice_seeds", _ptr(self.pred), OUT_PAD, self.lw, self.lh, self.step, self.gw,
+              self.gh, self.engine.subset_stride, C.c_float(TRANSLATION_SCALE), C.c_float(GRADIENT_SCALE),
+              _ptr(self.seeds), _ptr(self.active), stream)
+
+    def register_device(self, frame, *, reseed: bool = True, stream=None) -> dict:
+        """Learned-seed registration of a device frame into self.state;
+        returns counts (reseeded subsets)."""
+        torch = _torch()
+        eng = self.engine
+        cfg = C.byref(eng._cfg(eng._config))
+        self.propose(frame, stream)
+        _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
+                     _ptr(self.state), stream)
+        reseeded = 0
+        if reseed:
+            status = self.state.view(-1, 8)[:, 6]
+            failed = (status < 0.5) & self.usable
+            reseeded = int(failed.sum().item())
+            if reseeded:
+                self.mask.copy_(failed.to(torch.uint8))
+                _call_engine(eng, "gbdic_search_seeds_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active),
+                             _ptr(self.mask), self.radius, 1, stream)
+                self.active.copy_(failed.to(torch.int32))
+                retry = torch.empty_like(self.state)
+                _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
+                             _ptr(retry), stream)
+                rows = failed.nonzero().squeeze(1)
+                self.state.view(-1, 8)[rows] = retry.view(-1, 8)[rows]
+        return {"reseeded": reseeded}
+
+
+def _native_copy(dst, row0: int, src, n: int) -> None:
+    dst[row0:row0 + n].copy_(src[:n])
+
+
+def _call_engine(engine, name: str, *args) -> None:
+    code = getattr(engine._lib, name)(engine._handle, *args)
+    engine._check(code)
+
+
+def timed(fn, *args, repeats: int = 1, **kwargs) -> float:
+    torch = _torch()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        fn(*args, **kwargs)
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / repeats

@@ -932,16 +932,25 @@ void oracle_temporal_save_previous(int count, int model, const float *history, c
  * over exact integer sums of the 8-bit windows, lowest row-major index on
  * ties; windows leaving the image are skipped.  Writes a translation seed
  * and activity 1 (ROI-excluded subsets: zero seed, activity 0). */
-void oracle_seed_search(const uint8_t *ref, const uint8_t *tgt, int W, int H, int grid_w, int grid_h, int S,
-                        int stride, int R, int model, int only_missing, const uint8_t *selected, float *seed,
-                        uint32_t *active, float *score) {
+/* centered: shifts around the rounded seed translation; mask (or NULL):
+ * search only subsets whose byte is non-zero. */
+void oracle_seed_search_ex(const uint8_t *ref, const uint8_t *tgt, int W, int H, int grid_w, int grid_h, int S,
+                           int stride, int R, int model, int only_missing, const uint8_t *selected, float *seed,
+                           uint32_t *active, float *score, int centered, const uint8_t *mask) {
     const int ss = state_stride(model), sat = model == MODEL_QUADRATIC ? 12 : 6;
     const int count = grid_w * grid_h, side = 2 * R + 1;
     #pragma omp parallel for schedule(dynamic, 4)
     for (int idx = 0; idx < count; ++idx) {
         float *sd = seed + (size_t)idx * ss;
         if (only_missing && sd[sat] != -1.0f) continue;
-        const int px0 = (idx % grid_w) * stride, py0 = (idx / grid_w) * stride;
+        if (mask && !mask[idx]) continue;
+        int cx0 = 0, cy0 = 0;
+        if (centered) {
+            cx0 = fabsf(sd[0]) <= (float)W ? (int)rintf(sd[0]) : 0;
+            cy0 = fabsf(sd[3]) <= (float)H ? (int)rintf(sd[3]) : 0;
+        }
+        const int rx0 = (idx % grid_w) * stride, ry0 = (idx / grid_w) * stride;
+        const int px0 = rx0 + cx0, py0 = ry0 + cy0;
         if (selected && !selected[idx]) {
             if (!only_missing) {
                 for (int k = 0; k < ss; ++k) sd[k] = 0.0f;
@@ -953,7 +962,7 @@ void oracle_seed_search(const uint8_t *ref, const uint8_t *tgt, int W, int H, in
         long long sf = 0, sff = 0;
         for (int r = 0; r < S; ++r)
             for (int c = 0; c < S; ++c) {
-                const long long f = ref[(size_t)(py0 + r) * W + px0 + c];
+                const long long f = ref[(size_t)(ry0 + r) * W + rx0 + c];
                 sf += f;
                 sff += f * f;
             }
@@ -967,7 +976,7 @@ void oracle_seed_search(const uint8_t *ref, const uint8_t *tgt, int W, int H, in
             for (int r = 0; r < S; ++r)
                 for (int c = 0; c < S; ++c) {
                     const long long g = tgt[(size_t)(py0 + dy + r) * W + px0 + dx + c];
-                    const long long f = ref[(size_t)(py0 + r) * W + px0 + c];
+                    const long long f = ref[(size_t)(ry0 + r) * W + rx0 + c];
                     sg += g;
                     sgg += g * g;
                     sfg += f * g;
@@ -982,12 +991,19 @@ void oracle_seed_search(const uint8_t *ref, const uint8_t *tgt, int W, int H, in
         }
         for (int k = 0; k < ss; ++k) sd[k] = 0.0f;
         if (best_cand >= 0 && best > -1.5) {
-            sd[0] = (float)(best_cand % side - R);
-            sd[3] = (float)(best_cand / side - R);
+            sd[0] = (float)(cx0 + best_cand % side - R);
+            sd[3] = (float)(cy0 + best_cand / side - R);
         }
         active[idx] = 1u;
         if (score) score[idx] = (float)best;
     }
+}
+
+void oracle_seed_search(const uint8_t *ref, const uint8_t *tgt, int W, int H, int grid_w, int grid_h, int S,
+                        int stride, int R, int model, int only_missing, const uint8_t *selected, float *seed,
+                        uint32_t *active, float *score) {
+    oracle_seed_search_ex(ref, tgt, W, H, grid_w, grid_h, S, stride, R, model, only_missing, selected, seed, active,
+                          score, 0, NULL);
 }
 
 /* ------------------------------------------------------------ final ZNCC */

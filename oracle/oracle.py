@@ -226,7 +226,8 @@ def transfer_seed(
 
 def seed_search(reference: np.ndarray, target: np.ndarray, *, subset_size: int, subset_stride: int, radius: int,
                 model: str = "affine", seed: np.ndarray | None = None, only_missing: bool = False,
-                selected: np.ndarray | None = None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+                selected: np.ndarray | None = None, centered: bool = False,
+                mask: np.ndarray | None = None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     """Exhaustive integer ZNCC search; returns (seed states, activity, best scores)."""
     ref = np.ascontiguousarray(reference, dtype=np.uint8)
     tgt = np.ascontiguousarray(target, dtype=np.uint8)
@@ -238,9 +239,11 @@ def seed_search(reference: np.ndarray, target: np.ndarray, *, subset_size: int, 
     active = np.ones(gh * gw, np.uint32)
     score = np.full(gh * gw, -3.0, np.float32)
     sel = None if selected is None else np.ascontiguousarray(selected, dtype=np.uint8).ravel()
-    lib().oracle_seed_search(
+    msk = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8).ravel()
+    lib().oracle_seed_search_ex(
         _p(ref, C.c_uint8), _p(tgt, C.c_uint8), w, h, gw, gh, subset_size, subset_stride, radius, MODELS[model],
-        int(only_missing), _p(sel, C.c_uint8), _p(seeds), _p(active, C.c_uint32), _p(score),
+        int(only_missing), _p(sel, C.c_uint8), _p(seeds), _p(active, C.c_uint32), _p(score), int(centered),
+        _p(msk, C.c_uint8),
     )
     return seeds, active, score
 
