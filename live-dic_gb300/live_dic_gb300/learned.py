@@ -414,7 +414,7 @@ class LearnedSeeder:
     engine: network proposals on a subset lattice, seeded IC-GN, and ZNCC
     reseeding of failed or low-ZNCC subsets."""
 
-    def __init__(self, engine, net: SeedNet, *, step: int = 4, reseed_radius: int = 6) -> None:
+    def __init__(self, engine, net: SeedNet, *, step: int = 4, reseed_radius: int = 10) -> None:
         torch = _torch()
         if not engine._reference_ready or engine.motion_model != "affine":
             raise ValueError("LearnedSeeder needs an affine engine with a prepared reference")
@@ -438,13 +438,18 @@ class LearnedSeeder:
         usable = np.asarray(engine.reference_valid, dtype=bool)
         if engine.roi is not None:
             usable = usable & np.asarray(engine.roi.selected, dtype=bool)
-        self.usable = torch.from_numpy(np.ascontiguousarray(usable).ravel()).to(dev)
+        self.usable = torch.from_numpy(np.array(usable, dtype=bool).ravel()).to(dev)
         self.pred = torch.zeros(self.lattice, OUT_PAD, device=dev)
         self.seeds = torch.zeros(self.gh * self.gw * 8, device=dev)
         self.active = torch.zeros(self.gh * self.gw, dtype=torch.int32, device=dev)
         self.state = torch.zeros(self.gh * self.gw * 8, device=dev)
         self.mask = torch.zeros(self.gh * self.gw, dtype=torch.uint8, device=dev)
         self.batches = (self.lattice + net.B - 1) // net.B
+        # One non-default stream carries the network, the engine's kernels and
+        # the mask arithmetic in order (a NULL stream would select the
+        # engine's own stream).
+        self.stream = torch.cuda.Stream(device=dev)
+        self._handle = C.c_void_p(self.stream.cuda_stream)
 
     def set_reference_image(self, reference: np.ndarray) -> None:
         """Half-resolution reference for the network (the engine keeps its own)."""
@@ -452,8 +457,18 @@ class LearnedSeeder:
         self._ref_full.copy_(torch.from_numpy(np.ascontiguousarray(reference, dtype=np.uint8)))
         _call(self.lib, "gbdic_reduce_half", _ptr(self._ref_full), self.W, self.H, _ptr(self.ref_half), None)
 
-    def propose(self, frame, stream=None) -> None:
-        """Network proposals for device frame `frame` (uint8 H x W) -> self.seeds."""
+    def propose(self, frame) -> None:
+        """Network proposals for device frame `frame` (uint8 H x W) -> self.seeds
+        (on self.stream)."""
+        torch = _torch()
+        net = self.net
+        stream = self._handle
+        self.stream.wait_stream(torch.cuda.current_stream(net.device))
+        with torch.cuda.stream(self.stream):
+            self._propose(frame, stream)
+        torch.cuda.current_stream(net.device).wait_stream(self.stream)
+
+    def _propose(self, frame, stream) -> None:
         net = self.net
         _call(self.lib, "gbdic_reduce_half", _ptr(frame), self.W, self.H, _ptr(self.tgt_half), stream)
         for b in range(self.batches):
@@ -462,18 +477,26 @@ class LearnedSeeder:
             _call(self.lib, "gbdic_nn_patches", _ptr(self.ref_ptrs), _ptr(self.tgt_ptrs), None,
                   C.c_void_p(self.centres.data_ptr() + 8 * s0), n, self.W // 2, self.H // 2, _ptr(net.x0), stream)
             net.forward(stream)
-            _native_copy(self.pred, s0, net.out, n)
+            _native_copy(self.pred, s0, net.out, n)  # on the current stream, ordered with `stream`
         _call(self.lib, "gbdic_nn_lattice_seeds", _ptr(self.pred), OUT_PAD, self.lw, self.lh, self.step, self.gw,
               self.gh, self.engine.subset_stride, C.c_float(TRANSLATION_SCALE), C.c_float(GRADIENT_SCALE),
               _ptr(self.seeds), _ptr(self.active), stream)
 
-    def register_device(self, frame, *, reseed: bool = True, stream=None) -> dict:
-        """Learned-seed registration of a device frame into self.state;
-        returns counts (reseeded subsets)."""
+    def register_device(self, frame, *, reseed: bool = True) -> dict:
+        """Learned-seed registration of a device frame into self.state (on
+        self.stream; callers synchronise or wait on it); returns counts."""
+        torch = _torch()
+        self.stream.wait_stream(torch.cuda.current_stream(self.net.device))
+        with torch.cuda.stream(self.stream):
+            out = self._register(frame, reseed, self._handle)
+        torch.cuda.current_stream(self.net.device).wait_stream(self.stream)
+        return out
+
+    def _register(self, frame, reseed: bool, stream) -> dict:
         torch = _torch()
         eng = self.engine
         cfg = C.byref(eng._cfg(eng._config))
-        self.propose(frame, stream)
+        self._propose(frame, stream)
         _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
                      _ptr(self.state), stream)
         reseeded = 0
