@@ -164,6 +164,9 @@ struct NnPatchArgs {
     const float *centres;         // per patch (x, y), image pixels
     int count, W, H;
     void *out;                    // [count][64][64][2] BF16
+    const float *shift;           // per patch predictions displacing the target window, or nullptr
+    int shift_ld;                 // row stride of `shift` (translation at columns 0 and 3)
+    float shift_scale;            // prediction units -> image pixels
 };
 struct NnConvShape {
     int B, H, W, C;       // input NHWC
@@ -194,6 +197,7 @@ cudaError_t launch_nn_regression_loss(const float *pred, int ldp, const float *t
                                       float *grad_f32, int ldg, float *loss, cudaStream_t s);
 struct NnLatticeArgs {
     const float *pred;    // lattice_w * lattice_h rows, stride ldp, normalised outputs
+    const float *base;    // first-pass outputs (translations added), or nullptr
     int ldp, lattice_w, lattice_h, step, grid_w, grid_h, stride;
     float translation_scale, gradient_scale;
     float *seeds;         // grid_w * grid_h * 8

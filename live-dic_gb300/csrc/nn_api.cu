@@ -46,10 +46,11 @@ int gbdic_nn_gemm(const gbdic_nn_gemm_desc *d, int32_t *device_error, void *stre
 }
 
 int gbdic_nn_patches(const uint8_t *const *refs, const uint8_t *const *tgts, const int32_t *image_index,
-                     const float *centres, int32_t count, int32_t width, int32_t height, void *out, void *stream) {
-    if (!refs || !tgts || !centres || !out || count < 0 || width < 1 || height < 1)
+                     const float *centres, int32_t count, int32_t width, int32_t height, void *out,
+                     const float *shift, int32_t shift_ld, float shift_scale, void *stream) {
+    if (!refs || !tgts || !centres || !out || count < 0 || width < 1 || height < 1 || (shift && shift_ld < 4))
         return invalid("patch arguments are incomplete");
-    gbdic::NnPatchArgs a{refs, tgts, image_index, centres, count, width, height, out};
+    gbdic::NnPatchArgs a{refs, tgts, image_index, centres, count, width, height, out, shift, shift_ld, shift_scale};
     return rc(gbdic::launch_nn_patches(a, as_stream(stream)), "patch extraction");
 }
 
@@ -117,15 +118,15 @@ int gbdic_reduce_half(const uint8_t *src, int32_t width, int32_t height, uint8_t
     return rc(gbdic::launch_reduce_half(src, width, height, dst, as_stream(stream)), "pyramid reduction");
 }
 
-int gbdic_nn_lattice_seeds(const float *pred, int32_t ldp, int32_t lattice_w, int32_t lattice_h, int32_t step,
-                           int32_t grid_w, int32_t grid_h, int32_t subset_stride, float translation_scale,
+int gbdic_nn_lattice_seeds(const float *pred, const float *base, int32_t ldp, int32_t lattice_w, int32_t lattice_h,
+                           int32_t step, int32_t grid_w, int32_t grid_h, int32_t subset_stride, float translation_scale,
                            float gradient_scale, float *seeds, uint32_t *active, void *stream) {
     if (!pred || !seeds || !active || ldp < 6 || lattice_w < 1 || lattice_h < 1 || step < 1 || grid_w < 1 ||
         grid_h < 1 || subset_stride < 1 || (lattice_w - 1) * step < grid_w - step || (lattice_h - 1) * step < grid_h - step ||
         !(gradient_scale != 0.0f))
         return invalid("invalid lattice seed arguments");
-    gbdic::NnLatticeArgs a{pred, ldp, lattice_w, lattice_h, step, grid_w, grid_h, subset_stride, translation_scale,
-                           gradient_scale, seeds, active};
+    gbdic::NnLatticeArgs a{pred, base, ldp, lattice_w, lattice_h, step, grid_w, grid_h, subset_stride,
+                           translation_scale, gradient_scale, seeds, active};
     return rc(gbdic::launch_nn_lattice_seeds(a, as_stream(stream)), "lattice seeds");
 }
 

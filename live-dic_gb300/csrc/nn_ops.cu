@@ -27,15 +27,26 @@ __global__ void __launch_bounds__(256) patch_kernel(NnPatchArgs a) {
     if (b >= a.count) return;
     const int img = a.image_index ? a.image_index[b] : 0;
     const uint8_t *ref = a.refs[img], *tgt = a.tgts[img];
-    const int x0 = (int)floorf(a.centres[2 * b] + 0.5f) - 32, y0 = (int)floorf(a.centres[2 * b + 1] + 0.5f) - 32;
+    const float cx = a.centres[2 * b], cy = a.centres[2 * b + 1];
+    const int x0 = (int)floorf(cx + 0.5f) - 32, y0 = (int)floorf(cy + 0.5f) - 32;
+    // Target window: optionally displaced by a previous prediction.
+    float sx = 0.0f, sy = 0.0f;
+    if (a.shift) {
+        sx = a.shift[(size_t)b * a.shift_ld] * a.shift_scale;
+        sy = a.shift[(size_t)b * a.shift_ld + 3] * a.shift_scale;
+        if (!(fabsf(sx) < 1e4f)) sx = 0.0f;
+        if (!(fabsf(sy) < 1e4f)) sy = 0.0f;
+    }
+    const int tx0 = (int)floorf(cx + sx + 0.5f) - 32, ty0 = (int)floorf(cy + sy + 0.5f) - 32;
     float vr[16], vt[16];
     float sr = 0.0f, st = 0.0f, qr = 0.0f, qt = 0.0f;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
         const int p = threadIdx.x + 256 * i;
         const int x = min(max(x0 + (p & 63), 0), a.W - 1), y = min(max(y0 + (p >> 6), 0), a.H - 1);
+        const int u = min(max(tx0 + (p & 63), 0), a.W - 1), v = min(max(ty0 + (p >> 6), 0), a.H - 1);
         vr[i] = (float)ref[(size_t)y * a.W + x];
-        vt[i] = (float)tgt[(size_t)y * a.W + x];
+        vt[i] = (float)tgt[(size_t)v * a.W + u];
         sr += vr[i]; st += vt[i]; qr += vr[i] * vr[i]; qt += vt[i] * vt[i];
     }
     __shared__ float red[4][8];
@@ -213,7 +224,8 @@ __global__ void __launch_bounds__(256) regression_loss_kernel(const float *pred,
 
 // Seeds of every subset from a lattice of every `step`-th subset: bilinear
 // weights over the four surrounding lattice nodes, each node's affine warp
-// Taylor-recentred to the subset centre (offset (gx - lx step) stride).
+// Taylor-recentred to the subset centre (offset (gx - lx step) stride).  With
+// `base` (a first pass), translations are base + residual.
 __global__ void lattice_seed_kernel(NnLatticeArgs a) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= a.grid_w * a.grid_h) return;
@@ -227,9 +239,11 @@ __global__ void lattice_seed_kernel(NnLatticeArgs a) {
     for (int corner = 0; corner < 4; ++corner) {
         const int cx = min(lx + (corner & 1), a.lattice_w - 1), cy = min(ly + (corner >> 1), a.lattice_h - 1);
         const float w = ((corner & 1) ? fx : 1.0f - fx) * ((corner & 2) ? fy : 1.0f - fy);
-        const float *p = a.pred + (size_t)(cy * a.lattice_w + cx) * a.ldp;
-        const float tx = p[0] * a.translation_scale, ux = p[1] / a.gradient_scale, uy = p[2] / a.gradient_scale;
-        const float ty = p[3] * a.translation_scale, vx = p[4] / a.gradient_scale, vy = p[5] / a.gradient_scale;
+        const size_t row = (size_t)(cy * a.lattice_w + cx) * a.ldp;
+        const float *p = a.pred + row;
+        const float bx = a.base ? a.base[row] : 0.0f, by = a.base ? a.base[row + 3] : 0.0f;
+        const float tx = (p[0] + bx) * a.translation_scale, ux = p[1] / a.gradient_scale, uy = p[2] / a.gradient_scale;
+        const float ty = (p[3] + by) * a.translation_scale, vx = p[4] / a.gradient_scale, vy = p[5] / a.gradient_scale;
         const float dx = (float)(gx - cx * a.step) * (float)a.stride, dy = (float)(gy - cy * a.step) * (float)a.stride;
         acc[0] += w * (tx + ux * dx + uy * dy);
         acc[1] += w * ux;

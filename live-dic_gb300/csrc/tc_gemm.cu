@@ -258,8 +258,16 @@ bool make_map(CUtensorMap *map, const void *ptr, int rows, int cols, int box_row
 template <int BN>
 cudaError_t launch_bn(const CUtensorMap &ma, const CUtensorMap &mb, const TcGemmArgs &a, cudaStream_t stream) {
     const size_t smem = (size_t)kStages * (kBM * kBK * 2 + BN * kBK * 2) + 1024;
-    cudaError_t err = cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // The attribute is per device; set it once per device and tile width.
+    static thread_local int configured_device = -1;
+    int device = 0;
+    cudaError_t err = cudaGetDevice(&device);
     if (err != cudaSuccess) return err;
+    if (configured_device != device) {
+        err = cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return err;
+        configured_device = device;
+    }
     dim3 grid(a.N / BN, a.M / kBM, a.k_split);
     tc_gemm_kernel<BN><<<grid, 128, smem, stream>>>(ma, mb, a);
     return cudaGetLastError();

@@ -195,7 +195,7 @@ _SIGNATURES = {
     "gbdic_affine_frontier": (C.c_int, [P, P, P, P, P]),
     "gbdic_spatial_choose": (C.c_int, [P, P, P, P, C.POINTER(ChooseCfg), P, P, P]),
     "gbdic_nn_gemm": (C.c_int, [C.POINTER(NnGemmDesc), P, P]),
-    "gbdic_nn_patches": (C.c_int, [P, P, P, P, I32, I32, I32, P, P]),
+    "gbdic_nn_patches": (C.c_int, [P, P, P, P, I32, I32, I32, P, P, I32, C.c_float, P]),
     "gbdic_nn_im2col": (C.c_int, [C.POINTER(NnConvShape), P, P, P]),
     "gbdic_nn_dgrad_gather": (C.c_int, [C.POINTER(NnConvShape), P, P, P]),
     "gbdic_nn_transpose": (C.c_int, [P, I32, I32, I32, P, I32, I32, P]),
@@ -206,7 +206,7 @@ _SIGNATURES = {
     "gbdic_nn_pack_weights": (C.c_int, [P, I32, I32, I32, P, P, I32, P]),
     "gbdic_nn_regression_loss": (C.c_int, [P, I32, P, I32, I32, P, P, I32, P, P]),
     "gbdic_reduce_half": (C.c_int, [P, I32, I32, P, P]),
-    "gbdic_nn_lattice_seeds": (C.c_int, [P, I32, I32, I32, I32, I32, I32, I32, C.c_float, C.c_float, P, P, P]),
+    "gbdic_nn_lattice_seeds": (C.c_int, [P, P, I32, I32, I32, I32, I32, I32, I32, C.c_float, C.c_float, P, P, P]),
     "gbdic_register_seeded_device": (C.c_int, [P, P, P, P, C.POINTER(SolverCfg), P, P]),
     "gbdic_search_seeds_device": (C.c_int, [P, P, P, P, P, I32, I32, P]),
 }

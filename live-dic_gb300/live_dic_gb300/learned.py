@@ -19,10 +19,13 @@ the library's own kernels:
   speckle under random affine warps (translation +-20 px, strain +-5 %,
   rotation +-3 deg), labelled by IC-GN converged from the imposed warp.
 * ``LearnedSeeder`` -- per frame: half-resolution pyramid level, the network
-  on a lattice of every `step`-th subset, lattice -> per-subset seeds
-  (bilinear blend of Taylor-recentred warps), seeded IC-GN; subsets that
-  fail or whose ZNCC falls below the threshold are reseeded by the integer
-  ZNCC search around their proposal and solved again.
+  on a lattice of every `step`-th subset in several passes (after each, a
+  robust affine fit of the lattice translations displaces the target
+  windows and the next pass predicts the residual warp), lattice ->
+  per-subset seeds (bilinear blend of Taylor-recentred warps), seeded IC-GN;
+  subsets that do not converge or whose ZNCC falls below the threshold are
+  reseeded by the integer ZNCC search around their proposal and solved
+  again.
 
 Outputs are normalised as [tx / 16, ux * 20, uy * 20, ty / 16, vx * 20,
 vy * 20] (translations in full-resolution pixels).
@@ -263,7 +266,7 @@ class SeedNet:
     def load_patches(self, refs, tgts, image_index, centres, count: int, width: int, height: int, stream=None):
         """Patches into self.x0 (rows beyond `count` keep their contents)."""
         _call(self.lib, "gbdic_nn_patches", _ptr(refs), _ptr(tgts), _ptr(image_index), _ptr(centres), count, width,
-              height, _ptr(self.x0), stream)
+              height, _ptr(self.x0), None, 0, C.c_float(0.0), stream)
 
     def state_dict(self) -> dict[str, np.ndarray]:
         names = [f"w{i}" for i in range(len(self.w))] + [f"b{i}" for i in range(len(self.b))] + ["w6", "b6"]
@@ -414,11 +417,12 @@ class LearnedSeeder:
     engine: network proposals on a subset lattice, seeded IC-GN, and ZNCC
     reseeding of failed or low-ZNCC subsets."""
 
-    def __init__(self, engine, net: SeedNet, *, step: int = 4, reseed_radius: int = 10) -> None:
+    def __init__(self, engine, net: SeedNet, *, step: int = 4, reseed_radius: int = 10, passes: int = 2) -> None:
         torch = _torch()
         if not engine._reference_ready or engine.motion_model != "affine":
             raise ValueError("LearnedSeeder needs an affine engine with a prepared reference")
         self.engine, self.net, self.step, self.radius = engine, net, int(step), int(reseed_radius)
+        self.passes = max(1, int(passes))
         self.lib = _native.load()
         dev = net.device
         W, H = engine.width, engine.height
@@ -430,6 +434,8 @@ class LearnedSeeder:
         cx = gx * s + 0.5 * (S - 1)
         cy = gy * s + 0.5 * (S - 1)
         self.centres = torch.from_numpy(np.stack([cx.ravel() / 2.0, cy.ravel() / 2.0], -1).astype(np.float32)).to(dev)
+        self.node_xy = np.stack([cx.ravel(), cy.ravel()], -1).astype(np.float64)
+        self.base_host = np.zeros((self.lw * self.lh, OUT_PAD), np.float32)
         self.ref_half = torch.empty(H // 2, W // 2, dtype=torch.uint8, device=dev)
         self.tgt_half = torch.empty_like(self.ref_half)
         self.ref_ptrs = torch.tensor([self.ref_half.data_ptr()], dtype=torch.int64, device=dev)
@@ -440,11 +446,16 @@ class LearnedSeeder:
             usable = usable & np.asarray(engine.roi.selected, dtype=bool)
         self.usable = torch.from_numpy(np.array(usable, dtype=bool).ravel()).to(dev)
         self.pred = torch.zeros(self.lattice, OUT_PAD, device=dev)
+        self.base = torch.zeros(self.lattice, OUT_PAD, device=dev)
         self.seeds = torch.zeros(self.gh * self.gw * 8, device=dev)
         self.active = torch.zeros(self.gh * self.gw, dtype=torch.int32, device=dev)
         self.state = torch.zeros(self.gh * self.gw * 8, device=dev)
         self.mask = torch.zeros(self.gh * self.gw, dtype=torch.uint8, device=dev)
-        self.batches = (self.lattice + net.B - 1) // net.B
+        # Inference copy of the network sized to the whole lattice: one
+        # forward per pass.
+        self.inet = SeedNet(batch=_pad(self.lattice, 128), device=net.device.index or 0)
+        self.inet.load_state_dict(net.state_dict())
+        self.batches = 1
         # One non-default stream carries the network, the engine's kernels and
         # the mask arithmetic in order (a NULL stream would select the
         # engine's own stream).
@@ -468,19 +479,80 @@ class LearnedSeeder:
             self._propose(frame, stream)
         torch.cuda.current_stream(net.device).wait_stream(self.stream)
 
-    def _propose(self, frame, stream) -> None:
-        net = self.net
-        _call(self.lib, "gbdic_reduce_half", _ptr(frame), self.W, self.H, _ptr(self.tgt_half), stream)
+    def _network_pass(self, out, shift, stream) -> None:
+        net = self.inet
+        # level-1 pixels per normalised translation unit
+        scale = C.c_float(TRANSLATION_SCALE / 2.0)
         for b in range(self.batches):
             s0 = b * net.B
             n = min(net.B, self.lattice - s0)
             _call(self.lib, "gbdic_nn_patches", _ptr(self.ref_ptrs), _ptr(self.tgt_ptrs), None,
-                  C.c_void_p(self.centres.data_ptr() + 8 * s0), n, self.W // 2, self.H // 2, _ptr(net.x0), stream)
+                  C.c_void_p(self.centres.data_ptr() + 8 * s0), n, self.W // 2, self.H // 2, _ptr(net.x0),
+                  None if shift is None else C.c_void_p(shift.data_ptr() + 4 * OUT_PAD * s0), OUT_PAD, scale, stream)
             net.forward(stream)
-            _native_copy(self.pred, s0, net.out, n)  # on the current stream, ordered with `stream`
-        _call(self.lib, "gbdic_nn_lattice_seeds", _ptr(self.pred), OUT_PAD, self.lw, self.lh, self.step, self.gw,
-              self.gh, self.engine.subset_stride, C.c_float(TRANSLATION_SCALE), C.c_float(GRADIENT_SCALE),
-              _ptr(self.seeds), _ptr(self.active), stream)
+            _native_copy(out, s0, net.out, n)  # on the current stream, ordered with `stream`
+
+    def consensus(self, translations: np.ndarray, *, trials: int = 128, tolerance: float = 3.0) -> np.ndarray:
+        """Affine field through the lattice translations (P x 2, px) by
+        random sample consensus: affine maps through random node triples, the
+        one agreeing (within `tolerance` px) with the most nodes wins and is
+        refitted by least squares on its inliers.  Out-of-range network
+        predictions are outliers; a global affine fit is what lets the next
+        pass displace every window, including those whose motion exceeded
+        the network's training range."""
+        xy = (self.node_xy - self.node_xy.mean(0)) / 1000.0
+        A = np.concatenate([np.ones((len(xy), 1)), xy], 1)
+        finite = np.isfinite(translations).all(1)
+        idx = np.flatnonzero(finite)
+        if idx.size < 3:
+            return translations
+        rng = np.random.default_rng(12345)
+        tri = idx[rng.integers(0, idx.size, (trials, 3))]
+        sub = A[tri]                                               # trials x 3 x 3
+        usable = np.abs(np.linalg.det(sub)) > 1e-9
+        if not usable.any():
+            return translations
+        coef = np.linalg.solve(sub[usable], translations[tri[usable]])   # k x 3 x 2
+        # hypotheses are scored on at most 256 sampled nodes, the winner on all
+        probe = idx if idx.size <= 256 else idx[rng.choice(idx.size, 256, replace=False)]
+        x, y, t = xy[probe, 0][None], xy[probe, 1][None], translations[probe]
+        du = coef[:, 0, 0:1] + coef[:, 1, 0:1] * x + coef[:, 2, 0:1] * y - t[None, :, 0]
+        dv = coef[:, 0, 1:2] + coef[:, 1, 1:2] * x + coef[:, 2, 1:2] * y - t[None, :, 1]
+        winner = coef[int(np.argmax((np.hypot(du, dv) <= tolerance).sum(1)))]
+        d = A @ winner - translations
+        best = finite & (np.hypot(d[:, 0], d[:, 1]) <= tolerance)
+        if best.sum() < 3:
+            return translations
+        for _ in range(2):
+            fit_coef, *_ = np.linalg.lstsq(A[best], translations[best], rcond=None)
+            d = A @ fit_coef - translations
+            best = finite & (np.hypot(d[:, 0], d[:, 1]) <= tolerance)
+            if best.sum() < 3:
+                break
+        return A @ fit_coef
+
+    def _propose(self, frame, stream) -> None:
+        # Pass 1 on co-located windows; between passes a robust affine fit of
+        # the lattice translations displaces every target window, and the
+        # next pass predicts the residual warp around it.
+        torch = _torch()
+        _call(self.lib, "gbdic_reduce_half", _ptr(frame), self.W, self.H, _ptr(self.tgt_half), stream)
+        shift = None
+        self.base_host[:] = 0.0
+        for p in range(self.passes):
+            self._network_pass(self.pred, shift, stream)
+            if p == self.passes - 1:
+                break
+            self.stream.synchronize()
+            pred = self.pred[:, [0, 3]].cpu().numpy().astype(np.float64)
+            total = (self.base_host[:, [0, 3]] + pred) * TRANSLATION_SCALE
+            fitted = self.consensus(total) / TRANSLATION_SCALE
+            self.base_host[:, 0], self.base_host[:, 3] = fitted[:, 0], fitted[:, 1]
+            self.base.copy_(torch.from_numpy(self.base_host), non_blocking=False)
+            shift = self.base
+        _call(self.lib, "gbdic_nn_lattice_seeds", _ptr(self.pred), _ptr(self.base) if shift is not None else None,
+              OUT_PAD, self.lw, self.lh, self.step, self.gw, self.gh, self.engine.subset_stride,
+              C.c_float(TRANSLATION_SCALE), C.c_float(GRADIENT_SCALE), _ptr(self.seeds), _ptr(self.active), stream)
 
     def register_device(self, frame, *, reseed: bool = True) -> dict:
         """Learned-seed registration of a device frame into self.state (on
@@ -501,8 +573,10 @@ class LearnedSeeder:
                      _ptr(self.state), stream)
         reseeded = 0
         if reseed:
+            # not converged (0) or converged below the ZNCC threshold (-2);
+            # windows pushed off the image (-1) cannot be rescued by a search
             status = self.state.view(-1, 8)[:, 6]
-            failed = (status < 0.5) & self.usable
+            failed = ((status == 0.0) | (status == -2.0)) & self.usable
             reseeded = int(failed.sum().item())
             if reseeded:
                 self.mask.copy_(failed.to(torch.uint8))
