@@ -397,10 +397,13 @@ int gbdic_nn_gemm(const gbdic_nn_gemm_desc *desc, int32_t *device_error, void *s
 /* 64x64 reference/target patch pairs around `centres` ((x, y) per patch,
  * image pixels) of uint8 images W x H: refs / tgts are device arrays of
  * device image pointers, image_index (or NULL) selects the image of each
- * patch.  Output [count][64][64][2] BF16, each channel at zero mean and unit
- * variance; coordinates outside the image are clamped. */
+ * patch.  With `shift` (or NULL) the target window is displaced by
+ * (shift[b][0], shift[b][3]) * shift_scale pixels (a previous prediction,
+ * rows of shift_ld floats).  Output [count][64][64][2] BF16, each channel at
+ * zero mean and unit variance; coordinates outside the image are clamped. */
 int gbdic_nn_patches(const uint8_t *const *refs, const uint8_t *const *tgts, const int32_t *image_index,
-                     const float *centres, int32_t count, int32_t width, int32_t height, void *out, void *stream);
+                     const float *centres, int32_t count, int32_t width, int32_t height, void *out,
+                     const float *shift, int32_t shift_ld, float shift_scale, void *stream);
 
 /* 3x3, stride-2, pad-1 convolution shapes (NHWC BF16 activations). */
 typedef struct {
@@ -441,11 +444,11 @@ int gbdic_reduce_half(const uint8_t *src, int32_t width, int32_t height, uint8_t
 /* Seeds of every subset of a grid_w x grid_h grid from network outputs on a
  * lattice of every `step`-th subset in x and y (lattice_w x lattice_h rows of
  * `pred`, row stride ldp, normalised [tx/ts, ux*gs, uy*gs, ty/ts, vx*gs,
- * vy*gs]): bilinear blend of the four surrounding lattice warps, each
- * Taylor-recentred to the subset centre.  Writes affine seed states (8
- * floats) and activity 1. */
-int gbdic_nn_lattice_seeds(const float *pred, int32_t ldp, int32_t lattice_w, int32_t lattice_h, int32_t step,
-                           int32_t grid_w, int32_t grid_h, int32_t subset_stride, float translation_scale,
+ * vy*gs]; translations plus those of `base`, a first pass, when non-NULL):
+ * bilinear blend of the four surrounding lattice warps, each Taylor-recentred
+ * to the subset centre.  Writes affine seed states (8 floats) and activity 1. */
+int gbdic_nn_lattice_seeds(const float *pred, const float *base, int32_t ldp, int32_t lattice_w, int32_t lattice_h,
+                           int32_t step, int32_t grid_w, int32_t grid_h, int32_t subset_stride, float translation_scale,
                            float gradient_scale, float *seeds, uint32_t *active, void *stream);
 
 #ifdef __cplusplus
