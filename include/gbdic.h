@@ -248,7 +248,7 @@ typedef struct {
     int32_t iterations[4];          /* per level, coarsest first */
     float tolerance[4];             /* per level, coarsest first */
     float zncc_min;
-    int32_t initialization;         /* 0 zero, 1 temporal, 2 ZNCC seed search */
+    int32_t initialization;         /* 0 zero, 1 temporal, 2 ZNCC seed search, 3 global translation */
     uint32_t temporal_max_age;      /* 0xFFFFFFFE = never expire */
     int32_t temporal_prediction;    /* 0 none, 1 velocity */
     int32_t seed_search_radius;     /* integer search radius (pixels, coarsest level) */
@@ -314,6 +314,13 @@ int gbdic_fp32_peak_probe(int32_t device, double *tflops);
 int gbdic_set_solver_variant(gbdic_engine *engine, int32_t threads_per_subset, int32_t persistent);
 int gbdic_pyramid_set_solver_variant(gbdic_pyramid *pyramid, int32_t threads_per_subset, int32_t persistent);
 
+/* Global translation seed (full-resolution pixels) of the next frame run on
+ * `slot` (0 for gbdic_pyramid_register / register_device) when the pyramid
+ * was created with initialization 3 ("fourier"): every ROI-selected coarsest
+ * subset starts from (dx, dy) / 2^(levels - 1)
+ * (full_pyramid_backend.py:1704-1714). */
+int gbdic_pyramid_set_translation(gbdic_pyramid *pyramid, int32_t slot, float dx, float dy);
+
 /* ------------------------------------------------------------ batch */
 
 /* Batched registration of many fixed-reference jobs of uneven image size,
@@ -367,6 +374,25 @@ int gbdic_batch_run_device(gbdic_batch *batch, void *stream, int32_t profile, gb
 /* Copy job j's GBDIC_EXPORT_* array to host memory (OUTPUT_STATE, RAW_STATE,
  * METADATA, ADMISSIBLE). */
 int gbdic_batch_export(gbdic_batch *batch, int32_t job, int32_t what, void *host_out, int64_t bytes);
+
+/* ------------------------------------------------ Fourier initializer */
+
+/* FourierInitializer (fourier.py:16-111) on the GPU: linear phase
+ * correlation of a size x size window (a power of two, 32..1024) between the
+ * reference and each target, float64 radix-2 transforms.  Create with the
+ * reference window bytes (dense) and its ROI window (or NULL); estimate reads
+ * the same window at (x, y) of a target (host, or device when device_frame)
+ * and writes out[7] = {dx, dy, peak score, overlap, correlation, peak,
+ * target window std}; the caller applies the reference's acceptance rule
+ * (score >= 8, overlap >= 0.25, correlation >= 0.2, std >= 1).  Errors:
+ * gbdic_fourier_last_error(handle or NULL). */
+typedef struct gbdic_fourier gbdic_fourier;
+int gbdic_fourier_create(int32_t device, const uint8_t *window, const uint8_t *allowed, int32_t size,
+                         gbdic_fourier **out);
+int gbdic_fourier_destroy(gbdic_fourier *fourier);
+const char *gbdic_fourier_last_error(const gbdic_fourier *fourier);
+int gbdic_fourier_estimate(gbdic_fourier *fourier, const uint8_t *frame, int64_t row_stride, int32_t height,
+                           int32_t x, int32_t y, int32_t device_frame, double *out);
 
 /* ------------------------------------------------- learned seed network */
 

@@ -98,6 +98,9 @@ struct SeedArgs {
     int mark_missing;         // write status -1 into seeds that received no estimate
 };
 cudaError_t launch_transfer_seed(const SeedArgs &a, cudaStream_t stream);
+// Uniform translation seeds (shift * inv_scale; device shift[2]), activity = ROI selection.
+cudaError_t launch_uniform_seed(float *seed, uint32_t *active, const uint8_t *selected, int count, int model,
+                                const float *shift, float inv_scale, cudaStream_t stream);
 
 // ------------------------------------------------------------ ZNCC seed search
 struct SearchArgs {

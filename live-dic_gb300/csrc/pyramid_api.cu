@@ -19,6 +19,8 @@ namespace {
 struct PyramidSlot {
     gbdic::HostBuffer in, out, counters_host;
     gbdic::DeviceBuffer counters;  // 4 x u32
+    gbdic::HostBuffer shift_host;  // global translation seed (dx, dy), read at graph launch
+    gbdic::DeviceBuffer shift_dev;
     cudaEvent_t begin = nullptr, end = nullptr;
     cudaGraphExec_t graph = nullptr;
     bool pending = false;
@@ -29,6 +31,9 @@ struct PyramidSlot {
         check_cuda(cudaEventCreate(&end), "event");
         counters.ensure(4 * sizeof(uint32_t));
         counters_host.ensure(4 * sizeof(uint32_t));
+        shift_host.ensure(2 * sizeof(float));
+        shift_dev.ensure(2 * sizeof(float));
+        shift_host.as<float>()[0] = shift_host.as<float>()[1] = 0.0f;
     }
     void destroy() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -71,6 +76,8 @@ struct gbdic_pyramid {
     // temporal initialization with a search radius (subsets without history).
     bool search() const { return po.seed_search_radius > 0 && (po.initialization == 2 || po.initialization == 1); }
     bool velocity() const { return po.temporal_prediction == 1; }
+    // Global translation seed of the coarsest level (Fourier initialization).
+    bool global() const { return po.initialization == 3; }
     gbdic_solver_cfg cfg_of(int level) const {
         const int schedule = L() - 1 - level;  // options are coarsest first
         return gbdic_solver_cfg{po.iterations[schedule], po.tolerance[schedule], po.zncc_min};
@@ -137,6 +144,17 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
     auto &cslot = *coarse.slots[k];
     const uint8_t *cframe = c == 0 ? frame0 : nullptr;
     bool seeded = false;
+    if (p->global()) {
+        // full_pyramid_backend.py:1704-1714: every ROI-selected coarsest
+        // subset starts from (dx, dy) / 2^(levels - 1).
+        check_cuda(cudaMemcpyAsync(ps.shift_dev.get(), ps.shift_host.as<float>(), 2 * sizeof(float),
+                                   cudaMemcpyHostToDevice, s), "translation seed upload");
+        check_cuda(gbdic::launch_uniform_seed(cslot.seed.as<float>(), cslot.active.as<uint32_t>(),
+                                              coarse.roi ? coarse.selected.as<uint8_t>() : nullptr, coarse.count, model,
+                                              ps.shift_dev.as<float>(), 1.0f / (float)(1 << c), s),
+                   "translation seed launch");
+        seeded = true;
+    }
     if (p->temporal()) {
         auto &fine = *p->levels[0];
         gbdic::TemporalArgs t{};
@@ -285,7 +303,7 @@ int gbdic_pyramid_create(const gbdic_pyramid_options *options, gbdic_pyramid **o
             gbdic_solver_cfg c{po.iterations[i], po.tolerance[i], po.zncc_min};
             gbdic::validate_cfg(&c);
         }
-        if (po.initialization < 0 || po.initialization > 2) fail(GBDIC_EINVAL, "unsupported initialization");
+        if (po.initialization < 0 || po.initialization > 3) fail(GBDIC_EINVAL, "unsupported initialization");
         if (po.seed_search_radius < 0 || po.seed_search_radius > 64)
             fail(GBDIC_EINVAL, "seed_search_radius must be an integer from 1 to 64");
         if (po.initialization == 2 && po.seed_search_radius < 1)
@@ -509,6 +527,16 @@ int gbdic_pyramid_export(gbdic_pyramid *p, int32_t level, int32_t what, void *ho
 }  // extern "C"
 
 extern "C" {
+
+int gbdic_pyramid_set_translation(gbdic_pyramid *p, int32_t slot, float dx, float dy) {
+    return pguarded(p, [&] {
+        if (slot < 0 || slot >= (int)p->slots.size()) fail(GBDIC_EINVAL, "slot index out of range");
+        auto &ps = p->slots[slot];
+        if (ps.pending) fail(GBDIC_ESTATE, "slot is still in flight; retire it first");
+        ps.shift_host.as<float>()[0] = dx;
+        ps.shift_host.as<float>()[1] = dy;
+    });
+}
 
 int gbdic_pyramid_set_solver_variant(gbdic_pyramid *p, int32_t threads_per_subset, int32_t persistent) {
     return pguarded(p, [&] {

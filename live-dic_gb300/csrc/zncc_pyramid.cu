@@ -304,4 +304,29 @@ cudaError_t launch_temporal_merge(const TemporalArgs &a, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+namespace {
+
+// Every subset seeded with the translation (shift[0], shift[1]) * inv_scale
+// (zero gradients), active where ROI-selected.
+__global__ void uniform_seed_kernel(float *seed, uint32_t *active, const uint8_t *selected, int count, int ss,
+                                    const float *shift, float inv_scale) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    float *s = seed + (size_t)i * ss;
+    for (int k = 0; k < ss; ++k) s[k] = 0.0f;
+    s[0] = shift[0] * inv_scale;
+    s[3] = shift[1] * inv_scale;
+    active[i] = selected ? (selected[i] ? 1u : 0u) : 1u;
+}
+
+}  // namespace
+
+cudaError_t launch_uniform_seed(float *seed, uint32_t *active, const uint8_t *selected, int count, int model,
+                                const float *shift, float inv_scale, cudaStream_t stream) {
+    if (count <= 0) return cudaSuccess;
+    uniform_seed_kernel<<<(count + 255) / 256, 256, 0, stream>>>(seed, active, selected, count, state_stride(model),
+                                                                shift, inv_scale);
+    return cudaGetLastError();
+}
+
 }  // namespace gbdic

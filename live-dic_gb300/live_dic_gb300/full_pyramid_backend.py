@@ -24,6 +24,7 @@ import numpy as np
 from . import _native
 from . import autotune as _tuning
 from .engine import ICGNError, ImageInput, ReferenceInfo, RegistrationResult, _as_uint8_gray, result_from_packed
+from .fourier import FourierInitializer
 from .interpolation import normalize_interpolation
 from .motion import normalize_motion_model, parameter_count, state_float_count
 from .native_backend import DEFAULT_IN_FLIGHT_FRAMES, _normalize_device_type, _normalize_solver_workgroup_size, _validated_config, native_options
@@ -207,8 +208,8 @@ class ICGNWGPUFullPyramid:
         if slots < 1:
             raise ValueError("pipeline_depth must be a positive integer")
         # Options that the GPU engine does not provide fail loudly after validation.
-        if initialization in ("fourier", "wgpu-matching"):
-            raise ICGNError(f"initialization='{initialization}' is not available in this build")
+        if initialization == "wgpu-matching":
+            raise ICGNError("initialization='wgpu-matching' is not available in this build")
         if temporal_fine_correction:
             raise ICGNError("temporal_fine_correction is not available in this build")
         if pyramid_policy == "adaptive":
@@ -225,6 +226,7 @@ class ICGNWGPUFullPyramid:
         self._pipeline_slots = slots
         self._persistent = bool(persistent)
         self._zncc_min = 0.8
+        self._fourier: FourierInitializer | None = None
         self._lib = _native.load()
         self._registration_lock = threading.Lock()
         self._closed = False
@@ -262,7 +264,7 @@ class ICGNWGPUFullPyramid:
             po.iterations[i] = self.iterations_per_level[i]
             po.tolerance[i] = self.tolerance_per_level[i]
         po.zncc_min = self._zncc_min
-        po.initialization = {"zero": 0, "temporal": 1, "zncc": 2}[self.initialization]
+        po.initialization = {"zero": 0, "temporal": 1, "zncc": 2, "fourier": 3}[self.initialization]
         po.seed_search_radius = self.seed_search_radius or 0
         po.temporal_max_age = 0xFFFFFFFE if self.temporal_max_age is None else int(self.temporal_max_age)
         po.temporal_prediction = 1 if self.temporal_prediction == "velocity" else 0
@@ -367,6 +369,11 @@ class ICGNWGPUFullPyramid:
         self._roi_level_counts = [
             int(p.selected.sum()) if p is not None else d[2] * d[3] for p, d in zip(plans, dims, strict=True)
         ]
+        if self._fourier is not None:
+            self._fourier.close()
+        self._fourier = None
+        if self.initialization == "fourier" and (mask is None or mask.any()):
+            self._fourier = FourierInitializer(reference, mask, device=self.device_index)
         self._reference_ready = True
         usable = self.reference_valid if self.roi is None else self.reference_valid & self.roi.selected
         if self._autotune and usable.any():
@@ -422,6 +429,9 @@ class ICGNWGPUFullPyramid:
             )
             if self.temporal_prediction == "velocity":
                 echo["temporalPrediction"] = "velocity"
+        if self.initialization == "fourier":
+            echo.update(initialization="fourier",
+                        fourierWindow=None if self._fourier is None else self._fourier.window)
         if self.initialization == "zncc":
             echo["initialization"] = "zncc"
         if self.seed_search_radius:
@@ -487,6 +497,30 @@ class ICGNWGPUFullPyramid:
         )
 
     # ------------------------------------------------------------ registration
+    def _global_translation(self, slot: int, frame: np.ndarray | None = None, *, device_frame: int | None = None,
+                            row_stride: int = 0) -> dict | None:
+        """Fourier estimate of the target (full_pyramid_backend.py:1704-1714),
+        set as the slot's coarsest seed; ambiguous targets raise ICGNError."""
+        if self._fourier is None:
+            return None
+        try:
+            if device_frame is not None:
+                estimate = self._fourier.estimate_device(device_frame, row_stride)
+            else:
+                estimate = self._fourier.estimate(frame)
+        except ValueError as error:
+            raise ICGNError(str(error)) from error
+        self._check(self._lib.gbdic_pyramid_set_translation(self._handle, slot, float(estimate["dx"]),
+                                                            float(estimate["dy"])))
+        return estimate
+
+    @staticmethod
+    def _attach_translation(result: RegistrationResult, estimate: dict | None) -> RegistrationResult:
+        if estimate is not None:
+            result.config["globalTranslation"] = estimate
+            result.timing["fourierWallMs"] = estimate["wallMs"]
+        return result
+
     def register(self, target: ImageInput) -> RegistrationResult:
         """One upload, one graph launch, one readback (1815-1832)."""
         if not self._reference_ready:
@@ -498,6 +532,7 @@ class ICGNWGPUFullPyramid:
             frame = self._prepare_target(target)
             if self.roi is not None and self.roi.empty:
                 return self._empty_result(accepted_at)
+            estimate = self._global_translation(0, frame)
             prep_ms = (time.perf_counter() - accepted_at) * 1e3
             packed = np.empty((self.grid_height, self.grid_width, state_float_count(self.motion_model)), np.float32)
             counters = np.zeros(4, np.uint32)
@@ -505,7 +540,7 @@ class ICGNWGPUFullPyramid:
             self._check(self._lib.gbdic_pyramid_register(
                 self._handle, _native.ptr(frame), frame.strides[0], _native.ptr(packed), _native.ptr(counters),
                 C.byref(timing)))
-            return self._result(packed, counters, timing, accepted_at, prep_ms)
+            return self._attach_translation(self._result(packed, counters, timing, accepted_at, prep_ms), estimate)
         finally:
             self._registration_lock.release()
 
@@ -528,7 +563,7 @@ class ICGNWGPUFullPyramid:
         if not self._registration_lock.acquire(blocking=False):
             raise ICGNError("Another registration or registration stream is active.")
         available = deque(range(depth))
-        pending: deque[tuple[int, float, float]] = deque()
+        pending: deque[tuple[int, float, float, dict | None]] = deque()
         try:
             if self.roi is not None and self.roi.empty:
                 for target in targets:
@@ -538,14 +573,14 @@ class ICGNWGPUFullPyramid:
                 return
 
             def retire() -> RegistrationResult:
-                slot, accepted_at, prep_ms = pending.popleft()
+                slot, accepted_at, prep_ms, estimate = pending.popleft()
                 packed = np.empty((self.grid_height, self.grid_width, state_float_count(self.motion_model)), np.float32)
                 counters = np.zeros(4, np.uint32)
                 timing = _native.Timing()
                 self._check(self._lib.gbdic_pyramid_retire(self._handle, slot, _native.ptr(packed),
                                                            _native.ptr(counters), C.byref(timing)))
                 available.append(slot)
-                return self._result(packed, counters, timing, accepted_at, prep_ms)
+                return self._attach_translation(self._result(packed, counters, timing, accepted_at, prep_ms), estimate)
 
             for target in targets:
                 if not available:
@@ -553,14 +588,19 @@ class ICGNWGPUFullPyramid:
                 slot = available.popleft()
                 accepted_at = time.perf_counter()
                 frame = self._prepare_target(target)
+                try:
+                    estimate = self._global_translation(slot, frame)
+                except ICGNError:
+                    available.appendleft(slot)
+                    raise
                 prep_ms = (time.perf_counter() - accepted_at) * 1e3
                 self._check(self._lib.gbdic_pyramid_submit(self._handle, slot, _native.ptr(frame), frame.strides[0]))
-                pending.append((slot, accepted_at, prep_ms))
+                pending.append((slot, accepted_at, prep_ms, estimate))
             while pending:
                 yield retire()
         finally:
             while pending:
-                slot, _, _ = pending.popleft()
+                slot, _, _, _ = pending.popleft()
                 self._lib.gbdic_pyramid_retire(self._handle, slot, None, None, None)
             self._registration_lock.release()
 
@@ -568,6 +608,7 @@ class ICGNWGPUFullPyramid:
         """Resident registration of a device frame into a device state buffer."""
         if not self._reference_ready:
             raise ICGNError("Call set_reference() before register().")
+        self._global_translation(0, device_frame=device_frame, row_stride=self.width)
         self._check(self._lib.gbdic_pyramid_register_device(
             self._handle, C.c_void_p(device_frame), C.c_void_p(device_state), C.c_void_p(stream or 0)))
 
@@ -626,6 +667,9 @@ class ICGNWGPUFullPyramid:
             return
         self._reference_ready = False
         self._closed = True
+        if self._fourier is not None:
+            self._fourier.close()
+            self._fourier = None
         handle, self._handle = self._handle, None
         if handle:
             self._lib.gbdic_pyramid_destroy(handle)

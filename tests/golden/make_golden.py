@@ -170,6 +170,45 @@ def main(reference_root: str) -> None:
     out["gray_wide_out"] = engine._as_uint8_gray(wide)
 
     np.savez_compressed(HERE / "reference_vectors.npz", **out)
+    fourier_vectors(Path(reference_root))
+
+
+def fourier_vectors(reference_root: Path) -> None:
+    """FourierInitializer (fourier.py) on integer-shifted speckle crops, with
+    and without an ROI mask, plus a textured but unrelated target."""
+    _import_reference(reference_root)
+    import live_dic.fourier as fourier
+
+    rng = np.random.default_rng(4711)
+    big = speckle(rng, 360, 420, 900)
+    out: dict[str, np.ndarray] = {}
+    cases = [((12, -7), None), ((-30, 18), None), ((6, 10), "hole"), ((0, 0), "noise")]
+    for k, (shift, kind) in enumerate(cases):
+        dx, dy = shift
+        ref = np.ascontiguousarray(big[40:296, 50:370])
+        tgt = np.ascontiguousarray(big[40 - dy:296 - dy, 50 - dx:370 - dx])
+        mask = None
+        if kind == "hole":
+            yy, xx = np.mgrid[:256, :320]
+            mask = (xx - 160) ** 2 + (yy - 128) ** 2 >= 40 ** 2
+        if kind == "noise":
+            tgt = rng.integers(0, 256, ref.shape, dtype=np.uint8)
+        init = fourier.FourierInitializer(ref, mask)
+        out[f"fourier_{k}_ref"] = ref
+        out[f"fourier_{k}_tgt"] = tgt
+        out[f"fourier_{k}_mask"] = np.ones(ref.shape, bool) if mask is None else mask
+        out[f"fourier_{k}_has_mask"] = np.array(mask is not None)
+        w = init.window
+        out[f"fourier_{k}_window"] = np.array([w["x"], w["y"], w["size"]])
+        try:
+            est = init.estimate(tgt)
+            out[f"fourier_{k}_result"] = np.array([est["dx"], est["dy"], est["peakScore"], est["overlap"],
+                                                   est["correlation"]])
+            out[f"fourier_{k}_accepted"] = np.array(True)
+        except ValueError:
+            out[f"fourier_{k}_result"] = np.zeros(5)
+            out[f"fourier_{k}_accepted"] = np.array(False)
+    np.savez_compressed(HERE / "fourier_vectors.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'reference_vectors.npz'}")
 
 
