@@ -160,6 +160,17 @@ int gbdic_retire(gbdic_engine *engine, int32_t slot, float *out_state, gbdic_tim
 int gbdic_register_device(gbdic_engine *engine, const uint8_t *device_frame,
                           const gbdic_solver_cfg *cfg, float *device_state, void *stream);
 
+/* Partial-support ROI windows (roi_policy="partial": prepare_partial_reference,
+ * partial.py:26-121, and solve_partial, icgn.wgsl:1042-1085): `count` windows
+ * given by grid index, support bits (words_per_window = ceil(S*S / 32) words,
+ * row-major pixels, bit 0 first), support boxes (x0, y0, x1, y1 local
+ * pixels) and their host-prepared metadata / inverse rows (validity -4 for
+ * admitted windows), which replace the full-window rows.  Each registration
+ * then solves them after the complete windows.  count = 0 clears them. */
+int gbdic_set_partial_support(gbdic_engine *engine, int32_t count, const int32_t *indices, const uint32_t *words,
+                              int32_t words_per_window, const float *boxes, const float *metadata_rows,
+                              const float *inverse_rows);
+
 /* Resident variant of register_seeded(): device frame, seed states (state
  * layout), activity words and output state; `stream` as for
  * gbdic_register_device.  Inactive subsets get status -1 (-3 ROI-excluded). */

@@ -87,6 +87,8 @@ struct Level {
     DeviceBuffer intensity, spline, scratch, valid;  // preparation scratch
     DeviceBuffer admissible;                         // u8 per subset, ROI ignored
     DeviceBuffer ref_image;                          // reference bytes (seed search)
+    DeviceBuffer partial_index, partial_words, partial_boxes;  // partial-support windows
+    int partial_count = 0, support_words = 0;
     std::vector<std::unique_ptr<LevelSlot>> slots;
     int valid_count = 0;
 };

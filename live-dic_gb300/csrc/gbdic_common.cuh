@@ -153,6 +153,13 @@ struct SolveArgs {
     int div_patience, div_min;
     int persistent;
     unsigned long long *iteration_total;  // profiling: sum of executed iterations, or nullptr
+    // Partial-support windows (partial solver only): group g solves window
+    // partial_index[g] over the pixels set in its support words, bounded by
+    // its support box (x0, y0, x1, y1); count = number of partial windows.
+    const int *partial_index;
+    const uint32_t *support;
+    const float4 *support_box;
+    int support_words;
 };
 
 }  // namespace gbdic

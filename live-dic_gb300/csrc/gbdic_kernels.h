@@ -24,6 +24,11 @@ int icgn_occupancy(int model, int interp, int lanes, bool gauss);
 cudaError_t launch_icgn(const SolveArgs &a, int model, int interp, int lanes, bool gauss,
                         int persistent_grid, cudaStream_t stream);
 
+// Partial-support windows (a.count = number of partial windows; a.partial_index,
+// a.support, a.support_box, a.support_words set); translation and affine.
+cudaError_t launch_icgn_partial(const SolveArgs &a, int model, int interp, int lanes, bool gauss,
+                                cudaStream_t stream);
+
 // One persistent launch over many jobs (B-spline, uniform weighting).
 constexpr int kMaxBatchJobs = 256;
 struct BatchSolveArgs {

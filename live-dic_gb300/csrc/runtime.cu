@@ -226,6 +226,7 @@ double Runtime::prepare_reference(Level &level, const uint8_t *device_image, con
     level.ref_image.ensure(px);
     check_cuda(cudaMemcpyAsync(level.ref_image.get(), device_image, px, cudaMemcpyDeviceToDevice, stream_),
                "reference bytes");
+    level.partial_count = 0;
     level.roi = roi_selected != nullptr;
     if (roi_selected) {
         level.selected.ensure(level.count);
@@ -281,6 +282,7 @@ void Runtime::upload_reference_arrays(Level &level, const float *plane, const fl
     level.plane.ensure(px * sizeof(float4));
     level.meta.ensure((size_t)level.count * meta_stride(model) * sizeof(float));
     level.inv.ensure((size_t)level.count * n * n * sizeof(float));
+    level.partial_count = 0;
     check_cuda(cudaMemcpy(level.plane.get(), plane, px * sizeof(float4), cudaMemcpyHostToDevice), "plane upload");
     check_cuda(cudaMemcpy(level.meta.get(), meta, (size_t)level.count * meta_stride(model) * sizeof(float),
                           cudaMemcpyHostToDevice), "metadata upload");
@@ -357,6 +359,18 @@ void Runtime::enqueue_solve(Level &level, LevelSlot &slot, const gbdic_solver_cf
     if (timed) check_cuda(cudaEventRecord(profile_begin_[profile_used_], s), "profile event");
     check_cuda(launch_icgn(a, opt_.o.motion_model, opt_.o.interpolation, opt_.lanes, opt_.o.spatial_weighting == 1,
                            grid, s), "solver launch");
+    if (level.partial_count > 0) {
+        // Partial-support windows after the complete ones (their validity -4
+        // makes the complete-window launch skip them).
+        SolveArgs b = a;
+        b.count = level.partial_count;
+        b.partial_index = level.partial_index.as<int>();
+        b.support = level.partial_words.as<uint32_t>();
+        b.support_box = level.partial_boxes.as<float4>();
+        b.support_words = level.support_words;
+        check_cuda(launch_icgn_partial(b, opt_.o.motion_model, opt_.o.interpolation, opt_.lanes,
+                                       opt_.o.spatial_weighting == 1, s), "partial solver launch");
+    }
     if (timed) check_cuda(cudaEventRecord(profile_end_[profile_used_++], s), "profile event");
     if (profiling_) ++profile_launches_;
 }

@@ -103,6 +103,32 @@ __device__ __forceinline__ bool warp_inside(const Warp &w, int px0, int py0, int
     return inside;
 }
 
+// Partial-support variant of warp_inside (icgn.wgsl:635-690 with
+// PARTIAL_SUPPORT): the support box's corners instead of the window's.
+template <int MODEL>
+__device__ __forceinline__ bool warp_inside_box(const Warp &w, int px0, int py0, float half, float4 box, int W,
+                                                int H) {
+    const float xmax = (float)W - 3.0f, ymax = (float)H - 3.0f;
+    if (MODEL == kModelTranslation) {
+        const float x0 = ((float)px0 + box.x) + w.t0, y0 = ((float)py0 + box.y) + w.t1;
+        const float x1 = ((float)px0 + box.z) + w.t0, y1 = ((float)py0 + box.w) + w.t1;
+        return x0 >= 2.0f && y0 >= 2.0f && x1 <= xmax && y1 <= ymax;
+    }
+    const float lx0 = box.x - half, ly0 = box.y - half, lx1 = box.z - half, ly1 = box.w - half;
+    bool inside = true;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+        const float lx = (p == 1 || p == 3) ? lx1 : lx0;
+        const float ly = (p >= 2) ? ly1 : ly0;
+        float dx, dy;
+        displacement<MODEL>(w, lx, ly, 0.5f * lx * lx, lx * ly, 0.5f * ly * ly, dx, dy);
+        const float px = ((float)px0 + (half + lx)) + dx;
+        const float py = ((float)py0 + (half + ly)) + dy;
+        inside = inside && px >= 2.0f && py >= 2.0f && px <= xmax && py <= ymax;
+    }
+    return inside;
+}
+
 // Quadratic inverse composition (icgn.wgsl:393-513): lifted 6x6 warp matrix
 // of the increment, pivoted Gauss-Jordan in binary32 on the augmented 6x12
 // matrix [M | I].  The matrix is spread over a 16-lane segment of the warp,
@@ -321,13 +347,17 @@ __device__ __forceinline__ float gn_update(const SolveArgs &a, const float (&t)[
     return divergence_status(a, change, it1, conv, prev_change, stalled);
 }
 
-template <int MODEL, int INTERP, int LANES, bool GAUSS>
-__device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int glane, int lane_in_warp,
+template <int MODEL, int INTERP, int LANES, bool GAUSS, bool PART = false>
+__device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int glane, int lane_in_warp,
                                             float *red) {
     constexpr int N = SumCount<MODEL>::value;
     constexpr bool kBlock = LANES > 32;
     constexpr bool kClamp = MODEL == kModelQuadratic;
-    const bool exists = idx < a.count;
+    const bool exists = group < a.count;
+    // Partial windows: group -> window index; support words and box.
+    const int idx = PART ? (exists ? __ldg(a.partial_index + group) : 0) : group;
+    const uint32_t *support = PART ? a.support + (size_t)(exists ? group : 0) * a.support_words : nullptr;
+    const float4 box = PART ? __ldg(a.support_box + (exists ? group : 0)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const int sidx = exists ? idx : 0;
     const float *md = a.meta + (size_t)sidx * meta_stride(MODEL);
     const float *hi = a.inv + (size_t)sidx * parameter_count(MODEL) * parameter_count(MODEL);
@@ -346,8 +376,8 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int gla
     }
     if (MODEL == kModelTranslation) { w.l0 = w.l1 = w.l2 = w.l3 = 0.0f; }
     const float mvalid = __ldg(md + 1);
-    const bool valid = enabled && mvalid >= 0.5f;
-    const float rejected = a.roi_enabled ? fminf(-1.0f, mvalid) : -1.0f;
+    const bool valid = enabled && (PART ? mvalid == -4.0f : mvalid >= 0.5f);
+    const float rejected = (a.roi_enabled && !PART) ? fminf(-1.0f, mvalid) : -1.0f;
     float status = valid ? 0.0f : rejected;
     float iters = 0.0f;
     bool done = !exists;
@@ -355,8 +385,8 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int gla
     const int gx = sidx % a.grid_w, gy = sidx / a.grid_w;
     const int px0 = gx * a.stride, py0 = gy * a.stride;
     const float half = 0.5f * ((float)S - 1.0f);
-    const float ref_mean = a.use_mean ? __ldg(md + (MODEL == kModelQuadratic ? 26 : 14)) : 0.0f;
-    const float wsum = GAUSS ? __ldg(md + 3 + 2 * parameter_count(MODEL)) : (float)(S * S);
+    const float ref_mean = (a.use_mean || PART) ? __ldg(md + (MODEL == kModelQuadratic ? 26 : 14)) : 0.0f;
+    const float wsum = (GAUSS || PART) ? __ldg(md + 3 + 2 * parameter_count(MODEL)) : (float)(S * S);
     float prev_change = 3.402823e38f;
     unsigned stalled = 0u;
     const int npix = S * S;
@@ -370,7 +400,9 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int gla
     for (int it = 0; it < 30; ++it) {
         if (!done) {
             if (!(a.div_patience != 0 && status == 3.0f)) {
-                if (!warp_inside<MODEL>(w, px0, py0, S, half, W, H)) {
+                const bool in = PART ? warp_inside_box<MODEL>(w, px0, py0, half, box, W, H)
+                                     : warp_inside<MODEL>(w, px0, py0, S, half, W, H);
+                if (!in) {
                     if (!a.roi_enabled || status > -2.5f) status = -1.0f;
                 }
             }
@@ -387,6 +419,12 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int gla
         if (!done) {
             int col = col0, row = row0;
             for (int p = glane; p < npix; p += LANES) {
+                if (PART && !((__ldg(support + (p >> 5)) >> (p & 31)) & 1u)) {
+                    col += lmod;
+                    row += ldiv;
+                    if (col >= S) { col -= S; ++row; }
+                    continue;
+                }
                 const float lx = (float)col - half, ly = (float)row - half;
                 float hx2 = 0.0f, xy = 0.0f, hy2 = 0.0f;
                 if (MODEL == kModelQuadratic) {
@@ -459,7 +497,7 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int idx, int gla
     }
 }
 
-template <int MODEL, int INTERP, int LANES, bool GAUSS>
+template <int MODEL, int INTERP, int LANES, bool GAUSS, bool PART = false>
 __global__ void __launch_bounds__(128, MODEL == kModelQuadratic ? 5 : 1) icgn_kernel(SolveArgs a) {
     constexpr bool kBlock = LANES > 32;
     constexpr int kUnitThreads = kBlock ? 128 : 32;
@@ -491,7 +529,7 @@ __global__ void __launch_bounds__(128, MODEL == kModelQuadratic ? 5 : 1) icgn_ke
             base = unit * kGroups < (long long)a.count ? (int)(unit * kGroups) : a.count;
         }
         if (base >= a.count) break;
-        solve_group<MODEL, INTERP, LANES, GAUSS>(a, base + group_in_unit, glane, lane_in_warp, red);
+        solve_group<MODEL, INTERP, LANES, GAUSS, PART>(a, base + group_in_unit, glane, lane_in_warp, red);
         if (!a.persistent) break;
     }
 }

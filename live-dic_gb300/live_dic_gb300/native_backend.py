@@ -376,9 +376,8 @@ class ICGNWGPU:
             raise ValueError(f"Reference dimensions must each be at least {self.subset_size} pixels.")
         config = _validated_config(iterations, tolerance, zncc_min)
         mask = validate_roi(roi_mask, roi_policy, frame.shape, self.motion_model, roi_truncation)
-        if roi_policy == "partial" and mask is not None:
-            raise ICGNError("roi_policy='partial' is not available in this build; use roi_policy='full'.")
-        roi = prepare_roi(mask, self.subset_size, self.subset_stride, median_filter_size=self.median_filter_size)
+        roi = prepare_roi(mask, self.subset_size, self.subset_stride, policy=roi_policy, truncation=roi_truncation,
+                          median_filter_size=self.median_filter_size)
         selected = links = None
         if roi is not None and roi.effective:
             selected = np.ascontiguousarray(roi.selected, dtype=np.uint8).ravel()
@@ -397,6 +396,8 @@ class ICGNWGPU:
         prep_ms = (time.perf_counter() - prep_start) * 1e3
         self.width, self.height, self.grid_width, self.grid_height = width, height, gw, gh
         self._config = config
+        if roi is not None and roi.partial_indices is not None and roi.partial_indices.size:
+            roi = self._prepare_partial(roi)
         self.roi = roi
         admissible = self._export(_native.EXPORT_ADMISSIBLE, np.uint8, (gh, gw))
         self.reference_valid = immutable(admissible.astype(bool))
@@ -423,6 +424,30 @@ class ICGNWGPU:
             roi=roi,
             reference_valid=self.reference_valid,
         )
+
+    def _prepare_partial(self, roi: RoiPlan) -> RoiPlan:
+        """Partial-window metadata from the GPU-prepared plane (float64 host
+        preparation, partial.py:26-121), uploaded with the support tables."""
+        from .partial import prepare_partial_reference
+
+        n = parameter_count(self.motion_model)
+        count = self.grid_width * self.grid_height
+        plane = self._export(_native.EXPORT_PLANE, np.float32, (self.height * self.width * 4,))
+        inverse = self._export(_native.EXPORT_INVERSE, np.float32, (count * n * n,)).astype(np.float64)
+        metadata = self._export(_native.EXPORT_METADATA, np.float32, (count * 16,)).astype(np.float64)
+        roi = prepare_partial_reference(plane, inverse, metadata, roi, width=self.width, height=self.height,
+                                        size=self.subset_size, stride=self.subset_stride,
+                                        motion_model=self.motion_model, weighting=self.spatial_weighting,
+                                        sigma=self.gaussian_sigma)
+        idx = np.ascontiguousarray(roi.partial_indices, dtype=np.int32)
+        rows = np.ascontiguousarray(metadata.reshape(-1, 16)[idx], dtype=np.float32)
+        inv_rows = np.ascontiguousarray(inverse.reshape(-1, n * n)[idx], dtype=np.float32)
+        words = np.ascontiguousarray(roi.support_words, dtype=np.uint32)
+        boxes = np.ascontiguousarray(roi.support_boxes, dtype=np.float32)
+        self._check(self._lib.gbdic_set_partial_support(
+            self._handle, int(idx.size), _native.ptr(idx), _native.ptr(words), int(words.shape[1]),
+            _native.ptr(boxes), _native.ptr(rows), _native.ptr(inv_rows)))
+        return roi
 
     def set_reference_arrays(
         self,

@@ -20,6 +20,12 @@ import numpy as np
 from .outlier import normalize_median_filter_size
 from .subset import subset_grid_shape
 
+# Admission limits of partial-support windows (roi.py:20-21 of the reference):
+# Hessian condition on coordinates normalised by the subset size, and the
+# weighted RMS contrast in grey levels.
+PARTIAL_MAX_NORMALIZED_CONDITION = 1e8
+PARTIAL_MIN_WEIGHTED_CONTRAST = 1.0
+
 
 def immutable(array: np.ndarray) -> np.ndarray:
     """Read-only copy that owns its bytes."""
@@ -172,13 +178,17 @@ def prepare_roi(
     median_filter_size = normalize_median_filter_size(median_filter_size)
     if mask is None:
         return None
-    if policy != "full" or truncation != "none":
-        raise ValueError("Unknown ROI policy/truncation")
     height, width = mask.shape
     all_allowed = bool(mask.all())
     prefix = None if all_allowed else integral(mask)
     gw, gh = subset_grid_shape(width, height, subset_size=size, subset_stride=stride)
     selected = np.ones((gh, gw), dtype=bool) if all_allowed else select_windows(mask, size, stride, summed_area=prefix)
+    partial_indices = support_words = support_boxes = coverage = None
+    if policy == "partial":
+        selected, partial_indices, support_words, support_boxes, coverage = _partial_windows(
+            mask, selected, size, stride, truncation=truncation)
+    elif policy != "full" or truncation != "none":
+        raise ValueError("Unknown ROI policy/truncation")
     y, x = np.indices(selected.shape)
     ax = x * stride + (size - 1) / 2
     ay = y * stride + (size - 1) / 2
@@ -214,8 +224,103 @@ def prepare_roi(
         int(selected.sum()),
         policy,
         truncation,
+        partial_indices,
+        support_words,
+        support_boxes,
+        coverage,
         median_neighbour_words=median_words,
     )
+
+
+# ---------------------------------------------------------------- partial support
+def pack_support(support: np.ndarray) -> np.ndarray:
+    """Row-major pixel bits, bit 0 of little-endian uint32 words first
+    (roi.py:266-270)."""
+    bits = np.packbits(np.asarray(support, bool).ravel(), bitorder="little")
+    bits = np.pad(bits, (0, (-bits.size) % 4))
+    return bits.view("<u4").astype(np.uint32, copy=False)
+
+
+def unpack_support(words: np.ndarray, size: int) -> np.ndarray:
+    raw = np.asarray(words, dtype="<u4").view(np.uint8)
+    return np.unpackbits(raw, bitorder="little")[: size * size].reshape(size, size).astype(bool)
+
+
+def _central_component(support: np.ndarray) -> np.ndarray:
+    """Pixels 4-connected to the window centre (roi.py:279-300); an even
+    window needs all four central pixels allowed."""
+    size = support.shape[0]
+    lo, hi = (size - 1) // 2, size // 2
+    out = np.zeros_like(support, dtype=bool)
+    if not support[lo: hi + 1, lo: hi + 1].all():
+        return out
+    stack = [(lo, lo)]
+    out[lo, lo] = True
+    while stack:
+        y, x = stack.pop()
+        for ny, nx in ((y - 1, x), (y + 1, x), (y, x - 1), (y, x + 1)):
+            if 0 <= ny < size and 0 <= nx < size and support[ny, nx] and not out[ny, nx]:
+                out[ny, nx] = True
+                stack.append((ny, nx))
+    return out
+
+
+_VISIBILITY: dict[int, np.ndarray] = {}
+
+
+def _visibility_paths(size: int) -> np.ndarray:
+    """For every pixel, the packed set of pixel cells touched by the segment
+    from the window centre to it (roi.py:303-327): slab intersection of the
+    segment with each closed unit cell, boundary touches included."""
+    if size in _VISIBILITY:
+        return _VISIBILITY[size]
+    y, x = np.indices((size, size)).reshape(2, -1).astype(np.float64)
+    centre = (size - 1) / 2
+    lower = np.zeros((size * size, size * size))
+    upper = np.ones_like(lower)
+    for coord in (x, y):
+        delta = coord - centre
+        moving = delta != 0
+        a = np.full_like(lower, -np.inf)
+        b = np.full_like(upper, np.inf)
+        a[moving] = (coord[None, :] - 0.5 - centre) / delta[moving, None]
+        b[moving] = (coord[None, :] + 0.5 - centre) / delta[moving, None]
+        lower = np.maximum(lower, np.minimum(a, b))
+        upper = np.minimum(upper, np.maximum(a, b))
+        upper[np.ix_(~moving, np.abs(coord - centre) > 0.5)] = -1
+    paths = immutable(np.stack([pack_support(row) for row in lower <= upper]))
+    _VISIBILITY[size] = paths
+    return paths
+
+
+def _partial_windows(mask: np.ndarray, complete: np.ndarray, size: int, stride: int, *, truncation: str):
+    """Windows cut by the ROI whose central component survives
+    (roi.py:330-366): (selected, indices, support words, boxes, coverage)."""
+    if truncation not in ("none", "visibility"):
+        raise ValueError("roi_truncation must be 'none' or 'visibility'")
+    selected = complete.copy()
+    indices, words, boxes = [], [], []
+    coverage = complete.astype(np.float32)
+    for gy, gx in np.argwhere(~complete):
+        local = mask[gy * stride: gy * stride + size, gx * stride: gx * stride + size]
+        support = _central_component(local)
+        if not support.any():
+            continue
+        if truncation == "visibility":
+            visible = ~np.any(_visibility_paths(size) & ~pack_support(support), axis=1)
+            support = _central_component(support & visible.reshape(size, size))
+            if not support.any():
+                continue
+        selected[gy, gx] = True
+        indices.append(gy * complete.shape[1] + gx)
+        words.append(pack_support(support))
+        sy, sx = np.nonzero(support)
+        boxes.append((sx.min(), sy.min(), sx.max(), sy.max()))
+        coverage[gy, gx] = support.sum() / (size * size)
+    count = (size * size + 31) // 32
+    return (selected, immutable(np.asarray(indices, np.uint32)),
+            immutable(np.asarray(words, np.uint32).reshape(-1, count)),
+            immutable(np.asarray(boxes, np.float32).reshape(-1, 4)), immutable(coverage))
 
 
 def seed_permissions(

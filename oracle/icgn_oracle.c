@@ -291,10 +291,13 @@ static inline int parameter_count(int model) { return model == MODEL_QUADRATIC ?
 static inline int state_stride(int model) { return model == MODEL_QUADRATIC ? 16 : 8; }
 static inline int meta_stride(int model) { return model == MODEL_QUADRATIC ? 28 : 16; }
 
-/* One subset: icgn.wgsl:595-958. */
+/* One subset: icgn.wgsl:595-958.  support / box (partial windows,
+ * icgn.wgsl:1042-1085 with PARTIAL_SUPPORT): pixel bits of the window's
+ * support and its (x0, y0, x1, y1) pixel box; NULL for complete windows. */
 static void solve_one(const oracle_solve_cfg *c, int index, const uint8_t *img, const float *coef,
                       const float *refplane, const float *meta, const float *hinv,
-                      const warp_t *initial, int enabled, int preserve_disabled, float *state) {
+                      const warp_t *initial, int enabled, int preserve_disabled, float *state,
+                      const uint32_t *support, const float *box) {
     const int W = c->width, H = c->height, S = c->subset_size, st = c->subset_stride;
     const int model = c->model, L = c->lanes;
     const int n = parameter_count(model);
@@ -303,17 +306,20 @@ static void solve_one(const oracle_solve_cfg *c, int index, const uint8_t *img, 
     warp_t w = *initial;
     if (model == MODEL_TRANSLATION) memset(w.lin, 0, sizeof w.lin);
     if (model != MODEL_QUADRATIC) memset(w.curv, 0, sizeof w.curv);
-    int reference_valid = md[1] >= 0.5f;
+    int reference_valid = support ? md[1] == -4.0f : md[1] >= 0.5f;
     int valid = enabled && reference_valid;
     float rejected = -1.0f;
-    if (c->roi_enabled) rejected = fminf(-1.0f, md[1]);
+    if (c->roi_enabled && !support) rejected = fminf(-1.0f, md[1]);
     float status = valid ? 0.0f : rejected;
     float iters = 0.0f;
     const int gx = index % c->grid_w, gy = index / c->grid_w;
     const float half = 0.5f * ((float)S - 1.0f);
     const int mean_off = model == MODEL_QUADRATIC ? 26 : 14;
-    const float ref_mean = (st != S) ? md[mean_off] : 0.0f;
-    const float wsum = c->weights ? md[3 + 2 * n] : (float)(S * S);
+    const float ref_mean = (st != S || support) ? md[mean_off] : 0.0f;
+    const float wsum = (c->weights || support) ? md[3 + 2 * n] : (float)(S * S);
+    /* local extent checked against the image: the support box or the window */
+    const float bx0 = support ? box[0] - half : -half, by0 = support ? box[1] - half : -half;
+    const float bx1 = support ? box[2] - half : half, by1 = support ? box[3] - half : half;
     float previous_change = 3.402823e38f;
     unsigned stalled = 0;
     const int npix = S * S;
@@ -322,8 +328,14 @@ static void solve_one(const oracle_solve_cfg *c, int index, const uint8_t *img, 
         if (!(c->divergence_patience != 0 && status == 3.0f)) {
             int inside = 1;
             if (model == MODEL_TRANSLATION) {
-                float x0 = (float)(gx * st) + w.t[0], y0 = (float)(gy * st) + w.t[1];
-                float x1 = (float)(gx * st + S - 1) + w.t[0], y1 = (float)(gy * st + S - 1) + w.t[1];
+                float x0, y0, x1, y1;
+                if (support) {
+                    x0 = ((float)(gx * st) + box[0]) + w.t[0]; y0 = ((float)(gy * st) + box[1]) + w.t[1];
+                    x1 = ((float)(gx * st) + box[2]) + w.t[0]; y1 = ((float)(gy * st) + box[3]) + w.t[1];
+                } else {
+                    x0 = (float)(gx * st) + w.t[0]; y0 = (float)(gy * st) + w.t[1];
+                    x1 = (float)(gx * st + S - 1) + w.t[0]; y1 = (float)(gy * st + S - 1) + w.t[1];
+                }
                 inside = x0 >= 2.0f && y0 >= 2.0f && x1 <= (float)W - 3.0f && y1 <= (float)H - 3.0f;
             } else {
                 int count = model == MODEL_QUADRATIC ? 9 : 4;
@@ -333,8 +345,8 @@ static void solve_one(const oracle_solve_cfg *c, int index, const uint8_t *img, 
                         lx = (float)(p % 3 - 1) * half;
                         ly = (float)(p / 3 - 1) * half;
                     } else {
-                        lx = (p == 1 || p == 3) ? half : -half;
-                        ly = (p >= 2) ? half : -half;
+                        lx = (p == 1 || p == 3) ? bx1 : bx0;
+                        ly = (p >= 2) ? by1 : by0;
                     }
                     float dx, dy;
                     displacement(model, &w, lx, ly, 0.5f * lx * lx, lx * ly, 0.5f * ly * ly, &dx, &dy);
@@ -355,6 +367,7 @@ static void solve_one(const oracle_solve_cfg *c, int index, const uint8_t *img, 
             float s[15];
             for (int k = 0; k < 15; ++k) s[k] = 0.0f;
             for (int p = lane; p < npix; p += L) {
+                if (support && !((support[p >> 5] >> (p & 31)) & 1u)) continue;
                 int col = p % S, row = p / S;
                 float lx = (float)col - half, ly = (float)row - half;
                 float hx2 = 0.5f * lx * lx, xy = lx * ly, hy2 = 0.5f * ly * ly;
@@ -514,7 +527,32 @@ void oracle_solve(const oracle_solve_cfg *c, const uint8_t *img, const float *co
                 for (int j = 0; j < 6; ++j) w.curv[j] = s[6 + j];
             enabled = active[index] != 0u;
         }
-        solve_one(c, index, img, coef, refplane, meta, hinv, &w, enabled, preserve_disabled, state);
+        solve_one(c, index, img, coef, refplane, meta, hinv, &w, enabled, preserve_disabled, state, NULL, NULL);
+    }
+}
+
+/* Partial windows (solve_partial / solve_partial_seeded, icgn.wgsl:1062-1078):
+ * window indices[k] with support words words[k * words_per] and box
+ * boxes[4 k]; seed_state / active as for oracle_solve (NULL: zero seed). */
+void oracle_solve_partial(const oracle_solve_cfg *c, const uint8_t *img, const float *coef, const float *refplane,
+                          const float *meta, const float *hinv, const float *seed_state, const uint32_t *active,
+                          const int32_t *indices, int count, const uint32_t *words, int words_per, const float *boxes,
+                          float *state) {
+    const int ss = state_stride(c->model);
+    #pragma omp parallel for schedule(dynamic, 4)
+    for (int k = 0; k < count; ++k) {
+        int index = indices[k];
+        warp_t w;
+        memset(&w, 0, sizeof w);
+        int enabled = 1;
+        if (seed_state) {
+            const float *s = seed_state + (size_t)index * ss;
+            w.t[0] = s[0]; w.lin[0] = s[1]; w.lin[1] = s[2]; w.t[1] = s[3];
+            w.lin[2] = s[4]; w.lin[3] = s[5];
+            enabled = active[index] != 0u;
+        }
+        solve_one(c, index, img, coef, refplane, meta, hinv, &w, enabled, 0, state, words + (size_t)k * words_per,
+                  boxes + 4 * (size_t)k);
     }
 }
 

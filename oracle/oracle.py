@@ -119,7 +119,10 @@ def solve(
     subsets: np.ndarray | None = None,
     divergence_patience: int = 0,
     divergence_min_iterations: int = 4,
+    partial: tuple | None = None,
 ) -> np.ndarray:
+    """`partial` = (indices, support words, boxes): solve only those partial
+    windows with their supports (into `state`)."""
     img = np.ascontiguousarray(image, dtype=np.uint8)
     h, w = img.shape
     gw = 1 + (w - subset_size) // subset_stride
@@ -148,6 +151,16 @@ def solve(
     seed = None if seed_state is None else np.ascontiguousarray(seed_state, dtype=np.float32).reshape(-1)
     act = None if active is None else np.ascontiguousarray(active, dtype=np.uint32).ravel()
     sub = None if subsets is None else np.ascontiguousarray(subsets, dtype=np.int32)
+    if partial is not None:
+        indices, words, boxes = partial
+        idx = np.ascontiguousarray(indices, dtype=np.int32)
+        wds = np.ascontiguousarray(words, dtype=np.uint32)
+        bxs = np.ascontiguousarray(boxes, dtype=np.float32)
+        lib().oracle_solve_partial(
+            C.byref(cfg), _p(img, C.c_uint8), _p(coef_arr), _p(pl), _p(meta), _p(inv), _p(seed),
+            _p(act, C.c_uint32), _p(idx, C.c_int32), int(idx.size), _p(wds, C.c_uint32),
+            int(wds.shape[1]) if wds.ndim == 2 else 0, _p(bxs), _p(state))
+        return state
     lib().oracle_solve(
         C.byref(cfg), _p(img, C.c_uint8), _p(coef_arr), _p(pl), _p(meta), _p(inv),
         _p(seed), _p(act, C.c_uint32), int(preserve_disabled),

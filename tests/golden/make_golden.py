@@ -171,6 +171,39 @@ def main(reference_root: str) -> None:
 
     np.savez_compressed(HERE / "reference_vectors.npz", **out)
     fourier_vectors(Path(reference_root))
+    partial_vectors(Path(reference_root))
+
+
+def partial_vectors(reference_root: Path) -> None:
+    """Partial-support ROI planning (roi.py, both truncations) and the
+    partial reference preparation (partial.py) on a speckle reference."""
+    backend, _, roi, _ = _import_reference(reference_root)
+    import live_dic.partial as partial
+
+    rng = np.random.default_rng(515)
+    ref = speckle(rng, 150, 170, 420)
+    yy, xx = np.mgrid[:150, :170]
+    mask = ((xx - 80) ** 2 + (yy - 70) ** 2 >= 26 ** 2) & ~((xx > 120) & (yy > 100) & (xx < 130))
+    out: dict[str, np.ndarray] = {"partial_ref": ref, "partial_mask": mask}
+    for truncation in ("none", "visibility"):
+        plan = roi.prepare_roi(mask, 21, 10, policy="partial", truncation=truncation)
+        out[f"partial_{truncation}_selected"] = plan.selected
+        out[f"partial_{truncation}_indices"] = plan.partial_indices
+        out[f"partial_{truncation}_words"] = plan.support_words
+        out[f"partial_{truncation}_boxes"] = plan.support_boxes
+        out[f"partial_{truncation}_bits"] = plan.neighbour_bits
+    plan = roi.prepare_roi(mask, 21, 10, policy="partial", truncation="none")
+    plane, inverse, metadata = backend._reference_arrays(ref, subset_size=21, subset_stride=10)
+    out["partial_plane"] = plane
+    out["partial_metadata_in"] = metadata.copy()
+    out["partial_inverse_in"] = inverse.copy()
+    updated = partial.prepare_partial_reference(plane, inverse, metadata, plan, width=170, height=150, size=21,
+                                                stride=10, motion_model="affine", weighting="uniform", sigma=5.25)
+    out["partial_metadata_out"] = metadata
+    out["partial_inverse_out"] = inverse
+    out["partial_condition"] = updated.support_condition
+    out["partial_rank"] = updated.support_rank
+    np.savez_compressed(HERE / "partial_vectors.npz", **out)
 
 
 def fourier_vectors(reference_root: Path) -> None:

@@ -243,3 +243,29 @@ def test_recovery_seed_transfer_matches_reference(golden, model):
     closure = pyramid_dependency_mask(source_grid=(status.shape[1], status.shape[0]), source_scale=2,
                                       destination_scale=1, requested=requested, subset_size=21, subset_stride=10)
     assert closure.shape == status.shape and closure.any()
+
+
+@pytest.mark.parametrize("truncation", ["none", "visibility"])
+def test_partial_roi_planning_matches_reference(truncation):
+    g = np.load(ROOT / "tests" / "golden" / "partial_vectors.npz")
+    plan = roi.prepare_roi(g["partial_mask"], 21, 10, policy="partial", truncation=truncation)
+    np.testing.assert_array_equal(plan.selected, g[f"partial_{truncation}_selected"])
+    np.testing.assert_array_equal(plan.partial_indices, g[f"partial_{truncation}_indices"])
+    np.testing.assert_array_equal(plan.support_words, g[f"partial_{truncation}_words"])
+    np.testing.assert_array_equal(plan.support_boxes, g[f"partial_{truncation}_boxes"])
+    np.testing.assert_array_equal(plan.neighbour_bits, g[f"partial_{truncation}_bits"])
+
+
+def test_partial_reference_preparation_matches_reference():
+    from live_dic_gb300.partial import prepare_partial_reference
+
+    g = np.load(ROOT / "tests" / "golden" / "partial_vectors.npz")
+    plan = roi.prepare_roi(g["partial_mask"], 21, 10, policy="partial")
+    metadata = g["partial_metadata_in"].copy()
+    inverse = g["partial_inverse_in"].copy()
+    updated = prepare_partial_reference(g["partial_plane"], inverse, metadata, plan, width=170, height=150, size=21,
+                                        stride=10, motion_model="affine", weighting="uniform", sigma=5.25)
+    np.testing.assert_array_equal(metadata, g["partial_metadata_out"])
+    np.testing.assert_array_equal(inverse, g["partial_inverse_out"])
+    np.testing.assert_array_equal(updated.support_rank, g["partial_rank"])
+    np.testing.assert_allclose(updated.support_condition, g["partial_condition"], rtol=1e-12)
