@@ -332,6 +332,13 @@ int gbdic_pyramid_set_solver_variant(gbdic_pyramid *pyramid, int32_t threads_per
  * (full_pyramid_backend.py:1704-1714). */
 int gbdic_pyramid_set_translation(gbdic_pyramid *pyramid, int32_t slot, float dx, float dy);
 
+/* gbdic_set_partial_support() for one level of the pyramid (0 = finest):
+ * ICGNWGPUFullPyramid.set_reference applies roi_policy="partial" at every
+ * level (full_pyramid_backend.py:1222-1232). */
+int gbdic_pyramid_set_partial_support(gbdic_pyramid *pyramid, int32_t level, int32_t count, const int32_t *indices,
+                                      const uint32_t *words, int32_t words_per_window, const float *boxes,
+                                      const float *metadata_rows, const float *inverse_rows);
+
 /* ------------------------------------------------------------ batch */
 
 /* Batched registration of many fixed-reference jobs of uneven image size,

@@ -374,47 +374,8 @@ int gbdic_set_partial_support(gbdic_engine *e, int32_t count, const int32_t *ind
                               const float *inverse_rows) {
     return guarded(e, [&] {
         e->require_ready("set_partial_support");
-        auto &lvl = e->level;
-        const auto &o = e->rt->opts().o;
-        if (o.motion_model == GBDIC_MODEL_QUADRATIC) fail(GBDIC_EINVAL, "partial ROI windows support translation and affine models");
-        if (count < 0 || (count > 0 && (!indices || !words || !boxes || !metadata_rows || !inverse_rows)))
-            fail(GBDIC_EINVAL, "partial support tables are incomplete");
-        if (count > 0 && words_per_window != (o.subset_size * o.subset_size + 31) / 32)
-            fail(GBDIC_EINVAL, "words_per_window must be ceil(subset_size^2 / 32)");
-        for (int k = 0; k < count; ++k)
-            if (indices[k] < 0 || indices[k] >= lvl.count) fail(GBDIC_EINVAL, "partial window index out of range");
-        check_cuda(cudaStreamSynchronize(e->rt->stream()), "pending work");
-        const int ms = gbdic::meta_stride(o.motion_model), n = gbdic::parameter_count(o.motion_model);
-        std::vector<float> meta((size_t)lvl.count * ms), inv((size_t)lvl.count * n * n);
-        std::vector<uint8_t> adm((size_t)lvl.count);
-        check_cuda(cudaMemcpy(meta.data(), lvl.meta.get(), meta.size() * sizeof(float), cudaMemcpyDeviceToHost), "metadata");
-        check_cuda(cudaMemcpy(inv.data(), lvl.inv.get(), inv.size() * sizeof(float), cudaMemcpyDeviceToHost), "inverse");
-        check_cuda(cudaMemcpy(adm.data(), lvl.admissible.get(), adm.size(), cudaMemcpyDeviceToHost), "admissibility");
-        for (int k = 0; k < count; ++k) {
-            const size_t i = (size_t)indices[k];
-            std::memcpy(&meta[i * ms], metadata_rows + (size_t)k * ms, ms * sizeof(float));
-            std::memcpy(&inv[i * n * n], inverse_rows + (size_t)k * n * n, (size_t)n * n * sizeof(float));
-            adm[i] = meta[i * ms + 1] == -4.0f ? 1 : 0;
-        }
-        check_cuda(cudaMemcpy(lvl.meta.get(), meta.data(), meta.size() * sizeof(float), cudaMemcpyHostToDevice), "metadata");
-        check_cuda(cudaMemcpy(lvl.inv.get(), inv.data(), inv.size() * sizeof(float), cudaMemcpyHostToDevice), "inverse");
-        check_cuda(cudaMemcpy(lvl.admissible.get(), adm.data(), adm.size(), cudaMemcpyHostToDevice), "admissibility");
-        lvl.partial_count = count;
-        lvl.support_words = words_per_window;
-        if (count > 0) {
-            lvl.partial_index.ensure((size_t)count * sizeof(int32_t));
-            lvl.partial_words.ensure((size_t)count * words_per_window * sizeof(uint32_t));
-            lvl.partial_boxes.ensure((size_t)count * 4 * sizeof(float));
-            check_cuda(cudaMemcpy(lvl.partial_index.get(), indices, (size_t)count * sizeof(int32_t), cudaMemcpyHostToDevice),
-                       "partial indices");
-            check_cuda(cudaMemcpy(lvl.partial_words.get(), words, (size_t)count * words_per_window * sizeof(uint32_t),
-                                  cudaMemcpyHostToDevice), "support words");
-            check_cuda(cudaMemcpy(lvl.partial_boxes.get(), boxes, (size_t)count * 4 * sizeof(float), cudaMemcpyHostToDevice),
-                       "support boxes");
-        }
-        int valid = 0;
-        for (int i = 0; i < lvl.count; ++i) valid += meta[(size_t)i * ms + 1] > 0.5f;
-        lvl.valid_count = valid;
+        e->rt->set_partial_support(e->level, count, indices, words, words_per_window, boxes, metadata_rows,
+                                   inverse_rows);
         for (auto &h : e->host) {
             if (h.graph) cudaGraphExecDestroy(h.graph);
             h.graph = nullptr;

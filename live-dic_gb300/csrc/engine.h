@@ -116,6 +116,13 @@ class Runtime {
                              const float *roi_links);
     void upload_reference_arrays(Level &level, const float *plane, const float *meta,
                                  const float *inverse, const float *links);
+    // Partial-support windows: replaces the metadata / inverse rows of
+    // `count` windows by host-prepared ones and stores their support tables;
+    // every later solve of the level runs the partial solver after the
+    // complete windows.  count = 0 clears them.
+    void set_partial_support(Level &level, int count, const int32_t *indices, const uint32_t *words,
+                             int words_per_window, const float *boxes, const float *metadata_rows,
+                             const float *inverse_rows);
     // Per-frame stages of one level on `stream`.
     // `frame` (device bytes) and `state` / `out` override the slot's own
     // buffers when non-null.

@@ -538,6 +538,23 @@ int gbdic_pyramid_set_translation(gbdic_pyramid *p, int32_t slot, float dx, floa
     });
 }
 
+int gbdic_pyramid_set_partial_support(gbdic_pyramid *p, int32_t level, int32_t count, const int32_t *indices,
+                                      const uint32_t *words, int32_t words_per_window, const float *boxes,
+                                      const float *metadata_rows, const float *inverse_rows) {
+    return pguarded(p, [&] {
+        if (!p->ready) fail(GBDIC_ESTATE, "Call set_reference() before set_partial_support().");
+        if (level < 0 || level >= p->L()) fail(GBDIC_EINVAL, "level out of range");
+        for (auto &s : p->slots)
+            if (s.pending) fail(GBDIC_ESTATE, "retire every slot before changing the partial windows");
+        p->rt->set_partial_support(*p->levels[level], count, indices, words, words_per_window, boxes, metadata_rows,
+                                   inverse_rows);
+        for (auto &s : p->slots) {
+            if (s.graph) cudaGraphExecDestroy(s.graph);
+            s.graph = nullptr;
+        }
+    });
+}
+
 int gbdic_pyramid_set_solver_variant(gbdic_pyramid *p, int32_t threads_per_subset, int32_t persistent) {
     return pguarded(p, [&] {
         for (auto &s : p->slots)

@@ -310,6 +310,51 @@ void Runtime::upload_reference_arrays(Level &level, const float *plane, const fl
     check_cuda(cudaMemcpy(level.admissible.get(), adm.data(), adm.size(), cudaMemcpyHostToDevice), "admissibility upload");
 }
 
+void Runtime::set_partial_support(Level &level, int count, const int32_t *indices, const uint32_t *words,
+                                  int words_per_window, const float *boxes, const float *metadata_rows,
+                                  const float *inverse_rows) {
+    const auto &o = opt_.o;
+    if (o.motion_model == GBDIC_MODEL_QUADRATIC) fail(GBDIC_EINVAL, "partial ROI windows support translation and affine models");
+    if (count < 0 || (count > 0 && (!indices || !words || !boxes || !metadata_rows || !inverse_rows)))
+        fail(GBDIC_EINVAL, "partial support tables are incomplete");
+    if (count > 0 && words_per_window != (o.subset_size * o.subset_size + 31) / 32)
+        fail(GBDIC_EINVAL, "words_per_window must be ceil(subset_size^2 / 32)");
+    for (int k = 0; k < count; ++k)
+        if (indices[k] < 0 || indices[k] >= level.count) fail(GBDIC_EINVAL, "partial window index out of range");
+    check_cuda(cudaStreamSynchronize(stream_), "pending work");
+    const int ms = gbdic::meta_stride(o.motion_model), n = gbdic::parameter_count(o.motion_model);
+    std::vector<float> meta((size_t)level.count * ms), inv((size_t)level.count * n * n);
+    std::vector<uint8_t> adm((size_t)level.count);
+    check_cuda(cudaMemcpy(meta.data(), level.meta.get(), meta.size() * sizeof(float), cudaMemcpyDeviceToHost), "metadata");
+    check_cuda(cudaMemcpy(inv.data(), level.inv.get(), inv.size() * sizeof(float), cudaMemcpyDeviceToHost), "inverse");
+    check_cuda(cudaMemcpy(adm.data(), level.admissible.get(), adm.size(), cudaMemcpyDeviceToHost), "admissibility");
+    for (int k = 0; k < count; ++k) {
+        const size_t i = (size_t)indices[k];
+        std::memcpy(&meta[i * ms], metadata_rows + (size_t)k * ms, ms * sizeof(float));
+        std::memcpy(&inv[i * n * n], inverse_rows + (size_t)k * n * n, (size_t)n * n * sizeof(float));
+        adm[i] = meta[i * ms + 1] == -4.0f ? 1 : 0;
+    }
+    check_cuda(cudaMemcpy(level.meta.get(), meta.data(), meta.size() * sizeof(float), cudaMemcpyHostToDevice), "metadata");
+    check_cuda(cudaMemcpy(level.inv.get(), inv.data(), inv.size() * sizeof(float), cudaMemcpyHostToDevice), "inverse");
+    check_cuda(cudaMemcpy(level.admissible.get(), adm.data(), adm.size(), cudaMemcpyHostToDevice), "admissibility");
+    level.partial_count = count;
+    level.support_words = words_per_window;
+    if (count > 0) {
+        level.partial_index.ensure((size_t)count * sizeof(int32_t));
+        level.partial_words.ensure((size_t)count * words_per_window * sizeof(uint32_t));
+        level.partial_boxes.ensure((size_t)count * 4 * sizeof(float));
+        check_cuda(cudaMemcpy(level.partial_index.get(), indices, (size_t)count * sizeof(int32_t), cudaMemcpyHostToDevice),
+                   "partial indices");
+        check_cuda(cudaMemcpy(level.partial_words.get(), words, (size_t)count * words_per_window * sizeof(uint32_t),
+                              cudaMemcpyHostToDevice), "support words");
+        check_cuda(cudaMemcpy(level.partial_boxes.get(), boxes, (size_t)count * 4 * sizeof(float), cudaMemcpyHostToDevice),
+                   "support boxes");
+    }
+    int valid = 0;
+    for (int i = 0; i < level.count; ++i) valid += meta[(size_t)i * ms + 1] > 0.5f;
+    level.valid_count = valid;
+}
+
 void Runtime::enqueue_prefilter(Level &level, LevelSlot &slot, const uint8_t *frame, cudaStream_t s) {
     if (opt_.o.interpolation != kInterpBspline) return;
     check_cuda(launch_fir_prefilter(frame ? frame : slot.frame.as<uint8_t>(), level.W, level.H, level.W,

@@ -211,6 +211,7 @@ _SIGNATURES = {
     "gbdic_search_seeds_device": (C.c_int, [P, P, P, P, P, I32, I32, P]),
     "gbdic_pyramid_set_translation": (C.c_int, [P, I32, C.c_float, C.c_float]),
     "gbdic_set_partial_support": (C.c_int, [P, I32, P, P, I32, P, P, P]),
+    "gbdic_pyramid_set_partial_support": (C.c_int, [P, I32, I32, P, P, I32, P, P, P]),
     "gbdic_fourier_create": (C.c_int, [I32, P, P, I32, C.POINTER(P)]),
     "gbdic_fourier_destroy": (C.c_int, [P]),
     "gbdic_fourier_last_error": (C.c_char_p, [P]),

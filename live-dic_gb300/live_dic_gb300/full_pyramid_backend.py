@@ -308,8 +308,6 @@ class ICGNWGPUFullPyramid:
             _validated_config(it, tol, new_zncc)
         reference = _as_uint8_gray(image)
         mask = validate_roi(roi_mask, roi_policy, reference.shape, self.motion_model, roi_truncation)
-        if roi_policy == "partial" and mask is not None:
-            raise ICGNError("roi_policy='partial' is not available in this build; use roi_policy='full'.")
         height, width = reference.shape
         dims = []
         w, h = width, height
@@ -322,7 +320,8 @@ class ICGNWGPUFullPyramid:
         masks = [mask]
         for _ in range(1, self.pyramid_levels):
             masks.append(None if masks[-1] is None else reduce_mask(masks[-1]))
-        plans = [prepare_roi(m, self.subset_size, self.subset_stride, median_filter_size=self.median_filter_size) for m in masks]
+        plans = [prepare_roi(m, self.subset_size, self.subset_stride, policy=roi_policy, truncation=roi_truncation,
+                             median_filter_size=self.median_filter_size) for m in masks]
         effective = plans[0] is not None and plans[0].effective
         keep: list[np.ndarray] = []
         rois = (_native.LevelRoi * self.pyramid_levels)()
@@ -361,6 +360,9 @@ class ICGNWGPUFullPyramid:
         prep_ms = (time.perf_counter() - prep_start) * 1e3
         self.width, self.height = width, height
         self.grid_width, self.grid_height = dims[0][2], dims[0][3]
+        for level, plan in enumerate(plans):
+            if plan is not None and plan.partial_indices is not None and plan.partial_indices.size:
+                plans[level] = self._install_partial(level, plan, dims[level])
         self.roi = plans[0]
         admissible = np.empty(self.grid_width * self.grid_height, np.uint8)
         self._check(self._lib.gbdic_pyramid_export(self._handle, 0, _native.EXPORT_ADMISSIBLE,
@@ -395,6 +397,18 @@ class ICGNWGPUFullPyramid:
             roi=self.roi,
             reference_valid=self.reference_valid,
         )
+
+    def _install_partial(self, level: int, plan, dims) -> Any:
+        """Partial-support windows of one level (the reference applies the
+        policy at every scale, full_pyramid_backend.py:1222-1232)."""
+        from .partial import install_partial_reference
+
+        w, h = dims[0], dims[1]
+        return install_partial_reference(
+            plan, lambda what, dtype, shape: self.export_level(level, what, dtype, shape),
+            lambda *args: self._check(self._lib.gbdic_pyramid_set_partial_support(self._handle, level, *args)),
+            width=w, height=h, size=self.subset_size, stride=self.subset_stride, motion_model=self.motion_model,
+            weighting=self.spatial_weighting, sigma=self.gaussian_sigma)
 
     def _config_echo(self) -> dict[str, Any]:
         echo: dict[str, Any] = {

@@ -428,26 +428,13 @@ class ICGNWGPU:
     def _prepare_partial(self, roi: RoiPlan) -> RoiPlan:
         """Partial-window metadata from the GPU-prepared plane (float64 host
         preparation, partial.py:26-121), uploaded with the support tables."""
-        from .partial import prepare_partial_reference
+        from .partial import install_partial_reference
 
-        n = parameter_count(self.motion_model)
-        count = self.grid_width * self.grid_height
-        plane = self._export(_native.EXPORT_PLANE, np.float32, (self.height * self.width * 4,))
-        inverse = self._export(_native.EXPORT_INVERSE, np.float32, (count * n * n,)).astype(np.float64)
-        metadata = self._export(_native.EXPORT_METADATA, np.float32, (count * 16,)).astype(np.float64)
-        roi = prepare_partial_reference(plane, inverse, metadata, roi, width=self.width, height=self.height,
-                                        size=self.subset_size, stride=self.subset_stride,
-                                        motion_model=self.motion_model, weighting=self.spatial_weighting,
-                                        sigma=self.gaussian_sigma)
-        idx = np.ascontiguousarray(roi.partial_indices, dtype=np.int32)
-        rows = np.ascontiguousarray(metadata.reshape(-1, 16)[idx], dtype=np.float32)
-        inv_rows = np.ascontiguousarray(inverse.reshape(-1, n * n)[idx], dtype=np.float32)
-        words = np.ascontiguousarray(roi.support_words, dtype=np.uint32)
-        boxes = np.ascontiguousarray(roi.support_boxes, dtype=np.float32)
-        self._check(self._lib.gbdic_set_partial_support(
-            self._handle, int(idx.size), _native.ptr(idx), _native.ptr(words), int(words.shape[1]),
-            _native.ptr(boxes), _native.ptr(rows), _native.ptr(inv_rows)))
-        return roi
+        return install_partial_reference(
+            roi, self._export,
+            lambda *args: self._check(self._lib.gbdic_set_partial_support(self._handle, *args)),
+            width=self.width, height=self.height, size=self.subset_size, stride=self.subset_stride,
+            motion_model=self.motion_model, weighting=self.spatial_weighting, sigma=self.gaussian_sigma)
 
     def set_reference_arrays(
         self,
@@ -616,7 +603,9 @@ class ICGNWGPU:
                 device=self.device_index, pipeline_slots=1,
             )
             try:
-                engine.set_reference(reduced, iterations=12, tolerance=1e-2, zncc_min=zncc_min, roi_mask=mask)
+                engine.set_reference(reduced, iterations=12, tolerance=1e-2, zncc_min=zncc_min, roi_mask=mask,
+                                     roi_policy="full" if self.roi is None else self.roi.policy,
+                                     roi_truncation="none" if self.roi is None else self.roi.truncation)
             except Exception:
                 engine.close()
                 self._close_pyramid_engines()

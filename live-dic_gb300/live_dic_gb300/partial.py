@@ -16,6 +16,7 @@ from dataclasses import replace
 
 import numpy as np
 
+from . import _native
 from .roi import PARTIAL_MAX_NORMALIZED_CONDITION, PARTIAL_MIN_WEIGHTED_CONTRAST, RoiPlan, immutable, unpack_support
 
 
@@ -80,3 +81,26 @@ def prepare_partial_reference(plane: np.ndarray, inverse: np.ndarray, metadata: 
         rows[index, 15] = wsum
     return replace(roi, support_condition=immutable(conditions), support_rank=immutable(ranks),
                    support_contrast=immutable(contrasts))
+
+
+def install_partial_reference(roi: RoiPlan, export, upload, *, width: int, height: int, size: int, stride: int,
+                              motion_model: str, weighting: str, sigma: float) -> RoiPlan:
+    """Reads one level's GPU-prepared plane, inverse and metadata through
+    `export(what, dtype, shape)`, prepares the partial windows of `roi` and
+    hands the tables and replacement rows to `upload(count, indices, words,
+    words_per_window, boxes, metadata_rows, inverse_rows)` (a
+    gbdic_set_partial_support-shaped C entry)."""
+    count = roi.selected.size
+    plane = export(_native.EXPORT_PLANE, np.float32, (height * width * 4,))
+    inverse = export(_native.EXPORT_INVERSE, np.float32, (count * 36,)).astype(np.float64)
+    metadata = export(_native.EXPORT_METADATA, np.float32, (count * 16,)).astype(np.float64)
+    roi = prepare_partial_reference(plane, inverse, metadata, roi, width=width, height=height, size=size,
+                                    stride=stride, motion_model=motion_model, weighting=weighting, sigma=sigma)
+    idx = np.ascontiguousarray(roi.partial_indices, dtype=np.int32)
+    rows = np.ascontiguousarray(metadata.reshape(-1, 16)[idx], dtype=np.float32)
+    inv_rows = np.ascontiguousarray(inverse.reshape(-1, 36)[idx], dtype=np.float32)
+    words = np.ascontiguousarray(roi.support_words, dtype=np.uint32)
+    boxes = np.ascontiguousarray(roi.support_boxes, dtype=np.float32)
+    upload(int(idx.size), _native.ptr(idx), _native.ptr(words), int(words.shape[1]), _native.ptr(boxes),
+           _native.ptr(rows), _native.ptr(inv_rows))
+    return roi
