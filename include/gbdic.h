@@ -263,6 +263,9 @@ typedef struct {
     uint32_t temporal_max_age;      /* 0xFFFFFFFE = never expire */
     int32_t temporal_prediction;    /* 0 none, 1 velocity */
     int32_t seed_search_radius;     /* integer search radius (pixels, coarsest level) */
+    int32_t temporal_fine_correction; /* 1: finest seeds = fine history + coarse change (temporal, 2 levels) */
+    int32_t adaptive;               /* 1: pyramid_policy="adaptive" (temporal, 2 levels); the caller picks
+                                       the levels of each frame with gbdic_pyramid_set_active_levels() */
 } gbdic_pyramid_options;
 
 /* Static per-level ROI tables produced by host-side planning (roi.py). */
@@ -331,6 +334,12 @@ int gbdic_pyramid_set_solver_variant(gbdic_pyramid *pyramid, int32_t threads_per
  * subset starts from (dx, dy) / 2^(levels - 1)
  * (full_pyramid_backend.py:1704-1714). */
 int gbdic_pyramid_set_translation(gbdic_pyramid *pyramid, int32_t slot, float dx, float dy);
+
+/* Levels the next submitted frames run (pyramid_policy="adaptive",
+ * full_pyramid_backend.py:1448-1452,1781-1790): 1 = the finest level alone,
+ * seeded from the temporal history; `levels` = the whole pyramid.  Other
+ * values, or 1 without the adaptive policy, are rejected. */
+int gbdic_pyramid_set_active_levels(gbdic_pyramid *pyramid, int32_t levels);
 
 /* gbdic_set_partial_support() for one level of the pyramid (0 = finest):
  * ICGNWGPUFullPyramid.set_reference applies roi_policy="partial" at every

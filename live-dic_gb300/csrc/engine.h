@@ -89,6 +89,7 @@ struct Level {
     DeviceBuffer ref_image;                          // reference bytes (seed search)
     DeviceBuffer partial_index, partial_words, partial_boxes;  // partial-support windows
     int partial_count = 0, support_words = 0;
+    bool divergence = true;  // apply the divergence stop here (pyramids: finest level only)
     std::vector<std::unique_ptr<LevelSlot>> slots;
     int valid_count = 0;
 };

@@ -101,8 +101,18 @@ struct SeedArgs {
     int model;
     unsigned *projected;      // counter for temporal projection, or nullptr
     int mark_missing;         // write status -1 into seeds that received no estimate
+    int track;                // seed availability marker in the status slot: 0 complete stencil, -1 otherwise
+    // Temporal fine correction only (source = coarse accepted history):
+    const float *history;           // fine accepted history
+    const uint32_t *history_ages;   // its ages
+    const uint32_t *source_ages;    // coarse history ages
+    unsigned max_age;
 };
 cudaError_t launch_transfer_seed(const SeedArgs &a, cudaStream_t stream);
+// Temporal fine correction (full_pyramid.wgsl:452-506): the finest seeds
+// become the fine history plus the change of the coarse field since the
+// frame that history was accepted in.
+cudaError_t launch_refine_temporal_seed(const SeedArgs &a, cudaStream_t stream);
 // Uniform translation seeds (shift * inv_scale; device shift[2]), activity = ROI selection.
 cudaError_t launch_uniform_seed(float *seed, uint32_t *active, const uint8_t *selected, int count, int model,
                                 const float *shift, float inv_scale, cudaStream_t stream);
@@ -221,10 +231,11 @@ struct TemporalArgs {
     float *prev_history;      // velocity: previous accepted history
     uint32_t *prev_ages;
     float *prediction;        // velocity: predicted field
-    unsigned *counters;       // [projected, accepted updates, predicted, expired]
+    unsigned *counters;       // [projected, accepted updates, predicted, expired], or nullptr
     int count, model;
     unsigned max_age;
     int use_filtered;
+    int report_expiry;        // count histories expiring this frame in counters[3]
 };
 cudaError_t launch_temporal_predict(const TemporalArgs &a, cudaStream_t stream);
 cudaError_t launch_temporal_save_previous(const TemporalArgs &a, cudaStream_t stream);

@@ -22,7 +22,7 @@ struct PyramidSlot {
     gbdic::HostBuffer shift_host;  // global translation seed (dx, dy), read at graph launch
     gbdic::DeviceBuffer shift_dev;
     cudaEvent_t begin = nullptr, end = nullptr;
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // whole pyramid, finest level alone
     bool pending = false;
     std::chrono::steady_clock::time_point submitted;
     double upload_ms = 0.0;
@@ -35,11 +35,16 @@ struct PyramidSlot {
         shift_dev.ensure(2 * sizeof(float));
         shift_host.as<float>()[0] = shift_host.as<float>()[1] = 0.0f;
     }
+    void drop_graphs() {
+        for (auto &g : graph) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    }
     void destroy() {
-        if (graph) cudaGraphExecDestroy(graph);
+        drop_graphs();
         if (begin) cudaEventDestroy(begin);
         if (end) cudaEventDestroy(end);
-        graph = nullptr;
         begin = end = nullptr;
     }
 };
@@ -57,6 +62,9 @@ struct gbdic_pyramid {
     gbdic::DeviceBuffer temporal_links;
     bool has_temporal_links = false;
     gbdic::DeviceBuffer history, ages, prev_history, prev_ages, prediction;
+    gbdic::DeviceBuffer coarse_history, coarse_ages;  // temporal fine correction
+    gbdic::DeviceBuffer fine_links;                   // adaptive: projection onto the finest grid
+    int active_levels = 0;                            // levels the next frames run
     std::vector<PyramidSlot> slots;
     bool ready = false;
     std::string error;
@@ -76,6 +84,7 @@ struct gbdic_pyramid {
     // temporal initialization with a search radius (subsets without history).
     bool search() const { return po.seed_search_radius > 0 && (po.initialization == 2 || po.initialization == 1); }
     bool velocity() const { return po.temporal_prediction == 1; }
+    bool fine_correction() const { return po.temporal_fine_correction != 0; }
     // Global translation seed of the coarsest level (Fourier initialization).
     bool global() const { return po.initialization == 3; }
     gbdic_solver_cfg cfg_of(int level) const {
@@ -121,13 +130,24 @@ void reset_temporal(gbdic_pyramid *p, cudaStream_t s) {
                    "history");
         check_cuda(cudaMemset(p->prev_ages.get(), 0xff, (size_t)count * sizeof(uint32_t)), "ages");
     }
+    if (p->fine_correction()) {
+        const int cc = p->levels.back()->count;
+        std::vector<float> coarse((size_t)cc * ss, 0.0f);
+        for (int i = 0; i < cc; ++i) coarse[(size_t)i * ss + gbdic::parameter_count(model)] = -1.0f;
+        check_cuda(cudaMemcpy(p->coarse_history.get(), coarse.data(), coarse.size() * sizeof(float),
+                              cudaMemcpyHostToDevice), "history");
+        check_cuda(cudaMemset(p->coarse_ages.get(), 0xff, (size_t)cc * sizeof(uint32_t)), "ages");
+    }
+    p->active_levels = p->L();
     (void)s;
 }
 
 // Everything a frame does after its finest target is resident at `frame0`.
+// `L` = levels this frame runs (the whole pyramid, or 1 under the adaptive
+// policy: full_pyramid_backend.py:1447-1481).
 void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_state, cudaStream_t s) {
     auto &rt = *p->rt;
-    const int L = p->L();
+    const int L = p->active_levels;
     const int model = p->po.base.motion_model;
     const bool median = p->po.base.outlier_policy == GBDIC_OUTLIER_MEDIAN;
     auto &ps = p->slots[k];
@@ -171,7 +191,10 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
         a.source = p->velocity() ? p->prediction.as<float>() : p->history.as<float>();
         a.seed = cslot.seed.as<float>();
         a.active = cslot.active.as<uint32_t>();
-        a.links = p->has_temporal_links ? p->temporal_links.as<uint32_t>() : nullptr;
+        if (c == 0 && p->po.adaptive)
+            a.links = p->fine_links.as<uint32_t>();  // finest grid alone: selected windows only
+        else
+            a.links = p->has_temporal_links && c == p->L() - 1 ? p->temporal_links.as<uint32_t>() : nullptr;
         a.src_grid_w = fine.gw; a.src_grid_h = fine.gh;
         a.dst_grid_w = coarse.gw; a.dst_count = coarse.count;
         a.src_scale = 1.0f; a.dst_scale = (float)(1 << c);
@@ -179,10 +202,11 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
         a.model = model;
         a.projected = ps.counters.as<unsigned>();
         a.mark_missing = p->search() ? 1 : 0;
+        a.track = p->fine_correction() ? 1 : 0;
         check_cuda(gbdic::launch_transfer_seed(a, s), "projection launch");
         seeded = true;
     }
-    if (p->search()) {
+    if (p->search() && c == p->L() - 1) {
         // ZNCC integer search at the coarsest level: every subset (zncc
         // initialization) or only those without a temporal seed.
         gbdic::SearchArgs q{};
@@ -217,7 +241,17 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
         a.src_scale = (float)(1 << (l + 1)); a.dst_scale = (float)(1 << l);
         a.subset_size = (float)p->po.base.subset_size; a.subset_stride = (float)p->po.base.subset_stride;
         a.model = model;
+        a.track = p->fine_correction() ? 1 : 0;
         check_cuda(gbdic::launch_transfer_seed(a, s), "transfer launch");
+        if (l == 0 && p->temporal() && p->fine_correction()) {
+            gbdic::SeedArgs r = a;
+            r.source = p->coarse_history.as<float>();
+            r.history = p->history.as<float>();
+            r.history_ages = p->ages.as<uint32_t>();
+            r.source_ages = p->coarse_ages.as<uint32_t>();
+            r.max_age = p->po.temporal_max_age;
+            check_cuda(gbdic::launch_refine_temporal_seed(r, s), "temporal correction launch");
+        }
         const uint8_t *f = l == 0 ? frame0 : nullptr;
         rt.enqueue_prefilter(lvl, slot, f, s);
         rt.enqueue_solve(lvl, slot, p->cfg_of(l), true, false, f, nullptr, s);
@@ -238,8 +272,31 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
         t.model = model;
         t.max_age = p->po.temporal_max_age;
         t.use_filtered = (p->po.base.outlier_policy == GBDIC_OUTLIER_REPLACE && !p->velocity()) ? 1 : 0;
+        t.report_expiry = p->po.adaptive ? 1 : 0;
         if (p->velocity()) check_cuda(gbdic::launch_temporal_save_previous(t, s), "history save launch");
         check_cuda(gbdic::launch_temporal_merge(t, s), "history merge launch");
+        if (p->fine_correction()) {
+            // The coarse accepted history (no counters).  A frame that ran the
+            // finest level alone left the coarse grid unsolved: its states
+            // read as cleared (status 0), which ages the coarse history.
+            auto &top = *p->levels[p->L() - 1];
+            auto &tslot = *top.slots[k];
+            gbdic::TemporalArgs u = t;
+            if (L < p->L()) {
+                check_cuda(cudaMemsetAsync(tslot.state.get(), 0, p->state_bytes(p->L() - 1), s), "coarse clear");
+                if (rt.output_state(tslot) != tslot.state.as<float>())
+                    check_cuda(cudaMemsetAsync(tslot.filtered.get(), 0, p->state_bytes(p->L() - 1), s),
+                               "coarse clear");
+            }
+            u.history = p->coarse_history.as<float>();
+            u.ages = p->coarse_ages.as<uint32_t>();
+            u.raw = tslot.state.as<float>();
+            u.output = rt.output_state(tslot);
+            u.counters = nullptr;
+            u.count = top.count;
+            u.report_expiry = 0;
+            check_cuda(gbdic::launch_temporal_merge(u, s), "coarse history merge launch");
+        }
     }
     if (out_state != nullptr)
         check_cuda(cudaMemcpyAsync(out_state, rt.output_state(fslot), p->state_bytes(0), cudaMemcpyDeviceToDevice, s),
@@ -263,7 +320,8 @@ void launch_slot(gbdic_pyramid *p, int k) {
         check_cuda(cudaMemcpyAsync(ps.counters_host.as<uint32_t>(), ps.counters.get(), 4 * sizeof(uint32_t),
                                    cudaMemcpyDeviceToHost, st), "counter readback");
     };
-    if (ps.graph == nullptr) {
+    cudaGraphExec_t &exec = ps.graph[p->active_levels == p->L() ? 0 : 1];
+    if (exec == nullptr) {
         cudaGraph_t graph = nullptr;
         check_cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "graph capture");
         try {
@@ -274,12 +332,12 @@ void launch_slot(gbdic_pyramid *p, int k) {
             throw;
         }
         check_cuda(cudaStreamEndCapture(s, &graph), "graph capture end");
-        cudaError_t err = cudaGraphInstantiate(&ps.graph, graph, 0);
+        cudaError_t err = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
         check_cuda(err, "graph instantiate");
     }
     check_cuda(cudaEventRecord(ps.begin, s), "event");
-    check_cuda(cudaGraphLaunch(ps.graph, s), "graph launch");
+    check_cuda(cudaGraphLaunch(exec, s), "graph launch");
     check_cuda(cudaEventRecord(ps.end, s), "event");
 }
 
@@ -312,6 +370,10 @@ int gbdic_pyramid_create(const gbdic_pyramid_options *options, gbdic_pyramid **o
             fail(GBDIC_EINVAL, "subset_size + 2 * seed_search_radius is too large for the seed search tile");
         if (po.temporal_prediction != 0 && po.initialization != 1)
             fail(GBDIC_EINVAL, "temporal_prediction requires temporal initialization");
+        if (po.temporal_fine_correction && (po.initialization != 1 || po.levels != 2))
+            fail(GBDIC_EINVAL, "temporal_fine_correction requires temporal initialization and two levels");
+        if (po.adaptive && (po.initialization != 1 || po.levels != 2))
+            fail(GBDIC_EINVAL, "adaptive pyramid requires temporal initialization and two levels");
         gbdic::validate_options(po.base);
         p->po = po;
         p->device = po.base.device;
@@ -351,8 +413,7 @@ int gbdic_pyramid_set_reference(gbdic_pyramid *p, const uint8_t *image, int32_t 
         }
         p->ready = false;
         for (auto &s : p->slots) {
-            if (s.graph) cudaGraphExecDestroy(s.graph);
-            s.graph = nullptr;
+            s.drop_graphs();
             s.pending = false;
         }
         p->levels.clear();
@@ -360,6 +421,9 @@ int gbdic_pyramid_set_reference(gbdic_pyramid *p, const uint8_t *image, int32_t 
         for (int l = 0; l < L; ++l) {
             p->levels.push_back(std::make_unique<gbdic::Level>());
             p->rt->configure_level(*p->levels[l], dims[l].first, dims[l].second, slots);
+            // A premature coarse stop would poison every finer seed: the
+            // divergence stop applies at the finest level only (1215-1223).
+            p->levels[l]->divergence = l == 0;
         }
         auto &rt = *p->rt;
         cudaStream_t s = rt.stream();
@@ -401,8 +465,23 @@ int gbdic_pyramid_set_reference(gbdic_pyramid *p, const uint8_t *image, int32_t 
                 p->prev_ages.ensure(ab);
                 p->prediction.ensure(sb);
             }
+            if (p->fine_correction()) {
+                p->coarse_history.ensure(p->state_bytes(L - 1));
+                p->coarse_ages.ensure((size_t)p->levels[L - 1]->count * sizeof(uint32_t));
+            }
+            if (p->po.adaptive) {
+                // full_pyramid_backend.py:628-634: 31 for selected windows, 0 outside the ROI.
+                const int n = p->levels[0]->count;
+                std::vector<uint32_t> links((size_t)n, 31u);
+                if (rois && rois[0].selected)
+                    for (int i = 0; i < n; ++i) links[i] = rois[0].selected[i] ? 31u : 0u;
+                p->fine_links.ensure((size_t)n * sizeof(uint32_t));
+                check_cuda(cudaMemcpy(p->fine_links.get(), links.data(), links.size() * sizeof(uint32_t),
+                                      cudaMemcpyHostToDevice), "links");
+            }
             reset_temporal(p, s);
         }
+        p->active_levels = L;
         check_cuda(cudaStreamSynchronize(s), "reference preparation");
         p->ready = true;
         if (info) {
@@ -548,10 +627,16 @@ int gbdic_pyramid_set_partial_support(gbdic_pyramid *p, int32_t level, int32_t c
             if (s.pending) fail(GBDIC_ESTATE, "retire every slot before changing the partial windows");
         p->rt->set_partial_support(*p->levels[level], count, indices, words, words_per_window, boxes, metadata_rows,
                                    inverse_rows);
-        for (auto &s : p->slots) {
-            if (s.graph) cudaGraphExecDestroy(s.graph);
-            s.graph = nullptr;
-        }
+        for (auto &s : p->slots) s.drop_graphs();
+    });
+}
+
+int gbdic_pyramid_set_active_levels(gbdic_pyramid *p, int32_t levels) {
+    return pguarded(p, [&] {
+        if (!p->ready) fail(GBDIC_ESTATE, "Call set_reference() before set_active_levels().");
+        if (levels != p->L() && !(levels == 1 && p->po.adaptive))
+            fail(GBDIC_EINVAL, "levels must be the pyramid's level count, or 1 under the adaptive policy");
+        p->active_levels = levels;
     });
 }
 
@@ -561,10 +646,7 @@ int gbdic_pyramid_set_solver_variant(gbdic_pyramid *p, int32_t threads_per_subse
             if (s.pending) fail(GBDIC_ESTATE, "retire every slot before switching the solver variant");
         check_cuda(cudaStreamSynchronize(p->rt->stream()), "pending work");
         p->rt->set_variant(threads_per_subset, persistent != 0);
-        for (auto &s : p->slots) {
-            if (s.graph) cudaGraphExecDestroy(s.graph);
-            s.graph = nullptr;
-        }
+        for (auto &s : p->slots) s.drop_graphs();
     });
 }
 

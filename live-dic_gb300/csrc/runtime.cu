@@ -382,7 +382,7 @@ SolveArgs Runtime::solve_args(Level &level, LevelSlot &slot, const gbdic_solver_
     a.roi_enabled = level.roi ? 1 : 0;
     a.preserve_disabled = preserve ? 1 : 0;
     a.use_mean = opt_.o.subset_stride != opt_.o.subset_size;
-    a.div_patience = opt_.o.divergence_patience;
+    a.div_patience = level.divergence ? opt_.o.divergence_patience : 0;
     a.div_min = opt_.o.divergence_min_iterations;
     a.persistent = opt_.o.persistent;
     return a;

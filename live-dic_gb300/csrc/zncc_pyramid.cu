@@ -131,52 +131,63 @@ __device__ void accumulate_seed(const SeedArgs &a, int sidx, float weight, float
     wsum = wsum + weight;
 }
 
-// full_pyramid.wgsl:310-435
+// full_pyramid.wgsl:310-395: bilinear blend of the permitted source corners
+// at the destination centre (normalised); returns the weight sum.  `lx`,
+// `ly` receive the lower source corner.
+__device__ float interpolate_seed(const SeedArgs &a, int i, unsigned perm, float (&acc)[12], int &lx, int &ly) {
+    for (int k = 0; k < 12; ++k) acc[k] = 0.0f;
+    float wsum = 0.0f;
+    const int dxg = i % a.dst_grid_w, dyg = i / a.dst_grid_w;
+    const float soff = (1.0f - a.src_scale) * 0.5f, doff = (1.0f - a.dst_scale) * 0.5f;
+    const float dcx = fmaf(a.subset_stride, (float)dxg, 0.5f * a.subset_size);
+    const float dcy = fmaf(a.subset_stride, (float)dyg, 0.5f * a.subset_size);
+    const float scx = fmaf(a.dst_scale, dcx, doff - soff) / a.src_scale;
+    const float scy = fmaf(a.dst_scale, dcy, doff - soff) / a.src_scale;
+    const float gxf = (scx - 0.5f * a.subset_size) / a.subset_stride;
+    const float gyf = (scy - 0.5f * a.subset_size) / a.subset_stride;
+    const int maxx = a.src_grid_w - 2 > 0 ? a.src_grid_w - 2 : 0;
+    const int maxy = a.src_grid_h - 2 > 0 ? a.src_grid_h - 2 : 0;
+    lx = clampi((int)floorf(gxf), 0, maxx);
+    ly = clampi((int)floorf(gyf), 0, maxy);
+    const float fx = fminf(fmaxf(gxf - (float)lx, 0.0f), 1.0f);
+    const float fy = fminf(fmaxf(gyf - (float)ly, 0.0f), 1.0f);
+    const float tscale = a.src_scale / a.dst_scale;
+    for (int corner = 0; corner < 4; ++corner) {
+        if ((perm & (1u << corner)) == 0u) continue;
+        const int ox = corner & 1, oy = corner >> 1;
+        const int sx = lx + ox, sy = ly + oy;
+        if (sx >= a.src_grid_w || sy >= a.src_grid_h) continue;
+        const float wx = ox ? fx : 1.0f - fx, wy = oy ? fy : 1.0f - fy;
+        const float spx = fmaf(a.subset_stride, (float)sx, 0.5f * a.subset_size);
+        const float spy = fmaf(a.subset_stride, (float)sy, 0.5f * a.subset_size);
+        accumulate_seed(a, sy * a.src_grid_w + sx, wx * wy, spx, spy, scx, scy, tscale, acc, wsum);
+    }
+    const unsigned fallback = perm >> 5;
+    if (wsum == 0.0f && fallback != 0u) {
+        const int sidx = (int)fallback - 1;
+        const float st = a.source[(size_t)sidx * state_stride(a.model) + status_slot(a.model)];
+        if (st >= 0.5f) {
+            const int sx = sidx % a.src_grid_w, sy = sidx / a.src_grid_w;
+            const float spx = fmaf(a.subset_stride, (float)sx, 0.5f * a.subset_size);
+            const float spy = fmaf(a.subset_stride, (float)sy, 0.5f * a.subset_size);
+            accumulate_seed(a, sidx, 1.0f, spx, spy, scx, scy, tscale, acc, wsum);
+        }
+    }
+    if (wsum > 0.0f)
+        for (int k = 0; k < 12; ++k) acc[k] = acc[k] / wsum;
+    return wsum;
+}
+
+// full_pyramid.wgsl:397-450 (transfer_seed, transfer_seed_roi and, with a
+// projection counter, project_temporal_seed).
 __global__ void transfer_seed_kernel(SeedArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool projected = false;
     if (i < a.dst_count) {
         const unsigned perm = a.links ? a.links[i] : 31u;
         float acc[12];
-        for (int k = 0; k < 12; ++k) acc[k] = 0.0f;
-        float wsum = 0.0f;
-        const int dxg = i % a.dst_grid_w, dyg = i / a.dst_grid_w;
-        const float soff = (1.0f - a.src_scale) * 0.5f, doff = (1.0f - a.dst_scale) * 0.5f;
-        const float dcx = fmaf(a.subset_stride, (float)dxg, 0.5f * a.subset_size);
-        const float dcy = fmaf(a.subset_stride, (float)dyg, 0.5f * a.subset_size);
-        const float scx = fmaf(a.dst_scale, dcx, doff - soff) / a.src_scale;
-        const float scy = fmaf(a.dst_scale, dcy, doff - soff) / a.src_scale;
-        const float gxf = (scx - 0.5f * a.subset_size) / a.subset_stride;
-        const float gyf = (scy - 0.5f * a.subset_size) / a.subset_stride;
-        const int maxx = a.src_grid_w - 2 > 0 ? a.src_grid_w - 2 : 0;
-        const int maxy = a.src_grid_h - 2 > 0 ? a.src_grid_h - 2 : 0;
-        const int lx = clampi((int)floorf(gxf), 0, maxx), ly = clampi((int)floorf(gyf), 0, maxy);
-        const float fx = fminf(fmaxf(gxf - (float)lx, 0.0f), 1.0f);
-        const float fy = fminf(fmaxf(gyf - (float)ly, 0.0f), 1.0f);
-        const float tscale = a.src_scale / a.dst_scale;
-        for (int corner = 0; corner < 4; ++corner) {
-            if ((perm & (1u << corner)) == 0u) continue;
-            const int ox = corner & 1, oy = corner >> 1;
-            const int sx = lx + ox, sy = ly + oy;
-            if (sx >= a.src_grid_w || sy >= a.src_grid_h) continue;
-            const float wx = ox ? fx : 1.0f - fx, wy = oy ? fy : 1.0f - fy;
-            const float spx = fmaf(a.subset_stride, (float)sx, 0.5f * a.subset_size);
-            const float spy = fmaf(a.subset_stride, (float)sy, 0.5f * a.subset_size);
-            accumulate_seed(a, sy * a.src_grid_w + sx, wx * wy, spx, spy, scx, scy, tscale, acc, wsum);
-        }
-        const unsigned fallback = perm >> 5;
-        if (wsum == 0.0f && fallback != 0u) {
-            const int sidx = (int)fallback - 1;
-            const float st = a.source[(size_t)sidx * state_stride(a.model) + status_slot(a.model)];
-            if (st >= 0.5f) {
-                const int sx = sidx % a.src_grid_w, sy = sidx / a.src_grid_w;
-                const float spx = fmaf(a.subset_stride, (float)sx, 0.5f * a.subset_size);
-                const float spy = fmaf(a.subset_stride, (float)sy, 0.5f * a.subset_size);
-                accumulate_seed(a, sidx, 1.0f, spx, spy, scx, scy, tscale, acc, wsum);
-            }
-        }
-        if (wsum > 0.0f)
-            for (int k = 0; k < 12; ++k) acc[k] = acc[k] / wsum;
+        int lx, ly;
+        const float wsum = interpolate_seed(a, i, perm, acc, lx, ly);
         float4 *d = reinterpret_cast<float4 *>(a.seed + (size_t)i * state_stride(a.model));
         d[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
         if (a.model == kModelQuadratic) {
@@ -186,14 +197,49 @@ __global__ void transfer_seed_kernel(SeedArgs a) {
         } else {
             d[1] = make_float4(acc[4], acc[5], 0.0f, 0.0f);
         }
-        if (a.mark_missing && wsum == 0.0f) a.seed[(size_t)i * state_stride(a.model) + status_slot(a.model)] = -1.0f;
-        a.active[i] = (perm >> 4) & 1u;
         projected = wsum > 0.0f && (perm & 16u) != 0u;
+        float *status = a.seed + (size_t)i * state_stride(a.model) + status_slot(a.model);
+        if (a.track) *status = wsum >= 0.99999f ? 0.0f : -1.0f;
+        if (a.mark_missing && wsum == 0.0f) *status = -1.0f;
+        if (a.track && a.projected && !projected) *status = -1.0f;
+        a.active[i] = (perm >> 4) & 1u;
     }
     if (a.projected) {
         const int count = __syncthreads_count(projected);
         if (threadIdx.x == 0 && count > 0) atomicAdd(a.projected, (unsigned)count);
     }
+}
+
+// full_pyramid.wgsl:452-506.  Runs after the ordinary coarse-to-fine
+// transfer into `seed` (with availability markers); `source` is the coarse
+// accepted history, `history` the fine one.
+__global__ void refine_temporal_seed_kernel(SeedArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.dst_count) return;
+    if (a.active[i] == 0u) return;
+    const unsigned age = a.history_ages[i];
+    if (age == 0xffffffffu || age > a.max_age) return;
+    const int ss = state_stride(a.model);
+    float *seed = a.seed + (size_t)i * ss;
+    if (seed[status_slot(a.model)] < -0.5f) return;
+    const unsigned perm = a.links ? a.links[i] : 31u;
+    float predicted[12];
+    int lx, ly;
+    // The lower corner is the one interpolate_seed uses; every permitted
+    // corner's coarse history must date from the fine history's frame.
+    const float wsum = interpolate_seed(a, i, perm, predicted, lx, ly);
+    for (int corner = 0; corner < 4; ++corner) {
+        if ((perm & (1u << corner)) == 0u) continue;
+        const int sx = lx + (corner & 1), sy = ly + (corner >> 1);
+        if (sx >= a.src_grid_w || sy >= a.src_grid_h) continue;
+        if (a.source_ages[sy * a.src_grid_w + sx] != age) return;
+    }
+    if (wsum < 0.99999f) return;
+    const float *h = a.history + (size_t)i * ss;
+    // a = (tu, ux, uy, tv), b.xy = (vx, vy); quadratic: b.zw and c are the
+    // curvature terms.  Markers and iteration slots keep the transfer's.
+    const int n = a.model == kModelQuadratic ? 12 : 6;
+    for (int k = 0; k < n; ++k) seed[k] = h[k] + (seed[k] - predicted[k]);
 }
 
 // ------------------------------------------------------------ temporal
@@ -257,9 +303,9 @@ __global__ void temporal_merge_kernel(TemporalArgs a) {
     }
     const int na = __syncthreads_count(accepted);
     const int ne = __syncthreads_count(expired);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && a.counters) {
         if (na > 0) atomicAdd(a.counters + 1, (unsigned)na);
-        if (ne > 0) atomicAdd(a.counters + 3, (unsigned)ne);
+        if (ne > 0 && a.report_expiry) atomicAdd(a.counters + 3, (unsigned)ne);
     }
 }
 
@@ -286,6 +332,12 @@ cudaError_t launch_reduce_half(const uint8_t *src, int W, int H, uint8_t *dst, c
 cudaError_t launch_transfer_seed(const SeedArgs &a, cudaStream_t stream) {
     if (a.dst_count <= 0) return cudaSuccess;
     transfer_seed_kernel<<<(a.dst_count + 255) / 256, 256, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine_temporal_seed(const SeedArgs &a, cudaStream_t stream) {
+    if (a.dst_count <= 0) return cudaSuccess;
+    refine_temporal_seed_kernel<<<(a.dst_count + 255) / 256, 256, 0, stream>>>(a);
     return cudaGetLastError();
 }
 

@@ -99,6 +99,8 @@ class PyramidOptions(C.Structure):
         ("temporal_max_age", C.c_uint32),
         ("temporal_prediction", C.c_int32),
         ("seed_search_radius", C.c_int32),
+        ("temporal_fine_correction", C.c_int32),
+        ("adaptive", C.c_int32),
     ]
 
 
@@ -212,6 +214,7 @@ _SIGNATURES = {
     "gbdic_pyramid_set_translation": (C.c_int, [P, I32, C.c_float, C.c_float]),
     "gbdic_set_partial_support": (C.c_int, [P, I32, P, P, I32, P, P, P]),
     "gbdic_pyramid_set_partial_support": (C.c_int, [P, I32, I32, P, P, I32, P, P, P]),
+    "gbdic_pyramid_set_active_levels": (C.c_int, [P, I32]),
     "gbdic_fourier_create": (C.c_int, [I32, P, P, I32, C.POINTER(P)]),
     "gbdic_fourier_destroy": (C.c_int, [P]),
     "gbdic_fourier_last_error": (C.c_char_p, [P]),

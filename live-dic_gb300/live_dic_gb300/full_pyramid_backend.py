@@ -210,10 +210,6 @@ class ICGNWGPUFullPyramid:
         # Options that the GPU engine does not provide fail loudly after validation.
         if initialization == "wgpu-matching":
             raise ICGNError("initialization='wgpu-matching' is not available in this build")
-        if temporal_fine_correction:
-            raise ICGNError("temporal_fine_correction is not available in this build")
-        if pyramid_policy == "adaptive":
-            raise ICGNError("pyramid_policy='adaptive' is not available in this build")
         if self.device_type == "cpu":
             raise ICGNError("This engine executes on a CUDA GPU only; device_type='cpu' is not available.")
         self.initialization = initialization
@@ -222,6 +218,8 @@ class ICGNWGPUFullPyramid:
         self.temporal_prediction = temporal_prediction
         self.pyramid_policy = pyramid_policy
         self.adaptive_acceptance = float(adaptive_acceptance)
+        self._adaptive_next_levels = self.pyramid_levels
+        self._adaptive_population = 0
         self.power_preference = power_preference
         self._pipeline_slots = slots
         self._persistent = bool(persistent)
@@ -268,6 +266,8 @@ class ICGNWGPUFullPyramid:
         po.seed_search_radius = self.seed_search_radius or 0
         po.temporal_max_age = 0xFFFFFFFE if self.temporal_max_age is None else int(self.temporal_max_age)
         po.temporal_prediction = 1 if self.temporal_prediction == "velocity" else 0
+        po.temporal_fine_correction = int(self.temporal_fine_correction)
+        po.adaptive = int(self.pyramid_policy == "adaptive")
         handle = C.c_void_p()
         _native.check(self._lib.gbdic_pyramid_create(C.byref(po), C.byref(handle)), self._lib.gbdic_pyramid_last_error(None))
         return handle
@@ -368,6 +368,8 @@ class ICGNWGPUFullPyramid:
         self._check(self._lib.gbdic_pyramid_export(self._handle, 0, _native.EXPORT_ADMISSIBLE,
                                                    _native.ptr(admissible), admissible.nbytes))
         self.reference_valid = immutable(admissible.reshape(self.grid_height, self.grid_width).astype(bool))
+        self._adaptive_population = int(np.count_nonzero(self.reference_valid))
+        self._adaptive_next_levels = self.pyramid_levels
         self._roi_level_counts = [
             int(p.selected.sum()) if p is not None else d[2] * d[3] for p, d in zip(plans, dims, strict=True)
         ]
@@ -434,6 +436,12 @@ class ICGNWGPUFullPyramid:
             "solverWorkgroupSize": self.solver_workgroup_size,
             "gaussianSigma": self.gaussian_sigma,
         }
+        if self.pyramid_policy == "adaptive":
+            echo.update(pyramidPolicy="adaptive", adaptiveAcceptance=self.adaptive_acceptance,
+                        adaptiveFeedback="ordered-single-slot")
+        if self.divergence_patience is not None:
+            echo.update(divergencePatience=self.divergence_patience,
+                        divergenceMinIterations=self.divergence_min_iterations, divergenceLevels="finest")
         if self.initialization == "temporal":
             echo.update(
                 initialization="temporal",
@@ -441,6 +449,8 @@ class ICGNWGPUFullPyramid:
                 temporalSeedLevel="coarsest",
                 temporalSeedState="filtered" if self.outlier_policy == "replace" and self.temporal_prediction == "none" else "raw",
             )
+            if self.temporal_fine_correction:
+                echo["temporalFineCorrection"] = True
             if self.temporal_prediction == "velocity":
                 echo["temporalPrediction"] = "velocity"
         if self.initialization == "fourier":
@@ -463,8 +473,25 @@ class ICGNWGPUFullPyramid:
             )
         return frame
 
+    def _begin_frame(self) -> int:
+        """Levels the next frame runs (the adaptive policy's last decision)."""
+        levels = self._adaptive_next_levels if self.pyramid_policy == "adaptive" else self.pyramid_levels
+        if self.pyramid_policy == "adaptive":
+            self._check(self._lib.gbdic_pyramid_set_active_levels(self._handle, levels))
+        return levels
+
+    def _adaptive_feedback(self, counters: np.ndarray) -> None:
+        """full_pyramid_backend.py:1781-1790: the finest level alone while the
+        accepted history covers `adaptive_acceptance` of the reference-valid
+        windows and nothing expired; the whole pyramid otherwise."""
+        accepted, expired = float(counters[1]), float(counters[3])
+        self._adaptive_next_levels = (
+            1 if self._adaptive_population > 0 and accepted / self._adaptive_population >= self.adaptive_acceptance
+            and not expired else 2
+        )
+
     def _result(self, packed: np.ndarray, counters: np.ndarray, timing: _native.Timing, accepted_at: float,
-                prep_ms: float) -> RegistrationResult:
+                prep_ms: float, levels_used: int | None = None) -> RegistrationResult:
         times = {
             "inputPreparationWallMs": prep_ms,
             "uploadWallMs": timing.upload_ms,
@@ -472,7 +499,7 @@ class ICGNWGPUFullPyramid:
             "readbackCopyWallMs": timing.readback_ms,
             "executeReadbackWallMs": timing.execute_ms + timing.readback_ms,
             "deviceMs": timing.device_ms,
-            "pyramidLevels": float(self.pyramid_levels),
+            "pyramidLevels": float(levels_used or self.pyramid_levels),
             "queueSubmissions": 1.0,
         }
         if self.initialization == "temporal":
@@ -480,6 +507,8 @@ class ICGNWGPUFullPyramid:
             times["temporalAcceptedUpdates"] = float(counters[1])
             if self.temporal_prediction == "velocity":
                 times["velocityPredictedSubsets"] = float(counters[2])
+            if self.pyramid_policy == "adaptive":
+                times["temporalExpiredSubsets"] = float(counters[3])
         build = time.perf_counter()
         result = result_from_packed(
             packed,
@@ -493,6 +522,9 @@ class ICGNWGPUFullPyramid:
             roi=self.roi,
             reference_valid=self.reference_valid,
         )
+        if self.pyramid_policy == "adaptive":
+            self._adaptive_feedback(counters)
+            result.config["pyramidLevelsUsed"] = levels_used
         now = time.perf_counter()
         total = (now - accepted_at) * 1e3
         result.timing = {**result.timing, "resultBuildWallMs": (now - build) * 1e3, "pipelineLatencyWallMs": total,
@@ -551,10 +583,12 @@ class ICGNWGPUFullPyramid:
             packed = np.empty((self.grid_height, self.grid_width, state_float_count(self.motion_model)), np.float32)
             counters = np.zeros(4, np.uint32)
             timing = _native.Timing()
+            levels = self._begin_frame()
             self._check(self._lib.gbdic_pyramid_register(
                 self._handle, _native.ptr(frame), frame.strides[0], _native.ptr(packed), _native.ptr(counters),
                 C.byref(timing)))
-            return self._attach_translation(self._result(packed, counters, timing, accepted_at, prep_ms), estimate)
+            return self._attach_translation(self._result(packed, counters, timing, accepted_at, prep_ms, levels),
+                                            estimate)
         finally:
             self._registration_lock.release()
 
@@ -569,6 +603,9 @@ class ICGNWGPUFullPyramid:
             raise ValueError("pipeline_depth must be a positive integer") from error
         if isinstance(pipeline_depth, bool) or depth < 1:
             raise ValueError("pipeline_depth must be a positive integer")
+        if self.pyramid_policy == "adaptive":
+            # The level decision needs the preceding frame's result (1857-1860).
+            depth = 1
         if depth > self._pipeline_slots:
             raise ValueError(f"pipeline_depth must be at most {self._pipeline_slots} for this engine")
         return self._stream(targets, depth)
@@ -577,7 +614,7 @@ class ICGNWGPUFullPyramid:
         if not self._registration_lock.acquire(blocking=False):
             raise ICGNError("Another registration or registration stream is active.")
         available = deque(range(depth))
-        pending: deque[tuple[int, float, float, dict | None]] = deque()
+        pending: deque[tuple[int, float, float, dict | None, int]] = deque()
         try:
             if self.roi is not None and self.roi.empty:
                 for target in targets:
@@ -587,14 +624,15 @@ class ICGNWGPUFullPyramid:
                 return
 
             def retire() -> RegistrationResult:
-                slot, accepted_at, prep_ms, estimate = pending.popleft()
+                slot, accepted_at, prep_ms, estimate, levels = pending.popleft()
                 packed = np.empty((self.grid_height, self.grid_width, state_float_count(self.motion_model)), np.float32)
                 counters = np.zeros(4, np.uint32)
                 timing = _native.Timing()
                 self._check(self._lib.gbdic_pyramid_retire(self._handle, slot, _native.ptr(packed),
                                                            _native.ptr(counters), C.byref(timing)))
                 available.append(slot)
-                return self._attach_translation(self._result(packed, counters, timing, accepted_at, prep_ms), estimate)
+                return self._attach_translation(
+                    self._result(packed, counters, timing, accepted_at, prep_ms, levels), estimate)
 
             for target in targets:
                 if not available:
@@ -608,13 +646,14 @@ class ICGNWGPUFullPyramid:
                     available.appendleft(slot)
                     raise
                 prep_ms = (time.perf_counter() - accepted_at) * 1e3
+                levels = self._begin_frame()
                 self._check(self._lib.gbdic_pyramid_submit(self._handle, slot, _native.ptr(frame), frame.strides[0]))
-                pending.append((slot, accepted_at, prep_ms, estimate))
+                pending.append((slot, accepted_at, prep_ms, estimate, levels))
             while pending:
                 yield retire()
         finally:
             while pending:
-                slot, _, _, _ = pending.popleft()
+                slot = pending.popleft()[0]
                 self._lib.gbdic_pyramid_retire(self._handle, slot, None, None, None)
             self._registration_lock.release()
 
@@ -623,6 +662,7 @@ class ICGNWGPUFullPyramid:
         if not self._reference_ready:
             raise ICGNError("Call set_reference() before register().")
         self._global_translation(0, device_frame=device_frame, row_stride=self.width)
+        self._begin_frame()
         self._check(self._lib.gbdic_pyramid_register_device(
             self._handle, C.c_void_p(device_frame), C.c_void_p(device_state), C.c_void_p(stream or 0)))
 
@@ -662,7 +702,9 @@ class ICGNWGPUFullPyramid:
                 "iterations": iters.value}
 
     def reset_temporal_state(self) -> None:
-        """Forget the temporal history (676-694); no-op before set_reference."""
+        """Forget the temporal history (676-694); no-op before set_reference.
+        The adaptive policy starts again from the whole pyramid."""
+        self._adaptive_next_levels = self.pyramid_levels
         if self._handle is not None:
             self._check(self._lib.gbdic_pyramid_reset_temporal(self._handle))
 

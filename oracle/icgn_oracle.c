@@ -867,9 +867,10 @@ static float interpolate_seed(const oracle_seed_cfg *c, const float *src, int di
     return wsum;
 }
 
-/* full_pyramid.wgsl:397-433.  perms == NULL: every destination uses 31. */
+/* full_pyramid.wgsl:397-433.  perms == NULL: every destination uses 31.
+ * weights (or NULL) receives each destination's weight sum. */
 void oracle_transfer_seed(const oracle_seed_cfg *c, const float *src, const uint32_t *perms,
-                          float *dst_seed, uint32_t *dst_active) {
+                          float *dst_seed, uint32_t *dst_active, float *weights) {
     const int count = c->dst_grid_w * c->dst_grid_h;
     const int ss = state_stride(c->model);
     #pragma omp parallel for schedule(static)
@@ -887,6 +888,50 @@ void oracle_transfer_seed(const oracle_seed_cfg *c, const float *src, const uint
             d[c->model == MODEL_QUADRATIC ? 12 : 6] = marker;
         }
         dst_active[i] = (perm >> 4) & 1u;
+        if (weights) weights[i] = wsum;
+    }
+}
+
+/* full_pyramid.wgsl:452-506 (refine_temporal_seed).  src = coarse accepted
+ * history, src_ages its ages; history / ages = the fine accepted history;
+ * dst_seed holds the ordinary transfer (with availability markers). */
+void oracle_refine_temporal_seed(const oracle_seed_cfg *c, const float *src, const uint32_t *src_ages,
+                                 const uint32_t *perms, const float *history, const uint32_t *ages,
+                                 unsigned max_age, float *dst_seed, const uint32_t *dst_active) {
+    const int count = c->dst_grid_w * c->dst_grid_h;
+    const int ss = state_stride(c->model);
+    const int status_at = c->model == MODEL_QUADRATIC ? 12 : 6;
+    for (int i = 0; i < count; ++i) {
+        if (dst_active[i] == 0u) continue;
+        unsigned age = ages[i];
+        if (age == 0xffffffffu || age > max_age) continue;
+        float *d = dst_seed + (size_t)i * ss;
+        if (d[status_at] < -0.5f) continue;
+        unsigned perm = perms ? perms[i] : 31u;
+        /* lower corner of the bilinear stencil, as in interpolate_seed */
+        int dxg = i % c->dst_grid_w, dyg = i / c->dst_grid_w;
+        float soff = (1.0f - c->src_scale) * 0.5f, doff = (1.0f - c->dst_scale) * 0.5f;
+        float scx = fmaf(c->dst_scale, fmaf(c->subset_stride, (float)dxg, 0.5f * c->subset_size), doff - soff) / c->src_scale;
+        float scy = fmaf(c->dst_scale, fmaf(c->subset_stride, (float)dyg, 0.5f * c->subset_size), doff - soff) / c->src_scale;
+        int maxx = c->src_grid_w - 2 > 0 ? c->src_grid_w - 2 : 0;
+        int maxy = c->src_grid_h - 2 > 0 ? c->src_grid_h - 2 : 0;
+        int lx = clampi((int)floorf((scx - 0.5f * c->subset_size) / c->subset_stride), 0, maxx);
+        int ly = clampi((int)floorf((scy - 0.5f * c->subset_size) / c->subset_stride), 0, maxy);
+        int same = 1;
+        for (int corner = 0; corner < 4 && same; ++corner) {
+            if ((perm & (1u << corner)) == 0u) continue;
+            int sx = lx + (corner & 1), sy = ly + (corner >> 1);
+            if (sx >= c->src_grid_w || sy >= c->src_grid_h) continue;
+            if (src_ages[sy * c->src_grid_w + sx] != age) same = 0;
+        }
+        if (!same) continue;
+        float a[4], b[4], cc[4];
+        float wsum = interpolate_seed(c, src, i, perm, a, b, cc);
+        if (wsum < 0.99999f) continue;
+        const float *h = history + (size_t)i * ss;
+        float predicted[12] = {a[0], a[1], a[2], a[3], b[0], b[1], b[2], b[3], cc[0], cc[1], cc[2], cc[3]};
+        int n = c->model == MODEL_QUADRATIC ? 12 : 6;
+        for (int k = 0; k < n; ++k) d[k] = h[k] + (d[k] - predicted[k]);
     }
 }
 

@@ -220,7 +220,10 @@ def transfer_seed(
     model: str = "affine",
     permissions: np.ndarray | None = None,
     track_availability: bool = False,
-) -> tuple[np.ndarray, np.ndarray]:
+    return_weights: bool = False,
+):
+    """Seeds and activity of the destination grid (and, with
+    `return_weights`, each destination's interpolation weight sum)."""
     cfg = SeedCfg()
     cfg.src_grid_w, cfg.src_grid_h = source_grid
     cfg.dst_grid_w, cfg.dst_grid_h = destination_grid
@@ -233,8 +236,64 @@ def transfer_seed(
     active = np.zeros(count, np.uint32)
     src = np.ascontiguousarray(source_state, dtype=np.float32)
     perm = None if permissions is None else np.ascontiguousarray(permissions, dtype=np.uint32).ravel()
-    lib().oracle_transfer_seed(C.byref(cfg), _p(src), _p(perm, C.c_uint32), _p(seeds), _p(active, C.c_uint32))
-    return seeds, active
+    weights = np.zeros(count, np.float32)
+    lib().oracle_transfer_seed(C.byref(cfg), _p(src), _p(perm, C.c_uint32), _p(seeds), _p(active, C.c_uint32),
+                               _p(weights))
+    return (seeds, active, weights) if return_weights else (seeds, active)
+
+
+def _seed_cfg(source_grid, destination_grid, source_scale, destination_scale, subset_size, subset_stride, model,
+              track_availability=False) -> SeedCfg:
+    cfg = SeedCfg()
+    cfg.src_grid_w, cfg.src_grid_h = source_grid
+    cfg.dst_grid_w, cfg.dst_grid_h = destination_grid
+    cfg.src_scale, cfg.dst_scale = source_scale, destination_scale
+    cfg.subset_size, cfg.subset_stride = subset_size, subset_stride
+    cfg.model, cfg.track_availability = MODELS[model], int(track_availability)
+    return cfg
+
+
+def refine_temporal_seed(seeds: np.ndarray, active: np.ndarray, coarse_history: np.ndarray, coarse_ages: np.ndarray,
+                         history: np.ndarray, ages: np.ndarray, *, source_grid, destination_grid, source_scale: float,
+                         subset_size: int, subset_stride: int, model: str = "affine", max_age: int = 0xFFFFFFFE,
+                         permissions: np.ndarray | None = None) -> np.ndarray:
+    """full_pyramid.wgsl refine_temporal_seed on a copy of `seeds`."""
+    cfg = _seed_cfg(source_grid, destination_grid, source_scale, 1.0, subset_size, subset_stride, model, True)
+    out = np.ascontiguousarray(seeds, dtype=np.float32).copy()
+    perm = None if permissions is None else np.ascontiguousarray(permissions, dtype=np.uint32).ravel()
+    lib().oracle_refine_temporal_seed(
+        C.byref(cfg), _p(np.ascontiguousarray(coarse_history, np.float32)),
+        _p(np.ascontiguousarray(coarse_ages, np.uint32), C.c_uint32), _p(perm, C.c_uint32),
+        _p(np.ascontiguousarray(history, np.float32)), _p(np.ascontiguousarray(ages, np.uint32), C.c_uint32),
+        C.c_uint32(max_age), _p(out), _p(np.ascontiguousarray(active, np.uint32), C.c_uint32))
+    return out
+
+
+def temporal_merge(history: np.ndarray, ages: np.ndarray, raw: np.ndarray, output: np.ndarray, *, model: str,
+                   max_age: int, use_filtered: bool) -> tuple[int, int]:
+    """In place on `history` / `ages`; returns (accepted updates, expired)."""
+    acc, exp = C.c_uint32(), C.c_uint32()
+    lib().oracle_temporal_merge(int(ages.size), MODELS[model], C.c_uint32(max_age), int(use_filtered), _p(history),
+                                _p(ages, C.c_uint32), _p(np.ascontiguousarray(raw, np.float32)),
+                                _p(np.ascontiguousarray(output, np.float32)), C.byref(acc), C.byref(exp))
+    return acc.value, exp.value
+
+
+def temporal_predict(history: np.ndarray, previous: np.ndarray, ages: np.ndarray, previous_ages: np.ndarray, *,
+                     model: str) -> tuple[np.ndarray, int]:
+    out = np.empty_like(history)
+    lib().oracle_temporal_predict.restype = C.c_uint32
+    n = lib().oracle_temporal_predict(int(ages.size), MODELS[model], _p(history), _p(previous), _p(ages, C.c_uint32),
+                                      _p(previous_ages, C.c_uint32), _p(out))
+    return out, int(n)
+
+
+def temporal_save_previous(history: np.ndarray, ages: np.ndarray, raw: np.ndarray, output: np.ndarray,
+                           previous: np.ndarray, previous_ages: np.ndarray, *, model: str) -> None:
+    lib().oracle_temporal_save_previous(int(ages.size), MODELS[model], _p(history), _p(ages, C.c_uint32),
+                                        _p(np.ascontiguousarray(raw, np.float32)),
+                                        _p(np.ascontiguousarray(output, np.float32)), _p(previous),
+                                        _p(previous_ages, C.c_uint32))
 
 
 def seed_search(reference: np.ndarray, target: np.ndarray, *, subset_size: int, subset_stride: int, radius: int,

@@ -1,0 +1,142 @@
+"""CPU oracle of one full-pyramid frame (TEST INFRASTRUCTURE ONLY).
+
+Composes the C oracle's restatements in the order of the reference's
+ICGNWGPUFullPyramid._encode_slot (full_pyramid_backend.py:1436-1569):
+integer reductions, temporal velocity prediction and projection onto the
+coarsest active grid (full_pyramid.wgsl:83-122,437-450), the coarsest seeded
+solve and UOD, coarse-to-fine transfer (251-435) with the temporal fine
+correction on the finest grid (452-506), finer solves and UOD, then the
+history updates (126-148, 508-554) including the coarse history of the fine
+correction.  The per-level reference arrays are taken as given (the GPU
+engine's exported plane / metadata / inverse), so a comparison covers the
+per-frame path bit for bit.  Counters: [projected, accepted updates,
+velocity-predicted, expired (adaptive policy only)].
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import oracle as oc
+from . import reference_prep as rp
+
+
+@dataclass
+class LevelArrays:
+    width: int
+    height: int
+    grid_w: int
+    grid_h: int
+    plane: np.ndarray
+    metadata: np.ndarray
+    inverse: np.ndarray
+
+
+class PyramidOracle:
+    def __init__(self, levels: list[LevelArrays], *, subset_size: int, subset_stride: int,
+                 iterations: tuple[int, ...], tolerances: tuple[float, ...], zncc_min: float = 0.8,
+                 model: str = "affine", interpolation: str = "bspline", lanes: int = 32,
+                 outlier_policy: str = "replace", median_size: int = 3, temporal: bool = False,
+                 velocity: bool = False, fine_correction: bool = False, adaptive: bool = False,
+                 max_age: int = 0xFFFFFFFE, divergence_patience: int = 0, divergence_min_iterations: int = 4):
+        self.levels = levels
+        self.L = len(levels)
+        self.S, self.s = subset_size, subset_stride
+        self.iterations, self.tolerances, self.zncc_min = iterations, tolerances, zncc_min
+        self.model, self.interp, self.lanes = model, interpolation, lanes
+        self.policy, self.median_size = outlier_policy, median_size
+        self.temporal, self.velocity = temporal, velocity
+        self.fine_correction, self.adaptive = fine_correction, adaptive
+        self.max_age = max_age
+        self.patience, self.min_iterations = divergence_patience, divergence_min_iterations
+        self.ss = 16 if model == "quadratic" else 8
+        self.status_at = 12 if model == "quadratic" else 6
+        self.taps = rp.runtime_fir_taps()
+        self.reset()
+
+    def _empty_history(self, count: int) -> tuple[np.ndarray, np.ndarray]:
+        state = np.zeros((count, self.ss), np.float32)
+        state[:, self.status_at] = -1.0
+        return state, np.full(count, 0xFFFFFFFF, np.uint32)
+
+    def reset(self) -> None:
+        fine = self.levels[0].grid_w * self.levels[0].grid_h
+        self.history, self.ages = self._empty_history(fine)
+        self.prev_history, self.prev_ages = self._empty_history(fine)
+        top = self.levels[-1]
+        self.coarse_history, self.coarse_ages = self._empty_history(top.grid_w * top.grid_h)
+
+    def _grid(self, level: int) -> tuple[int, int]:
+        return self.levels[level].grid_w, self.levels[level].grid_h
+
+    def _solve_level(self, level: int, frame: np.ndarray, seed, active) -> tuple[np.ndarray, np.ndarray]:
+        lv = self.levels[level]
+        coef = oc.prefilter(frame, self.taps) if self.interp == "bspline" else None
+        schedule = self.L - 1 - level
+        raw = oc.solve(frame, coef, lv.plane, lv.metadata, lv.inverse, subset_size=self.S, subset_stride=self.s,
+                       model=self.model, interpolation=self.interp, lanes=self.lanes,
+                       iterations=self.iterations[schedule], tolerance=self.tolerances[schedule],
+                       zncc_min=self.zncc_min, seed_state=seed, active=active,
+                       divergence_patience=self.patience if level == 0 else 0,
+                       divergence_min_iterations=self.min_iterations)
+        if self.policy == "disabled":
+            return raw, raw
+        out = oc.uod(raw, lv.metadata, grid=self._grid(level), subset_stride=self.s, model=self.model,
+                     policy=self.policy, median_size=self.median_size,
+                     seed_mode=self.policy == "median" and level > 0)
+        return raw, out
+
+    def register(self, frame: np.ndarray, levels_used: int | None = None) -> tuple[np.ndarray, list[int]]:
+        L = levels_used or self.L
+        frames = [np.ascontiguousarray(frame, dtype=np.uint8)]
+        for _ in range(1, L):
+            frames.append(oc.reduce(frames[-1]))
+        counters = [0, 0, 0, 0]
+        c = L - 1
+        seed = active = None
+        if self.temporal:
+            source = self.history
+            if self.velocity:
+                source, counters[2] = oc.temporal_predict(self.history, self.prev_history, self.ages,
+                                                          self.prev_ages, model=self.model)
+            seed, active, weights = oc.transfer_seed(
+                source, source_grid=self._grid(0), destination_grid=self._grid(c), source_scale=1.0,
+                destination_scale=float(1 << c), subset_size=self.S, subset_stride=self.s, model=self.model,
+                track_availability=self.fine_correction, return_weights=True)
+            projected = weights > 0.0
+            counters[0] = int(projected.sum())
+            if self.fine_correction:
+                seed[~projected, self.status_at] = -1.0
+        raws, outs = {}, {}
+        raws[c], outs[c] = self._solve_level(c, frames[c], seed, active)
+        for level in range(L - 2, -1, -1):
+            seed, active = oc.transfer_seed(
+                outs[level + 1], source_grid=self._grid(level + 1), destination_grid=self._grid(level),
+                source_scale=float(1 << (level + 1)), destination_scale=float(1 << level), subset_size=self.S,
+                subset_stride=self.s, model=self.model, track_availability=self.fine_correction)
+            if level == 0 and self.temporal and self.fine_correction:
+                seed = oc.refine_temporal_seed(
+                    seed, active, self.coarse_history, self.coarse_ages, self.history, self.ages,
+                    source_grid=self._grid(1), destination_grid=self._grid(0), source_scale=2.0,
+                    subset_size=self.S, subset_stride=self.s, model=self.model, max_age=self.max_age)
+            raws[level], outs[level] = self._solve_level(level, frames[level], seed, active)
+        if self.temporal:
+            use_filtered = self.policy == "replace" and not self.velocity
+            if self.velocity:
+                oc.temporal_save_previous(self.history, self.ages, raws[0], outs[0], self.prev_history,
+                                          self.prev_ages, model=self.model)
+            accepted, expired = oc.temporal_merge(self.history, self.ages, raws[0], outs[0], model=self.model,
+                                                  max_age=self.max_age, use_filtered=use_filtered)
+            counters[1] = accepted
+            counters[3] = expired if self.adaptive else 0
+            if self.fine_correction:
+                top = self.L - 1
+                if top in raws:
+                    raw_top, out_top = raws[top], outs[top]
+                else:
+                    raw_top = out_top = np.zeros_like(self.coarse_history)
+                oc.temporal_merge(self.coarse_history, self.coarse_ages, raw_top, out_top, model=self.model,
+                                  max_age=self.max_age, use_filtered=use_filtered)
+        return outs[0], counters
