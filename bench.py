@@ -55,7 +55,7 @@ def parse_args() -> argparse.Namespace:
     ap.add_argument("--frames", type=int, default=60)
     ap.add_argument("--hole", type=float, default=300.0)
     ap.add_argument("--peak", type=float, default=2.0)
-    ap.add_argument("--lanes", type=int, default=32)
+    ap.add_argument("--lanes", type=int, default=16)
     ap.add_argument("--persistent", action="store_true")
     ap.add_argument("--autotune", action="store_true", help="pick lanes/persistence with the solver autotuner")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -42,7 +42,7 @@ struct gbdic_batch {
                 solve_end = nullptr;
     std::string error;
     std::vector<std::unique_ptr<BatchJobHost>> jobs;
-    int lanes = 32, mode = GBDIC_BATCH_PERSISTENT, ctas_per_sm = 0;
+    int lanes = 16, mode = GBDIC_BATCH_PERSISTENT, ctas_per_sm = 0;
     ClassQueue light, heavy;
     gbdic::HostBuffer in, out;
     size_t in_bytes = 0, out_bytes = 0;
@@ -327,7 +327,8 @@ int gbdic_batch_add(gbdic_batch *b, const gbdic_batch_job *job, const uint8_t *r
 
 int gbdic_batch_set_variant(gbdic_batch *b, int32_t lanes, int32_t mode, int32_t ctas_per_sm) {
     return guarded(b, [&] {
-        if (lanes != 32 && lanes != 64 && lanes != 128) fail(GBDIC_EINVAL, "threads_per_subset must be 32, 64, or 128");
+        if (lanes != 16 && lanes != 32 && lanes != 64 && lanes != 128)
+            fail(GBDIC_EINVAL, "threads_per_subset must be 16, 32, 64, or 128");
         if (mode != GBDIC_BATCH_PERSISTENT && mode != GBDIC_BATCH_PER_JOB) fail(GBDIC_EINVAL, "unknown batch mode");
         if (ctas_per_sm < 0 || ctas_per_sm > 32) fail(GBDIC_EINVAL, "ctas_per_sm must be in [0, 32]");
         check_cuda(cudaStreamSynchronize(b->stream), "pending work");

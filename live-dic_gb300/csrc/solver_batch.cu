@@ -24,7 +24,7 @@ namespace gbdic {
 namespace {
 
 template <int LANES, bool QUAD>
-__global__ void __launch_bounds__(128, QUAD ? 5 : 8) icgn_batch_kernel(BatchSolveArgs b) {
+__global__ void __launch_bounds__(128, QUAD ? 5 : GBDIC_SOLVER_MIN_BLOCKS) icgn_batch_kernel(BatchSolveArgs b) {
     constexpr bool kBlock = LANES > 32;
     constexpr int kUnitThreads = kBlock ? 128 : 32;
     constexpr int kGroups = kUnitThreads / LANES;
@@ -74,6 +74,7 @@ template <bool QUAD>
 int occupancy(int lanes) {
     int blocks = 0;
     cudaError_t err = cudaErrorInvalidValue;
+    if (lanes == 16) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, icgn_batch_kernel<16, QUAD>, 128, 0);
     if (lanes == 32) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, icgn_batch_kernel<32, QUAD>, 128, 0);
     if (lanes == 64) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, icgn_batch_kernel<64, QUAD>, 128, 0);
     if (lanes == 128) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, icgn_batch_kernel<128, QUAD>, 128, 0);
@@ -83,6 +84,7 @@ int occupancy(int lanes) {
 template <bool QUAD>
 cudaError_t launch(const BatchSolveArgs &b, int lanes, int grid, cudaStream_t stream) {
     switch (lanes) {
+    case 16: icgn_batch_kernel<16, QUAD><<<grid, 128, 0, stream>>>(b); break;
     case 32: icgn_batch_kernel<32, QUAD><<<grid, 128, 0, stream>>>(b); break;
     case 64: icgn_batch_kernel<64, QUAD><<<grid, 128, 0, stream>>>(b); break;
     case 128: icgn_batch_kernel<128, QUAD><<<grid, 128, 0, stream>>>(b); break;

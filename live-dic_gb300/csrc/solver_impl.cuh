@@ -19,6 +19,16 @@
 
 #include "gbdic_common.cuh"
 
+// Resident CTAs per SM the translation / affine solver is compiled for
+// (register budget 65536 / (128 x this)); the quadratic solver uses 5.
+#ifndef GBDIC_SOLVER_MIN_BLOCKS
+#define GBDIC_SOLVER_MIN_BLOCKS 5
+#endif
+// Packed-pair pixel loop (FADD2 / FMUL2 / FFMA2) for B-spline windows.
+#ifndef GBDIC_SOLVER_PAIRS
+#define GBDIC_SOLVER_PAIRS 1
+#endif
+
 namespace gbdic {
 
 template <int MODEL>
@@ -347,12 +357,97 @@ __device__ __forceinline__ float gn_update(const SolveArgs &a, const float (&t)[
     return divergence_status(a, change, it1, conv, prev_change, stalled);
 }
 
+// One pixel's contribution to the lane's sums (icgn.wgsl:712-780), in the
+// reference's order: sum w g, w g^2, w f g, then the Jacobian-weighted terms.
+template <int MODEL, bool GAUSS, int N>
+__device__ __forceinline__ void accumulate_pixel(float (&s)[N], const SolveArgs &a, float g, unsigned ridx, int p,
+                                                 float lx, float ly, float ref_mean, float hx2, float xy,
+                                                 float hy2) {
+    const float4 rv = __ldg(a.plane + ridx);
+    const float f = rv.x - ref_mean;
+    float wc = g, wf = f;
+    if (GAUSS) {
+        const float wt = __ldg(a.weights + p);
+        wc = wt * g;
+        wf = wt * f;
+    }
+    const float gxg = rv.y * wc, gyg = rv.z * wc;
+    s[0] = s[0] + wc;
+    s[1] = fmaf(wc, g, s[1]);
+    s[2] = fmaf(wf, g, s[2]);
+    if (MODEL == kModelTranslation) {
+        s[3] = s[3] + gxg;
+        s[4] = s[4] + gyg;
+    } else {
+        s[3] = s[3] + gxg;
+        s[4] = fmaf(gxg, lx, s[4]);
+        s[5] = fmaf(gxg, ly, s[5]);
+        s[6] = s[6] + gyg;
+        s[7] = fmaf(gyg, lx, s[7]);
+        s[8] = fmaf(gyg, ly, s[8]);
+        if (MODEL == kModelQuadratic) {
+            s[9] = fmaf(gxg, hx2, s[9]);
+            s[10] = fmaf(gxg, xy, s[10]);
+            s[11] = fmaf(gxg, hy2, s[11]);
+            s[12] = fmaf(gyg, hx2, s[12]);
+            s[13] = fmaf(gyg, xy, s[13]);
+            s[14] = fmaf(gyg, hy2, s[14]);
+        }
+    }
+}
+
+// Packed FP32 pairs (sm_100 FADD2 / FMUL2 / FFMA2): component k of every
+// operation is the scalar operation of pixel k, rounded identically.
+__device__ __forceinline__ float2 pair(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// bspline_weights() of two fractions.  1 - t and px - fx are formed as
+// fma(t, -1, 1) and fma(fx, -1, px): exact products, so each equals the
+// scalar subtraction bit for bit.
+__device__ __forceinline__ void bspline_weights2(float2 t, float2 w[4]) {
+    const float2 k6 = pair(1.0f / 6.0f), one = pair(1.0f), m1 = pair(-1.0f), three = pair(3.0f);
+    const float2 t2 = mul2(t, t), t3 = mul2(t2, t), s = fma2(t, m1, one);
+    w[0] = mul2(mul2(mul2(s, s), s), k6);
+    w[1] = mul2(fma2(fma2(three, t, pair(-6.0f)), t2, pair(4.0f)), k6);
+    w[2] = mul2(fma2(fma2(fma2(pair(-3.0f), t, three), t, three), t, one), k6);
+    w[3] = mul2(t3, k6);
+}
+
+// sample_target<kInterpBspline, false> of two positions: the 4x4 coefficient
+// taps of each pixel in one register pair per tap, the row and column sums
+// as packed FMAs in the scalar order.
+__device__ __forceinline__ float2 sample_bspline_pair(const float *__restrict__ coef, int W, float2 px, float2 py) {
+    const float fxa = floorf(px.x), fxb = floorf(px.y), fya = floorf(py.x), fyb = floorf(py.y);
+    const float2 m1 = pair(-1.0f);
+    float2 wx[4], wy[4];
+    bspline_weights2(fma2(make_float2(fxa, fxb), m1, px), wx);
+    bspline_weights2(fma2(make_float2(fya, fyb), m1, py), wy);
+    const float *ra = coef + (size_t)((int)fya - 1) * W + ((int)fxa - 1);
+    const float *rb = coef + (size_t)((int)fyb - 1) * W + ((int)fxb - 1);
+    float2 value = pair(0.0f);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float2 row = pair(0.0f);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) row = fma2(wx[i], make_float2(__ldg(ra + i), __ldg(rb + i)), row);
+        value = fma2(wy[j], row, value);
+        ra += W;
+        rb += W;
+    }
+    return value;
+}
+
 template <int MODEL, int INTERP, int LANES, bool GAUSS, bool PART = false>
 __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int glane, int lane_in_warp,
                                             float *red) {
     constexpr int N = SumCount<MODEL>::value;
     constexpr bool kBlock = LANES > 32;
     constexpr bool kClamp = MODEL == kModelQuadratic;
+    // Pixel pairs with packed FP32 arithmetic: B-spline global-load sampling
+    // of complete windows, translation and affine warps.
+    constexpr bool kPair = GBDIC_SOLVER_PAIRS && INTERP == kInterpBspline && !PART && MODEL != kModelQuadratic;
     const bool exists = group < a.count;
     // Partial windows: group -> window index; support words and box.
     const int idx = PART ? (exists ? __ldg(a.partial_index + group) : 0) : group;
@@ -393,6 +488,14 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int g
     const int ldiv = LANES / S, lmod = LANES % S;
     const int col0 = glane % S, row0 = glane / S;
     const int W = a.W, H = a.H;
+    // Pixel bookkeeping without conversions: column / row as exact small
+    // float integers, the window origin plus `half` (so origin + lx is the
+    // pixel's integer coordinate exactly), and the reference-plane index.
+    const float fS = (float)S, flmod = (float)lmod, fldiv = (float)ldiv;
+    const float fcol0 = (float)col0, frow0 = (float)row0;
+    const float ox = (float)px0 + half, oy = (float)py0 + half;
+    const unsigned ridx0 = (unsigned)(py0 + row0) * (unsigned)W + (unsigned)(px0 + col0);
+    const unsigned rstep = (unsigned)lmod + (unsigned)ldiv * (unsigned)W, rwrap = (unsigned)(W - S);
     // Lanes that run the update together: the group's half warp for 16-lane
     // groups (groups are uniform in `done`), else the whole warp.
     const unsigned seg_mask = LANES == 16 ? (0xffffu << (lane_in_warp & 16)) : kFullMask;
@@ -417,15 +520,45 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int g
 #pragma unroll
         for (int k = 0; k < N; ++k) s[k] = 0.0f;
         if (!done) {
-            int col = col0, row = row0;
-            for (int p = glane; p < npix; p += LANES) {
+            float fcol = fcol0, frow = frow0;
+            unsigned ridx = ridx0;
+            int p = glane;
+            if (kPair) {
+                // Two consecutive pixels of the lane per step (p and
+                // p + LANES), sampled with packed FP32 pairs and accumulated
+                // one after the other, as in the scalar loop.
+                const float2 nh = pair(-half), ox2 = pair(ox), oy2 = pair(oy);
+                const float2 t0 = pair(w.t0), t1 = pair(w.t1);
+                const float2 l0 = pair(w.l0), l1 = pair(w.l1), l2 = pair(w.l2), l3 = pair(w.l3);
+                for (; p + LANES < npix; p += 2 * LANES) {
+                    float fcolb = fcol + flmod, frowb = frow + fldiv;
+                    unsigned ridxb = ridx + rstep;
+                    if (fcolb >= fS) { fcolb -= fS; frowb += 1.0f; ridxb += rwrap; }
+                    const float2 lx = add2(make_float2(fcol, fcolb), nh), ly = add2(make_float2(frow, frowb), nh);
+                    float2 dx = t0, dy = t1;
+                    if (MODEL != kModelTranslation) {
+                        dx = add2(t0, fma2(l0, lx, mul2(l1, ly)));
+                        dy = add2(t1, fma2(l2, lx, mul2(l3, ly)));
+                    }
+                    const float2 g = sample_bspline_pair(a.coef, W, add2(add2(ox2, lx), dx), add2(add2(oy2, ly), dy));
+                    accumulate_pixel<MODEL, GAUSS, N>(s, a, g.x, ridx, p, lx.x, ly.x, ref_mean, 0.0f, 0.0f, 0.0f);
+                    accumulate_pixel<MODEL, GAUSS, N>(s, a, g.y, ridxb, p + LANES, lx.y, ly.y, ref_mean, 0.0f, 0.0f,
+                                                      0.0f);
+                    fcol = fcolb + flmod;
+                    frow = frowb + fldiv;
+                    ridx = ridxb + rstep;
+                    if (fcol >= fS) { fcol -= fS; frow += 1.0f; ridx += rwrap; }
+                }
+            }
+            for (; p < npix; p += LANES) {
                 if (PART && !((__ldg(support + (p >> 5)) >> (p & 31)) & 1u)) {
-                    col += lmod;
-                    row += ldiv;
-                    if (col >= S) { col -= S; ++row; }
+                    fcol += flmod;
+                    frow += fldiv;
+                    ridx += rstep;
+                    if (fcol >= fS) { fcol -= fS; frow += 1.0f; ridx += rwrap; }
                     continue;
                 }
-                const float lx = (float)col - half, ly = (float)row - half;
+                const float lx = fcol - half, ly = frow - half;
                 float hx2 = 0.0f, xy = 0.0f, hy2 = 0.0f;
                 if (MODEL == kModelQuadratic) {
                     hx2 = 0.5f * lx * lx;
@@ -434,43 +567,12 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int g
                 }
                 float dx, dy;
                 displacement<MODEL>(w, lx, ly, hx2, xy, hy2, dx, dy);
-                const int pxi = px0 + col, pyi = py0 + row;
-                const float g = sample_target<INTERP, kClamp>(a.coef, a.img, W, H, (float)pxi + dx,
-                                                              (float)pyi + dy);
-                const float4 rv = __ldg(a.plane + (size_t)pyi * W + pxi);
-                const float f = rv.x - ref_mean;
-                float wc = g, wf = f;
-                if (GAUSS) {
-                    const float wt = __ldg(a.weights + p);
-                    wc = wt * g;
-                    wf = wt * f;
-                }
-                const float gxg = rv.y * wc, gyg = rv.z * wc;
-                s[0] = s[0] + wc;
-                s[1] = fmaf(wc, g, s[1]);
-                s[2] = fmaf(wf, g, s[2]);
-                if (MODEL == kModelTranslation) {
-                    s[3] = s[3] + gxg;
-                    s[4] = s[4] + gyg;
-                } else {
-                    s[3] = s[3] + gxg;
-                    s[4] = fmaf(gxg, lx, s[4]);
-                    s[5] = fmaf(gxg, ly, s[5]);
-                    s[6] = s[6] + gyg;
-                    s[7] = fmaf(gyg, lx, s[7]);
-                    s[8] = fmaf(gyg, ly, s[8]);
-                    if (MODEL == kModelQuadratic) {
-                        s[9] = fmaf(gxg, hx2, s[9]);
-                        s[10] = fmaf(gxg, xy, s[10]);
-                        s[11] = fmaf(gxg, hy2, s[11]);
-                        s[12] = fmaf(gyg, hx2, s[12]);
-                        s[13] = fmaf(gyg, xy, s[13]);
-                        s[14] = fmaf(gyg, hy2, s[14]);
-                    }
-                }
-                col += lmod;
-                row += ldiv;
-                if (col >= S) { col -= S; ++row; }
+                const float g = sample_target<INTERP, kClamp>(a.coef, a.img, W, H, (ox + lx) + dx, (oy + ly) + dy);
+                accumulate_pixel<MODEL, GAUSS, N>(s, a, g, ridx, p, lx, ly, ref_mean, hx2, xy, hy2);
+                fcol += flmod;
+                frow += fldiv;
+                ridx += rstep;
+                if (fcol >= fS) { fcol -= fS; frow += 1.0f; ridx += rwrap; }
             }
         }
         if (kBlock) reduce_block<LANES, N>(s, red, glane);
@@ -498,7 +600,7 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int g
 }
 
 template <int MODEL, int INTERP, int LANES, bool GAUSS, bool PART = false>
-__global__ void __launch_bounds__(128, MODEL == kModelQuadratic ? 5 : 1) icgn_kernel(SolveArgs a) {
+__global__ void __launch_bounds__(128, MODEL == kModelQuadratic ? 5 : GBDIC_SOLVER_MIN_BLOCKS) icgn_kernel(SolveArgs a) {
     constexpr bool kBlock = LANES > 32;
     constexpr int kUnitThreads = kBlock ? 128 : 32;
     constexpr int kGroups = kUnitThreads / LANES;

@@ -35,7 +35,7 @@ from .subset import normalize_subset_size, normalize_subset_stride, subset_grid_
 
 _POLICY = {"disabled": 0, "replace": 1, "flag": 2}
 _MODES = {"persistent": _native.BATCH_PERSISTENT, "per-job": _native.BATCH_PER_JOB}
-LANE_CHOICES = (32, 64, 128)
+LANE_CHOICES = (16, 32, 64, 128)
 
 
 @dataclass(frozen=True)
@@ -61,7 +61,7 @@ class ICGNBatch:
     """Many registration jobs of uneven image size, subset size and shape
     function, registered together."""
 
-    def __init__(self, *, device: int = 0, solver_workgroup_size: int = 32, mode: str = "persistent",
+    def __init__(self, *, device: int = 0, solver_workgroup_size: int = 16, mode: str = "persistent",
                  ctas_per_sm: int = 0) -> None:
         self._check_variant(solver_workgroup_size, mode, ctas_per_sm)
         self._lib = _native.load()

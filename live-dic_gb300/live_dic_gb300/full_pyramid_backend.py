@@ -87,7 +87,7 @@ class ICGNWGPUFullPyramid:
         tolerance_per_level: tuple[float, ...] | None = None,
         power_preference: str = "high-performance",
         device_type: str = "auto",
-        solver_workgroup_size: int = 32,
+        solver_workgroup_size: int = 16,
         interpolation: str = "bspline",
         motion_model: str = "affine",
         outlier_policy: str = "replace",

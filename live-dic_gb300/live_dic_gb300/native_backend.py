@@ -160,7 +160,7 @@ class ICGNWGPU:
         power_preference: str = "high-performance",
         device_type: str = "auto",
         prefer_subgroups: bool | None = None,
-        solver_workgroup_size: int = 32,
+        solver_workgroup_size: int = 16,
         pyramid_levels: int = DEFAULT_PYRAMID_LEVELS,
         interpolation: str = "bspline",
         motion_model: str = "affine",

@@ -48,7 +48,7 @@ def _packed(result):
     return np.concatenate([result.parameters, result.status[..., None], result.iterations[..., None]], -1)
 
 
-@pytest.mark.parametrize("lanes", [32, 64, 128])
+@pytest.mark.parametrize("lanes", [16, 32, 64, 128])
 def test_batch_matches_solo_engines(pairs, lanes):
     expected = [_solo(job, lanes) for job in pairs]
     with _batch(pairs, solver_workgroup_size=lanes) as batch:

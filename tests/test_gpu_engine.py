@@ -41,7 +41,7 @@ def test_c0_parity_with_oracle_and_truth(c0_pair):
         result = engine.register(tgt)
     plane, inverse, metadata = rp.reference_arrays(ref, subset_size=S, subset_stride=s)
     coef = oracle_c.prefilter(tgt, rp.runtime_fir_taps())
-    expected = oracle_c.solve(tgt, coef, plane, metadata, inverse, subset_size=S, subset_stride=s, lanes=32,
+    expected = oracle_c.solve(tgt, coef, plane, metadata, inverse, subset_size=S, subset_stride=s, lanes=16,
                               tolerance=1e-4).reshape(_packed(result).shape)
     status, estatus = result.status, expected[..., 6]
     both = (status == 1) & (estatus == 1)

@@ -105,7 +105,7 @@ def test_seeded_and_retry_bit_exact(pair):
     coef = oracle_c.prefilter(tgt, rp.runtime_fir_taps())
     packed_seeds = np.zeros((gh * gw, 8), np.float32)
     packed_seeds[:, :6] = np.where(active.reshape(-1, 1), seeds.reshape(-1, 6), 0)
-    expected = oracle_c.solve(tgt, coef, plane, metadata, inverse, subset_size=21, subset_stride=10, lanes=32,
+    expected = oracle_c.solve(tgt, coef, plane, metadata, inverse, subset_size=21, subset_stride=10, lanes=16,
                               iterations=12, seed_state=packed_seeds, active=active.ravel().astype(np.uint32))
     np.testing.assert_array_equal(_packed(result), expected.reshape(gh, gw, 8))
     assert (result.status[~active] == -1).all()
@@ -166,7 +166,7 @@ def test_register_with_uod_matches_oracle_pipeline(pair):
         engine.set_reference_arrays(W, H, plane, metadata, inverse)
         result = engine.register(tgt)
     coef = oracle_c.prefilter(tgt, rp.runtime_fir_taps())
-    raw = oracle_c.solve(tgt, coef, plane, metadata, inverse, subset_size=21, subset_stride=10, lanes=32)
+    raw = oracle_c.solve(tgt, coef, plane, metadata, inverse, subset_size=21, subset_stride=10, lanes=16)
     expected = oracle_c.uod(raw, metadata, grid=(gw, gh), subset_stride=10, policy="replace")
     np.testing.assert_array_equal(_packed(result), expected.reshape(gh, gw, 8))
 

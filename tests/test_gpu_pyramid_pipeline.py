@@ -48,7 +48,8 @@ def _oracle(engine: ICGNWGPUFullPyramid, **kw) -> PyramidOracle:
             engine.export_level(level, _native.EXPORT_INVERSE, np.float32, (gw * gh * 36,))))
     return PyramidOracle(levels, subset_size=engine.subset_size, subset_stride=engine.subset_stride,
                          iterations=engine.iterations_per_level, tolerances=engine.tolerance_per_level,
-                         outlier_policy=engine.outlier_policy, temporal=True, **kw)
+                         outlier_policy=engine.outlier_policy, lanes=engine.solver_workgroup_size, temporal=True,
+                         **kw)
 
 
 def _packed(result):

@@ -192,7 +192,7 @@ def test_bench_replica_throughput_two_gloo_ranks():
 @pytest.mark.parametrize(
     "kwargs,message",
     [
-        ({"solver_workgroup_size": 16}, "solver_workgroup_size"),
+        ({"solver_workgroup_size": 48}, "solver_workgroup_size"),
         ({"solver_workgroup_size": True}, "solver_workgroup_size"),
         ({"mode": "sequential"}, "mode"),
         ({"ctas_per_sm": 33}, "ctas_per_sm"),
