@@ -104,7 +104,7 @@ def test_batch_autotuner_keeps_a_valid_variant(pairs):
         best = batch.autotune([j["target"] for j in pairs], repeats=1)
         assert batch.validation[batch.variant_name]["valid"]
         assert best == batch.variant
-        assert len(batch.tuning_ms) == 9
+        assert len(batch.tuning_ms) == 12  # 4 lane counts x (persistent, persistent 2/SM, per-job)
 
 
 def test_batch_argument_errors(pairs):
