@@ -222,11 +222,124 @@ __global__ void uod_kernel(UodArgs a) {
     store_state(a.out + (size_t)index * ss, ss, out);
 }
 
+// Stable sort of 8 values (odd-even transposition, swap only when strictly
+// greater): the same arrangement as a bubble sort of the compacted values,
+// with the +inf padding of missing neighbours at the end.
+__device__ __forceinline__ void sort8(float (&v)[8]) {
+#pragma unroll
+    for (int round = 0; round < 8; ++round) {
+#pragma unroll
+        for (int i = round & 1; i + 1 < 8; i += 2) {
+            const float lo = v[i], hi = v[i + 1];
+            const bool swap = lo > hi;
+            v[i] = swap ? hi : lo;
+            v[i + 1] = swap ? lo : hi;
+        }
+    }
+}
+
+// median_small() of the first `count` (4..8) sorted values.
+__device__ __forceinline__ float median_sorted8(const float (&v)[8], int count) {
+    switch (count) {
+    case 4: return 0.5f * (v[1] + v[2]);
+    case 5: return v[2];
+    case 6: return 0.5f * (v[2] + v[3]);
+    case 7: return v[3];
+    default: return 0.5f * (v[3] + v[4]);
+    }
+}
+
+// 3x3 UOD (replace / flag) of translation and affine states with every
+// neighbour in registers: the neighbour slots keep the scan order of the
+// generic kernel, missing ones read +inf, and the order statistics come
+// from sort8, so the result equals uod_kernel's bit for bit.
+template <int MODEL>
+__global__ void __launch_bounds__(128) uod3_kernel(UodArgs a) {
+    constexpr int ss = state_stride(MODEL), sat = status_slot(MODEL), nc = parameter_count(MODEL);
+    const int index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= a.count) return;
+    float own[ss];
+    load_state(a.state + (size_t)index * ss, ss, own);
+    float out[ss];
+#pragma unroll
+    for (int k = 0; k < ss; ++k) out[k] = own[k];
+    if (own[sat] >= 0.5f) {
+        const int px = index % a.grid_w, py = index / a.grid_w;
+        const float kInf = __int_as_float(0x7f800000);
+        float nb[8][nc];
+        bool valid[8];
+        int count = 0;
+#pragma unroll
+        for (int slot = 0; slot < 8; ++slot) {
+            const int cell = slot < 4 ? slot : slot + 1;  // 3x3 scan order without the centre
+            const int dx = cell % 3 - 1, dy = cell / 3 - 1;
+            const int nx = px + dx, ny = py + dy;
+            bool ok = nx >= 0 && ny >= 0 && nx < a.grid_w && ny < a.grid_h && allowed(a, index, dx, dy, false);
+            float nbr[ss];
+            if (ok) {
+                load_state(a.state + ((size_t)ny * a.grid_w + nx) * ss, ss, nbr);
+                ok = nbr[sat] >= 0.5f;
+            }
+            valid[slot] = ok;
+            count += ok ? 1 : 0;
+            const float ox = -(float)a.subset_stride * (float)dx, oy = -(float)a.subset_stride * (float)dy;
+#pragma unroll
+            for (int k = 0; k < nc; ++k) nb[slot][k] = ok ? recentered(MODEL, nbr, k, ox, oy) : kInf;
+        }
+        if (count >= 4) {
+            float filtered[nc], medians[nc];
+#pragma unroll
+            for (int k = 0; k < nc; ++k) filtered[k] = medians[k] = own[k];
+            constexpr int model_components = MODEL == kModelTranslation ? 2 : nc;
+            const int median_count = a.policy == 1 ? model_components : 2;
+#pragma unroll
+            for (int ai = 0; ai < model_components; ++ai) {
+                if (ai >= median_count) break;
+                const int comp = ai == 0 ? 0 : (ai == 1 ? 3 : (ai == 2 ? 1 : (ai == 3 ? 2 : ai)));
+                float v[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v[i] = nb[i][comp];
+                sort8(v);
+                medians[comp] = median_sorted8(v, count);
+            }
+            bool flagged = false;
+#pragma unroll
+            for (int ai = 0; ai < 2; ++ai) {
+                const int comp = ai == 0 ? 0 : 3;
+                float v[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v[i] = valid[i] ? fabsf(nb[i][comp] - medians[comp]) : kInf;
+                sort8(v);
+                const float spread = median_sorted8(v, count);
+                const float score = fabsf(filtered[comp] - medians[comp]) / (spread + 0.1f);
+                if (score > 2.0f) flagged = true;
+            }
+            if (flagged) {
+                if (a.policy == 1) {
+#pragma unroll
+                    for (int k = 0; k < model_components; ++k) {
+                        const int comp = k == 0 ? 0 : (k == 1 ? 3 : (k == 2 ? 1 : (k == 3 ? 2 : k)));
+                        filtered[comp] = medians[comp];
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < nc; ++k) out[k] = filtered[k];
+                out[6] = 2.0f;
+                out[7] = own[7];
+            }
+        }
+    }
+    store_state(a.out + (size_t)index * ss, ss, out);
+}
+
 }  // namespace
 
 cudaError_t launch_uod(const UodArgs &a, cudaStream_t stream) {
     if (a.count <= 0) return cudaSuccess;
-    uod_kernel<<<(a.count + 127) / 128, 128, 0, stream>>>(a);
+    const int grid = (a.count + 127) / 128;
+    if (a.policy != 3 && a.model == kModelAffine) uod3_kernel<kModelAffine><<<grid, 128, 0, stream>>>(a);
+    else if (a.policy != 3 && a.model == kModelTranslation) uod3_kernel<kModelTranslation><<<grid, 128, 0, stream>>>(a);
+    else uod_kernel<<<grid, 128, 0, stream>>>(a);
     return cudaGetLastError();
 }
 

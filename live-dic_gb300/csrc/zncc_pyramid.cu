@@ -75,27 +75,41 @@ __global__ void __launch_bounds__(128) final_zncc_kernel(ZnccArgs a) {
 // full_pyramid.wgsl:218-249: exact integer 5x5 [1 4 6 4 1]^2 sum over the
 // reflected source, truncating division by 256; 16x16 outputs per CTA
 // from a 36x36 byte footprint staged in shared memory.
-__global__ void reduce_half_kernel(const uint8_t *__restrict__ src, int W, int H,
-                                   uint8_t *__restrict__ dst) {
-    __shared__ unsigned tile[36 * 36];
+// Separable form of the exact integer 5x5 reduction: the [1 4 6 4 1] sum of
+// every footprint row at the even columns, then the same sum down the rows.
+// Integer sums are exact in any order, so the output equals the 5x5 form.
+// One CTA: 64 x 16 outputs from a (2*16 + 3) x (2*64 + 3) byte footprint.
+constexpr int kRX = 64, kRY = 16;
+constexpr int kFX = 2 * kRX + 3, kFY = 2 * kRY + 3;
+
+__global__ void __launch_bounds__(256) reduce_half_kernel(const uint8_t *__restrict__ src, int W, int H,
+                                                          uint8_t *__restrict__ dst) {
+    __shared__ uint8_t tile[kFY * kFX];
+    __shared__ unsigned rows[kFY * kRX];
     const int W2 = W / 2, H2 = H / 2;
-    const int ox = blockIdx.x * 32 - 2, oy = blockIdx.y * 32 - 2;
-    const int tid = threadIdx.y * 16 + threadIdx.x;
-    for (int i = tid; i < 36 * 36; i += 256) {
-        const int sx = mirror_clamp(ox + i % 36, W), sy = mirror_clamp(oy + i / 36, H);
-        tile[i] = src[(size_t)sy * W + sx];
+    const int fx0 = 2 * (int)blockIdx.x * kRX - 2, fy0 = 2 * (int)blockIdx.y * kRY - 2;
+    const int tid = threadIdx.x;
+    const bool interior = fx0 >= 0 && fy0 >= 0 && fx0 + kFX <= W && fy0 + kFY <= H;
+    for (int i = tid; i < kFY * kFX; i += 256) {
+        const int r = i / kFX, c = i - r * kFX;
+        const int sx = interior ? fx0 + c : mirror_clamp(fx0 + c, W);
+        const int sy = interior ? fy0 + r : mirror_clamp(fy0 + r, H);
+        tile[i] = __ldg(src + (size_t)sy * W + sx);
     }
     __syncthreads();
-    const int x = blockIdx.x * 16 + threadIdx.x, y = blockIdx.y * 16 + threadIdx.y;
-    if (x >= W2 || y >= H2) return;
-    const unsigned taps[5] = {1u, 4u, 6u, 4u, 1u};
-    unsigned acc = 0u;
-#pragma unroll
-    for (int j = 0; j < 5; ++j)
-#pragma unroll
-        for (int i = 0; i < 5; ++i)
-            acc += taps[j] * taps[i] * tile[(2 * threadIdx.y + j) * 36 + 2 * threadIdx.x + i];
-    dst[(size_t)y * W2 + x] = (uint8_t)(acc / 256u);
+    for (int i = tid; i < kFY * kRX; i += 256) {
+        const int r = i / kRX, c = i - r * kRX;
+        const uint8_t *t = tile + r * kFX + 2 * c;
+        rows[i] = (unsigned)t[0] + 4u * t[1] + 6u * t[2] + 4u * t[3] + (unsigned)t[4];
+    }
+    __syncthreads();
+    for (int i = tid; i < kRY * kRX; i += 256) {
+        const int y = i / kRX, c = i - y * kRX;
+        const unsigned *v = rows + 2 * y * kRX + c;
+        const unsigned acc = v[0] + 4u * v[kRX] + 6u * v[2 * kRX] + 4u * v[3 * kRX] + v[4 * kRX];
+        const int X = (int)blockIdx.x * kRX + c, Y = (int)blockIdx.y * kRY + y;
+        if (X < W2 && Y < H2) dst[(size_t)Y * W2 + X] = (uint8_t)(acc / 256u);
+    }
 }
 
 // ------------------------------------------------------------ seed transfer
@@ -325,7 +339,7 @@ cudaError_t launch_final_zncc(const ZnccArgs &a, cudaStream_t stream) {
 cudaError_t launch_reduce_half(const uint8_t *src, int W, int H, uint8_t *dst, cudaStream_t stream) {
     const int W2 = W / 2, H2 = H / 2;
     if (W2 <= 0 || H2 <= 0) return cudaSuccess;
-    reduce_half_kernel<<<dim3((W2 + 15) / 16, (H2 + 15) / 16), dim3(16, 16), 0, stream>>>(src, W, H, dst);
+    reduce_half_kernel<<<dim3((W2 + kRX - 1) / kRX, (H2 + kRY - 1) / kRY), 256, 0, stream>>>(src, W, H, dst);
     return cudaGetLastError();
 }
 
