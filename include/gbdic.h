@@ -321,6 +321,14 @@ int gbdic_pyramid_profile_read(gbdic_pyramid *pyramid, double *solver_ms, int64_
  * denominator of the solver's FP32 roofline. */
 int gbdic_fp32_peak_probe(int32_t device, double *tflops);
 
+/* Host summary of one packed field (`count` states of `stride` floats, the
+ * status at float `n`): the number of subsets with status > 0.5 and > 1.5,
+ * and the translations (floats 0 and 3) and iteration counts (float n + 1)
+ * of the accepted subsets in grid order, for the FP64 means of
+ * RegistrationResult (engine.py:106-327; wgpu_backend.py:2595-2668). */
+int gbdic_field_summary(const float *packed, int64_t count, int32_t stride, int32_t n, float *accepted_tx,
+                        float *accepted_ty, float *accepted_iterations, int64_t *accepted, int64_t *replaced);
+
 /* Switch the IC-GN solver variant (lanes per subset 16/32/64/128, persistent
  * work queue on/off) of a prepared handle without re-preparing the reference;
  * the autotuner's actuator (reference: ICGNWGPU._autotune_solver,

@@ -353,11 +353,7 @@ int gbdic_batch_register(gbdic_batch *b, const uint8_t *const *frames, const int
             const int64_t stride = row_strides ? row_strides[j] : (int64_t)W;
             if (stride < (int64_t)W) fail(GBDIC_EINVAL, "row_stride must be at least the width");
             uint8_t *dst = b->in.as<uint8_t>() + job.in_offset;
-            if (stride == (int64_t)W) {
-                std::memcpy(dst, frames[j], W * H);
-            } else {
-                for (size_t r = 0; r < H; ++r) std::memcpy(dst + r * W, frames[j] + r * stride, W);
-            }
+            gbdic::host_copy_rows(dst, frames[j], W, H, stride);
         }
         const double upload_ms = gbdic::ms_since(t0);
         if (!b->host_graph) b->host_graph = b->capture(true);
@@ -370,7 +366,7 @@ int gbdic_batch_register(gbdic_batch *b, const uint8_t *const *frames, const int
         const auto t2 = std::chrono::steady_clock::now();
         for (size_t j = 0; j < b->jobs.size(); ++j) {
             auto &job = *b->jobs[j];
-            std::memcpy(out_states[j], b->out.as<uint8_t>() + job.out_offset, job.state_bytes);
+            gbdic::host_copy(out_states[j], b->out.as<uint8_t>() + job.out_offset, job.state_bytes);
         }
         if (timing) {
             float dev = 0.0f;

@@ -214,7 +214,7 @@ void readback(gbdic_engine *e, int k, float *out_state, gbdic_timing *timing, st
     gbdic::wait_event(h.done, gbdic::kWaitMs);
     const double exec_ms = gbdic::ms_since(t_exec);
     const auto t_copy = std::chrono::steady_clock::now();
-    if (out_state) std::memcpy(out_state, h.out.as<float>(), bytes);
+    if (out_state) gbdic::host_copy(out_state, h.out.as<float>(), bytes);
     fill_timing(timing, h, exec_ms, gbdic::ms_since(t_copy));
 }
 
@@ -347,7 +347,7 @@ int gbdic_retire(gbdic_engine *e, int32_t slot_index, float *out_state, gbdic_ti
         const double wait_ms = gbdic::ms_since(t_wait);
         const auto t_copy = std::chrono::steady_clock::now();
         const size_t bytes = (size_t)e->level.count * gbdic::state_stride(e->rt->opts().o.motion_model) * sizeof(float);
-        if (out_state) std::memcpy(out_state, h.out.as<float>(), bytes);
+        if (out_state) gbdic::host_copy(out_state, h.out.as<float>(), bytes);
         fill_timing(timing, h, wait_ms, gbdic::ms_since(t_copy));
     });
 }
@@ -367,6 +367,30 @@ int gbdic_register_device(gbdic_engine *e, const uint8_t *device_frame, const gb
         rt.enqueue_solve(lvl, slot, *cfg, false, false, device_frame, disabled ? device_state : nullptr, s);
         if (!disabled) rt.enqueue_uod(lvl, slot, false, device_state, s);
     });
+}
+
+int gbdic_field_summary(const float *packed, int64_t count, int32_t stride, int32_t n, float *accepted_tx,
+                        float *accepted_ty, float *accepted_iterations, int64_t *accepted, int64_t *replaced) {
+    if (!packed || count < 0 || n < 4 || stride < n + 2 || !accepted_tx || !accepted_ty || !accepted_iterations ||
+        !accepted || !replaced) {
+        gbdic::set_thread_error("field summary arguments are invalid");
+        return GBDIC_EINVAL;
+    }
+    int64_t a = 0, r = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        const float *s = packed + i * stride;
+        const float status = s[n];
+        if (status > 0.5f) {
+            accepted_tx[a] = s[0];
+            accepted_ty[a] = s[3];
+            accepted_iterations[a] = s[n + 1];
+            ++a;
+        }
+        r += status > 1.5f ? 1 : 0;
+    }
+    *accepted = a;
+    *replaced = r;
+    return GBDIC_OK;
 }
 
 int gbdic_set_partial_support(gbdic_engine *e, int32_t count, const int32_t *indices, const uint32_t *words,

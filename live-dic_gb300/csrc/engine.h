@@ -32,6 +32,12 @@ void grid_of(int W, int H, int S, int st, int &gw, int &gh);
 void fir_taps(float out[25]);
 // Message returned by gbdic_last_error(NULL) on the calling thread.
 void set_thread_error(const std::string &message);
+// Host copies of frames and fields into / out of pinned staging, split over
+// a small pool of worker threads when large (one core's memcpy bandwidth is
+// a frame's largest host cost at UHD).  Rows: `height` rows of `width`
+// bytes, source rows `stride` bytes apart.
+void host_copy(void *dst, const void *src, size_t bytes);
+void host_copy_rows(uint8_t *dst, const uint8_t *src, size_t width, size_t height, int64_t stride);
 constexpr double kWaitMs = 120000.0;
 
 // Owning device allocation.

@@ -513,11 +513,7 @@ int gbdic_pyramid_submit(gbdic_pyramid *p, int32_t slot, const uint8_t *frame, i
         ps.submitted = std::chrono::steady_clock::now();
         ps.in.ensure((size_t)fine.W * fine.H);
         uint8_t *dst = ps.in.as<uint8_t>();
-        if (row_stride == fine.W) {
-            std::memcpy(dst, frame, (size_t)fine.W * fine.H);
-        } else {
-            for (int r = 0; r < fine.H; ++r) std::memcpy(dst + (size_t)r * fine.W, frame + (size_t)r * row_stride, fine.W);
-        }
+        gbdic::host_copy_rows(dst, frame, (size_t)fine.W, (size_t)fine.H, row_stride);
         ps.upload_ms = gbdic::ms_since(ps.submitted);
         launch_slot(p, slot);
         ps.pending = true;
@@ -534,7 +530,7 @@ int gbdic_pyramid_retire(gbdic_pyramid *p, int32_t slot, float *out_state, uint3
         gbdic::wait_event(ps.end, gbdic::kWaitMs);
         const double wait_ms = gbdic::ms_since(t_wait);
         const auto t_copy = std::chrono::steady_clock::now();
-        if (out_state) std::memcpy(out_state, ps.out.as<float>(), p->state_bytes(0));
+        if (out_state) gbdic::host_copy(out_state, ps.out.as<float>(), p->state_bytes(0));
         if (counters) std::memcpy(counters, ps.counters_host.as<uint32_t>(), 4 * sizeof(uint32_t));
         if (timing) {
             float dev = 0.0f;

@@ -4,10 +4,15 @@
 // (reference plane, metadata, inverse Hessians) and, per pipeline slot, its
 // own target, coefficient plane and solver states, so that several frames can
 // be in flight.  Frames are staged through pinned host buffers.
+#include <unistd.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
+#include <mutex>
 #include <string>
 #include <thread>
 
@@ -484,12 +489,114 @@ void Runtime::upload_frame(Level &level, LevelSlot &slot, const uint8_t *frame, 
     const size_t W = (size_t)level.W, H = (size_t)level.H;
     staging.ensure(W * H);
     uint8_t *dst = staging.as<uint8_t>();
-    if (row_stride == (int64_t)W) {
-        std::memcpy(dst, frame, W * H);
-    } else {
-        for (size_t r = 0; r < H; ++r) std::memcpy(dst + r * W, frame + (size_t)r * row_stride, W);
-    }
+    host_copy_rows(dst, frame, W, H, row_stride);
     check_cuda(cudaMemcpyAsync(slot.frame.get(), dst, W * H, cudaMemcpyHostToDevice, s), "frame upload");
+}
+
+namespace {
+
+// Fixed pool of copy workers.  run() executes part 0 on the caller and parts
+// 1..n-1 on the workers and returns when all are done; calls are
+// serialised.  A process forked after the pool started gets a new pool.
+class CopyPool {
+  public:
+    static CopyPool &get() {
+        static std::mutex guard;
+        static CopyPool *pool = nullptr;
+        std::lock_guard<std::mutex> lock(guard);
+        if (pool == nullptr || pool->pid_ != getpid()) pool = new CopyPool();  // a forked child abandons the old one
+        return *pool;
+    }
+    int width() const { return (int)workers_.size() + 1; }
+    void run(int parts, const std::function<void(int)> &fn) {
+        std::lock_guard<std::mutex> serial(run_mutex_);
+        parts = std::min(parts, width());
+        {
+            std::lock_guard<std::mutex> lock(m_);
+            job_ = &fn;
+            parts_ = parts;
+            next_ = 1;
+            pending_ = parts - 1;
+            ++generation_;
+        }
+        cv_.notify_all();
+        fn(0);
+        std::unique_lock<std::mutex> lock(m_);
+        done_.wait(lock, [&] { return pending_ == 0; });
+        job_ = nullptr;
+    }
+
+  private:
+    CopyPool() : pid_(getpid()) {
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const int extra = (int)std::min(3u, hw > 1 ? hw - 1 : 0u);
+        for (int i = 0; i < extra; ++i) {
+            std::thread t([this] { loop(); });
+            t.detach();
+            workers_.push_back(0);
+        }
+    }
+    void loop() {
+        unsigned long long seen = 0;
+        for (;;) {
+            const std::function<void(int)> *fn = nullptr;
+            int part = -1;
+            {
+                std::unique_lock<std::mutex> lock(m_);
+                cv_.wait(lock, [&] { return generation_ != seen && next_ < parts_; });
+                part = next_++;
+                if (next_ >= parts_) seen = generation_;
+                fn = job_;
+            }
+            (*fn)(part);
+            std::lock_guard<std::mutex> lock(m_);
+            if (--pending_ == 0) done_.notify_all();
+        }
+    }
+    pid_t pid_;
+    std::vector<int> workers_;
+    std::mutex run_mutex_, m_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)> *job_ = nullptr;
+    int parts_ = 0, next_ = 0, pending_ = 0;
+    unsigned long long generation_ = 0;
+};
+
+constexpr size_t kParallelCopyBytes = 2u << 20;
+
+}  // namespace
+
+void host_copy(void *dst, const void *src, size_t bytes) {
+    if (bytes < kParallelCopyBytes) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    CopyPool &pool = CopyPool::get();
+    const int parts = std::max(1, std::min(pool.width(), (int)(bytes / (1u << 20))));
+    const size_t chunk = (bytes + parts - 1) / parts;
+    pool.run(parts, [&](int k) {
+        const size_t begin = (size_t)k * chunk, end = std::min(bytes, begin + chunk);
+        if (begin < end) std::memcpy(static_cast<uint8_t *>(dst) + begin, static_cast<const uint8_t *>(src) + begin,
+                                     end - begin);
+    });
+}
+
+void host_copy_rows(uint8_t *dst, const uint8_t *src, size_t width, size_t height, int64_t stride) {
+    if (stride == (int64_t)width) {
+        host_copy(dst, src, width * height);
+        return;
+    }
+    if (width * height < kParallelCopyBytes) {
+        for (size_t r = 0; r < height; ++r) std::memcpy(dst + r * width, src + (size_t)r * stride, width);
+        return;
+    }
+    CopyPool &pool = CopyPool::get();
+    const int parts = pool.width();
+    const size_t rows = (height + parts - 1) / parts;
+    pool.run(parts, [&](int k) {
+        const size_t begin = (size_t)k * rows, end = std::min(height, begin + rows);
+        for (size_t r = begin; r < end; ++r) std::memcpy(dst + r * width, src + (size_t)r * stride, width);
+    });
 }
 
 }  // namespace gbdic

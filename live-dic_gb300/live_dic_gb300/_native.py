@@ -213,6 +213,7 @@ _SIGNATURES = {
     "gbdic_search_seeds_device": (C.c_int, [P, P, P, P, P, I32, I32, P]),
     "gbdic_pyramid_set_translation": (C.c_int, [P, I32, C.c_float, C.c_float]),
     "gbdic_set_partial_support": (C.c_int, [P, I32, P, P, I32, P, P, P]),
+    "gbdic_field_summary": (C.c_int, [P, I64, I32, I32, P, P, P, C.POINTER(I64), C.POINTER(I64)]),
     "gbdic_pyramid_set_partial_support": (C.c_int, [P, I32, I32, P, P, I32, P, P, P]),
     "gbdic_pyramid_set_active_levels": (C.c_int, [P, I32]),
     "gbdic_fourier_create": (C.c_int, [I32, P, P, I32, C.POINTER(P)]),

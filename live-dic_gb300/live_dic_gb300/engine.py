@@ -180,26 +180,40 @@ def result_from_packed(
 ) -> RegistrationResult:
     """Zero-copy views of one packed (grid_h, grid_w, stride) float32 field
     (reference: wgpu_backend.py:_result_from_raw, 2595-2668)."""
+    from . import _native
+
     n = len(parameter_order(motion_model))
     parameters = packed[..., :n]
     status = packed[..., n]
     iterations = packed[..., n + 1]
-    accepted_mask = status > 0.5
-    accepted = int(np.count_nonzero(accepted_mask))
+    # One pass in the library gathers the accepted subsets' translations and
+    # iteration counts in grid order (the values and order of the boolean
+    # selections parameters[..., 0][status > 0.5] etc.); the FP64 means are
+    # then NumPy's over those contiguous arrays.
+    flat = np.ascontiguousarray(packed, dtype=np.float32)
+    count = flat.size // flat.shape[-1]
+    picked = np.empty((3, count), np.float32)
+    accepted_c, replaced_c = _native.C.c_int64(), _native.C.c_int64()
+    lib = _native.load()
+    _native.check(lib.gbdic_field_summary(
+        _native.ptr(flat), count, flat.shape[-1], n, _native.ptr(picked[0]), _native.ptr(picked[1]),
+        _native.ptr(picked[2]), _native.C.byref(accepted_c), _native.C.byref(replaced_c)),
+        lib.gbdic_last_error(None))
+    accepted = int(accepted_c.value)
     mean_translation = None
     mean_iterations = None
     if accepted:
         mean_translation = (
-            float(np.mean(parameters[..., 0][accepted_mask], dtype=np.float64)),
-            float(np.mean(parameters[..., 3][accepted_mask], dtype=np.float64)),
+            float(np.mean(picked[0, :accepted], dtype=np.float64)),
+            float(np.mean(picked[1, :accepted], dtype=np.float64)),
         )
-        mean_iterations = float(np.mean(iterations[accepted_mask], dtype=np.float64))
+        mean_iterations = float(np.mean(picked[2, :accepted], dtype=np.float64))
     return RegistrationResult(
         parameters=parameters,
         status=status,
         iterations=iterations,
         accepted=accepted,
-        replaced=int(np.count_nonzero(status > 1.5)),
+        replaced=int(replaced_c.value),
         mean_translation=mean_translation,
         mean_iterations=mean_iterations,
         timing=dict(timing),

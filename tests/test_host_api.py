@@ -269,3 +269,25 @@ def test_partial_reference_preparation_matches_reference():
     np.testing.assert_array_equal(inverse, g["partial_inverse_out"])
     np.testing.assert_array_equal(updated.support_rank, g["partial_rank"])
     np.testing.assert_allclose(updated.support_condition, g["partial_condition"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("model", ["affine", "quadratic"])
+def test_result_summary_matches_numpy_selection(model):
+    """RegistrationResult counts and FP64 means (engine.py:106-327) from the
+    library's one-pass summary equal the boolean-selection formulas."""
+    from live_dic_gb300.engine import result_from_packed
+
+    rng = np.random.default_rng(17)
+    stride, n = (16, 12) if model == "quadratic" else (8, 6)
+    packed = rng.normal(size=(37, 53, stride)).astype(np.float32)
+    packed[..., n] = rng.choice([2.0, 1.0, 0.0, -1.0, -3.0, np.nan], size=(37, 53),
+                                p=[0.05, 0.8, 0.05, 0.04, 0.04, 0.02]).astype(np.float32)
+    r = result_from_packed(packed, motion_model=model, timing={}, config={}, width=600, height=400,
+                           subset_size=21, subset_stride=10)
+    mask = packed[..., n] > 0.5
+    assert r.accepted == int(mask.sum())
+    assert r.replaced == int((packed[..., n] > 1.5).sum())
+    assert r.mean_translation == (float(np.mean(packed[..., 0][mask], dtype=np.float64)),
+                                  float(np.mean(packed[..., 3][mask], dtype=np.float64)))
+    assert r.mean_iterations == float(np.mean(packed[..., n + 1][mask], dtype=np.float64))
+    assert np.shares_memory(r.parameters, packed)
