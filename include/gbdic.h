@@ -118,6 +118,13 @@ int gbdic_set_reference(gbdic_engine *engine, const uint8_t *image, int32_t widt
                         int64_t row_stride, const uint8_t *roi_selected, const float *roi_links,
                         gbdic_ref_info *info);
 
+/* set_reference() of a device-resident image (dense 8-bit rows `row_stride`
+ * bytes apart): a reference rebuilt on the GPU for every pair without a host
+ * copy (config "reference rebuilt every pair"); same preparation. */
+int gbdic_set_reference_device(gbdic_engine *engine, const uint8_t *device_image, int32_t width, int32_t height,
+                               int64_t row_stride, const uint8_t *roi_selected, const float *roi_links,
+                               gbdic_ref_info *info);
+
 /* Upload of host-prepared reference arrays in the reference's own layout
  * (_allocate_runtime, wgpu_backend.py:1569-1590), e.g. from _reference_arrays. */
 int gbdic_set_reference_arrays(gbdic_engine *engine, int32_t width, int32_t height,

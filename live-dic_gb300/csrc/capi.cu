@@ -133,8 +133,10 @@ int gbdic_create(const gbdic_options *options, gbdic_engine **out) {
 
 void gbdic_destroy(gbdic_engine *engine) { delete engine; }
 
-int gbdic_set_reference(gbdic_engine *e, const uint8_t *image, int32_t width, int32_t height, int64_t row_stride,
-                        const uint8_t *roi_selected, const float *roi_links, gbdic_ref_info *info) {
+namespace {
+// set_reference of a host (device = false) or device image.
+int set_reference_impl(gbdic_engine *e, const uint8_t *image, bool device, int32_t width, int32_t height,
+                       int64_t row_stride, const uint8_t *roi_selected, const float *roi_links, gbdic_ref_info *info) {
     return guarded(e, [&] {
         const auto &o = e->rt->opts().o;
         if (!image) fail(GBDIC_EINVAL, "image is required");
@@ -147,7 +149,12 @@ int gbdic_set_reference(gbdic_engine *e, const uint8_t *image, int32_t width, in
         e->ready = false;
         e->rt->configure_level(e->level, width, height, (int)e->host.size());
         auto &slot = *e->level.slots[0];
-        e->rt->upload_frame(e->level, slot, image, row_stride, e->host[0].in, e->rt->stream());
+        if (device)
+            check_cuda(cudaMemcpy2DAsync(slot.frame.get(), (size_t)width, image, (size_t)row_stride, (size_t)width,
+                                         (size_t)height, cudaMemcpyDeviceToDevice, e->rt->stream()),
+                       "reference copy");
+        else
+            e->rt->upload_frame(e->level, slot, image, row_stride, e->host[0].in, e->rt->stream());
         const double ms = e->rt->prepare_reference(e->level, slot.frame.as<uint8_t>(), roi_selected, roi_links);
         for (auto &h : e->host) {
             if (h.graph) cudaGraphExecDestroy(h.graph);
@@ -162,6 +169,19 @@ int gbdic_set_reference(gbdic_engine *e, const uint8_t *image, int32_t width, in
             info->device_ms = ms;
         }
     });
+}
+
+}  // namespace
+
+int gbdic_set_reference(gbdic_engine *e, const uint8_t *image, int32_t width, int32_t height, int64_t row_stride,
+                        const uint8_t *roi_selected, const float *roi_links, gbdic_ref_info *info) {
+    return set_reference_impl(e, image, false, width, height, row_stride, roi_selected, roi_links, info);
+}
+
+int gbdic_set_reference_device(gbdic_engine *e, const uint8_t *device_image, int32_t width, int32_t height,
+                               int64_t row_stride, const uint8_t *roi_selected, const float *roi_links,
+                               gbdic_ref_info *info) {
+    return set_reference_impl(e, device_image, true, width, height, row_stride, roi_selected, roi_links, info);
 }
 
 int gbdic_set_reference_arrays(gbdic_engine *e, int32_t width, int32_t height, const float *plane,

@@ -24,7 +24,7 @@ namespace gbdic {
 namespace {
 
 template <int LANES, bool QUAD>
-__global__ void __launch_bounds__(128, QUAD ? 5 : GBDIC_SOLVER_MIN_BLOCKS) icgn_batch_kernel(BatchSolveArgs b) {
+__global__ void __launch_bounds__(128, QUAD ? GBDIC_QUAD_MIN_BLOCKS : GBDIC_SOLVER_MIN_BLOCKS) icgn_batch_kernel(BatchSolveArgs b) {
     constexpr bool kBlock = LANES > 32;
     constexpr int kUnitThreads = kBlock ? 128 : 32;
     constexpr int kGroups = kUnitThreads / LANES;

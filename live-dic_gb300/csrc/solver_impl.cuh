@@ -25,6 +25,12 @@
 #define GBDIC_SOLVER_MIN_BLOCKS 5
 #endif
 // Packed-pair pixel loop (FADD2 / FMUL2 / FFMA2) for B-spline windows.
+#ifndef GBDIC_QUAD_MIN_BLOCKS
+#define GBDIC_QUAD_MIN_BLOCKS 5
+#endif
+#ifndef GBDIC_QUAD_PAIRS
+#define GBDIC_QUAD_PAIRS 1
+#endif
 #ifndef GBDIC_SOLVER_PAIRS
 #define GBDIC_SOLVER_PAIRS 1
 #endif
@@ -418,15 +424,37 @@ __device__ __forceinline__ void bspline_weights2(float2 t, float2 w[4]) {
 // sample_target<kInterpBspline, false> of two positions: the 4x4 coefficient
 // taps of each pixel in one register pair per tap, the row and column sums
 // as packed FMAs in the scalar order.
-__device__ __forceinline__ float2 sample_bspline_pair(const float *__restrict__ coef, int W, float2 px, float2 py) {
+template <bool CLAMP>
+__device__ __forceinline__ float2 sample_bspline_pair(const float *__restrict__ coef, int W, int H, float2 px,
+                                                      float2 py) {
     const float fxa = floorf(px.x), fxb = floorf(px.y), fya = floorf(py.x), fyb = floorf(py.y);
     const float2 m1 = pair(-1.0f);
     float2 wx[4], wy[4];
     bspline_weights2(fma2(make_float2(fxa, fxb), m1, px), wx);
     bspline_weights2(fma2(make_float2(fya, fyb), m1, py), wy);
-    const float *ra = coef + (size_t)((int)fya - 1) * W + ((int)fxa - 1);
-    const float *rb = coef + (size_t)((int)fyb - 1) * W + ((int)fxb - 1);
+    const int bxa = (int)fxa, bxb = (int)fxb, bya = (int)fya, byb = (int)fyb;
     float2 value = pair(0.0f);
+    if (CLAMP) {
+        // Every tap index clamped to the plane, as sample_target<.., true>.
+        int xa[4], xb[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            xa[i] = clampi(bxa + i - 1, 0, W - 1);
+            xb[i] = clampi(bxb + i - 1, 0, W - 1);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float *ra = coef + (size_t)clampi(bya + j - 1, 0, H - 1) * W;
+            const float *rb = coef + (size_t)clampi(byb + j - 1, 0, H - 1) * W;
+            float2 row = pair(0.0f);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) row = fma2(wx[i], make_float2(__ldg(ra + xa[i]), __ldg(rb + xb[i])), row);
+            value = fma2(wy[j], row, value);
+        }
+        return value;
+    }
+    const float *ra = coef + (size_t)(bya - 1) * W + (bxa - 1);
+    const float *rb = coef + (size_t)(byb - 1) * W + (bxb - 1);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         float2 row = pair(0.0f);
@@ -445,9 +473,10 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int g
     constexpr int N = SumCount<MODEL>::value;
     constexpr bool kBlock = LANES > 32;
     constexpr bool kClamp = MODEL == kModelQuadratic;
-    // Pixel pairs with packed FP32 arithmetic: B-spline global-load sampling
-    // of complete windows, translation and affine warps.
-    constexpr bool kPair = GBDIC_SOLVER_PAIRS && INTERP == kInterpBspline && !PART && MODEL != kModelQuadratic;
+    // Pixel pairs with packed FP32 arithmetic: B-spline sampling of
+    // complete windows.
+    constexpr bool kPair = GBDIC_SOLVER_PAIRS && INTERP == kInterpBspline && !PART &&
+                           (MODEL != kModelQuadratic || GBDIC_QUAD_PAIRS);
     const bool exists = group < a.count;
     // Partial windows: group -> window index; support words and box.
     const int idx = PART ? (exists ? __ldg(a.partial_index + group) : 0) : group;
@@ -530,20 +559,31 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int g
                 const float2 nh = pair(-half), ox2 = pair(ox), oy2 = pair(oy);
                 const float2 t0 = pair(w.t0), t1 = pair(w.t1);
                 const float2 l0 = pair(w.l0), l1 = pair(w.l1), l2 = pair(w.l2), l3 = pair(w.l3);
+                const float2 half2 = pair(0.5f);
                 for (; p + LANES < npix; p += 2 * LANES) {
                     float fcolb = fcol + flmod, frowb = frow + fldiv;
                     unsigned ridxb = ridx + rstep;
                     if (fcolb >= fS) { fcolb -= fS; frowb += 1.0f; ridxb += rwrap; }
                     const float2 lx = add2(make_float2(fcol, fcolb), nh), ly = add2(make_float2(frow, frowb), nh);
                     float2 dx = t0, dy = t1;
+                    float2 hx2 = pair(0.0f), xy = pair(0.0f), hy2 = pair(0.0f);
                     if (MODEL != kModelTranslation) {
                         dx = add2(t0, fma2(l0, lx, mul2(l1, ly)));
                         dy = add2(t1, fma2(l2, lx, mul2(l3, ly)));
                     }
-                    const float2 g = sample_bspline_pair(a.coef, W, add2(add2(ox2, lx), dx), add2(add2(oy2, ly), dy));
-                    accumulate_pixel<MODEL, GAUSS, N>(s, a, g.x, ridx, p, lx.x, ly.x, ref_mean, 0.0f, 0.0f, 0.0f);
-                    accumulate_pixel<MODEL, GAUSS, N>(s, a, g.y, ridxb, p + LANES, lx.y, ly.y, ref_mean, 0.0f, 0.0f,
-                                                      0.0f);
+                    if (MODEL == kModelQuadratic) {
+                        // displacement<kModelQuadratic> on both pixels.
+                        hx2 = mul2(mul2(half2, lx), lx);
+                        xy = mul2(lx, ly);
+                        hy2 = mul2(mul2(half2, ly), ly);
+                        dx = add2(dx, fma2(pair(w.c0), hx2, fma2(pair(w.c1), xy, mul2(pair(w.c2), hy2))));
+                        dy = add2(dy, fma2(pair(w.c3), hx2, fma2(pair(w.c4), xy, mul2(pair(w.c5), hy2))));
+                    }
+                    const float2 g = sample_bspline_pair<kClamp>(a.coef, W, H, add2(add2(ox2, lx), dx),
+                                                                 add2(add2(oy2, ly), dy));
+                    accumulate_pixel<MODEL, GAUSS, N>(s, a, g.x, ridx, p, lx.x, ly.x, ref_mean, hx2.x, xy.x, hy2.x);
+                    accumulate_pixel<MODEL, GAUSS, N>(s, a, g.y, ridxb, p + LANES, lx.y, ly.y, ref_mean, hx2.y, xy.y,
+                                                      hy2.y);
                     fcol = fcolb + flmod;
                     frow = frowb + fldiv;
                     ridx = ridxb + rstep;
@@ -600,7 +640,7 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int g
 }
 
 template <int MODEL, int INTERP, int LANES, bool GAUSS, bool PART = false>
-__global__ void __launch_bounds__(128, MODEL == kModelQuadratic ? 5 : GBDIC_SOLVER_MIN_BLOCKS) icgn_kernel(SolveArgs a) {
+__global__ void __launch_bounds__(128, MODEL == kModelQuadratic ? GBDIC_QUAD_MIN_BLOCKS : GBDIC_SOLVER_MIN_BLOCKS) icgn_kernel(SolveArgs a) {
     constexpr bool kBlock = LANES > 32;
     constexpr int kUnitThreads = kBlock ? 128 : 32;
     constexpr int kGroups = kUnitThreads / LANES;

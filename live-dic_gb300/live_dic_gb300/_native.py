@@ -157,6 +157,7 @@ _SIGNATURES = {
     "gbdic_last_error": (C.c_char_p, [P]),
     "gbdic_set_reference": (C.c_int, [P, P, I32, I32, I64, P, P, C.POINTER(RefInfo)]),
     "gbdic_set_reference_arrays": (C.c_int, [P, I32, I32, P, P, P, P, C.POINTER(RefInfo)]),
+    "gbdic_set_reference_device": (C.c_int, [P, P, I32, I32, I64, P, P, C.POINTER(RefInfo)]),
     "gbdic_register": (C.c_int, [P, P, I64, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),
     "gbdic_register_seeded": (C.c_int, [P, P, I64, P, P, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),
     "gbdic_retry_seeded": (C.c_int, [P, I32, P, P, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),

@@ -425,6 +425,46 @@ class ICGNWGPU:
             reference_valid=self.reference_valid,
         )
 
+    def set_profiling(self, enable: bool) -> None:
+        """Time every solver launch of the resident path with CUDA events and
+        count executed Gauss-Newton iterations (resets the counters)."""
+        self._check(self._lib.gbdic_profile(self._handle, int(bool(enable))))
+
+    def read_profile(self) -> dict[str, float]:
+        ms, launches, timed, iters = C.c_double(), C.c_int64(), C.c_int64(), C.c_uint64()
+        self._check(self._lib.gbdic_profile_read(
+            self._handle, C.byref(ms), C.byref(launches), C.byref(timed), C.byref(iters)))
+        return {"solver_ms": ms.value, "launches": launches.value, "timed_launches": timed.value,
+                "iterations": iters.value}
+
+    def set_reference_device(self, device_image: int, width: int, height: int, *, row_stride: int | None = None,
+                             iterations: int = 30, tolerance: float = 1e-3, zncc_min: float = 0.8) -> float:
+        """GPU reference preparation of a device-resident 8-bit image (dense
+        rows `row_stride` bytes apart), without ROI; returns the device
+        preparation time in ms.  For pipelines that rebuild the reference for
+        every pair on the GPU."""
+        if self._closed:
+            raise ICGNError("This engine is closed; create a new engine before set_reference().")
+        if self.pyramid_levels > 1:
+            raise ICGNError("set_reference_device() supports pyramid_levels=1; use set_reference().")
+        gw, gh = subset_grid_shape(width, height, subset_size=self.subset_size, subset_stride=self.subset_stride)
+        if gw < 1 or gh < 1:
+            raise ValueError(f"Reference dimensions must each be at least {self.subset_size} pixels.")
+        config = _validated_config(iterations, tolerance, zncc_min)
+        self._reference_ready = False
+        self._target_ready = False
+        info = _native.RefInfo()
+        self._check(self._lib.gbdic_set_reference_device(
+            self._handle, C.c_void_p(device_image), int(width), int(height), int(row_stride or width), None, None,
+            C.byref(info)))
+        self.width, self.height, self.grid_width, self.grid_height = int(width), int(height), gw, gh
+        self._config = config
+        self.roi = None
+        admissible = self._export(_native.EXPORT_ADMISSIBLE, np.uint8, (gh, gw))
+        self.reference_valid = immutable(admissible.astype(bool))
+        self._reference_ready = True
+        return float(info.device_ms)
+
     def _prepare_partial(self, roi: RoiPlan) -> RoiPlan:
         """Partial-window metadata from the GPU-prepared plane (float64 host
         preparation, partial.py:26-121), uploaded with the support tables."""
