@@ -172,25 +172,33 @@ __host__ __device__ constexpr int pair_index(int nm, int i, int j) {
     return i * nm - i * (i - 1) / 2 + (j - i);
 }
 
+// All moments of one pixel in the order of Moments (f^2; gx f m; gy f m;
+// gx m; gy m; then gx^2, gx gy, gy^2 times m_i m_j for i <= j), with
+// compile-time indices so that a pass keeps only the values it sums.
 template <int MODEL>
-__device__ __forceinline__ float moment_value(int k, float w, float f, float gx, float gy, const float *m) {
-    constexpr int nm = Moments<MODEL>::nm, P = Moments<MODEL>::pairs;
-    if (k == 0) return (w * f) * f;
-    int q = k - 1;
-    if (q < nm) return ((w * gx) * f) * m[q];
-    q -= nm;
-    if (q < nm) return ((w * gy) * f) * m[q];
-    q -= nm;
-    if (q < nm) return (w * gx) * m[q];
-    q -= nm;
-    if (q < nm) return (w * gy) * m[q];
-    q -= nm;
-    int block = q / P, r = q % P;
-    int i = 0;
-    while (r >= nm - i) { r -= nm - i; ++i; }
-    const int j = i + r;
-    const float g = block == 0 ? gx * gx : (block == 1 ? gx * gy : gy * gy);
-    return ((w * g) * m[i]) * m[j];
+__device__ __forceinline__ void moment_values(float w, float f, float gx, float gy, const float *m,
+                                              float (&out)[Moments<MODEL>::count]) {
+    constexpr int nm = Moments<MODEL>::nm;
+    out[0] = (w * f) * f;
+    const float wgxf = (w * gx) * f, wgyf = (w * gy) * f, wgx = w * gx, wgy = w * gy;
+#pragma unroll
+    for (int q = 0; q < nm; ++q) {
+        out[1 + q] = wgxf * m[q];
+        out[1 + nm + q] = wgyf * m[q];
+        out[1 + 2 * nm + q] = wgx * m[q];
+        out[1 + 3 * nm + q] = wgy * m[q];
+    }
+    int k = 1 + 4 * nm;
+#pragma unroll
+    for (int block = 0; block < 3; ++block) {
+        const float wg = w * (block == 0 ? gx * gx : (block == 1 ? gx * gy : gy * gy));
+#pragma unroll
+        for (int i = 0; i < nm; ++i) {
+            const float wgi = wg * m[i];
+#pragma unroll
+            for (int j = i; j < nm; ++j) out[k++] = wgi * m[j];
+        }
+    }
 }
 
 __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
@@ -284,7 +292,7 @@ __global__ void __launch_bounds__(128) subset_prep_kernel(PrepArgs a) {
     using T = typename std::conditional<MODEL == kModelQuadratic, double, float>::type;
     constexpr int n = parameter_count(MODEL);
     constexpr int nm = Moments<MODEL>::nm, P = Moments<MODEL>::pairs, NM = Moments<MODEL>::count;
-    constexpr int kChunkM = 16;
+    constexpr int kChunkM = MODEL == kModelTranslation ? 8 : 32;
     __shared__ float s_tot[4][NM];
     __shared__ T s_A[4][n * n];
     __shared__ T s_X[4][n * n];
@@ -296,11 +304,18 @@ __global__ void __launch_bounds__(128) subset_prep_kernel(PrepArgs a) {
     const int gx0 = (idx % a.grid_w) * a.stride, gy0 = (idx / a.grid_w) * a.stride;
     const float half = 0.5f * ((float)S - 1.0f);
     // pass 1: weighted mean of the intensity
+    // Pixel p = lane + 32 k of the window, tracked without divisions.
+    const int ldiv = 32 / S, lmod = 32 % S, col0 = lane % S, row0 = lane / S;
     float s = 0.0f, c = 0.0f;
-    for (int p = lane; p < npix; p += 32) {
-        const int col = p % S, row = p / S;
-        const float I = a.plane[(size_t)(gy0 + row) * a.W + gx0 + col].x;
-        kahan_add(s, c, a.weights[p] * I);
+    {
+        int col = col0, row = row0;
+        for (int p = lane; p < npix; p += 32) {
+            const float I = a.plane[(size_t)(gy0 + row) * a.W + gx0 + col].x;
+            kahan_add(s, c, a.weights[p] * I);
+            col += lmod;
+            row += ldiv;
+            if (col >= S) { col -= S; ++row; }
+        }
     }
     warp_compensated_sum(s, c);
     const float mean = __shfl_sync(kFullMask, s + c, 0) / a.weight_sum;
@@ -310,16 +325,21 @@ __global__ void __launch_bounds__(128) subset_prep_kernel(PrepArgs a) {
         float ms[kChunkM], mc[kChunkM];
 #pragma unroll
         for (int q = 0; q < kChunkM; ++q) { ms[q] = 0.0f; mc[q] = 0.0f; }
+        int col = col0, row = row0;
         for (int p = lane; p < npix; p += 32) {
-            const int col = p % S, row = p / S;
             const float4 v = a.plane[(size_t)(gy0 + row) * a.W + gx0 + col];
             const float f = v.x - mean;
             const float w = a.weights[p];
             const float x = (float)col - half, y = (float)row - half;
             float m[6] = {1.0f, x, y, 0.5f * x * x, x * y, 0.5f * y * y};
+            float mv[NM];
+            moment_values<MODEL>(w, f, v.y, v.z, m, mv);
 #pragma unroll
             for (int q = 0; q < kChunkM; ++q)
-                if (base + q < NM) kahan_add(ms[q], mc[q], moment_value<MODEL>(base + q, w, f, v.y, v.z, m));
+                if (base + q < NM) kahan_add(ms[q], mc[q], mv[base + q]);
+            col += lmod;
+            row += ldiv;
+            if (col >= S) { col -= S; ++row; }
         }
 #pragma unroll
         for (int q = 0; q < kChunkM; ++q) {

@@ -190,6 +190,17 @@ int Runtime::persistent_grid(int lanes) {
 }
 
 void Runtime::configure_level(Level &level, int W, int H, int slots) {
+    if (level.W == W && level.H == H && !level.slots.empty()) {
+        // Same geometry (a reference rebuilt for every pair): keep the slot
+        // allocations, clear their states as fresh slots would be.
+        const size_t ss = (size_t)level.count * state_stride(opt_.o.motion_model) * sizeof(float);
+        for (auto &sl : level.slots) {
+            check_cuda(cudaMemsetAsync(sl->state.get(), 0, ss, stream_), "clear state");
+            check_cuda(cudaMemsetAsync(sl->filtered.get(), 0, ss, stream_), "clear state");
+        }
+        ensure_slots(level, slots);
+        return;
+    }
     level.W = W;
     level.H = H;
     grid_of(W, H, opt_.o.subset_size, opt_.o.subset_stride, level.gw, level.gh);
