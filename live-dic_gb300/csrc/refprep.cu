@@ -322,9 +322,12 @@ __global__ void __launch_bounds__(128) subset_prep_kernel(PrepArgs a) {
     // passes over the moments, kChunkM at a time (unrolled: constant indices)
 #pragma unroll
     for (int base = 0; base < NM; base += kChunkM) {
-        float ms[kChunkM], mc[kChunkM];
+        // Kahan sums of moment pairs in packed FP32 (FADD2 / FFMA2): every
+        // component follows kahan_add's sequence, a - b written as
+        // fma(b, -1, a) (an exact product, so the same rounding).
+        float2 ms2[kChunkM / 2], mc2[kChunkM / 2];
 #pragma unroll
-        for (int q = 0; q < kChunkM; ++q) { ms[q] = 0.0f; mc[q] = 0.0f; }
+        for (int q = 0; q < kChunkM / 2; ++q) { ms2[q] = make_float2(0.0f, 0.0f); mc2[q] = make_float2(0.0f, 0.0f); }
         int col = col0, row = row0;
         for (int p = lane; p < npix; p += 32) {
             const float4 v = a.plane[(size_t)(gy0 + row) * a.W + gx0 + col];
@@ -334,9 +337,17 @@ __global__ void __launch_bounds__(128) subset_prep_kernel(PrepArgs a) {
             float m[6] = {1.0f, x, y, 0.5f * x * x, x * y, 0.5f * y * y};
             float mv[NM];
             moment_values<MODEL>(w, f, v.y, v.z, m, mv);
+            const float2 m1 = make_float2(-1.0f, -1.0f);
 #pragma unroll
-            for (int q = 0; q < kChunkM; ++q)
-                if (base + q < NM) kahan_add(ms[q], mc[q], mv[base + q]);
+            for (int q = 0; q < kChunkM / 2; ++q) {
+                if (base + 2 * q < NM) {
+                    const float2 val = make_float2(mv[base + 2 * q], base + 2 * q + 1 < NM ? mv[base + 2 * q + 1] : 0.0f);
+                    const float2 y = __ffma2_rn(mc2[q], m1, val);
+                    const float2 t = __fadd2_rn(ms2[q], y);
+                    mc2[q] = __ffma2_rn(y, m1, __ffma2_rn(ms2[q], m1, t));
+                    ms2[q] = t;
+                }
+            }
             col += lmod;
             row += ldiv;
             if (col >= S) { col -= S; ++row; }
@@ -344,8 +355,9 @@ __global__ void __launch_bounds__(128) subset_prep_kernel(PrepArgs a) {
 #pragma unroll
         for (int q = 0; q < kChunkM; ++q) {
             if (base + q < NM) {
-                warp_compensated_sum(ms[q], mc[q]);
-                if (lane == 0) s_tot[warp][base + q] = ms[q] + mc[q];
+                float sq = (q & 1) ? ms2[q / 2].y : ms2[q / 2].x, cq = (q & 1) ? mc2[q / 2].y : mc2[q / 2].x;
+                warp_compensated_sum(sq, cq);
+                if (lane == 0) s_tot[warp][base + q] = sq + cq;
             }
         }
     }
