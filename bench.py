@@ -64,7 +64,7 @@ def parse_args() -> argparse.Namespace:
                     help="uhd-plate: the headline UHD sequence; batch: 16 uneven pairs in one batched step; "
                          "learned: learned-seed vs pyramid+ZNCC seeding on large-translation UHD frames")
     ap.add_argument("--train-images", type=int, default=512, help="learned workload: training images (320x320)")
-    ap.add_argument("--train-steps", type=int, default=6000, help="learned workload: Adam steps (batch 512)")
+    ap.add_argument("--train-steps", type=int, default=8000, help="learned workload: Adam steps (batch 512)")
     ap.add_argument("--lattice", type=int, default=8, help="learned workload: network on every n-th subset")
     ap.add_argument("--plain-radius", type=int, default=18,
                     help="learned workload: ZNCC search radius of the plain path at the coarsest level")
@@ -602,7 +602,7 @@ def run_learned_workload(args) -> None:
         plain_times, plain_acc = run(plain_step, gh, gw)
         plain.close()
         # learned
-        engine = ICGNWGPU(subset_size=S, subset_stride=st, device=local)
+        engine = ICGNWGPU(subset_size=S, subset_stride=st, device=local, solver_workgroup_size=args.lanes)
         engine.set_reference(ref)
         seeder = learned.LearnedSeeder(engine, net, step=args.lattice)
         seeder.set_reference_image(ref)
