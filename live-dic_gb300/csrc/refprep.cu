@@ -229,13 +229,26 @@ __device__ __forceinline__ void warp_compensated_sum(float &s, float &c) {
 // Warp-cooperative Cholesky inverse of an SPD n x n matrix held in shared
 // memory (row-major A), with Jacobi scaling d_i = 1/sqrt(A_ii).  On return
 // X holds A^-1; returns false if A is not numerically positive definite.
+// Reciprocal square root: the double path (12x12 quadratic Hessians, FP64
+// pipe-bound) uses rsqrt() so that each pivot costs one sequence and every
+// later division becomes a multiplication; the float path keeps sqrt and
+// IEEE division.
+template <typename T>
+__device__ __forceinline__ T recip_sqrt(T v) {
+    if constexpr (std::is_same<T, double>::value) return rsqrt(v);
+    else return T(1) / sqrt(v);
+}
+
 template <typename T>
 __device__ bool cholesky_inverse(T *A, T *X, T *d, int n, int lane) {
+    constexpr bool kRecip = std::is_same<T, double>::value;
+    __shared__ T s_r[4][12];  // 1 / L_kk per warp (double path)
+    T *rdiag = s_r[(threadIdx.x >> 5) & 3];
     bool ok = true;
     if (lane < n) {
         const T aii = A[lane * n + lane];
         ok = aii > T(0);
-        d[lane] = ok ? T(1) / sqrt(aii) : T(0);
+        d[lane] = ok ? recip_sqrt(aii) : T(0);
     }
     ok = __all_sync(kFullMask, ok);
     if (!ok) return false;
@@ -247,10 +260,16 @@ __device__ bool cholesky_inverse(T *A, T *X, T *d, int n, int lane) {
         T pivot = A[k * n + k];
         ok = pivot > T(0);
         if (!__all_sync(kFullMask, ok)) return false;
-        const T lkk = sqrt(pivot);
         __syncwarp();
-        if (lane == k) A[k * n + k] = lkk;
-        if (lane > k && lane < n) A[lane * n + k] = A[lane * n + k] / lkk;
+        if (kRecip) {
+            const T r = recip_sqrt(pivot);
+            if (lane == k) { A[k * n + k] = pivot * r; rdiag[k] = r; }
+            if (lane > k && lane < n) A[lane * n + k] = A[lane * n + k] * r;
+        } else {
+            const T lkk = sqrt(pivot);
+            if (lane == k) A[k * n + k] = lkk;
+            if (lane > k && lane < n) A[lane * n + k] = A[lane * n + k] / lkk;
+        }
         __syncwarp();
         if (lane > k && lane < n) {
             const T lik = A[lane * n + k];
@@ -262,11 +281,11 @@ __device__ bool cholesky_inverse(T *A, T *X, T *d, int n, int lane) {
     if (lane < n) {
         const int j = lane;
         for (int i = 0; i < n; ++i) X[i * n + j] = T(0);
-        X[j * n + j] = T(1) / A[j * n + j];
+        X[j * n + j] = kRecip ? rdiag[j] : T(1) / A[j * n + j];
         for (int i = j + 1; i < n; ++i) {
             T acc = T(0);
             for (int k = j; k < i; ++k) acc = acc + A[i * n + k] * X[k * n + j];
-            X[i * n + j] = -acc / A[i * n + i];
+            X[i * n + j] = kRecip ? -acc * rdiag[i] : -acc / A[i * n + i];
         }
     }
     __syncwarp();
@@ -283,6 +302,71 @@ __device__ bool cholesky_inverse(T *A, T *X, T *d, int n, int lane) {
     __syncwarp();
     if (lane < n)
         for (int j = 0; j < n; ++j) X[lane * n + j] = A[lane * n + j];
+    __syncwarp();
+    return true;
+}
+
+// FP64 Cholesky inverse of the 12x12 quadratic Hessian with two lanes per
+// row (lane & 15 = row, lane >> 4 = half): the Jacobi-scaled factorisation,
+// L^-1 and L^-T L^-1 of cholesky_inverse, with every row's j loops and
+// k sums split by parity between the two halves (partial sums combined by
+// one shuffle), so the warp issues about half the FP64 instructions.
+__device__ bool cholesky_inverse_split(double *A, double *X, double *d, int n, int lane) {
+    __shared__ double s_r[4][12];
+    double *rdiag = s_r[(threadIdx.x >> 5) & 3];
+    const int row = lane & 15, half = lane >> 4;
+    const bool mine = row < n;
+    bool ok = true;
+    if (mine && half == 0) {
+        const double aii = A[row * n + row];
+        ok = aii > 0.0;
+        d[row] = ok ? rsqrt(aii) : 0.0;
+    }
+    if (!__all_sync(kFullMask, ok)) return false;
+    __syncwarp();
+    if (mine)
+        for (int j = half; j < n; j += 2) A[row * n + j] = A[row * n + j] * d[row] * d[j];
+    __syncwarp();
+    for (int k = 0; k < n; ++k) {
+        const double pivot = A[k * n + k];
+        if (!__all_sync(kFullMask, pivot > 0.0)) return false;
+        __syncwarp();
+        const double r = rsqrt(pivot);
+        if (half == 0 && row == k) { A[k * n + k] = pivot * r; rdiag[k] = r; }
+        if (half == 0 && mine && row > k) A[row * n + k] = A[row * n + k] * r;
+        __syncwarp();
+        if (mine && row > k) {
+            const double lik = A[row * n + k];
+            for (int j = k + 1 + half; j <= row; j += 2) A[row * n + j] = A[row * n + j] - lik * A[j * n + k];
+        }
+        __syncwarp();
+    }
+    // L^-1, column `row`: X[i][row] = -(sum_k L[i][k] X[k][row]) / L[i][i]
+    if (mine && half == 0) {
+        for (int i = 0; i < n; ++i) X[i * n + row] = 0.0;
+        X[row * n + row] = rdiag[row];
+    }
+    __syncwarp();
+    for (int i = 1; i < n; ++i) {
+        double acc = 0.0;
+        if (mine && i > row)
+            for (int k = row + half; k < i; k += 2) acc = acc + A[i * n + k] * X[k * n + row];
+        acc = acc + __shfl_xor_sync(kFullMask, acc, 16);
+        if (mine && half == 0 && i > row) X[i * n + row] = -acc * rdiag[i];
+        __syncwarp();
+    }
+    // A^-1 = D L^-T L^-1 D; row `row`, columns split by parity, into A.
+    if (mine) {
+        for (int j = half; j < n; j += 2) {
+            const int k0 = row > j ? row : j;
+            double acc = 0.0;
+            for (int k = k0; k < n; ++k) acc = acc + X[k * n + row] * X[k * n + j];
+            A[row * n + j] = acc * d[row] * d[j];
+        }
+    }
+    __syncwarp();
+    if (mine)
+        for (int j = half; j < n; j += 2) X[row * n + j] = A[row * n + j];
     __syncwarp();
     return true;
 }
@@ -417,7 +501,9 @@ __global__ void __launch_bounds__(128) subset_prep_kernel(PrepArgs a) {
             }
         }
         __syncwarp();
-        const bool ok = cholesky_inverse<T>(A, X, s_d[warp], n, lane);
+        bool ok;
+        if constexpr (std::is_same<T, double>::value) ok = cholesky_inverse_split(A, X, s_d[warp], n, lane);
+        else ok = cholesky_inverse<T>(A, X, s_d[warp], n, lane);
         valid = valid && ok;
         if (ok) {
             bool finite = true;
