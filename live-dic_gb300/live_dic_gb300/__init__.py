@@ -11,6 +11,7 @@ from .full_pyramid_backend import DEFAULT_FULL_PYRAMID_LEVELS, ICGNWGPUFullPyram
 from .motion import AFFINE_PARAMETER_ORDER, MOTION_MODELS, QUADRATIC_PARAMETER_ORDER
 from .native_backend import DEFAULT_IN_FLIGHT_FRAMES, DEFAULT_PYRAMID_LEVELS, ICGNWGPU
 from .outlier import OUTLIER_POLICIES
+from .pair import BenchmarkResult, EngineInfo, register_pair
 
 SEEDED_SOLVE_API_VERSION = 1
 # GB300 names for the same engines (ICGNBatch has no reference counterpart).
@@ -19,9 +20,11 @@ ICGNCUDAFullPyramid = ICGNWGPUFullPyramid
 
 __all__ = [
     "AFFINE_PARAMETER_ORDER",
+    "BenchmarkResult",
     "DEFAULT_FULL_PYRAMID_LEVELS",
     "DEFAULT_IN_FLIGHT_FRAMES",
     "DEFAULT_PYRAMID_LEVELS",
+    "EngineInfo",
     "ICGNBatch",
     "ICGNCUDA",
     "ICGNCUDAFullPyramid",
@@ -36,4 +39,5 @@ __all__ = [
     "ReferenceInfo",
     "RegistrationResult",
     "SEEDED_SOLVE_API_VERSION",
+    "register_pair",
 ]

@@ -192,3 +192,16 @@ def test_selective_pyramid_recovery_of_failed_subsets():
     for r in streamed:
         np.testing.assert_array_equal(r.status, result.status)
         np.testing.assert_array_equal(r.parameters, result.parameters)
+
+
+def test_register_pair_one_shot(c0_pair):
+    from live_dic_gb300 import register_pair
+
+    ref, tgt = c0_pair
+    one = register_pair(ref, tgt, subset_size=21, subset_stride=10, pyramid_levels=2)
+    with ICGNWGPUFullPyramid(pyramid_levels=2, subset_size=21, subset_stride=10) as engine:
+        engine.set_reference(ref)
+        expected = engine.register(tgt)
+    np.testing.assert_array_equal(one.parameters, expected.parameters)
+    np.testing.assert_array_equal(one.status, expected.status)
+    assert (one.status >= 1).mean() > 0.9

@@ -291,3 +291,28 @@ def test_result_summary_matches_numpy_selection(model):
                                   float(np.mean(packed[..., 3][mask], dtype=np.float64)))
     assert r.mean_iterations == float(np.mean(packed[..., n + 1][mask], dtype=np.float64))
     assert np.shares_memory(r.parameters, packed)
+
+
+def test_package_exports_cover_the_reference_api():
+    """live_dic.__all__ (__init__.py:21-41) without the headless-browser engine."""
+    import live_dic_gb300
+
+    expected = {"BenchmarkResult", "AFFINE_PARAMETER_ORDER", "DEFAULT_IN_FLIGHT_FRAMES", "DEFAULT_FULL_PYRAMID_LEVELS",
+                "DEFAULT_PYRAMID_LEVELS", "EngineInfo", "ImageInput", "ICGNError", "ICGNWGPU",
+                "ICGNWGPUFullPyramid", "MOTION_MODELS", "OUTLIER_POLICIES", "PARAMETER_ORDER",
+                "QUADRATIC_PARAMETER_ORDER", "ReferenceInfo", "RegistrationResult", "SEEDED_SOLVE_API_VERSION",
+                "register_pair"}
+    assert expected <= set(live_dic_gb300.__all__)
+    assert live_dic_gb300.SEEDED_SOLVE_API_VERSION == 1
+
+
+def test_register_pair_argument_errors():
+    from live_dic_gb300 import ICGNError, register_pair
+
+    image = np.zeros((64, 64), np.uint8)
+    with pytest.raises(ValueError, match="ROI requires"):
+        register_pair(image, image, roi_mask=np.ones((64, 64), bool))
+    with pytest.raises(ValueError, match="ROI requires"):
+        register_pair(image, image, roi_policy="partial")
+    with pytest.raises(ICGNError, match="CUDA engine"):
+        register_pair(image, image, backend="regl")
