@@ -229,26 +229,15 @@ __device__ __forceinline__ void warp_compensated_sum(float &s, float &c) {
 // Warp-cooperative Cholesky inverse of an SPD n x n matrix held in shared
 // memory (row-major A), with Jacobi scaling d_i = 1/sqrt(A_ii).  On return
 // X holds A^-1; returns false if A is not numerically positive definite.
-// Reciprocal square root: the double path (12x12 quadratic Hessians, FP64
-// pipe-bound) uses rsqrt() so that each pivot costs one sequence and every
-// later division becomes a multiplication; the float path keeps sqrt and
-// IEEE division.
-template <typename T>
-__device__ __forceinline__ T recip_sqrt(T v) {
-    if constexpr (std::is_same<T, double>::value) return rsqrt(v);
-    else return T(1) / sqrt(v);
-}
-
+// Used for the FP32 6x6 Hessians; the FP64 12x12 quadratic ones go through
+// cholesky_inverse_split.
 template <typename T>
 __device__ bool cholesky_inverse(T *A, T *X, T *d, int n, int lane) {
-    constexpr bool kRecip = std::is_same<T, double>::value;
-    __shared__ T s_r[4][12];  // 1 / L_kk per warp (double path)
-    T *rdiag = s_r[(threadIdx.x >> 5) & 3];
     bool ok = true;
     if (lane < n) {
         const T aii = A[lane * n + lane];
         ok = aii > T(0);
-        d[lane] = ok ? recip_sqrt(aii) : T(0);
+        d[lane] = ok ? T(1) / sqrt(aii) : T(0);
     }
     ok = __all_sync(kFullMask, ok);
     if (!ok) return false;
@@ -260,16 +249,10 @@ __device__ bool cholesky_inverse(T *A, T *X, T *d, int n, int lane) {
         T pivot = A[k * n + k];
         ok = pivot > T(0);
         if (!__all_sync(kFullMask, ok)) return false;
+        const T lkk = sqrt(pivot);
         __syncwarp();
-        if (kRecip) {
-            const T r = recip_sqrt(pivot);
-            if (lane == k) { A[k * n + k] = pivot * r; rdiag[k] = r; }
-            if (lane > k && lane < n) A[lane * n + k] = A[lane * n + k] * r;
-        } else {
-            const T lkk = sqrt(pivot);
-            if (lane == k) A[k * n + k] = lkk;
-            if (lane > k && lane < n) A[lane * n + k] = A[lane * n + k] / lkk;
-        }
+        if (lane == k) A[k * n + k] = lkk;
+        if (lane > k && lane < n) A[lane * n + k] = A[lane * n + k] / lkk;
         __syncwarp();
         if (lane > k && lane < n) {
             const T lik = A[lane * n + k];
@@ -281,11 +264,11 @@ __device__ bool cholesky_inverse(T *A, T *X, T *d, int n, int lane) {
     if (lane < n) {
         const int j = lane;
         for (int i = 0; i < n; ++i) X[i * n + j] = T(0);
-        X[j * n + j] = kRecip ? rdiag[j] : T(1) / A[j * n + j];
+        X[j * n + j] = T(1) / A[j * n + j];
         for (int i = j + 1; i < n; ++i) {
             T acc = T(0);
             for (int k = j; k < i; ++k) acc = acc + A[i * n + k] * X[k * n + j];
-            X[i * n + j] = kRecip ? -acc * rdiag[i] : -acc / A[i * n + i];
+            X[i * n + j] = -acc / A[i * n + i];
         }
     }
     __syncwarp();
