@@ -93,6 +93,49 @@ __global__ void im2col_kernel(NnConvShape s, const __nv_bfloat16 *x, __nv_bfloat
     A[idx] = v;
 }
 
+// Vectorised im2col for C a multiple of 8: thread (m, q) writes the 16 bytes
+// A[m][8q .. 8q+7], which lie in one tap (ci0 = 8q mod C) and so come from
+// one 16-byte load of the input pixel, or are zero (padding tap or k >= 9 C).
+__global__ void im2col_vec_kernel(NnConvShape s, const uint4 *x, uint4 *A) {
+    const int chunks = s.Kp / 8;
+    const int rows = s.B * s.OH * s.OW;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= rows * chunks) return;
+    const int q = idx % chunks, m = idx / chunks;
+    const int k0 = 8 * q;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (k0 < 9 * s.C) {
+        const int tap = k0 / s.C, ci0 = k0 - tap * s.C, ky = tap / 3, kx = tap - 3 * ky;
+        const int ox = m % s.OW, t = m / s.OW, oy = t % s.OH, b = t / s.OH;
+        const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
+        if (iy >= 0 && iy < s.H && ix >= 0 && ix < s.W)
+            v = __ldg(x + ((((size_t)b * s.H + iy) * s.W + ix) * s.C + ci0) / 8);
+    }
+    A[idx] = v;
+}
+
+// im2col for the 2-channel input layer: one row (Kp bf16) per thread, each
+// tap's channel pair one 4-byte load, the row written as 16-byte stores.
+__global__ void im2col_c2_kernel(NnConvShape s, const uint32_t *x, uint4 *A) {
+    const int rows = s.B * s.OH * s.OW;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= rows) return;
+    const int ox = m % s.OW, t = m / s.OW, oy = t % s.OH, b = t / s.OH;
+    uint32_t w[12];
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
+        const int ky = tap / 3, kx = tap - 3 * ky;
+        const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
+        w[tap] = (iy >= 0 && iy < s.H && ix >= 0 && ix < s.W) ? __ldg(x + ((size_t)b * s.H + iy) * s.W + ix) : 0u;
+    }
+    w[9] = w[10] = w[11] = 0u;
+    uint4 *row = A + (size_t)m * (s.Kp / 8);
+    row[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    row[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    row[2] = make_uint4(w[8], w[9], w[10], w[11]);
+    for (int q = 3; q < s.Kp / 8; ++q) row[q] = make_uint4(0u, 0u, 0u, 0u);
+}
+
 // G[m][k] for input pixel m = (b, iy, ix) and k = (ky, kx, co) < 9 Cout: the
 // output gradient at (oy, ox) = ((iy + 1 - ky) / 2, (ix + 1 - kx) / 2) when
 // both are integral and inside the output, else zero.
@@ -109,6 +152,23 @@ __global__ void dgrad_gather_kernel(NnConvShape s, const __nv_bfloat16 *dz, __nv
     __nv_bfloat16 v = __float2bfloat16(0.0f);
     if (ty >= 0 && tx >= 0 && !(ty & 1) && !(tx & 1) && (ty >> 1) < s.OH && (tx >> 1) < s.OW)
         v = dz[(((size_t)b * s.OH + (ty >> 1)) * s.OW + (tx >> 1)) * s.Cout + co];
+    G[idx] = v;
+}
+
+// Vectorised dgrad_gather for Cout a multiple of 8: 16 bytes (8 output
+// channels of one tap) per thread.
+__global__ void dgrad_gather_vec_kernel(NnConvShape s, const uint4 *dz, uint4 *G) {
+    const int chunks = 9 * s.Cout / 8;
+    const int rows = s.B * s.H * s.W;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= rows * chunks) return;
+    const int q = idx % chunks, m = idx / chunks;
+    const int k0 = 8 * q, tap = k0 / s.Cout, co0 = k0 - tap * s.Cout, ky = tap / 3, kx = tap - 3 * ky;
+    const int ix = m % s.W, t = m / s.W, iy = t % s.H, b = t / s.H;
+    const int ty = iy + 1 - ky, tx = ix + 1 - kx;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (ty >= 0 && tx >= 0 && !(ty & 1) && !(tx & 1) && (ty >> 1) < s.OH && (tx >> 1) < s.OW)
+        v = __ldg(dz + ((((size_t)b * s.OH + (ty >> 1)) * s.OW + (tx >> 1)) * s.Cout + co0) / 8);
     G[idx] = v;
 }
 
@@ -270,12 +330,28 @@ cudaError_t launch_nn_patches(const NnPatchArgs &a, cudaStream_t s) {
 
 cudaError_t launch_nn_im2col(const NnConvShape &sh, const void *x, void *A, cudaStream_t s) {
     const long long n = (long long)sh.B * sh.OH * sh.OW * sh.Kp;
+    const bool aligned = (reinterpret_cast<uintptr_t>(x) & 15) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
+    if (sh.C % 8 == 0 && sh.Kp % 8 == 0 && aligned && n / 8 < (1ll << 31)) {
+        im2col_vec_kernel<<<blocks(n / 8, 256), 256, 0, s>>>(sh, static_cast<const uint4 *>(x), static_cast<uint4 *>(A));
+        return cudaGetLastError();
+    }
+    if (sh.C == 2 && sh.Kp % 8 == 0 && sh.Kp >= 24 && aligned && (long long)sh.B * sh.OH * sh.OW < (1ll << 31)) {
+        im2col_c2_kernel<<<blocks((long long)sh.B * sh.OH * sh.OW, 256), 256, 0, s>>>(
+            sh, static_cast<const uint32_t *>(x), static_cast<uint4 *>(A));
+        return cudaGetLastError();
+    }
     im2col_kernel<<<blocks(n, 256), 256, 0, s>>>(sh, static_cast<const __nv_bfloat16 *>(x), static_cast<__nv_bfloat16 *>(A));
     return cudaGetLastError();
 }
 
 cudaError_t launch_nn_dgrad_gather(const NnConvShape &sh, const void *dz, void *G, cudaStream_t s) {
     const long long n = (long long)sh.B * sh.H * sh.W * 9 * sh.Cout;
+    const bool aligned = (reinterpret_cast<uintptr_t>(dz) & 15) == 0 && (reinterpret_cast<uintptr_t>(G) & 15) == 0;
+    if (sh.Cout % 8 == 0 && aligned && n / 8 < (1ll << 31)) {
+        dgrad_gather_vec_kernel<<<blocks(n / 8, 256), 256, 0, s>>>(sh, static_cast<const uint4 *>(dz),
+                                                                    static_cast<uint4 *>(G));
+        return cudaGetLastError();
+    }
     dgrad_gather_kernel<<<blocks(n, 256), 256, 0, s>>>(sh, static_cast<const __nv_bfloat16 *>(dz),
                                                       static_cast<__nv_bfloat16 *>(G));
     return cudaGetLastError();

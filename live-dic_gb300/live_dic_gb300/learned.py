@@ -414,15 +414,20 @@ def predict(net: SeedNet, refs_ptrs, tgts_ptrs, image_index, centres, width: int
 # ---------------------------------------------------------------- inference
 class LearnedSeeder:
     """Learned-seed registration for one fixed reference on the single-scale
-    engine: network proposals on a subset lattice, seeded IC-GN, and ZNCC
-    reseeding of failed or low-ZNCC subsets."""
+    engine: the global translation by GPU phase correlation, network
+    proposals on a subset lattice (two passes with an affine consensus
+    between them), seeded IC-GN, and ZNCC reseeding of failed or low-ZNCC
+    subsets."""
 
-    def __init__(self, engine, net: SeedNet, *, step: int = 4, reseed_radius: int = 10, passes: int = 2) -> None:
+    def __init__(self, engine, net: SeedNet, *, step: int = 4, reseed_radius: int = 10, passes: int = 2,
+                 global_alignment: bool = True) -> None:
         torch = _torch()
         if not engine._reference_ready or engine.motion_model != "affine":
             raise ValueError("LearnedSeeder needs an affine engine with a prepared reference")
         self.engine, self.net, self.step, self.radius = engine, net, int(step), int(reseed_radius)
         self.passes = max(1, int(passes))
+        self.global_alignment = bool(global_alignment)
+        self.fourier = None
         self.lib = _native.load()
         dev = net.device
         W, H = engine.width, engine.height
@@ -463,10 +468,22 @@ class LearnedSeeder:
         self._handle = C.c_void_p(self.stream.cuda_stream)
 
     def set_reference_image(self, reference: np.ndarray) -> None:
-        """Half-resolution reference for the network (the engine keeps its own)."""
+        """Half-resolution reference for the network (the engine keeps its own),
+        and the GPU phase correlation that removes the global translation
+        before the first network pass."""
         torch = _torch()
+        from .fourier import FourierInitializer
+
         self._ref_full.copy_(torch.from_numpy(np.ascontiguousarray(reference, dtype=np.uint8)))
         _call(self.lib, "gbdic_reduce_half", _ptr(self._ref_full), self.W, self.H, _ptr(self.ref_half), None)
+        if self.fourier is not None:
+            self.fourier.close()
+        self.fourier = None
+        if self.global_alignment:
+            try:
+                self.fourier = FourierInitializer(np.asarray(reference), device=self.net.device.index or 0)
+            except ValueError:
+                self.fourier = None
 
     def propose(self, frame) -> None:
         """Network proposals for device frame `frame` (uint8 H x W) -> self.seeds
@@ -492,14 +509,16 @@ class LearnedSeeder:
             net.forward(stream)
             _native_copy(out, s0, net.out, n)  # on the current stream, ordered with `stream`
 
-    def consensus(self, translations: np.ndarray, *, trials: int = 128, tolerance: float = 3.0) -> np.ndarray:
+    def consensus(self, translations: np.ndarray, *, trials: int = 128, tolerances=(8.0, 6.0, 4.0, 3.0)) -> np.ndarray:
         """Affine field through the lattice translations (P x 2, px) by
-        random sample consensus: affine maps through random node triples, the
-        one agreeing (within `tolerance` px) with the most nodes wins and is
-        refitted by least squares on its inliers.  Out-of-range network
-        predictions are outliers; a global affine fit is what lets the next
-        pass displace every window, including those whose motion exceeded
-        the network's training range."""
+        random sample consensus.  Hypotheses are single-node translations
+        (which stay likely to be inliers when few predictions are right) and
+        affine maps through node triples; the one agreeing with the most
+        probe nodes within the first tolerance wins, and is refitted by least
+        squares on its inliers while the tolerance tightens.  Out-of-range
+        network predictions are outliers; a global affine fit is what lets
+        the next pass displace every window, including those whose motion
+        exceeded the network's training range."""
         xy = (self.node_xy - self.node_xy.mean(0)) / 1000.0
         A = np.concatenate([np.ones((len(xy), 1)), xy], 1)
         finite = np.isfinite(translations).all(1)
@@ -507,28 +526,26 @@ class LearnedSeeder:
         if idx.size < 3:
             return translations
         rng = np.random.default_rng(12345)
+        single = idx[rng.integers(0, idx.size, 2 * trials)]
+        hyp = [np.stack([translations[single], np.zeros((single.size, 2)), np.zeros((single.size, 2))], 1)]
         tri = idx[rng.integers(0, idx.size, (trials, 3))]
         sub = A[tri]                                               # trials x 3 x 3
         usable = np.abs(np.linalg.det(sub)) > 1e-9
-        if not usable.any():
-            return translations
-        coef = np.linalg.solve(sub[usable], translations[tri[usable]])   # k x 3 x 2
+        if usable.any():
+            hyp.append(np.linalg.solve(sub[usable], translations[tri[usable]]))   # k x 3 x 2
+        coef = np.concatenate(hyp, 0)
         # hypotheses are scored on at most 256 sampled nodes, the winner on all
         probe = idx if idx.size <= 256 else idx[rng.choice(idx.size, 256, replace=False)]
         x, y, t = xy[probe, 0][None], xy[probe, 1][None], translations[probe]
         du = coef[:, 0, 0:1] + coef[:, 1, 0:1] * x + coef[:, 2, 0:1] * y - t[None, :, 0]
         dv = coef[:, 0, 1:2] + coef[:, 1, 1:2] * x + coef[:, 2, 1:2] * y - t[None, :, 1]
-        winner = coef[int(np.argmax((np.hypot(du, dv) <= tolerance).sum(1)))]
-        d = A @ winner - translations
-        best = finite & (np.hypot(d[:, 0], d[:, 1]) <= tolerance)
-        if best.sum() < 3:
-            return translations
-        for _ in range(2):
-            fit_coef, *_ = np.linalg.lstsq(A[best], translations[best], rcond=None)
+        fit_coef = coef[int(np.argmax((np.hypot(du, dv) <= tolerances[0]).sum(1)))]
+        for tol in tolerances:
             d = A @ fit_coef - translations
-            best = finite & (np.hypot(d[:, 0], d[:, 1]) <= tolerance)
+            best = finite & (np.hypot(d[:, 0], d[:, 1]) <= tol)
             if best.sum() < 3:
                 break
+            fit_coef, *_ = np.linalg.lstsq(A[best], translations[best], rcond=None)
         return A @ fit_coef
 
     def _propose(self, frame, stream) -> None:
@@ -539,6 +556,20 @@ class LearnedSeeder:
         _call(self.lib, "gbdic_reduce_half", _ptr(frame), self.W, self.H, _ptr(self.tgt_half), stream)
         shift = None
         self.base_host[:] = 0.0
+        if self.fourier is not None:
+            # Global translation by phase correlation: the first pass then
+            # sees only the strain-induced residual, inside the network's
+            # training range even for translations beyond it.
+            self.stream.synchronize()
+            try:
+                est = self.fourier.estimate_device(frame.data_ptr(), self.W)
+            except (ValueError, ICGNError):
+                est = None
+            if est is not None:
+                self.base_host[:, 0] = est["dx"] / TRANSLATION_SCALE
+                self.base_host[:, 3] = est["dy"] / TRANSLATION_SCALE
+                self.base.copy_(torch.from_numpy(self.base_host), non_blocking=False)
+                shift = self.base
         for p in range(self.passes):
             self._network_pass(self.pred, shift, stream)
             if p == self.passes - 1:

@@ -184,3 +184,21 @@ def test_final_zncc_matches_oracle(pair):
     expected[expected < -1.0] = np.nan
     np.testing.assert_array_equal(result.zncc.ravel(), expected)
     assert np.nanmin(result.zncc[result.status == 1]) > 0.8
+
+
+@pytest.mark.parametrize("width,height", [(3840, 2160), (1920, 1080), (161, 143), (64, 18), (130, 35)])
+def test_reduce_half_bit_exact(width, height):
+    """Pyramid reduction (full_pyramid.wgsl reduce_fused, exact integer 5x5 / 256)."""
+    import torch
+
+    from live_dic_gb300 import _native
+
+    rng = np.random.default_rng(width * 7 + height)
+    img = rng.integers(0, 256, size=(height, width), dtype=np.uint8)
+    src = torch.from_numpy(img).cuda()
+    dst = torch.empty((height // 2, width // 2), dtype=torch.uint8, device="cuda")
+    lib = _native.load()
+    _native.check(lib.gbdic_reduce_half(src.data_ptr(), width, height, dst.data_ptr(), None),
+                  lib.gbdic_last_error(None))
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dst.cpu().numpy(), oracle_c.reduce(img))
