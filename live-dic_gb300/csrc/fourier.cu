@@ -89,9 +89,25 @@ __global__ void reduce_taper_kernel(const uint8_t *img, long long pitch, int x0,
     spectrum_in[i] = make_double2(reduced * taper[r] * taper[c], 0.0);
 }
 
+// Twiddle factors of an n-point transform, k < n/2: (cos, sin) of
+// sign * 2 pi k / n for sign -1 (forward, first half) and +1 (inverse).
+// Stage s of the transform uses entry pos * (n / 2^s), whose argument
+// sign * 2 * pos / 2^s is the same double, so the factors equal a per-stage
+// sincospi() bit for bit.
+__global__ void twiddle_kernel(double2 *tw, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n / 2) return;
+    double sn, cs;
+    sincospi(-1.0 * 2.0 * (double)k / (double)n, &sn, &cs);
+    tw[k] = make_double2(cs, sn);
+    sincospi(1.0 * 2.0 * (double)k / (double)n, &sn, &cs);
+    tw[n / 2 + k] = make_double2(cs, sn);
+}
+
 // In-place radix-2 transform of `lines` lines of n points: element k of line
-// l at data[l * dist + k * step]; sign -1 forward, +1 inverse (unscaled).
-__global__ void fft_lines_kernel(double2 *data, int n, int logn, long long step, long long dist, double sign) {
+// l at data[l * dist + k * step]; twiddles from `tw` (the forward or inverse
+// half of the table), unscaled.
+__global__ void fft_lines_kernel(double2 *data, int n, int logn, long long step, long long dist, const double2 *tw) {
     extern __shared__ double2 line[];
     double2 *base = data + (size_t)blockIdx.x * dist;
     for (int k = threadIdx.x; k < n; k += blockDim.x) line[__brev((unsigned)k) >> (32 - logn)] = base[(size_t)k * step];
@@ -100,9 +116,7 @@ __global__ void fft_lines_kernel(double2 *data, int n, int logn, long long step,
         const int m = 1 << s, h = m >> 1;
         for (int j = threadIdx.x; j < n / 2; j += blockDim.x) {
             const int pos = j & (h - 1), i0 = (j >> (s - 1)) * m + pos, i1 = i0 + h;
-            double sn, cs;
-            sincospi(sign * 2.0 * (double)pos / (double)m, &sn, &cs);
-            const double2 t = cmul(make_double2(cs, sn), line[i1]), u = line[i0];
+            const double2 t = cmul(__ldg(tw + (pos << (logn - s))), line[i1]), u = line[i0];
             line[i0] = make_double2(u.x + t.x, u.y + t.y);
             line[i1] = make_double2(u.x - t.x, u.y - t.y);
         }
@@ -120,21 +134,25 @@ __global__ void cross_power_kernel(double2 *cur, const double2 *ref, int count) 
     cur[i] = make_double2(c.x / m, c.y / m);
 }
 
-// One CTA: first maximum of the correlation (real part / n^2), the sums of
-// all values and of their squares, then of the wrapped 11 x 11 block.
-__global__ void __launch_bounds__(1024) peak_kernel(const double2 *corr, int size, double *out) {
+// Stage 1 of the peak search over the correlation (real part / n^2): per CTA
+// the first maximum (lowest index on ties) and the sums of the values and
+// of their squares.
+constexpr int kPeakCtas = 128, kPeakThreads = 256;
+
+__global__ void __launch_bounds__(kPeakThreads) peak_partial_kernel(const double2 *corr, int size, double *pbest,
+                                                                     int *pidx, double *psum, double *psq) {
     const int n = size * size;
     const double scale = 1.0 / (double)n;
     double best = -1e300, s = 0.0, q = 0.0;
     int best_i = 0x7fffffff;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double v = corr[i].x * scale;
         s += v;
         q += v * v;
         if (v > best) { best = v; best_i = i; }
     }
-    __shared__ double sb[1024], ss[1024], sq[1024];
-    __shared__ int si[1024];
+    __shared__ double sb[kPeakThreads], ss[kPeakThreads], sq[kPeakThreads];
+    __shared__ int si[kPeakThreads];
     sb[threadIdx.x] = best; si[threadIdx.x] = best_i; ss[threadIdx.x] = s; sq[threadIdx.x] = q;
     __syncthreads();
     for (int off = blockDim.x / 2; off > 0; off >>= 1) {
@@ -151,6 +169,40 @@ __global__ void __launch_bounds__(1024) peak_kernel(const double2 *corr, int siz
         __syncthreads();
     }
     if (threadIdx.x == 0) {
+        pbest[blockIdx.x] = sb[0];
+        pidx[blockIdx.x] = si[0];
+        psum[blockIdx.x] = ss[0];
+        psq[blockIdx.x] = sq[0];
+    }
+}
+
+// Stage 2 (one CTA): combine the partials in a fixed order, then the mean
+// and deviation of the correlation outside the wrapped 11 x 11 block
+// around the peak.
+__global__ void __launch_bounds__(kPeakCtas) peak_final_kernel(const double2 *corr, int size, const double *pbest,
+                                                                const int *pidx, const double *psum,
+                                                                const double *psq, double *out) {
+    __shared__ double sb[kPeakCtas], ss[kPeakCtas], sq[kPeakCtas];
+    __shared__ int si[kPeakCtas];
+    sb[threadIdx.x] = pbest[threadIdx.x]; si[threadIdx.x] = pidx[threadIdx.x];
+    ss[threadIdx.x] = psum[threadIdx.x]; sq[threadIdx.x] = psq[threadIdx.x];
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) {
+            const double b2 = sb[threadIdx.x + off];
+            const int i2 = si[threadIdx.x + off];
+            if (b2 > sb[threadIdx.x] || (b2 == sb[threadIdx.x] && i2 < si[threadIdx.x])) {
+                sb[threadIdx.x] = b2;
+                si[threadIdx.x] = i2;
+            }
+            ss[threadIdx.x] += ss[threadIdx.x + off];
+            sq[threadIdx.x] += sq[threadIdx.x + off];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int n = size * size;
+        const double scale = 1.0 / (double)n;
         const int py = si[0] / size, px = si[0] % size;
         double bs = 0.0, bq = 0.0;
         for (int dy = -5; dy <= 5; ++dy)
@@ -172,21 +224,37 @@ __global__ void __launch_bounds__(1024) peak_kernel(const double2 *corr, int siz
 }
 
 // Normalised correlation of reference and current reduced samples over the
-// overlap for shift (sx, sy) in samples, allowed reference samples only.
-__global__ void __launch_bounds__(512) overlap_corr_kernel(const double *ref, const uint8_t *allowed,
-                                                            const double *cur, int half, int sx, int sy, double *out) {
+// overlap for shift (sx, sy) in samples, allowed reference samples only:
+// per-CTA partial sums (stage 1), combined in a fixed order (stage 2).
+constexpr int kCorrCtas = 64, kCorrThreads = 256;
+
+__global__ void __launch_bounds__(kCorrThreads) overlap_partial_kernel(const double *ref, const uint8_t *allowed,
+                                                                        const double *cur, int half, int sx, int sy,
+                                                                        double *partial) {
     const int y0 = max(0, -sy), y1 = min(half, half - sy), x0 = max(0, -sx), x1 = min(half, half - sx);
     const int w = max(0, x1 - x0), h = max(0, y1 - y0);
     double sa = 0, sb = 0, sab = 0, saa = 0, sbb = 0, n = 0;
-    for (int i = threadIdx.x; i < w * h; i += blockDim.x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w * h; i += gridDim.x * blockDim.x) {
         const int r = y0 + i / w, c = x0 + i % w;
         if (!allowed[r * half + c]) continue;
         const double a = ref[r * half + c], b = cur[(r + sy) * half + (c + sx)];
         sa += a; sb += b; sab += a * b; saa += a * a; sbb += b * b; n += 1.0;
     }
-    __shared__ double red[6][512];
+    __shared__ double red[6][kCorrThreads];
     const double v[6] = {sa, sb, sab, saa, sbb, n};
     for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off)
+            for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) partial[threadIdx.x * kCorrCtas + blockIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(kCorrCtas) overlap_final_kernel(const double *partial, double *out) {
+    __shared__ double red[6][kCorrCtas];
+    for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = partial[k * kCorrCtas + threadIdx.x];
     __syncthreads();
     for (int off = blockDim.x / 2; off > 0; off >>= 1) {
         if (threadIdx.x < off)
@@ -221,7 +289,7 @@ struct gbdic_fourier {
     int device = 0, size = 0, half = 0, logn = 0;
     cudaStream_t stream = nullptr;
     gbdic::DeviceBuffer window, allowed, taper, ref_spectrum, ref_samples, allowed_samples, cur_samples, work, sums,
-        result;
+        result, twiddle, partials;
     gbdic::HostBuffer host_window, host_result;
     std::string error;
     ~gbdic_fourier() {
@@ -236,9 +304,10 @@ struct gbdic_fourier {
         const size_t smem = (size_t)n * sizeof(double2);
         const int threads = n / 2 < 512 ? n / 2 : 512;
         double2 *d = work.as<double2>();
-        fft_lines_kernel<<<n, threads, smem, stream>>>(d, n, logn, 1, n, sign);  // rows
+        const double2 *tw = twiddle.as<double2>() + (sign < 0.0 ? 0 : n / 2);
+        fft_lines_kernel<<<n, threads, smem, stream>>>(d, n, logn, 1, n, tw);  // rows
         check_cuda(cudaGetLastError(), "FFT rows");
-        fft_lines_kernel<<<n, threads, smem, stream>>>(d, n, logn, n, 1, sign);  // columns
+        fft_lines_kernel<<<n, threads, smem, stream>>>(d, n, logn, n, 1, tw);  // columns
         check_cuda(cudaGetLastError(), "FFT columns");
     }
     // window bytes (device, dense size x size) -> work (spectrum), samples
@@ -311,8 +380,12 @@ int gbdic_fourier_create(int32_t device, const uint8_t *window, const uint8_t *a
         f->allowed_samples.ensure(hpx);
         f->sums.ensure(3 * sizeof(unsigned long long));
         f->result.ensure(8 * sizeof(double));
+        f->twiddle.ensure((size_t)size * sizeof(double2));
+        f->partials.ensure((size_t)(4 * kPeakCtas + 6 * kCorrCtas) * sizeof(double));
         f->host_window.ensure(px);
         f->host_result.ensure(8 * sizeof(double));
+        twiddle_kernel<<<(size / 2 + 255) / 256, 256, 0, f->stream>>>(f->twiddle.as<double2>(), size);
+        check_cuda(cudaGetLastError(), "twiddles");
         // Hann taper of `half` points: 0.5 - 0.5 cos(2 pi k / (half - 1)).
         std::vector<double> taper((size_t)f->half);
         const double pi = 3.14159265358979323846;
@@ -364,7 +437,15 @@ int gbdic_fourier_estimate(gbdic_fourier *f, const uint8_t *frame, int64_t row_s
                                                                       count);
         check_cuda(cudaGetLastError(), "cross power");
         f->transform(+1.0);
-        peak_kernel<<<1, 1024, 0, f->stream>>>(f->work.as<double2>(), n, f->result.as<double>());
+        double *pb = f->partials.as<double>();
+        peak_partial_kernel<<<kPeakCtas, kPeakThreads, 0, f->stream>>>(
+            f->work.as<double2>(), n, pb, reinterpret_cast<int *>(pb + kPeakCtas), pb + 2 * kPeakCtas,
+            pb + 3 * kPeakCtas);
+        check_cuda(cudaGetLastError(), "peak");
+        peak_final_kernel<<<1, kPeakCtas, 0, f->stream>>>(f->work.as<double2>(), n, pb,
+                                                          reinterpret_cast<const int *>(pb + kPeakCtas),
+                                                          pb + 2 * kPeakCtas, pb + 3 * kPeakCtas,
+                                                          f->result.as<double>());
         check_cuda(cudaGetLastError(), "peak");
         check_cuda(cudaMemcpyAsync(f->host_result.as<double>(), f->result.get(), 5 * sizeof(double), cudaMemcpyDeviceToHost,
                                    f->stream), "peak readback");
@@ -378,9 +459,12 @@ int gbdic_fourier_estimate(gbdic_fourier *f, const uint8_t *frame, int64_t row_s
         const int half = f->half;
         const int px = (int)r[1], py = (int)r[2];
         const int dx = 2 * (px < half ? px : px - n), dy = 2 * (py < half ? py : py - n);
-        overlap_corr_kernel<<<1, 512, 0, f->stream>>>(f->ref_samples.as<double>(), f->allowed_samples.as<uint8_t>(),
-                                                       f->cur_samples.as<double>(), half, dx / 2, dy / 2,
-                                                       f->result.as<double>());
+        double *pc = f->partials.as<double>() + 4 * kPeakCtas;
+        overlap_partial_kernel<<<kCorrCtas, kCorrThreads, 0, f->stream>>>(
+            f->ref_samples.as<double>(), f->allowed_samples.as<uint8_t>(), f->cur_samples.as<double>(), half, dx / 2,
+            dy / 2, pc);
+        check_cuda(cudaGetLastError(), "overlap correlation");
+        overlap_final_kernel<<<1, kCorrCtas, 0, f->stream>>>(pc, f->result.as<double>());
         check_cuda(cudaGetLastError(), "overlap correlation");
         check_cuda(cudaMemcpyAsync(f->host_result.as<double>() + 5, f->result.as<double>() + 5, sizeof(double),
                                    cudaMemcpyDeviceToHost, f->stream), "correlation readback");
