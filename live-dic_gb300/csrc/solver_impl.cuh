@@ -434,7 +434,11 @@ __device__ __forceinline__ float2 sample_bspline_pair(const float *__restrict__ 
     bspline_weights2(fma2(make_float2(fya, fyb), m1, py), wy);
     const int bxa = (int)fxa, bxb = (int)fxb, bya = (int)fya, byb = (int)fyb;
     float2 value = pair(0.0f);
-    if (CLAMP) {
+    // Clamping changes a tap only when a footprint reaches the plane border;
+    // footprints inside take the unclamped addressing below (same taps).
+    const bool border = CLAMP && (min(bxa, bxb) < 1 || max(bxa, bxb) > W - 3 || min(bya, byb) < 1 ||
+                                  max(bya, byb) > H - 3);
+    if (border) {
         // Every tap index clamped to the plane, as sample_target<.., true>.
         int xa[4], xb[4];
 #pragma unroll
