@@ -65,6 +65,10 @@ struct gbdic_pyramid {
     gbdic::DeviceBuffer coarse_history, coarse_ages;  // temporal fine correction
     gbdic::DeviceBuffer fine_links;                   // adaptive: projection onto the finest grid
     int active_levels = 0;                            // levels the next frames run
+    // Side stream and events of the prefilter branch: the finer levels'
+    // B-spline prefilters run beside the reductions and coarse solves.
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, reduced_ev[4] = {}, filtered_ev[4] = {};
     std::vector<PyramidSlot> slots;
     bool ready = false;
     std::string error;
@@ -75,6 +79,15 @@ struct gbdic_pyramid {
             cudaSetDevice(device);
             cudaStreamSynchronize(rt->stream());
         }
+        if (side) {
+            cudaStreamSynchronize(side);
+            cudaStreamDestroy(side);
+        }
+        if (fork_ev) cudaEventDestroy(fork_ev);
+        for (auto &e : reduced_ev)
+            if (e) cudaEventDestroy(e);
+        for (auto &e : filtered_ev)
+            if (e) cudaEventDestroy(e);
         for (auto &s : slots) s.destroy();
         levels.clear();
     }
@@ -151,12 +164,28 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
     const int model = p->po.base.motion_model;
     const bool median = p->po.base.outlier_policy == GBDIC_OUTLIER_MEDIAN;
     auto &ps = p->slots[k];
+    // Levels 0 .. L-2 are prefiltered on the side stream (frame 0 as soon as
+    // it is resident, level l after its reduction); each seeded solve waits
+    // for its level's prefilter.  The coarsest level stays on `s`.
+    const bool branch = L > 1 && p->rt->opts().o.interpolation == GBDIC_INTERP_BSPLINE;
+    if (branch) {
+        check_cuda(cudaEventRecord(p->fork_ev, s), "fork");
+        check_cuda(cudaStreamWaitEvent(p->side, p->fork_ev, 0), "fork");
+        rt.enqueue_prefilter(*p->levels[0], *p->levels[0]->slots[k], frame0, p->side);
+        check_cuda(cudaEventRecord(p->filtered_ev[0], p->side), "prefilter event");
+    }
     const uint8_t *prev = frame0;
     for (int l = 1; l < L; ++l) {
         auto &lvl = *p->levels[l];
         auto &src = *p->levels[l - 1];
         check_cuda(gbdic::launch_reduce_half(prev, src.W, src.H, lvl.slots[k]->frame.as<uint8_t>(), s), "reduce launch");
         prev = lvl.slots[k]->frame.as<uint8_t>();
+        if (branch && l < L - 1) {
+            check_cuda(cudaEventRecord(p->reduced_ev[l], s), "reduce event");
+            check_cuda(cudaStreamWaitEvent(p->side, p->reduced_ev[l], 0), "reduce event");
+            rt.enqueue_prefilter(lvl, *lvl.slots[k], nullptr, p->side);
+            check_cuda(cudaEventRecord(p->filtered_ev[l], p->side), "prefilter event");
+        }
     }
     check_cuda(cudaMemsetAsync(ps.counters.get(), 0, 4 * sizeof(uint32_t), s), "counter reset");
     const int c = L - 1;
@@ -253,7 +282,8 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
             check_cuda(gbdic::launch_refine_temporal_seed(r, s), "temporal correction launch");
         }
         const uint8_t *f = l == 0 ? frame0 : nullptr;
-        rt.enqueue_prefilter(lvl, slot, f, s);
+        if (branch) check_cuda(cudaStreamWaitEvent(s, p->filtered_ev[l], 0), "prefilter join");
+        else rt.enqueue_prefilter(lvl, slot, f, s);
         rt.enqueue_solve(lvl, slot, p->cfg_of(l), true, false, f, nullptr, s);
         rt.enqueue_uod(lvl, slot, median && l > 0, nullptr, s);
     }
@@ -378,6 +408,12 @@ int gbdic_pyramid_create(const gbdic_pyramid_options *options, gbdic_pyramid **o
         p->po = po;
         p->device = po.base.device;
         p->rt = std::make_unique<gbdic::Runtime>(po.base);
+        check_cuda(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking), "stream");
+        check_cuda(cudaEventCreateWithFlags(&p->fork_ev, cudaEventDisableTiming), "event");
+        for (int l = 0; l < 4; ++l) {
+            check_cuda(cudaEventCreateWithFlags(&p->reduced_ev[l], cudaEventDisableTiming), "event");
+            check_cuda(cudaEventCreateWithFlags(&p->filtered_ev[l], cudaEventDisableTiming), "event");
+        }
         p->slots = std::vector<PyramidSlot>(po.base.pipeline_slots);
         for (auto &s : p->slots) s.create();
     } catch (const Failure &x) {
