@@ -2,13 +2,13 @@
 // 11-candidate translation scorer `choose`, shaders/spatial_seed.wgsl:65-190;
 // an exhaustive search is new here).
 //
-// One CTA (4 warps) per subset.  The subset's reference bytes (S x S) and the
-// target tile covering every candidate shift ((S + 2R)^2 bytes) are staged in
-// shared memory.  Warp w scans candidates w, w+4, ... of the (2R+1)^2 integer
-// shifts in row-major (dy, dx) order; for each, the lanes accumulate the five
-// correlation sums sum f, sum g, sum f^2, sum g^2, sum f g over lane-strided
-// pixels and combine them with warp shuffles.  The sums are exact integers
-// (8-bit inputs), so the result does not depend on the reduction order; ZNCC
+// One CTA (128 threads) per subset.  The subset's reference bytes (S x S) and
+// the target tile covering every candidate shift ((S + 2R)^2 bytes) are
+// staged in shared memory, 4 bytes per word.  Thread t scores candidates t,
+// t+128, ... of the (2R+1)^2 integer shifts in row-major (dy, dx) order: the
+// five correlation sums sum f, sum g, sum f^2, sum g^2, sum f g come from
+// 4-pixel DP4A dot products of packed bytes.  The sums are exact integers
+// (8-bit inputs), so the result does not depend on the summation order; ZNCC
 // is evaluated in binary64 from the exact sums,
 //   (n Sfg - Sf Sg) / sqrt((n Sff - Sf^2) (n Sgg - Sg^2)),
 // and the best candidate (lowest index on ties) becomes a translation seed.
@@ -23,8 +23,15 @@ namespace gbdic {
 
 namespace {
 
+// Shared layout: the subset's reference rows packed 4 bytes per word and
+// zero-padded to RW = ceil(S / 4) words; the target tile (T = S + 2R rows)
+// with rows of TW = ceil(T / 4) + 1 words (one spare word so that an
+// unaligned 4-byte window never reads past its row).
+__host__ __device__ inline int ref_words(int S) { return (S + 3) / 4; }
+__host__ __device__ inline int tile_words(int S, int R) { return (S + 2 * R + 3) / 4 + 1; }
+
 __global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
-    extern __shared__ uint8_t smem[];
+    extern __shared__ uint32_t smem_words[];
     const int idx = blockIdx.x;
     if (idx >= a.count) return;
     const int ss = state_stride(a.model), sat = status_slot(a.model);
@@ -42,9 +49,9 @@ __global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
     }
     const int px0 = (idx % a.grid_w) * a.stride + cx0, py0 = (idx / a.grid_w) * a.stride + cy0;
     const int rx0 = (idx % a.grid_w) * a.stride, ry0 = (idx / a.grid_w) * a.stride;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    __shared__ double s_best[4];
-    __shared__ int s_cand[4];
+    const int tid = threadIdx.x;
+    __shared__ double s_best[128];
+    __shared__ int s_cand[128];
     if (!selected) {
         if (!a.only_missing && tid == 0) {
             for (int k = 0; k < ss; ++k) seed[k] = 0.0f;
@@ -53,74 +60,85 @@ __global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
         }
         return;
     }
-    uint8_t *ref = smem;
-    uint8_t *tile = smem + S * S;
-    for (int i = tid; i < S * S; i += blockDim.x) {
-        const int col = i % S, row = i / S;
-        ref[i] = a.ref[(size_t)(ry0 + row) * a.W + rx0 + col];
+    const int RW = ref_words(S), TW = tile_words(S, R);
+    uint32_t *ref = smem_words;               // S x RW
+    uint32_t *tile = smem_words + S * RW;     // T x TW
+    for (int i = tid; i < S * RW; i += blockDim.x) {
+        const int row = i / RW, w = i - row * RW;
+        uint32_t v = 0u;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int col = 4 * w + b;
+            if (col < S) v |= (uint32_t)a.ref[(size_t)(ry0 + row) * a.W + rx0 + col] << (8 * b);
+        }
+        ref[i] = v;
     }
-    for (int i = tid; i < T * T; i += blockDim.x) {
-        const int col = i % T, row = i / T;
-        const int x = clampi(px0 - R + col, 0, a.W - 1), y = clampi(py0 - R + row, 0, a.H - 1);
-        tile[i] = a.tgt[(size_t)y * a.W + x];
+    for (int i = tid; i < T * TW; i += blockDim.x) {
+        const int row = i / TW, w = i - row * TW;
+        const int y = clampi(py0 - R + row, 0, a.H - 1);
+        uint32_t v = 0u;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int col = 4 * w + b;
+            if (col < T) v |= (uint32_t)a.tgt[(size_t)y * a.W + clampi(px0 - R + col, 0, a.W - 1)] << (8 * b);
+        }
+        tile[i] = v;
     }
     __syncthreads();
-    // reference sums (exact)
-    long long sf = 0, sff = 0;
-    for (int p = lane; p < S * S; p += 32) {
-        const int f = ref[p];
-        sf += f;
-        sff += f * f;
-    }
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) {
-        sf += __shfl_xor_sync(kFullMask, sf, off);
-        sff += __shfl_xor_sync(kFullMask, sff, off);
+    // Reference sums (exact): sum f and sum f^2 over the packed words.
+    unsigned sf = 0u, sff = 0u;  // unsigned bytes: the u32 DP4A form
+    for (int i = 0; i < S * RW; ++i) {
+        const uint32_t f4 = ref[i];
+        sf = __dp4a(f4, 0x01010101u, sf);
+        sff = __dp4a(f4, f4, sff);
     }
     const long long n = (long long)S * S;
-    const long long vf = n * sff - sf * sf;
+    const long long vf = n * (long long)sff - (long long)sf * (long long)sf;
+    // Byte mask of the last word of a window row (columns beyond S).
+    const int tail = S - 4 * (RW - 1);
+    const uint32_t last_mask = tail >= 4 ? 0xffffffffu : (0xffffffffu >> (8 * (4 - tail)));
+    // One candidate per thread: candidates tid, tid + 128, ... in row-major
+    // (dy, dx) order; the window's 4-byte groups are funnel-shifted out of
+    // the tile words and summed with DP4A (exact 32-bit integer sums).
     double best = -3.0;
     int best_cand = -1;
-    for (int cand = warp; cand < C; cand += 4) {
+    for (int cand = tid; cand < C; cand += blockDim.x) {
         const int dy = cand / side - R, dx = cand % side - R;
         if (px0 + dx < 0 || py0 + dy < 0 || px0 + dx + S - 1 > a.W - 1 || py0 + dy + S - 1 > a.H - 1) continue;
-        int sg = 0, sgg = 0, sfg = 0;
-        for (int p = lane; p < S * S; p += 32) {
-            const int col = p % S, row = p / S;
-            const int g = tile[(row + R + dy) * T + col + R + dx];
-            const int f = ref[p];
-            sg += g;
-            sgg += g * g;
-            sfg += f * g;
+        const int c0 = R + dx, shift = 8 * (c0 & 3), w0 = c0 >> 2;
+        unsigned sg = 0u, sgg = 0u, sfg = 0u;
+        for (int row = 0; row < S; ++row) {
+            const uint32_t *trow = tile + (row + R + dy) * TW + w0;
+            const uint32_t *frow = ref + row * RW;
+            for (int w = 0; w < RW; ++w) {
+                uint32_t g4 = __funnelshift_r(trow[w], trow[w + 1], shift);
+                if (w == RW - 1) g4 &= last_mask;
+                const uint32_t f4 = frow[w];
+                sg = __dp4a(g4, 0x01010101u, sg);
+                sgg = __dp4a(g4, g4, sgg);
+                sfg = __dp4a(f4, g4, sfg);
+            }
         }
-        long long lg = sg, lgg = sgg, lfg = sfg;
-#pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) {
-            lg += __shfl_xor_sync(kFullMask, lg, off);
-            lgg += __shfl_xor_sync(kFullMask, lgg, off);
-            lfg += __shfl_xor_sync(kFullMask, lfg, off);
-        }
-        const long long vg = n * lgg - lg * lg;
+        const long long vg = n * (long long)sgg - (long long)sg * (long long)sg;
         double score = -2.0;
-        if (vf > 0 && vg > 0) score = (double)(n * lfg - sf * lg) / sqrt((double)vf * (double)vg);
+        if (vf > 0 && vg > 0)
+            score = (double)(n * (long long)sfg - (long long)sf * (long long)sg) / sqrt((double)vf * (double)vg);
         if (score > best) {
             best = score;
             best_cand = cand;
         }
     }
-    if (lane == 0) {
-        s_best[warp] = best;
-        s_cand[warp] = best_cand;
-    }
+    s_best[tid] = best;
+    s_cand[tid] = best_cand;
     __syncthreads();
     if (tid == 0) {
         double b = -3.0;
         int c = -1;
-        for (int w = 0; w < 4; ++w) {
-            if (s_cand[w] < 0) continue;
-            if (s_best[w] > b || (s_best[w] == b && s_cand[w] < c)) {
-                b = s_best[w];
-                c = s_cand[w];
+        for (int t = 0; t < (int)blockDim.x; ++t) {
+            if (s_cand[t] < 0) continue;
+            if (s_best[t] > b || (s_best[t] == b && s_cand[t] < c)) {
+                b = s_best[t];
+                c = s_cand[t];
             }
         }
         for (int k = 0; k < ss; ++k) seed[k] = 0.0f;
@@ -138,7 +156,7 @@ __global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
 
 size_t zncc_search_smem(int S, int radius) {
     const size_t T = (size_t)S + 2 * (size_t)radius;
-    return (size_t)S * S + T * T;
+    return ((size_t)S * ref_words(S) + T * tile_words(S, radius)) * sizeof(uint32_t);
 }
 
 cudaError_t launch_zncc_search(const SearchArgs &a, cudaStream_t stream) {
