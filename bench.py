@@ -65,7 +65,7 @@ def parse_args() -> argparse.Namespace:
                          "learned: learned-seed vs pyramid+ZNCC seeding on large-translation UHD frames")
     ap.add_argument("--train-images", type=int, default=512, help="learned workload: training images (320x320)")
     ap.add_argument("--train-steps", type=int, default=8000, help="learned workload: Adam steps (batch 512)")
-    ap.add_argument("--lattice", type=int, default=8, help="learned workload: network on every n-th subset")
+    ap.add_argument("--lattice", type=int, default=16, help="learned workload: network on every n-th subset")
     ap.add_argument("--plain-radius", type=int, default=18,
                     help="learned workload: ZNCC search radius of the plain path at the coarsest level")
     ap.add_argument("--pairs", type=int, default=16, help="batch workload: number of image pairs")
@@ -522,8 +522,10 @@ def run_learned_workload(args) -> None:
     subset 31 / step 8.  Plain method: 3-level GPU pyramid with the integer
     ZNCC seed search at the coarsest level, IC-GN at every level.  Learned
     method: the seed network (trained here on engine-generated pairs) on a
-    lattice of subsets, seeded IC-GN at full resolution, failed or low-ZNCC
-    subsets reseeded by the ZNCC search and solved again."""
+    lattice of subsets after a GPU phase correlation, IC-GN at the lattice
+    nodes, every subset seeded from the node warps and solved at full
+    resolution with the plain path's finest-level settings, failed or
+    low-ZNCC subsets reseeded by the ZNCC search and solved again."""
     import torch
 
     from live_dic_gb300 import ICGNWGPU, ICGNWGPUFullPyramid, learned, synthetic
@@ -571,7 +573,7 @@ def run_learned_workload(args) -> None:
         return (float((ok & inside).sum() / inside.sum()), float(np.sqrt(np.mean(err[good] ** 2))),
                 float(1.0 - good.mean()) if err.size else 0.0)
 
-    def run(step_fn, gh, gw):
+    def run(step_fn, gh, gw, after=None):
         for k in range(args.warmup):
             step_fn(k)
         torch.cuda.synchronize()
@@ -582,6 +584,8 @@ def run_learned_workload(args) -> None:
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t1)
             acc.append(score(state, k, gh, gw))
+            if after is not None:
+                after(k)
         return times, acc
 
     with ClockSampler(local) as clocks:
@@ -600,19 +604,25 @@ def run_learned_workload(args) -> None:
             return pstate
 
         plain_times, plain_acc = run(plain_step, gh, gw)
+        plain_schedule = (plain.iterations_per_level[-1], plain.tolerance_per_level[-1])
         plain.close()
         # learned
+        # the same IC-GN settings as the plain path's full-resolution level
+        fine_iterations, fine_tolerance = plain_schedule
         engine = ICGNWGPU(subset_size=S, subset_stride=st, device=local, solver_workgroup_size=args.lanes)
-        engine.set_reference(ref)
+        engine.set_reference(ref, iterations=fine_iterations, tolerance=fine_tolerance)
         seeder = learned.LearnedSeeder(engine, net, step=args.lattice)
         seeder.set_reference_image(ref)
         reseeded = []
 
         def learned_step(k):
-            reseeded.append(seeder.register_device(frames[k])["reseeded"])
+            seeder.register_device(frames[k], counts=False)
             return seeder.state
 
-        learned_times, learned_acc = run(learned_step, engine.grid_height, engine.grid_width)
+        def learned_count(k):
+            reseeded.append(int(seeder.reseed_count.item()))
+
+        learned_times, learned_acc = run(learned_step, engine.grid_height, engine.grid_width, learned_count)
         engine.close()
     if rank != 0:
         return
@@ -632,9 +642,12 @@ def run_learned_workload(args) -> None:
         "dtype": "f32 solver, bf16 network (fp32 accumulate)",
         "data": "synthetic",
         "config": {"workload": f"{W}x{H}, S{S}/s{st}, rigid translation 15-30 px + uniform strain within 2 % about "
-                               f"the frame centre, network on every {args.lattice}-th subset (2 passes, affine "
-                               f"consensus), plain = 3-level pyramid + ZNCC search radius {args.plain_radius} at "
-                               "the coarsest level",
+                               f"the frame centre, network on every {args.lattice}-th subset (Fourier global "
+                               f"shift, 2 passes with an affine consensus), IC-GN at the lattice nodes, interpolated "
+                               f"seeds for every subset, IC-GN ({plain_schedule[0]} iterations, tolerance "
+                               f"{plain_schedule[1]:g} as the plain path's finest level), ZNCC reseeding of failures; "
+                               f"plain = 3-level pyramid + ZNCC search radius {args.plain_radius} at the coarsest "
+                               "level",
                    "train_pairs": data.size, "train_images": args.train_images, "train_steps": args.train_steps,
                    "train_batch": 512, "pair_generation_s": gen_s, "training_s": train_s,
                    "loss_first_last": [losses[0], losses[-1]]},
@@ -648,7 +661,7 @@ def run_learned_workload(args) -> None:
         "plain_outliers": float(np.mean([o for _, _, o in plain_acc])),
         "accuracy_note": "accepted = status >= 1 among windows whose displaced footprint stays in the frame; "
                          "rmse over accepted windows within 0.5 px of the FP64 field, outliers = the rest",
-        "reseeded_per_frame": float(np.mean(reseeded[args.warmup:])) if len(reseeded) > args.warmup else None,
+        "reseeded_per_frame": float(np.mean(reseeded)) if reseeded else None,
         "clocks": {"sm_mhz": summary["sm_mhz"], "sm_max_mhz": summary["sm_max_mhz"], "reasons": summary["reasons"]},
     }
     print(json.dumps(line), flush=True)

@@ -184,6 +184,13 @@ int gbdic_set_partial_support(gbdic_engine *engine, int32_t count, const int32_t
 int gbdic_register_seeded_device(gbdic_engine *engine, const uint8_t *device_frame, const float *device_seed,
                                  const uint32_t *device_active, const gbdic_solver_cfg *cfg, float *device_state,
                                  void *stream);
+/* Second seeded solve of the same device frame as the previous
+ * gbdic_register_seeded_device call (its B-spline coefficients are reused,
+ * not recomputed): typically only a few subsets active after a reseeding
+ * search.  Calling it with another frame solves against stale coefficients. */
+int gbdic_resolve_seeded_device(gbdic_engine *engine, const uint8_t *device_frame, const float *device_seed,
+                                const uint32_t *device_active, const gbdic_solver_cfg *cfg, float *device_state,
+                                void *stream);
 
 /* Integer ZNCC search (new here; nearest reference component
  * spatial_seed.wgsl:65-190) of the device target against the prepared
@@ -435,6 +442,16 @@ int gbdic_fourier_destroy(gbdic_fourier *fourier);
 const char *gbdic_fourier_last_error(const gbdic_fourier *fourier);
 int gbdic_fourier_estimate(gbdic_fourier *fourier, const uint8_t *frame, int64_t row_stride, int32_t height,
                            int32_t x, int32_t y, int32_t device_frame, double *out);
+/* Stream-ordered phase correlation of a device frame's window (no host
+ * synchronisation) that writes the accepted integer shift into rows of affine
+ * parameters: rows[i * pitch] = dx * multiplier, rows[i * pitch + 3] =
+ * dy * multiplier for i < count.  Accepted when the window's standard
+ * deviation is >= 1, the peak score >= 8 and the overlap >= 0.25, else zero
+ * (the sample-correlation test of gbdic_fourier_estimate is not applied).
+ * Calls on one handle run in stream order and must not overlap. */
+int gbdic_fourier_shift_device(gbdic_fourier *fourier, const uint8_t *frame, int64_t row_stride, int32_t height,
+                               int32_t x, int32_t y, float multiplier, float *rows, int32_t count, int32_t pitch,
+                               void *stream);
 
 /* ------------------------------------------------- learned seed network */
 
@@ -518,6 +535,37 @@ int gbdic_reduce_half(const uint8_t *src, int32_t width, int32_t height, uint8_t
 int gbdic_nn_lattice_seeds(const float *pred, const float *base, int32_t ldp, int32_t lattice_w, int32_t lattice_h,
                            int32_t step, int32_t grid_w, int32_t grid_h, int32_t subset_stride, float translation_scale,
                            float gradient_scale, float *seeds, uint32_t *active, void *stream);
+/* Robust affine field through lattice translations, in one launch: totals
+ * (base + pred) * translation_scale (columns 0 and 3 of rows of ldp floats);
+ * hypotheses = single-node translations (`singles`) then affine maps through
+ * node triples (`triples`, n_triple x 3), scored by the `probes` (at most
+ * 256) within tolerances[0] px, as FP32 squared distances (node_xy:
+ * normalised node coordinates, nodes x 2 floats);
+ * the most supported hypothesis (lowest index on ties) is refitted by least
+ * squares on its inliers for each tolerance in turn (n_tol <= 4), stopping
+ * below three inliers.  base columns 0 and 3 receive fitted / scale.  Indices
+ * outside [0, nodes) are ignored; non-finite totals are outliers. */
+int gbdic_nn_consensus(const float *pred, float *base, int32_t ldp, int32_t nodes, const float *node_xy,
+                       const int32_t *singles, int32_t n_single, const int32_t *triples, int32_t n_triple,
+                       const int32_t *probes, int32_t n_probe, const float *tolerances, int32_t n_tol,
+                       float translation_scale, void *stream);
+/* Subsets to reseed from an affine state field (rows of row_floats floats,
+ * status at column 6): status 0 (not converged) or -2 (below the ZNCC
+ * threshold), where usable[i] != 0 (usable may be NULL).  mask / active = 1
+ * for those, 0 else; *counter (device, may be NULL) = their number. */
+int gbdic_nn_reseed_select(const float *state, int32_t row_floats, const uint8_t *usable, int32_t count,
+                           uint8_t *mask, uint32_t *active, uint32_t *counter, void *stream);
+/* Lattice rows of `pred` (layout of gbdic_nn_lattice_seeds) from solved
+ * node subsets: node (lx, ly) is grid subset (lx * step, ly * step) of the
+ * affine state field `state` (8 floats per subset); where that subset
+ * converged (status >= 1, finite parameters) its row becomes the solved warp,
+ * translations relative to `base` (or NULL); other rows are left unchanged. */
+int gbdic_nn_node_rows(const float *state, int32_t grid_w, int32_t grid_h, int32_t step, int32_t lattice_w,
+                       int32_t lattice_h, float *pred, const float *base, int32_t ldp, float translation_scale,
+                       float gradient_scale, void *stream);
+/* dst row i = src row i where mask[i] != 0 (rows of row_floats floats). */
+int gbdic_nn_merge_rows(const float *src, const uint8_t *mask, int32_t count, int32_t row_floats, float *dst,
+                        void *stream);
 
 #ifdef __cplusplus
 }

@@ -450,6 +450,30 @@ int gbdic_register_seeded_device(gbdic_engine *e, const uint8_t *device_frame, c
     });
 }
 
+int gbdic_resolve_seeded_device(gbdic_engine *e, const uint8_t *device_frame, const float *device_seed,
+                                const uint32_t *device_active, const gbdic_solver_cfg *cfg, float *device_state,
+                                void *stream) {
+    return guarded(e, [&] {
+        e->require_ready("resolve_seeded");
+        gbdic::validate_cfg(cfg);
+        if (!device_frame || !device_seed || !device_active || !device_state)
+            fail(GBDIC_EINVAL, "device frame, seed, activity and state are required");
+        auto &rt = *e->rt;
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        cudaStream_t s = stream ? (cudaStream_t)stream : rt.stream();
+        const size_t sb = (size_t)lvl.count * gbdic::state_stride(rt.opts().o.motion_model) * sizeof(float);
+        check_cuda(cudaMemcpyAsync(slot.seed.get(), device_seed, sb, cudaMemcpyDeviceToDevice, s), "seed copy");
+        check_cuda(cudaMemcpyAsync(slot.active.get(), device_active, (size_t)lvl.count * sizeof(uint32_t),
+                                   cudaMemcpyDeviceToDevice, s), "activity copy");
+        // Same frame as the previous seeded registration: its B-spline
+        // coefficients are still in the slot.
+        const bool disabled = rt.opts().o.outlier_policy == GBDIC_OUTLIER_DISABLED;
+        rt.enqueue_solve(lvl, slot, *cfg, true, false, device_frame, disabled ? device_state : nullptr, s);
+        if (!disabled) rt.enqueue_uod(lvl, slot, false, device_state, s);
+    });
+}
+
 int gbdic_search_seeds_device(gbdic_engine *e, const uint8_t *device_frame, float *device_seed,
                               uint32_t *device_active, const uint8_t *device_mask, int32_t radius, int32_t centered,
                               void *stream) {

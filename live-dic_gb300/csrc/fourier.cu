@@ -275,6 +275,36 @@ __global__ void __launch_bounds__(kCorrCtas) overlap_final_kernel(const double *
     }
 }
 
+// Accepted shift of the last phase correlation written into rows of affine
+// parameters without a host round trip: the integer peak shift (the same
+// unwrapping as the host path), accepted when the target window has texture
+// (standard deviation >= 1), the peak score reaches 8 and the overlap 0.25;
+// rows[i * pitch] = dx * multiplier, rows[i * pitch + 3] = dy * multiplier,
+// zero when rejected.  The sample-correlation test of the host path needs the
+// shift on the host to launch and is not applied here.
+__global__ void shift_rows_kernel(const double *result, const unsigned long long *sums, int size, float multiplier,
+                                  float *rows, int count, int pitch) {
+    __shared__ float su, sv;
+    if (threadIdx.x == 0) {
+        const double wn = (double)sums[1], wmean = wn > 0 ? (double)sums[0] / wn : 0.0;
+        const double texture = wn > 0 ? sqrt(fmax((double)sums[2] / wn - wmean * wmean, 0.0)) : 0.0;
+        const int half = size / 2, px = (int)result[1], py = (int)result[2];
+        const int dx = 2 * (px < half ? px : px - size), dy = 2 * (py < half ? py : py - size);
+        const double sd = result[4];
+        const double score = (result[0] - result[3]) / (sd > 1e-12 ? sd : 1e-12);
+        const double ox = (double)max(size - abs(dx), 0), oy = (double)max(size - abs(dy), 0);
+        const double overlap = ox * oy / ((double)size * size);
+        const bool ok = texture >= 1.0 && score >= 8.0 && overlap >= 0.25;
+        su = ok ? (float)dx * multiplier : 0.0f;
+        sv = ok ? (float)dy * multiplier : 0.0f;
+    }
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        rows[(size_t)i * pitch] = su;
+        rows[(size_t)i * pitch + 3] = sv;
+    }
+}
+
 int log2i(int n) {
     int l = 0;
     while ((1 << l) < n) ++l;
@@ -288,6 +318,7 @@ thread_local std::string g_fourier_error;
 struct gbdic_fourier {
     int device = 0, size = 0, half = 0, logn = 0;
     cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     gbdic::DeviceBuffer window, allowed, taper, ref_spectrum, ref_samples, allowed_samples, cur_samples, work, sums,
         result, twiddle, partials;
     gbdic::HostBuffer host_window, host_result;
@@ -298,29 +329,36 @@ struct gbdic_fourier {
             cudaStreamSynchronize(stream);
             cudaStreamDestroy(stream);
         }
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
     }
-    void transform(double sign) {
+    void transform(double sign) { transform(sign, stream); }
+    void transform(double sign, cudaStream_t st) {
         const int n = size;
         const size_t smem = (size_t)n * sizeof(double2);
         const int threads = n / 2 < 512 ? n / 2 : 512;
         double2 *d = work.as<double2>();
         const double2 *tw = twiddle.as<double2>() + (sign < 0.0 ? 0 : n / 2);
-        fft_lines_kernel<<<n, threads, smem, stream>>>(d, n, logn, 1, n, tw);  // rows
+        fft_lines_kernel<<<n, threads, smem, st>>>(d, n, logn, 1, n, tw);  // rows
         check_cuda(cudaGetLastError(), "FFT rows");
-        fft_lines_kernel<<<n, threads, smem, stream>>>(d, n, logn, n, 1, tw);  // columns
+        fft_lines_kernel<<<n, threads, smem, st>>>(d, n, logn, n, 1, tw);  // columns
         check_cuda(cudaGetLastError(), "FFT columns");
     }
     // window bytes (device, dense size x size) -> work (spectrum), samples
     void spectrum_of(const uint8_t *win, const uint8_t *allow, double *samples, uint8_t *allowed_out) {
-        check_cuda(cudaMemsetAsync(sums.get(), 0, 3 * sizeof(unsigned long long), stream), "clear");
-        window_sum_kernel<<<256, 256, 0, stream>>>(win, size, 0, 0, size, allow, sums.as<unsigned long long>());
+        spectrum_of(win, allow, samples, allowed_out, stream);
+    }
+    void spectrum_of(const uint8_t *win, const uint8_t *allow, double *samples, uint8_t *allowed_out,
+                     cudaStream_t st) {
+        check_cuda(cudaMemsetAsync(sums.get(), 0, 3 * sizeof(unsigned long long), st), "clear");
+        window_sum_kernel<<<256, 256, 0, st>>>(win, size, 0, 0, size, allow, sums.as<unsigned long long>());
         check_cuda(cudaGetLastError(), "window mean");
         const int count = size * size;
-        reduce_taper_kernel<<<(count + 255) / 256, 256, 0, stream>>>(win, size, 0, 0, size, allow,
-                                                                      sums.as<unsigned long long>(), taper.as<double>(),
-                                                                      samples, allowed_out, work.as<double2>());
+        reduce_taper_kernel<<<(count + 255) / 256, 256, 0, st>>>(win, size, 0, 0, size, allow,
+                                                                  sums.as<unsigned long long>(), taper.as<double>(),
+                                                                  samples, allowed_out, work.as<double2>());
         check_cuda(cudaGetLastError(), "reduction and taper");
-        transform(-1.0);
+        transform(-1.0, st);
     }
 };
 
@@ -367,6 +405,8 @@ int gbdic_fourier_create(int32_t device, const uint8_t *window, const uint8_t *a
         f->device = device;
         check_cuda(cudaSetDevice(device), "cudaSetDevice");
         check_cuda(cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking), "stream");
+        check_cuda(cudaEventCreateWithFlags(&f->fork, cudaEventDisableTiming), "event");
+        check_cuda(cudaEventCreateWithFlags(&f->join, cudaEventDisableTiming), "event");
         f->size = size;
         f->half = size / 2;
         f->logn = log2i(size);
@@ -477,6 +517,45 @@ int gbdic_fourier_estimate(gbdic_fourier *f, const uint8_t *frame, int64_t row_s
         out[3] = ox * oy / ((double)n * n);
         out[4] = r[5];
         out[5] = peak;
+    });
+}
+
+int gbdic_fourier_shift_device(gbdic_fourier *f, const uint8_t *frame, int64_t row_stride, int32_t height, int32_t x,
+                               int32_t y, float multiplier, float *rows, int32_t count, int32_t pitch, void *stream) {
+    return fguarded(f, [&] {
+        if (!frame || !rows || count < 0 || pitch < 4) fail(GBDIC_EINVAL, "frame, rows (pitch >= 4) and count >= 0 are required");
+        const int n = f->size;
+        if (row_stride < x + n || x < 0 || y < 0 || y + n > height) fail(GBDIC_EINVAL, "window outside the frame");
+        // The caller's stream orders everything: the transform buffers belong
+        // to this handle, so calls on one handle must not overlap.
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        check_cuda(cudaEventRecord(f->fork, f->stream), "event");
+        check_cuda(cudaStreamWaitEvent(s, f->fork, 0), "event wait");
+        check_cuda(cudaMemcpy2DAsync(f->window.get(), n, frame + (size_t)y * row_stride + x, (size_t)row_stride, n, n,
+                                     cudaMemcpyDeviceToDevice, s), "window copy");
+        f->spectrum_of(f->window.as<uint8_t>(), nullptr, f->cur_samples.as<double>(), nullptr, s);
+        const int px = n * n;
+        cross_power_kernel<<<(px + 255) / 256, 256, 0, s>>>(f->work.as<double2>(), f->ref_spectrum.as<double2>(), px);
+        check_cuda(cudaGetLastError(), "cross power");
+        f->transform(+1.0, s);
+        double *pb = f->partials.as<double>();
+        peak_partial_kernel<<<kPeakCtas, kPeakThreads, 0, s>>>(f->work.as<double2>(), n, pb,
+                                                               reinterpret_cast<int *>(pb + kPeakCtas),
+                                                               pb + 2 * kPeakCtas, pb + 3 * kPeakCtas);
+        check_cuda(cudaGetLastError(), "peak");
+        peak_final_kernel<<<1, kPeakCtas, 0, s>>>(f->work.as<double2>(), n, pb,
+                                                  reinterpret_cast<const int *>(pb + kPeakCtas), pb + 2 * kPeakCtas,
+                                                  pb + 3 * kPeakCtas, f->result.as<double>());
+        check_cuda(cudaGetLastError(), "peak");
+        if (count > 0) {
+            const int blocks = count < 256 * 64 ? (count + 255) / 256 : 64;
+            shift_rows_kernel<<<blocks, 256, 0, s>>>(f->result.as<double>(), f->sums.as<unsigned long long>(), n,
+                                                     multiplier, rows, count, pitch);
+            check_cuda(cudaGetLastError(), "shift rows");
+        }
+        // Later host-path estimates on the handle's own stream wait for this one.
+        check_cuda(cudaEventRecord(f->join, s), "event");
+        check_cuda(cudaStreamWaitEvent(f->stream, f->join, 0), "event wait");
     });
 }
 

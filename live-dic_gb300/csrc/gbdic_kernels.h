@@ -223,6 +223,30 @@ struct NnLatticeArgs {
 };
 cudaError_t launch_nn_lattice_seeds(const NnLatticeArgs &a, cudaStream_t s);
 
+struct NnConsensusArgs {
+    const float *pred;    // nodes rows, stride ldp: network residuals (translation columns 0 and 3)
+    float *base;          // nodes rows, stride ldp: shift the pass ran with; receives the fitted field
+    int ldp, nodes;
+    const float2 *xy;     // normalised node coordinates
+    const int *single;    // n_single node indices (translation hypotheses)
+    int n_single;
+    const int *triple;    // n_triple x 3 node indices (affine hypotheses)
+    int n_triple;
+    const int *probe;     // n_probe node indices that score hypotheses
+    int n_probe;
+    float tol[4];         // pixel tolerances, first scores, all refit
+    int n_tol;
+    float scale;          // pixels per normalised translation unit
+};
+cudaError_t launch_nn_consensus(const NnConsensusArgs &a, cudaStream_t s);
+cudaError_t launch_nn_reseed_select(const float *state, int row_floats, const uint8_t *usable, int count,
+                                    uint8_t *mask, uint32_t *active, unsigned *counter, cudaStream_t s);
+cudaError_t launch_nn_node_rows(const float *state, int grid_w, int grid_h, int step, int lattice_w, int lattice_h,
+                                float *pred, const float *base, int ldp, float translation_scale, float gradient_scale,
+                                cudaStream_t s);
+cudaError_t launch_nn_merge_rows(const float *src, const uint8_t *mask, int count, int row_floats, float *dst,
+                                 cudaStream_t s);
+
 struct TemporalArgs {
     float *history;           // fine accepted history
     uint32_t *ages;

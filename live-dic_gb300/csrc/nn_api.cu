@@ -130,4 +130,50 @@ int gbdic_nn_lattice_seeds(const float *pred, const float *base, int32_t ldp, in
     return rc(gbdic::launch_nn_lattice_seeds(a, as_stream(stream)), "lattice seeds");
 }
 
+int gbdic_nn_consensus(const float *pred, float *base, int32_t ldp, int32_t nodes, const float *node_xy,
+                       const int32_t *singles, int32_t n_single, const int32_t *triples, int32_t n_triple,
+                       const int32_t *probes, int32_t n_probe, const float *tolerances, int32_t n_tol,
+                       float translation_scale, void *stream) {
+    if (!pred || !base || !node_xy || ldp < 4 || nodes < 0 || n_single < 0 || n_triple < 0 || n_probe < 0 ||
+        (n_single && !singles) || (n_triple && !triples) || (n_probe && !probes) || n_probe > 256 || !tolerances || n_tol < 1 ||
+        n_tol > 4 || !(translation_scale > 0.0f) || (reinterpret_cast<uintptr_t>(node_xy) & 7))
+        return invalid("invalid consensus arguments");
+    gbdic::NnConsensusArgs a{};
+    a.pred = pred; a.base = base; a.ldp = ldp; a.nodes = nodes;
+    a.xy = reinterpret_cast<const float2 *>(node_xy);
+    a.single = singles; a.n_single = n_single;
+    a.triple = triples; a.n_triple = n_triple;
+    a.probe = probes; a.n_probe = n_probe;
+    for (int k = 0; k < n_tol; ++k) a.tol[k] = tolerances[k];
+    a.n_tol = n_tol;
+    a.scale = translation_scale;
+    return rc(gbdic::launch_nn_consensus(a, as_stream(stream)), "consensus");
+}
+
+int gbdic_nn_reseed_select(const float *state, int32_t row_floats, const uint8_t *usable, int32_t count,
+                           uint8_t *mask, uint32_t *active, uint32_t *counter, void *stream) {
+    if (!state || !mask || !active || row_floats < 7 || count < 0) return invalid("invalid reseed selection arguments");
+    return rc(gbdic::launch_nn_reseed_select(state, row_floats, usable, count, mask, active, counter,
+                                             as_stream(stream)),
+              "reseed selection");
+}
+
+int gbdic_nn_merge_rows(const float *src, const uint8_t *mask, int32_t count, int32_t row_floats, float *dst,
+                        void *stream) {
+    if (!src || !mask || !dst || count < 0 || row_floats < 1) return invalid("invalid merge arguments");
+    return rc(gbdic::launch_nn_merge_rows(src, mask, count, row_floats, dst, as_stream(stream)), "row merge");
+}
+
+int gbdic_nn_node_rows(const float *state, int32_t grid_w, int32_t grid_h, int32_t step, int32_t lattice_w,
+                       int32_t lattice_h, float *pred, const float *base, int32_t ldp, float translation_scale,
+                       float gradient_scale, void *stream) {
+    if (!state || !pred || ldp < 6 || grid_w < 1 || grid_h < 1 || step < 1 || lattice_w < 1 || lattice_h < 1 ||
+        (lattice_w - 1) * step >= grid_w || (lattice_h - 1) * step >= grid_h || !(translation_scale != 0.0f) ||
+        (reinterpret_cast<uintptr_t>(state) & 15))
+        return invalid("invalid node row arguments");
+    return rc(gbdic::launch_nn_node_rows(state, grid_w, grid_h, step, lattice_w, lattice_h, pred, base, ldp,
+                                         translation_scale, gradient_scale, as_stream(stream)),
+              "node rows");
+}
+
 }  // extern "C"

@@ -318,6 +318,278 @@ __global__ void lattice_seed_kernel(NnLatticeArgs a) {
     a.active[idx] = 1u;
 }
 
+// Robust affine field through the lattice translations, on the device (one
+// CTA, no host round trip).  Totals t_i = (base_i + pred_i) * scale in pixels
+// (columns 0 and 3); nodes with a non-finite total are outliers.  Hypotheses:
+// single-node translations, then affine maps through node triples
+// (|det| > 1e-9 on rows (1, x, y)); each is scored by the probe nodes within
+// the first tolerance, the most supported (lowest index on ties) wins and is
+// refitted by least squares (normal equations in FP64) on its inliers while
+// the tolerance tightens; a refit with fewer than three inliers (or a
+// singular system) stops the loop.  base columns 0 and 3 receive the fitted
+// field / scale.  Fewer than three finite nodes: base receives the totals.
+constexpr int kConsensusThreads = 256, kConsensusProbes = 256;
+
+__device__ inline bool node_total(const NnConsensusArgs &a, int i, double &u, double &v) {
+    if (i < 0 || i >= a.nodes) return false;
+    const size_t row = (size_t)i * a.ldp;
+    u = ((double)a.base[row] + (double)a.pred[row]) * (double)a.scale;
+    v = ((double)a.base[row + 3] + (double)a.pred[row + 3]) * (double)a.scale;
+    return isfinite(u) && isfinite(v);
+}
+
+// Block sums: FP32 within a warp, FP64 across warps (result in red[0]).
+template <int N>
+__device__ inline void block_sum(const float (&x)[N], double (*red)[N]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float y[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        y[k] = x[k];
+        for (int off = 16; off > 0; off >>= 1) y[k] += __shfl_down_sync(0xffffffffu, y[k], off);
+    }
+    if (lane == 0)
+        for (int k = 0; k < N; ++k) red[warp][k] = (double)y[k];
+    __syncthreads();
+    if (threadIdx.x < N) {
+        double t = 0.0;
+        for (int w = 0; w < kConsensusThreads / 32; ++w) t += red[w][threadIdx.x];
+        red[0][threadIdx.x] = t;
+    }
+    __syncthreads();
+}
+
+// 3x3 solve by the adjugate; false when |det| <= eps.
+__device__ inline bool solve3(const double m[3][3], const double (&b)[2][3], double eps, double (&c)[6]) {
+    const double c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1], c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2],
+                 c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+    const double det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
+    if (!(fabs(det) > eps)) return false;
+    const double inv[3][3] = {
+        {c00, m[0][2] * m[2][1] - m[0][1] * m[2][2], m[0][1] * m[1][2] - m[0][2] * m[1][1]},
+        {c01, m[0][0] * m[2][2] - m[0][2] * m[2][0], m[0][2] * m[1][0] - m[0][0] * m[1][2]},
+        {c02, m[0][1] * m[2][0] - m[0][0] * m[2][1], m[0][0] * m[1][1] - m[0][1] * m[1][0]}};
+    for (int o = 0; o < 2; ++o)
+        for (int r = 0; r < 3; ++r)
+            c[3 * o + r] = (inv[r][0] * b[o][0] + inv[r][1] * b[o][1] + inv[r][2] * b[o][2]) / det;
+    return true;
+}
+
+__global__ void __launch_bounds__(kConsensusThreads) consensus_kernel(NnConsensusArgs a) {
+    __shared__ double red[kConsensusThreads / 32][12];
+    __shared__ int best_count[kConsensusThreads / 32], best_index[kConsensusThreads / 32];
+    __shared__ double coef[6];
+    __shared__ int finite_nodes, winner, stop;
+    __shared__ float2 probe_t[kConsensusProbes], probe_xy[kConsensusProbes];
+    __shared__ uint8_t probe_ok[kConsensusProbes];
+    // finite nodes
+    {
+        int n = 0;
+        for (int i = threadIdx.x; i < a.nodes; i += kConsensusThreads) {
+            double u, v;
+            n += node_total(a, i, u, v) ? 1 : 0;
+        }
+        n = __reduce_add_sync(0xffffffffu, n);
+        if (threadIdx.x == 0) finite_nodes = 0;
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) atomicAdd(&finite_nodes, n);
+        __syncthreads();
+    }
+    if (finite_nodes < 3) {
+        for (int i = threadIdx.x; i < a.nodes; i += kConsensusThreads) {
+            double u, v;
+            node_total(a, i, u, v);
+            const size_t row = (size_t)i * a.ldp;
+            const float fu = (float)(u / a.scale), fv = (float)(v / a.scale);
+            a.base[row] = fu;
+            a.base[row + 3] = fv;
+        }
+        return;
+    }
+    // probe totals in shared memory, FP32 (the inlier test is a squared
+    // distance against the squared tolerance)
+    for (int k = threadIdx.x; k < a.n_probe; k += kConsensusThreads) {
+        double u, v;
+        const int j = a.probe[k];
+        const bool ok = node_total(a, j, u, v);
+        probe_t[k] = ok ? make_float2((float)u, (float)v) : make_float2(0.0f, 0.0f);
+        probe_xy[k] = ok ? a.xy[j] : make_float2(0.0f, 0.0f);
+        probe_ok[k] = ok ? 1 : 0;
+    }
+    __syncthreads();
+    const float tol2 = a.tol[0] * a.tol[0];
+    // hypotheses
+    const int hyps = a.n_single + a.n_triple;
+    int my_count = -1, my_index = 0x7fffffff;
+    for (int h = threadIdx.x; h < hyps; h += kConsensusThreads) {
+        double c[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        bool ok;
+        if (h < a.n_single) {
+            double u, v;
+            ok = node_total(a, a.single[h], u, v);
+            c[0] = u;
+            c[3] = v;
+        } else {
+            const int *t = a.triple + 3 * (h - a.n_single);
+            double m[3][3], b[2][3];
+            ok = true;
+            for (int r = 0; r < 3 && ok; ++r) {
+                double u, v;
+                ok = node_total(a, t[r], u, v);
+                if (!ok) break;
+                const float2 p = a.xy[t[r]];
+                m[r][0] = 1.0; m[r][1] = (double)p.x; m[r][2] = (double)p.y;
+                b[0][r] = u; b[1][r] = v;
+            }
+            ok = ok && solve3(m, b, 1e-9, c);
+        }
+        if (!ok) continue;
+        const float c0 = (float)c[0], c1 = (float)c[1], c2 = (float)c[2];
+        const float c3 = (float)c[3], c4 = (float)c[4], c5 = (float)c[5];
+        int count = 0;
+        for (int k = 0; k < a.n_probe; ++k) {
+            const float2 p = probe_xy[k], t = probe_t[k];
+            const float du = c0 + c1 * p.x + c2 * p.y - t.x, dv = c3 + c4 * p.x + c5 * p.y - t.y;
+            count += (probe_ok[k] && du * du + dv * dv <= tol2) ? 1 : 0;
+        }
+        if (count > my_count) { my_count = count; my_index = h; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const int oc = __shfl_down_sync(0xffffffffu, my_count, off), oi = __shfl_down_sync(0xffffffffu, my_index, off);
+        if (oc > my_count || (oc == my_count && oi < my_index)) { my_count = oc; my_index = oi; }
+    }
+    if ((threadIdx.x & 31) == 0) { best_count[threadIdx.x >> 5] = my_count; best_index[threadIdx.x >> 5] = my_index; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int bc = best_count[0], bi = best_index[0];
+        for (int w = 1; w < kConsensusThreads / 32; ++w)
+            if (best_count[w] > bc || (best_count[w] == bc && best_index[w] < bi)) { bc = best_count[w]; bi = best_index[w]; }
+        winner = bc >= 0 ? bi : -1;
+        stop = 0;
+        // the winner's coefficients, recomputed
+        double c[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (winner >= 0 && winner < a.n_single) {
+            double u, v;
+            node_total(a, a.single[winner], u, v);
+            c[0] = u;
+            c[3] = v;
+        } else if (winner >= 0) {
+            const int *t = a.triple + 3 * (winner - a.n_single);
+            double m[3][3], b[2][3];
+            for (int r = 0; r < 3; ++r) {
+                double u, v;
+                node_total(a, t[r], u, v);
+                const float2 p = a.xy[t[r]];
+                m[r][0] = 1.0; m[r][1] = (double)p.x; m[r][2] = (double)p.y;
+                b[0][r] = u; b[1][r] = v;
+            }
+            solve3(m, b, 1e-9, c);
+        }
+        for (int k = 0; k < 6; ++k) coef[k] = c[k];
+    }
+    __syncthreads();
+    // refits
+    for (int t = 0; t < a.n_tol && winner >= 0; ++t) {
+        float x[12] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        const float tol2 = a.tol[t] * a.tol[t];
+        const float c0 = (float)coef[0], c1 = (float)coef[1], c2 = (float)coef[2];
+        const float c3 = (float)coef[3], c4 = (float)coef[4], c5 = (float)coef[5];
+        for (int i = threadIdx.x; i < a.nodes; i += kConsensusThreads) {
+            double u, v;
+            if (!node_total(a, i, u, v)) continue;
+            const float2 p = a.xy[i];
+            // inlier test in FP32 squared distances; per-thread and per-warp
+            // sums in FP32, across warps in FP64
+            const float du = c0 + c1 * p.x + c2 * p.y - (float)u, dv = c3 + c4 * p.x + c5 * p.y - (float)v;
+            if (!(du * du + dv * dv <= tol2)) continue;
+            const float px = p.x, py = p.y, fu = (float)u, fv = (float)v;
+            x[0] += 1.0f; x[1] += px; x[2] += py; x[3] += px * px; x[4] += px * py; x[5] += py * py;
+            x[6] += fu; x[7] += px * fu; x[8] += py * fu; x[9] += fv; x[10] += px * fv; x[11] += py * fv;
+        }
+        block_sum<12>(x, red);
+        if (threadIdx.x == 0) {
+            const double *r = red[0];
+            double c[6];
+            const double m[3][3] = {{r[0], r[1], r[2]}, {r[1], r[3], r[4]}, {r[2], r[4], r[5]}};
+            const double b[2][3] = {{r[6], r[7], r[8]}, {r[9], r[10], r[11]}};
+            const double scale = r[0] * r[3] * r[5] + 1e-300;
+            if (r[0] < 3.0 || !solve3(m, b, 1e-12 * scale, c)) {
+                stop = 1;
+            } else {
+                for (int k = 0; k < 6; ++k) coef[k] = c[k];
+            }
+        }
+        __syncthreads();
+        if (stop) break;
+    }
+    // fitted field (winner < 0: no usable hypothesis, totals kept)
+    for (int i = threadIdx.x; i < a.nodes; i += kConsensusThreads) {
+        double u, v;
+        node_total(a, i, u, v);
+        if (winner >= 0) {
+            const float2 p = a.xy[i];
+            u = coef[0] + coef[1] * p.x + coef[2] * p.y;
+            v = coef[3] + coef[4] * p.x + coef[5] * p.y;
+        }
+        const size_t row = (size_t)i * a.ldp;
+        const float fu = (float)(u / a.scale), fv = (float)(v / a.scale);
+        a.base[row] = fu;
+        a.base[row + 3] = fv;
+    }
+}
+
+// Subsets to reseed: not converged (status 0) or converged below the ZNCC
+// threshold (-2), among usable subsets; mask / activity 1 for those, 0 else,
+// and their count.
+__global__ void reseed_select_kernel(const float *state, int row_floats, const uint8_t *usable, int count,
+                                     uint8_t *mask, uint32_t *active, unsigned *counter) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool pick = false;
+    if (i < count) {
+        const float status = state[(size_t)i * row_floats + 6];
+        pick = (status == 0.0f || status == -2.0f) && (!usable || usable[i]);
+        mask[i] = pick ? 1 : 0;
+        active[i] = pick ? 1u : 0u;
+    }
+    const unsigned votes = __popc(__ballot_sync(0xffffffffu, pick));
+    if ((threadIdx.x & 31) == 0 && votes && counter) atomicAdd(counter, votes);
+}
+
+// dst row i = src row i where mask[i] (rows of row_floats floats).
+__global__ void merge_rows_kernel(const float *src, const uint8_t *mask, int count, int row_floats, float *dst) {
+    const long long n = (long long)count * row_floats;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        if (mask[k / row_floats]) dst[k] = src[k];
+}
+
+// Lattice rows from solved node subsets: node (lx, ly) is grid subset
+// (lx step, ly step); where its affine state converged (status >= 1, finite
+// parameters) its row of `pred` becomes the solved warp in the network's
+// normalised layout, translations relative to `base` (when non-NULL), so that
+// lattice_seed_kernel reproduces the solved warp at the node.  Other rows keep
+// the network's prediction.
+__global__ void node_rows_kernel(const float *state, int grid_w, int grid_h, int step, int lattice_w, int lattice_h,
+                                 float *pred, const float *base, int ldp, float translation_scale,
+                                 float gradient_scale) {
+    const int node = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= lattice_w * lattice_h) return;
+    const int gx = (node % lattice_w) * step, gy = (node / lattice_w) * step;
+    if (gx >= grid_w || gy >= grid_h) return;
+    const float4 *st = reinterpret_cast<const float4 *>(state + ((size_t)gy * grid_w + gx) * 8);
+    const float4 s0 = st[0], s1 = st[1];
+    const bool ok = s1.z >= 1.0f && isfinite(s0.x) && isfinite(s0.y) && isfinite(s0.z) && isfinite(s0.w) &&
+                    isfinite(s1.x) && isfinite(s1.y);
+    if (!ok) return;
+    float *row = pred + (size_t)node * ldp;
+    const float bu = base ? base[(size_t)node * ldp] : 0.0f, bv = base ? base[(size_t)node * ldp + 3] : 0.0f;
+    row[0] = s0.x / translation_scale - bu;
+    row[1] = s0.y * gradient_scale;
+    row[2] = s0.z * gradient_scale;
+    row[3] = s0.w / translation_scale - bv;
+    row[4] = s1.x * gradient_scale;
+    row[5] = s1.y * gradient_scale;
+}
+
 unsigned blocks(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
@@ -406,6 +678,42 @@ cudaError_t launch_nn_lattice_seeds(const NnLatticeArgs &a, cudaStream_t s) {
     const long long n = (long long)a.grid_w * a.grid_h;
     if (n <= 0) return cudaSuccess;
     lattice_seed_kernel<<<blocks(n, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_consensus(const NnConsensusArgs &a, cudaStream_t s) {
+    if (a.nodes <= 0) return cudaSuccess;
+    consensus_kernel<<<1, kConsensusThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_reseed_select(const float *state, int row_floats, const uint8_t *usable, int count,
+                                    uint8_t *mask, uint32_t *active, unsigned *counter, cudaStream_t s) {
+    if (counter) {
+        const cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) return e;
+    }
+    if (count <= 0) return cudaSuccess;
+    reseed_select_kernel<<<blocks(count, 256), 256, 0, s>>>(state, row_floats, usable, count, mask, active, counter);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_merge_rows(const float *src, const uint8_t *mask, int count, int row_floats, float *dst,
+                                 cudaStream_t s) {
+    const long long n = (long long)count * row_floats;
+    if (n <= 0) return cudaSuccess;
+    const unsigned g = blocks(n, 256);
+    merge_rows_kernel<<<g < 152u * 16u ? g : 152u * 16u, 256, 0, s>>>(src, mask, count, row_floats, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_node_rows(const float *state, int grid_w, int grid_h, int step, int lattice_w, int lattice_h,
+                                float *pred, const float *base, int ldp, float translation_scale, float gradient_scale,
+                                cudaStream_t s) {
+    const long long n = (long long)lattice_w * lattice_h;
+    if (n <= 0) return cudaSuccess;
+    node_rows_kernel<<<blocks(n, 256), 256, 0, s>>>(state, grid_w, grid_h, step, lattice_w, lattice_h, pred, base, ldp,
+                                                   translation_scale, gradient_scale);
     return cudaGetLastError();
 }
 

@@ -210,7 +210,12 @@ _SIGNATURES = {
     "gbdic_nn_regression_loss": (C.c_int, [P, I32, P, I32, I32, P, P, I32, P, P]),
     "gbdic_reduce_half": (C.c_int, [P, I32, I32, P, P]),
     "gbdic_nn_lattice_seeds": (C.c_int, [P, P, I32, I32, I32, I32, I32, I32, I32, C.c_float, C.c_float, P, P, P]),
+    "gbdic_nn_consensus": (C.c_int, [P, P, I32, I32, P, P, I32, P, I32, P, I32, P, I32, C.c_float, P]),
+    "gbdic_nn_reseed_select": (C.c_int, [P, I32, P, I32, P, P, P, P]),
+    "gbdic_nn_merge_rows": (C.c_int, [P, P, I32, I32, P, P]),
+    "gbdic_nn_node_rows": (C.c_int, [P, I32, I32, I32, I32, I32, P, P, I32, C.c_float, C.c_float, P]),
     "gbdic_register_seeded_device": (C.c_int, [P, P, P, P, C.POINTER(SolverCfg), P, P]),
+    "gbdic_resolve_seeded_device": (C.c_int, [P, P, P, P, C.POINTER(SolverCfg), P, P]),
     "gbdic_search_seeds_device": (C.c_int, [P, P, P, P, P, I32, I32, P]),
     "gbdic_pyramid_set_translation": (C.c_int, [P, I32, C.c_float, C.c_float]),
     "gbdic_set_partial_support": (C.c_int, [P, I32, P, P, I32, P, P, P]),
@@ -221,6 +226,7 @@ _SIGNATURES = {
     "gbdic_fourier_destroy": (C.c_int, [P]),
     "gbdic_fourier_last_error": (C.c_char_p, [P]),
     "gbdic_fourier_estimate": (C.c_int, [P, P, I64, I32, I32, I32, I32, P]),
+    "gbdic_fourier_shift_device": (C.c_int, [P, P, I64, I32, I32, I32, C.c_float, P, I32, I32, P]),
 }
 EXPORTED_SYMBOLS = tuple(_SIGNATURES)
 

@@ -50,6 +50,7 @@ OUT_PAD = 16          # linear-layer output columns (GEMM tile)
 LOSS_PAD = 64         # K padding of the output gradient
 TRANSLATION_SCALE = 16.0
 GRADIENT_SCALE = 20.0
+CONSENSUS_TOLERANCES = (8.0, 6.0, 4.0, 3.0)   # px: hypothesis scoring, then refits
 NORMALISATION = np.array([1 / TRANSLATION_SCALE, GRADIENT_SCALE, GRADIENT_SCALE, 1 / TRANSLATION_SCALE,
                           GRADIENT_SCALE, GRADIENT_SCALE], np.float32)
 
@@ -412,21 +413,82 @@ def predict(net: SeedNet, refs_ptrs, tgts_ptrs, image_index, centres, width: int
 
 
 # ---------------------------------------------------------------- inference
+def consensus_tables(nodes: int, *, trials: int = 128, seed: int = 12345):
+    """Hypothesis and probe tables of the lattice consensus: 2 * trials
+    single-node translations, `trials` node triples, and the probe nodes
+    (all nodes up to 256, else 256 distinct ones), from a fixed seed."""
+    rng = np.random.default_rng(seed)
+    probes = np.arange(nodes) if nodes <= 256 else rng.choice(nodes, 256, replace=False)
+    singles = rng.integers(0, nodes, 2 * trials)
+    triples = rng.integers(0, nodes, (trials, 3))
+    return singles.astype(np.int32), np.ascontiguousarray(triples, dtype=np.int32), np.asarray(probes, np.int32)
+
+
+def fit_consensus(translations: np.ndarray, xy: np.ndarray, tables, tolerances=CONSENSUS_TOLERANCES) -> np.ndarray:
+    """Affine field through lattice translations (P x 2, px) at normalised
+    node coordinates xy (P x 2) by random sample consensus -- the host
+    statement of gbdic_nn_consensus.  Hypotheses are single-node
+    translations (likely inliers even when few predictions are right), then
+    affine maps through node triples with |det| > 1e-9; the one agreeing with
+    the most probe nodes within the first tolerance wins (lowest index on
+    ties), and is refitted by least squares on its inliers while the
+    tolerance tightens, stopping below three inliers.  Non-finite
+    translations are outliers; fewer than three finite ones return the input.
+    A global affine fit is what lets the next network pass displace every
+    window, including those whose motion exceeded the training range."""
+    singles, triples, probes = tables
+    A = np.concatenate([np.ones((len(xy), 1)), xy], 1)
+    finite = np.isfinite(translations).all(1)
+    if finite.sum() < 3:
+        return translations
+    hyp = []
+    for j in singles:
+        if finite[j]:
+            hyp.append(np.stack([translations[j], np.zeros(2), np.zeros(2)]))
+    for t in triples:
+        sub = A[t]
+        if finite[t].all() and abs(np.linalg.det(sub)) > 1e-9:
+            hyp.append(np.linalg.solve(sub, translations[t]))
+    if not hyp:
+        return translations
+    coef = np.stack(hyp)
+    probe = probes[finite[probes]]
+    # scoring in FP32 squared distances, as on the device
+    c32 = coef.astype(np.float32)
+    x, y = xy[probe, 0].astype(np.float32)[None], xy[probe, 1].astype(np.float32)[None]
+    t = translations[probe].astype(np.float32)
+    du = c32[:, 0, 0:1] + c32[:, 1, 0:1] * x + c32[:, 2, 0:1] * y - t[None, :, 0]
+    dv = c32[:, 0, 1:2] + c32[:, 1, 1:2] * x + c32[:, 2, 1:2] * y - t[None, :, 1]
+    tol2 = np.float32(tolerances[0]) * np.float32(tolerances[0])
+    fit_coef = coef[int(np.argmax((du * du + dv * dv <= tol2).sum(1)))]
+    A32, t32 = A.astype(np.float32), np.where(finite[:, None], translations, 0.0).astype(np.float32)
+    for tol in tolerances:
+        d = A32 @ fit_coef.astype(np.float32) - t32
+        best = finite & ((d * d).sum(1) <= np.float32(tol) * np.float32(tol))
+        if best.sum() < 3:
+            break
+        fit_coef, *_ = np.linalg.lstsq(A[best], translations[best], rcond=None)
+    return A @ fit_coef
+
+
 class LearnedSeeder:
     """Learned-seed registration for one fixed reference on the single-scale
     engine: the global translation by GPU phase correlation, network
     proposals on a subset lattice (two passes with an affine consensus
-    between them), seeded IC-GN, and ZNCC reseeding of failed or low-ZNCC
-    subsets."""
+    between them), IC-GN on the lattice nodes from those proposals (with
+    `refine_nodes`), every subset seeded by interpolation of the node warps,
+    seeded IC-GN, and ZNCC reseeding of failed or low-ZNCC subsets.  Every
+    step runs on the device in stream order, without host round trips."""
 
     def __init__(self, engine, net: SeedNet, *, step: int = 4, reseed_radius: int = 10, passes: int = 2,
-                 global_alignment: bool = True) -> None:
+                 global_alignment: bool = True, refine_nodes: bool = True) -> None:
         torch = _torch()
         if not engine._reference_ready or engine.motion_model != "affine":
             raise ValueError("LearnedSeeder needs an affine engine with a prepared reference")
         self.engine, self.net, self.step, self.radius = engine, net, int(step), int(reseed_radius)
         self.passes = max(1, int(passes))
         self.global_alignment = bool(global_alignment)
+        self.refine_nodes = bool(refine_nodes)
         self.fourier = None
         self.lib = _native.load()
         dev = net.device
@@ -440,7 +502,6 @@ class LearnedSeeder:
         cy = gy * s + 0.5 * (S - 1)
         self.centres = torch.from_numpy(np.stack([cx.ravel() / 2.0, cy.ravel() / 2.0], -1).astype(np.float32)).to(dev)
         self.node_xy = np.stack([cx.ravel(), cy.ravel()], -1).astype(np.float64)
-        self.base_host = np.zeros((self.lw * self.lh, OUT_PAD), np.float32)
         self.ref_half = torch.empty(H // 2, W // 2, dtype=torch.uint8, device=dev)
         self.tgt_half = torch.empty_like(self.ref_half)
         self.ref_ptrs = torch.tensor([self.ref_half.data_ptr()], dtype=torch.int64, device=dev)
@@ -466,11 +527,31 @@ class LearnedSeeder:
         # engine's own stream).
         self.stream = torch.cuda.Stream(device=dev)
         self._handle = C.c_void_p(self.stream.cuda_stream)
+        # Consensus tables (fixed seed): single-node and triple hypotheses and
+        # the probe nodes that score them; node coordinates centred and in
+        # units of 1000 px.
+        singles, triples, probes = consensus_tables(self.lattice)
+        xy = (self.node_xy - self.node_xy.mean(0)) / 1000.0
+        self._xy = torch.from_numpy(np.ascontiguousarray(xy, dtype=np.float32)).to(dev)
+        self._singles = torch.from_numpy(singles.astype(np.int32)).to(dev)
+        self._triples = torch.from_numpy(np.ascontiguousarray(triples, dtype=np.int32)).to(dev)
+        self._probes = torch.from_numpy(np.asarray(probes, dtype=np.int32)).to(dev)
+        self._tolerances = np.array(CONSENSUS_TOLERANCES, np.float32)
+        self._usable8 = self.usable.to(torch.uint8)
+        self._retry = torch.empty_like(self.state)
+        node_active = np.zeros((self.gh, self.gw), np.int32)
+        node_active[::self.step, ::self.step] = 1
+        self._node_active = torch.from_numpy(node_active.ravel()).to(dev)
+        self._shifted = False
+        self.reseed_count = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._fourier_window = None
 
     def set_reference_image(self, reference: np.ndarray) -> None:
         """Half-resolution reference for the network (the engine keeps its own),
         and the GPU phase correlation that removes the global translation
-        before the first network pass."""
+        before the first network pass: a 256-pixel window at the centre of the
+        half-resolution reference (a 512-pixel region of the frame; the shift
+        is resolved to 4 frame pixels, well inside the network's range)."""
         torch = _torch()
         from .fourier import FourierInitializer
 
@@ -479,12 +560,19 @@ class LearnedSeeder:
         if self.fourier is not None:
             self.fourier.close()
         self.fourier = None
+        self._fourier_window = None
         if self.global_alignment:
+            half = self.ref_half.cpu().numpy()
+            hh, hw = half.shape
+            side = min(256, hh, hw)
+            x0, y0 = (hw - side) // 2, (hh - side) // 2
             try:
-                self.fourier = FourierInitializer(np.asarray(reference), device=self.net.device.index or 0)
+                self.fourier = FourierInitializer(half[y0:y0 + side, x0:x0 + side], device=self.net.device.index or 0)
             except ValueError:
                 self.fourier = None
-
+            if self.fourier is not None:
+                win = self.fourier.window
+                self._fourier_window = (x0 + win["x"], y0 + win["y"])
     def propose(self, frame) -> None:
         """Network proposals for device frame `frame` (uint8 H x W) -> self.seeds
         (on self.stream)."""
@@ -509,117 +597,99 @@ class LearnedSeeder:
             net.forward(stream)
             _native_copy(out, s0, net.out, n)  # on the current stream, ordered with `stream`
 
-    def consensus(self, translations: np.ndarray, *, trials: int = 128, tolerances=(8.0, 6.0, 4.0, 3.0)) -> np.ndarray:
-        """Affine field through the lattice translations (P x 2, px) by
-        random sample consensus.  Hypotheses are single-node translations
-        (which stay likely to be inliers when few predictions are right) and
-        affine maps through node triples; the one agreeing with the most
-        probe nodes within the first tolerance wins, and is refitted by least
-        squares on its inliers while the tolerance tightens.  Out-of-range
-        network predictions are outliers; a global affine fit is what lets
-        the next pass displace every window, including those whose motion
-        exceeded the network's training range."""
-        xy = (self.node_xy - self.node_xy.mean(0)) / 1000.0
-        A = np.concatenate([np.ones((len(xy), 1)), xy], 1)
-        finite = np.isfinite(translations).all(1)
-        idx = np.flatnonzero(finite)
-        if idx.size < 3:
-            return translations
-        rng = np.random.default_rng(12345)
-        single = idx[rng.integers(0, idx.size, 2 * trials)]
-        hyp = [np.stack([translations[single], np.zeros((single.size, 2)), np.zeros((single.size, 2))], 1)]
-        tri = idx[rng.integers(0, idx.size, (trials, 3))]
-        sub = A[tri]                                               # trials x 3 x 3
-        usable = np.abs(np.linalg.det(sub)) > 1e-9
-        if usable.any():
-            hyp.append(np.linalg.solve(sub[usable], translations[tri[usable]]))   # k x 3 x 2
-        coef = np.concatenate(hyp, 0)
-        # hypotheses are scored on at most 256 sampled nodes, the winner on all
-        probe = idx if idx.size <= 256 else idx[rng.choice(idx.size, 256, replace=False)]
-        x, y, t = xy[probe, 0][None], xy[probe, 1][None], translations[probe]
-        du = coef[:, 0, 0:1] + coef[:, 1, 0:1] * x + coef[:, 2, 0:1] * y - t[None, :, 0]
-        dv = coef[:, 0, 1:2] + coef[:, 1, 1:2] * x + coef[:, 2, 1:2] * y - t[None, :, 1]
-        fit_coef = coef[int(np.argmax((np.hypot(du, dv) <= tolerances[0]).sum(1)))]
-        for tol in tolerances:
-            d = A @ fit_coef - translations
-            best = finite & (np.hypot(d[:, 0], d[:, 1]) <= tol)
-            if best.sum() < 3:
-                break
-            fit_coef, *_ = np.linalg.lstsq(A[best], translations[best], rcond=None)
-        return A @ fit_coef
+    def consensus(self, translations: np.ndarray) -> np.ndarray:
+        """Host restatement of the device consensus for inspection (see
+        fit_consensus)."""
+        xy = self._xy.cpu().numpy().astype(np.float64)
+        tables = (self._singles.cpu().numpy(), self._triples.cpu().numpy(), self._probes.cpu().numpy())
+        return fit_consensus(translations, xy, tables)
+
+    def _consensus_device(self, stream) -> None:
+        """self.base (columns 0, 3) <- the fitted field through the totals
+        self.base + self.pred, on the device."""
+        _call(self.lib, "gbdic_nn_consensus", _ptr(self.pred), _ptr(self.base), OUT_PAD, self.lattice, _ptr(self._xy),
+              _ptr(self._singles), int(self._singles.numel()), _ptr(self._triples), int(self._triples.shape[0]),
+              _ptr(self._probes), int(self._probes.numel()), self._tolerances.ctypes.data_as(C.c_void_p),
+              len(self._tolerances), C.c_float(TRANSLATION_SCALE), stream)
 
     def _propose(self, frame, stream) -> None:
-        # Pass 1 on co-located windows; between passes a robust affine fit of
-        # the lattice translations displaces every target window, and the
-        # next pass predicts the residual warp around it.
-        torch = _torch()
+        # Pass 1 on co-located windows (displaced by the global phase
+        # correlation); between passes a robust affine fit of the lattice
+        # translations displaces every target window, and the next pass
+        # predicts the residual warp around it.  Everything stays on the
+        # device, in stream order.
         _call(self.lib, "gbdic_reduce_half", _ptr(frame), self.W, self.H, _ptr(self.tgt_half), stream)
         shift = None
-        self.base_host[:] = 0.0
         if self.fourier is not None:
-            # Global translation by phase correlation: the first pass then
-            # sees only the strain-induced residual, inside the network's
-            # training range even for translations beyond it.
-            self.stream.synchronize()
-            try:
-                est = self.fourier.estimate_device(frame.data_ptr(), self.W)
-            except (ValueError, ICGNError):
-                est = None
-            if est is not None:
-                self.base_host[:, 0] = est["dx"] / TRANSLATION_SCALE
-                self.base_host[:, 3] = est["dy"] / TRANSLATION_SCALE
-                self.base.copy_(torch.from_numpy(self.base_host), non_blocking=False)
-                shift = self.base
+            fx, fy = self._fourier_window
+            code = self.lib.gbdic_fourier_shift_device(
+                self.fourier._handle, _ptr(self.tgt_half), self.W // 2, self.H // 2, fx, fy,
+                C.c_float(2.0 / TRANSLATION_SCALE), _ptr(self.base), self.lattice, OUT_PAD, stream)
+            _native.check(code, self.lib.gbdic_fourier_last_error(self.fourier._handle))
+            shift = self.base
         for p in range(self.passes):
             self._network_pass(self.pred, shift, stream)
             if p == self.passes - 1:
                 break
-            self.stream.synchronize()
-            pred = self.pred[:, [0, 3]].cpu().numpy().astype(np.float64)
-            total = (self.base_host[:, [0, 3]] + pred) * TRANSLATION_SCALE
-            fitted = self.consensus(total) / TRANSLATION_SCALE
-            self.base_host[:, 0], self.base_host[:, 3] = fitted[:, 0], fitted[:, 1]
-            self.base.copy_(torch.from_numpy(self.base_host), non_blocking=False)
+            if shift is None:
+                self.base.zero_()
+            self._consensus_device(stream)
             shift = self.base
-        _call(self.lib, "gbdic_nn_lattice_seeds", _ptr(self.pred), _ptr(self.base) if shift is not None else None,
+        self._shifted = shift is not None
+        self._lattice_seeds(stream)
+
+    def _lattice_seeds(self, stream) -> None:
+        _call(self.lib, "gbdic_nn_lattice_seeds", _ptr(self.pred), _ptr(self.base) if self._shifted else None,
               OUT_PAD, self.lw, self.lh, self.step, self.gw, self.gh, self.engine.subset_stride,
               C.c_float(TRANSLATION_SCALE), C.c_float(GRADIENT_SCALE), _ptr(self.seeds), _ptr(self.active), stream)
 
-    def register_device(self, frame, *, reseed: bool = True) -> dict:
+    def register_device(self, frame, *, reseed: bool = True, counts: bool = True) -> dict:
         """Learned-seed registration of a device frame into self.state (on
-        self.stream; callers synchronise or wait on it); returns counts."""
+        self.stream; callers synchronise or wait on it).  The number of
+        reseeded subsets stays in self.reseed_count (device); with `counts`
+        it is also returned (one host synchronisation), else None."""
         torch = _torch()
         self.stream.wait_stream(torch.cuda.current_stream(self.net.device))
         with torch.cuda.stream(self.stream):
-            out = self._register(frame, reseed, self._handle)
+            self._register(frame, reseed, self._handle)
         torch.cuda.current_stream(self.net.device).wait_stream(self.stream)
-        return out
+        return {"reseeded": int(self.reseed_count.item()) if counts and reseed else (0 if counts else None)}
 
-    def _register(self, frame, reseed: bool, stream) -> dict:
-        torch = _torch()
+    def _register(self, frame, reseed: bool, stream) -> None:
         eng = self.engine
         cfg = C.byref(eng._cfg(eng._config))
         self._propose(frame, stream)
-        _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
-                     _ptr(self.state), stream)
-        reseeded = 0
-        if reseed:
-            # not converged (0) or converged below the ZNCC threshold (-2);
-            # windows pushed off the image (-1) cannot be rescued by a search
-            status = self.state.view(-1, 8)[:, 6]
-            failed = ((status == 0.0) | (status == -2.0)) & self.usable
-            reseeded = int(failed.sum().item())
-            if reseeded:
-                self.mask.copy_(failed.to(torch.uint8))
-                _call_engine(eng, "gbdic_search_seeds_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active),
-                             _ptr(self.mask), self.radius, 1, stream)
-                self.active.copy_(failed.to(torch.int32))
-                retry = torch.empty_like(self.state)
-                _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
-                             _ptr(retry), stream)
-                rows = failed.nonzero().squeeze(1)
-                self.state.view(-1, 8)[rows] = retry.view(-1, 8)[rows]
-        return {"reseeded": reseeded}
+        if self.refine_nodes:
+            # IC-GN on the lattice nodes alone (one subset in step^2) from the
+            # network's proposals; their solved warps replace the network rows
+            # and the interpolated seeds of every subset come from them.  The
+            # full solve then reuses the node solve's B-spline coefficients.
+            _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self._node_active),
+                         cfg, _ptr(self.state), stream)
+            _call(self.lib, "gbdic_nn_node_rows", _ptr(self.state), self.gw, self.gh, self.step, self.lw, self.lh,
+                  _ptr(self.pred), _ptr(self.base) if self._shifted else None, OUT_PAD, C.c_float(TRANSLATION_SCALE),
+                  C.c_float(GRADIENT_SCALE), stream)
+            self._lattice_seeds(stream)
+            _call_engine(eng, "gbdic_resolve_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
+                         _ptr(self.state), stream)
+        else:
+            _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
+                         _ptr(self.state), stream)
+        if not reseed:
+            return
+        # Not converged (0) or converged below the ZNCC threshold (-2): ZNCC
+        # search around the current seed, a second solve of those subsets
+        # only, and their rows merged back.  Windows pushed off the image (-1)
+        # cannot be rescued by a search.  No host round trip: an empty
+        # selection costs three near-empty launches.
+        count = self.gh * self.gw
+        _call(self.lib, "gbdic_nn_reseed_select", _ptr(self.state), 8, _ptr(self._usable8), count, _ptr(self.mask),
+              _ptr(self.active), _ptr(self.reseed_count), stream)
+        _call_engine(eng, "gbdic_search_seeds_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active),
+                     _ptr(self.mask), self.radius, 1, stream)
+        _call_engine(eng, "gbdic_resolve_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
+                     _ptr(self._retry), stream)
+        _call(self.lib, "gbdic_nn_merge_rows", _ptr(self._retry), _ptr(self.mask), count, 8, _ptr(self.state), stream)
 
 
 def _native_copy(dst, row0: int, src, n: int) -> None:

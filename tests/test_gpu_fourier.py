@@ -70,3 +70,38 @@ def test_fourier_seeds_the_pyramid_beyond_its_capture_range():
     assert good.mean() > 0.6 and good_zero.mean() < 0.1
     for r in streamed:
         np.testing.assert_array_equal(r.parameters, result.parameters)
+
+
+@pytest.mark.parametrize("shift", [(23.4, -17.7), (-41.0, 9.5)])
+def test_device_shift_rows_match_host_estimate(shift):
+    """The stream-ordered variant leaves the host path's accepted integer shift
+    in rows of affine parameters on the device (columns 0 and 3)."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+
+    from live_dic_gb300 import _native
+
+    ref, sp = synthetic.reference_image(700, 520, seed=19, device="cpu")
+    tgt = synthetic.deformed_image(sp, synthetic.affine_field(shift[0], 0.0, 0.0, shift[1], 0.0, 0.0),
+                                   noise_seed=20, device="cpu")
+    init = FourierInitializer(ref)
+    est = init.estimate(tgt)
+    lib = _native.load()
+    frame = torch.from_numpy(tgt).cuda()
+    rows = torch.full((37, 16), 7.0, device="cuda")
+    flat = torch.zeros(520, 700, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    for image, accepted in ((frame, True), (flat, False)):
+        code = lib.gbdic_fourier_shift_device(init._handle, C.c_void_p(image.data_ptr()), 700, 520, init.window["x"],
+                                              init.window["y"], C.c_float(0.5), C.c_void_p(rows.data_ptr()), 37, 16,
+                                              C.c_void_p(stream))
+        _native.check(code, lib.gbdic_fourier_last_error(init._handle))
+        r = rows.cpu().numpy()
+        expected = (0.5 * est["dx"], 0.5 * est["dy"]) if accepted else (0.0, 0.0)
+        np.testing.assert_array_equal(r[:, 0], np.full(37, expected[0], np.float32))
+        np.testing.assert_array_equal(r[:, 3], np.full(37, expected[1], np.float32))
+        assert (r[:, [1, 2, 4, 5]] == 7.0).all()
+    # the host path still agrees after a device-path call on the same handle
+    again = init.estimate(tgt)
+    assert (again["dx"], again["dy"], again["peakScore"]) == (est["dx"], est["dy"], est["peakScore"])
+    init.close()

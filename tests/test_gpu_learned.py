@@ -99,3 +99,116 @@ def test_training_and_learned_seeding_gain():
     proposal_error = np.abs(proposals[..., [0, 3]] - truth)[inside].max(-1)
     assert np.median(proposal_error) < 5.0
     assert stats["reseeded"] < 0.3 * inside.sum()
+
+
+@pytest.mark.parametrize("lw,lh,outliers", [(40, 23, 0.3), (4, 3, 0.0), (12, 9, 0.6)])
+def test_device_consensus_matches_host_statement(lw, lh, outliers):
+    """gbdic_nn_consensus against fit_consensus on the same tables: an affine
+    field through lattice translations with planted outliers and non-finite
+    predictions."""
+    import ctypes as C
+
+    from live_dic_gb300 import _native
+
+    lib = _native.load()
+    rng = np.random.default_rng(lw * 100 + lh)
+    n = lw * lh
+    gy, gx = np.mgrid[0:lh, 0:lw] * 64.0
+    node = np.stack([gx.ravel(), gy.ravel()], -1)
+    xy = ((node - node.mean(0)) / 1000.0).astype(np.float32)
+    truth = np.stack([12.0 + 8.0 * xy[:, 0] - 5.0 * xy[:, 1], -7.0 + 3.0 * xy[:, 0] + 11.0 * xy[:, 1]], -1)
+    t = truth + rng.normal(0.0, 0.4, truth.shape)
+    bad = rng.random(n) < outliers
+    t[bad] = rng.uniform(-40.0, 40.0, (int(bad.sum()), 2))
+    if n > 20:
+        t[[3, 17]] = np.nan
+    scale = learned.TRANSLATION_SCALE
+    pred = np.zeros((n, learned.OUT_PAD), np.float32)
+    base = np.zeros((n, learned.OUT_PAD), np.float32)
+    split = rng.uniform(-0.3, 0.3, (n, 2)).astype(np.float32)
+    base[:, [0, 3]] = split
+    pred[:, [0, 3]] = (t / scale - split).astype(np.float32)
+    totals = (base[:, [0, 3]].astype(np.float64) + pred[:, [0, 3]].astype(np.float64)) * scale
+    tables = learned.consensus_tables(n)
+    expected = learned.fit_consensus(totals, xy.astype(np.float64), tables)
+    d_pred, d_base = torch.from_numpy(pred).cuda(), torch.from_numpy(base).cuda()
+    d_xy = torch.from_numpy(xy).cuda()
+    d_tab = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in tables]
+    tol = np.array(learned.CONSENSUS_TOLERANCES, np.float32)
+    code = lib.gbdic_nn_consensus(C.c_void_p(d_pred.data_ptr()), C.c_void_p(d_base.data_ptr()), learned.OUT_PAD, n,
+                                  C.c_void_p(d_xy.data_ptr()), C.c_void_p(d_tab[0].data_ptr()), len(tables[0]),
+                                  C.c_void_p(d_tab[1].data_ptr()), len(tables[1]), C.c_void_p(d_tab[2].data_ptr()),
+                                  len(tables[2]), tol.ctypes.data_as(C.c_void_p), len(tol), C.c_float(scale), None)
+    assert code == 0
+    torch.cuda.synchronize()
+    got = d_base.cpu().numpy()
+    np.testing.assert_allclose(got[:, [0, 3]].astype(np.float64) * scale, expected, atol=1e-3)
+    assert (got[:, [1, 2, 4, 5]] == base[:, [1, 2, 4, 5]]).all()
+    if outliers <= 0.3:
+        np.testing.assert_allclose(expected, truth, atol=0.6)
+
+
+def test_reseed_selection_and_row_merge():
+    import ctypes as C
+
+    from live_dic_gb300 import _native
+
+    lib = _native.load()
+    rng = np.random.default_rng(3)
+    n = 5000
+    state = rng.normal(size=(n, 8)).astype(np.float32)
+    state[:, 6] = rng.choice([1.0, 0.0, -1.0, -2.0, 2.0], n)
+    usable = (rng.random(n) < 0.9).astype(np.uint8)
+    d_state, d_usable = torch.from_numpy(state).cuda(), torch.from_numpy(usable).cuda()
+    mask = torch.full((n,), 9, dtype=torch.uint8, device="cuda")
+    active = torch.full((n,), 9, dtype=torch.int32, device="cuda")
+    counter = torch.full((1,), 123, dtype=torch.int32, device="cuda")
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    assert lib.gbdic_nn_reseed_select(P(d_state), 8, P(d_usable), n, P(mask), P(active), P(counter), None) == 0
+    expected = ((state[:, 6] == 0.0) | (state[:, 6] == -2.0)) & (usable != 0)
+    np.testing.assert_array_equal(mask.cpu().numpy(), expected.astype(np.uint8))
+    np.testing.assert_array_equal(active.cpu().numpy(), expected.astype(np.int32))
+    assert int(counter.item()) == int(expected.sum())
+    src = torch.from_numpy(rng.normal(size=(n, 8)).astype(np.float32)).cuda()
+    assert lib.gbdic_nn_merge_rows(P(src), P(mask), n, 8, P(d_state), None) == 0
+    merged = d_state.cpu().numpy()
+    np.testing.assert_array_equal(merged[expected], src.cpu().numpy()[expected])
+    np.testing.assert_array_equal(merged[~expected], state[~expected])
+
+
+def test_resolve_reuses_the_prefiltered_frame():
+    """gbdic_resolve_seeded_device on the frame of the previous seeded
+    registration gives the same states as a fresh seeded registration."""
+    import ctypes as C
+
+    ref, sp = synthetic.reference_image(320, 256, seed=41, device="cpu")
+    tgt = synthetic.deformed_image(sp, synthetic.affine_field(2.3, 0.004, -0.002, -1.6, 0.001, 0.003),
+                                   noise_seed=42, device="cpu")
+    with ICGNWGPU(subset_size=21, subset_stride=10) as engine:
+        engine.set_reference(ref)
+        n = engine.grid_width * engine.grid_height
+        rng = np.random.default_rng(5)
+        seeds = np.zeros((n, 8), np.float32)
+        seeds[:, 0] = 2.3 + rng.normal(0, 0.3, n)
+        seeds[:, 3] = -1.6 + rng.normal(0, 0.3, n)
+        active = (rng.random(n) < 0.3).astype(np.int32)
+        d_frame = torch.from_numpy(tgt).cuda()
+        d_seed, d_active = torch.from_numpy(seeds).cuda(), torch.from_numpy(active).cuda()
+        other = torch.from_numpy(np.ascontiguousarray(tgt[::-1])).cuda()
+        a, b = torch.zeros(n * 8, device="cuda"), torch.zeros(n * 8, device="cuda")
+        cfg = C.byref(engine._cfg(engine._config))
+        P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+        lib = engine._lib
+        engine._check(lib.gbdic_register_seeded_device(engine._handle, P(d_frame), P(d_seed), P(d_active), cfg, P(a),
+                                                       None))
+        # prefilter another frame, then the frame of interest, then resolve
+        engine._check(lib.gbdic_register_seeded_device(engine._handle, P(other), P(d_seed), P(d_active), cfg, P(b),
+                                                       None))
+        engine._check(lib.gbdic_register_seeded_device(engine._handle, P(d_frame), P(d_seed), P(d_active), cfg, P(b),
+                                                       None))
+        b.zero_()
+        engine._check(lib.gbdic_resolve_seeded_device(engine._handle, P(d_frame), P(d_seed), P(d_active), cfg, P(b),
+                                                      None))
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+        assert (a.view(-1, 8)[:, 6].cpu().numpy()[active == 1] >= 1).mean() > 0.9
