@@ -9,7 +9,7 @@ displacement RMSE below 0.05 px against the Kirsch solution at 250 MPa;
 under "partial" the 24 partial windows are all admitted and accepted.  The
 images are a 768 x 768 window around the hole of assets/uhd_plate_hole
 (reference.png, frame_095.png), cut on the 16-px subset grid with the truth
-at its subset centres (tests/golden/make_plate_fixture.py); the border
+at its subset centres (tests/golden/make_uhd_fixtures.py); the border
 margin applies to that window.
 """
 
