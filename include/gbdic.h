@@ -496,6 +496,12 @@ typedef struct {
 } gbdic_nn_conv_shape;
 /* Forward GEMM operand A[(b, oy, ox)][(ky, kx, ci)] (zero beyond 9 C). */
 int gbdic_nn_im2col(const gbdic_nn_conv_shape *shape, const void *x, void *a, void *stream);
+/* Inference form of the 2-channel input layer (Cout 32): the 3x3 stride-2
+ * convolution, bias and ReLU in one pass, y[(b, oy, ox)][co] BF16 (row of 32),
+ * without the im2col operand.  `weights` (32 x 18 floats, taps (ky, kx, ci))
+ * and `bias` (32 floats) are HOST arrays, passed by value with the launch. */
+int gbdic_nn_conv_c2_direct(const gbdic_nn_conv_shape *shape, const void *x, const float *weights, const float *bias,
+                            void *y, void *stream);
 /* Data-gradient operand G[(b, iy, ix)][(ky, kx, co)] from output gradients. */
 int gbdic_nn_dgrad_gather(const gbdic_nn_conv_shape *shape, const void *dz, void *g, void *stream);
 /* dst (Cp x Rp) = src (R x C, row stride ld_src) transposed, zero padded. */

@@ -239,6 +239,14 @@ struct NnConsensusArgs {
     float scale;          // pixels per normalised translation unit
 };
 cudaError_t launch_nn_consensus(const NnConsensusArgs &a, cudaStream_t s);
+// First-layer weights passed by value (kernel parameters, read as constant
+// operands): 2 input channels, 32 outputs, taps ordered (ky, kx, ci).
+struct NnConv1Weights {
+    float w[32][18];
+    float bias[32];
+};
+cudaError_t launch_nn_conv_c2_direct(const NnConvShape &sh, const void *x, const NnConv1Weights &w, void *y,
+                                     cudaStream_t s);
 cudaError_t launch_nn_reseed_select(const float *state, int row_floats, const uint8_t *usable, int count,
                                     uint8_t *mask, uint32_t *active, unsigned *counter, cudaStream_t s);
 cudaError_t launch_nn_node_rows(const float *state, int grid_w, int grid_h, int step, int lattice_w, int lattice_h,

@@ -59,6 +59,21 @@ int gbdic_nn_im2col(const gbdic_nn_conv_shape *s, const void *x, void *a, void *
     return rc(gbdic::launch_nn_im2col(shape_of(s), x, a, as_stream(stream)), "im2col");
 }
 
+int gbdic_nn_conv_c2_direct(const gbdic_nn_conv_shape *s, const void *x, const float *weights, const float *bias,
+                            void *y, void *stream) {
+    if (!valid_shape(s) || s->C != 2 || s->Cout != 32 || !x || !y || !weights || !bias ||
+        (reinterpret_cast<uintptr_t>(x) & 3) || (reinterpret_cast<uintptr_t>(y) & 15) ||
+        (long long)s->B * s->OH * s->OW >= (1ll << 31))
+        return invalid("direct convolution needs 2 input and 32 output channels, 4-byte aligned input, "
+                       "16-byte aligned output and host weights");
+    gbdic::NnConv1Weights w;
+    for (int co = 0; co < 32; ++co) {
+        for (int k = 0; k < 18; ++k) w.w[co][k] = weights[co * 18 + k];
+        w.bias[co] = bias[co];
+    }
+    return rc(gbdic::launch_nn_conv_c2_direct(shape_of(s), x, w, y, as_stream(stream)), "direct convolution");
+}
+
 int gbdic_nn_dgrad_gather(const gbdic_nn_conv_shape *s, const void *dz, void *g, void *stream) {
     if (!valid_shape(s) || !dz || !g) return invalid("invalid convolution shape or pointers");
     return rc(gbdic::launch_nn_dgrad_gather(shape_of(s), dz, g, as_stream(stream)), "gradient gather");

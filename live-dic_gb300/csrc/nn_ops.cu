@@ -320,21 +320,24 @@ __global__ void lattice_seed_kernel(NnLatticeArgs a) {
 
 // Robust affine field through the lattice translations, on the device (one
 // CTA, no host round trip).  Totals t_i = (base_i + pred_i) * scale in pixels
-// (columns 0 and 3); nodes with a non-finite total are outliers.  Hypotheses:
-// single-node translations, then affine maps through node triples
+// (columns 0 and 3, FP32); nodes with a non-finite total are outliers.
+// Hypotheses: single-node translations, then affine maps through node triples
 // (|det| > 1e-9 on rows (1, x, y)); each is scored by the probe nodes within
 // the first tolerance, the most supported (lowest index on ties) wins and is
-// refitted by least squares (normal equations in FP64) on its inliers while
-// the tolerance tightens; a refit with fewer than three inliers (or a
-// singular system) stops the loop.  base columns 0 and 3 receive the fitted
-// field / scale.  Fewer than three finite nodes: base receives the totals.
+// refitted by least squares on its inliers while the tolerance tightens (sums
+// in FP32 within a warp and FP64 across warps, normal equations solved in
+// FP64); a refit with fewer than three inliers (or a singular system) stops
+// the loop.  base columns 0 and 3 receive the fitted field / scale.  Fewer
+// than three finite nodes: base receives the totals.  GB300's FP64 rate is a
+// small fraction of its FP32 rate, so FP64 is kept to the 3x3 solves of the
+// refits.
 constexpr int kConsensusThreads = 256, kConsensusProbes = 256;
 
-__device__ inline bool node_total(const NnConsensusArgs &a, int i, double &u, double &v) {
+__device__ inline bool node_total(const NnConsensusArgs &a, int i, float &u, float &v) {
     if (i < 0 || i >= a.nodes) return false;
     const size_t row = (size_t)i * a.ldp;
-    u = ((double)a.base[row] + (double)a.pred[row]) * (double)a.scale;
-    v = ((double)a.base[row + 3] + (double)a.pred[row + 3]) * (double)a.scale;
+    u = (a.base[row] + a.pred[row]) * a.scale;
+    v = (a.base[row + 3] + a.pred[row + 3]) * a.scale;
     return isfinite(u) && isfinite(v);
 }
 
@@ -360,25 +363,44 @@ __device__ inline void block_sum(const float (&x)[N], double (*red)[N]) {
 }
 
 // 3x3 solve by the adjugate; false when |det| <= eps.
-__device__ inline bool solve3(const double m[3][3], const double (&b)[2][3], double eps, double (&c)[6]) {
-    const double c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1], c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2],
-                 c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
-    const double det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
+template <typename T>
+__device__ inline bool solve3(const T m[3][3], const T (&b)[2][3], T eps, T (&c)[6]) {
+    const T c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1], c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2],
+            c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+    const T det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
     if (!(fabs(det) > eps)) return false;
-    const double inv[3][3] = {
+    const T inv[3][3] = {
         {c00, m[0][2] * m[2][1] - m[0][1] * m[2][2], m[0][1] * m[1][2] - m[0][2] * m[1][1]},
         {c01, m[0][0] * m[2][2] - m[0][2] * m[2][0], m[0][2] * m[1][0] - m[0][0] * m[1][2]},
         {c02, m[0][1] * m[2][0] - m[0][0] * m[2][1], m[0][0] * m[1][1] - m[0][1] * m[1][0]}};
+    const T rdet = T(1) / det;
+#pragma unroll
     for (int o = 0; o < 2; ++o)
-        for (int r = 0; r < 3; ++r)
-            c[3 * o + r] = (inv[r][0] * b[o][0] + inv[r][1] * b[o][1] + inv[r][2] * b[o][2]) / det;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) c[3 * o + r] = (inv[r][0] * b[o][0] + inv[r][1] * b[o][1] + inv[r][2] * b[o][2]) * rdet;
     return true;
+}
+
+// Coefficients (u0, ux, uy, v0, vx, vy) of hypothesis h; false if unusable.
+__device__ inline bool hypothesis(const NnConsensusArgs &a, int h, float (&c)[6]) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) c[k] = 0.0f;
+    if (h < a.n_single) return node_total(a, a.single[h], c[0], c[3]);
+    const int *t = a.triple + 3 * (h - a.n_single);
+    float m[3][3], b[2][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        if (!node_total(a, t[r], b[0][r], b[1][r])) return false;
+        const float2 p = a.xy[t[r]];
+        m[r][0] = 1.0f; m[r][1] = p.x; m[r][2] = p.y;
+    }
+    return solve3<float>(m, b, 1e-9f, c);
 }
 
 __global__ void __launch_bounds__(kConsensusThreads) consensus_kernel(NnConsensusArgs a) {
     __shared__ double red[kConsensusThreads / 32][12];
     __shared__ int best_count[kConsensusThreads / 32], best_index[kConsensusThreads / 32];
-    __shared__ double coef[6];
+    __shared__ float coef[6];
     __shared__ int finite_nodes, winner, stop;
     __shared__ float2 probe_t[kConsensusProbes], probe_xy[kConsensusProbes];
     __shared__ uint8_t probe_ok[kConsensusProbes];
@@ -386,7 +408,7 @@ __global__ void __launch_bounds__(kConsensusThreads) consensus_kernel(NnConsensu
     {
         int n = 0;
         for (int i = threadIdx.x; i < a.nodes; i += kConsensusThreads) {
-            double u, v;
+            float u, v;
             n += node_total(a, i, u, v) ? 1 : 0;
         }
         n = __reduce_add_sync(0xffffffffu, n);
@@ -397,59 +419,35 @@ __global__ void __launch_bounds__(kConsensusThreads) consensus_kernel(NnConsensu
     }
     if (finite_nodes < 3) {
         for (int i = threadIdx.x; i < a.nodes; i += kConsensusThreads) {
-            double u, v;
+            float u, v;
             node_total(a, i, u, v);
             const size_t row = (size_t)i * a.ldp;
-            const float fu = (float)(u / a.scale), fv = (float)(v / a.scale);
-            a.base[row] = fu;
-            a.base[row + 3] = fv;
+            a.base[row] = u / a.scale;
+            a.base[row + 3] = v / a.scale;
         }
         return;
     }
-    // probe totals in shared memory, FP32 (the inlier test is a squared
-    // distance against the squared tolerance)
+    // probe totals in shared memory (the inlier test is a squared distance
+    // against the squared tolerance)
     for (int k = threadIdx.x; k < a.n_probe; k += kConsensusThreads) {
-        double u, v;
+        float u, v;
         const int j = a.probe[k];
         const bool ok = node_total(a, j, u, v);
-        probe_t[k] = ok ? make_float2((float)u, (float)v) : make_float2(0.0f, 0.0f);
+        probe_t[k] = ok ? make_float2(u, v) : make_float2(0.0f, 0.0f);
         probe_xy[k] = ok ? a.xy[j] : make_float2(0.0f, 0.0f);
         probe_ok[k] = ok ? 1 : 0;
     }
     __syncthreads();
     const float tol2 = a.tol[0] * a.tol[0];
-    // hypotheses
     const int hyps = a.n_single + a.n_triple;
     int my_count = -1, my_index = 0x7fffffff;
     for (int h = threadIdx.x; h < hyps; h += kConsensusThreads) {
-        double c[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        bool ok;
-        if (h < a.n_single) {
-            double u, v;
-            ok = node_total(a, a.single[h], u, v);
-            c[0] = u;
-            c[3] = v;
-        } else {
-            const int *t = a.triple + 3 * (h - a.n_single);
-            double m[3][3], b[2][3];
-            ok = true;
-            for (int r = 0; r < 3 && ok; ++r) {
-                double u, v;
-                ok = node_total(a, t[r], u, v);
-                if (!ok) break;
-                const float2 p = a.xy[t[r]];
-                m[r][0] = 1.0; m[r][1] = (double)p.x; m[r][2] = (double)p.y;
-                b[0][r] = u; b[1][r] = v;
-            }
-            ok = ok && solve3(m, b, 1e-9, c);
-        }
-        if (!ok) continue;
-        const float c0 = (float)c[0], c1 = (float)c[1], c2 = (float)c[2];
-        const float c3 = (float)c[3], c4 = (float)c[4], c5 = (float)c[5];
+        float c[6];
+        if (!hypothesis(a, h, c)) continue;
         int count = 0;
         for (int k = 0; k < a.n_probe; ++k) {
             const float2 p = probe_xy[k], t = probe_t[k];
-            const float du = c0 + c1 * p.x + c2 * p.y - t.x, dv = c3 + c4 * p.x + c5 * p.y - t.y;
+            const float du = c[0] + c[1] * p.x + c[2] * p.y - t.x, dv = c[3] + c[4] * p.x + c[5] * p.y - t.y;
             count += (probe_ok[k] && du * du + dv * dv <= tol2) ? 1 : 0;
         }
         if (count > my_count) { my_count = count; my_index = h; }
@@ -466,45 +464,25 @@ __global__ void __launch_bounds__(kConsensusThreads) consensus_kernel(NnConsensu
             if (best_count[w] > bc || (best_count[w] == bc && best_index[w] < bi)) { bc = best_count[w]; bi = best_index[w]; }
         winner = bc >= 0 ? bi : -1;
         stop = 0;
-        // the winner's coefficients, recomputed
-        double c[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        if (winner >= 0 && winner < a.n_single) {
-            double u, v;
-            node_total(a, a.single[winner], u, v);
-            c[0] = u;
-            c[3] = v;
-        } else if (winner >= 0) {
-            const int *t = a.triple + 3 * (winner - a.n_single);
-            double m[3][3], b[2][3];
-            for (int r = 0; r < 3; ++r) {
-                double u, v;
-                node_total(a, t[r], u, v);
-                const float2 p = a.xy[t[r]];
-                m[r][0] = 1.0; m[r][1] = (double)p.x; m[r][2] = (double)p.y;
-                b[0][r] = u; b[1][r] = v;
-            }
-            solve3(m, b, 1e-9, c);
-        }
+        float c[6];
+        if (winner < 0 || !hypothesis(a, winner, c))
+            for (int k = 0; k < 6; ++k) c[k] = 0.0f;
         for (int k = 0; k < 6; ++k) coef[k] = c[k];
     }
     __syncthreads();
     // refits
     for (int t = 0; t < a.n_tol && winner >= 0; ++t) {
         float x[12] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        const float tol2 = a.tol[t] * a.tol[t];
-        const float c0 = (float)coef[0], c1 = (float)coef[1], c2 = (float)coef[2];
-        const float c3 = (float)coef[3], c4 = (float)coef[4], c5 = (float)coef[5];
+        const float tol2t = a.tol[t] * a.tol[t];
+        const float c0 = coef[0], c1 = coef[1], c2 = coef[2], c3 = coef[3], c4 = coef[4], c5 = coef[5];
         for (int i = threadIdx.x; i < a.nodes; i += kConsensusThreads) {
-            double u, v;
+            float u, v;
             if (!node_total(a, i, u, v)) continue;
             const float2 p = a.xy[i];
-            // inlier test in FP32 squared distances; per-thread and per-warp
-            // sums in FP32, across warps in FP64
-            const float du = c0 + c1 * p.x + c2 * p.y - (float)u, dv = c3 + c4 * p.x + c5 * p.y - (float)v;
-            if (!(du * du + dv * dv <= tol2)) continue;
-            const float px = p.x, py = p.y, fu = (float)u, fv = (float)v;
-            x[0] += 1.0f; x[1] += px; x[2] += py; x[3] += px * px; x[4] += px * py; x[5] += py * py;
-            x[6] += fu; x[7] += px * fu; x[8] += py * fu; x[9] += fv; x[10] += px * fv; x[11] += py * fv;
+            const float du = c0 + c1 * p.x + c2 * p.y - u, dv = c3 + c4 * p.x + c5 * p.y - v;
+            if (!(du * du + dv * dv <= tol2t)) continue;
+            x[0] += 1.0f; x[1] += p.x; x[2] += p.y; x[3] += p.x * p.x; x[4] += p.x * p.y; x[5] += p.y * p.y;
+            x[6] += u; x[7] += p.x * u; x[8] += p.y * u; x[9] += v; x[10] += p.x * v; x[11] += p.y * v;
         }
         block_sum<12>(x, red);
         if (threadIdx.x == 0) {
@@ -513,10 +491,10 @@ __global__ void __launch_bounds__(kConsensusThreads) consensus_kernel(NnConsensu
             const double m[3][3] = {{r[0], r[1], r[2]}, {r[1], r[3], r[4]}, {r[2], r[4], r[5]}};
             const double b[2][3] = {{r[6], r[7], r[8]}, {r[9], r[10], r[11]}};
             const double scale = r[0] * r[3] * r[5] + 1e-300;
-            if (r[0] < 3.0 || !solve3(m, b, 1e-12 * scale, c)) {
+            if (r[0] < 3.0 || !solve3<double>(m, b, 1e-12 * scale, c)) {
                 stop = 1;
             } else {
-                for (int k = 0; k < 6; ++k) coef[k] = c[k];
+                for (int k = 0; k < 6; ++k) coef[k] = (float)c[k];
             }
         }
         __syncthreads();
@@ -524,7 +502,7 @@ __global__ void __launch_bounds__(kConsensusThreads) consensus_kernel(NnConsensu
     }
     // fitted field (winner < 0: no usable hypothesis, totals kept)
     for (int i = threadIdx.x; i < a.nodes; i += kConsensusThreads) {
-        double u, v;
+        float u, v;
         node_total(a, i, u, v);
         if (winner >= 0) {
             const float2 p = a.xy[i];
@@ -532,9 +510,8 @@ __global__ void __launch_bounds__(kConsensusThreads) consensus_kernel(NnConsensu
             v = coef[3] + coef[4] * p.x + coef[5] * p.y;
         }
         const size_t row = (size_t)i * a.ldp;
-        const float fu = (float)(u / a.scale), fv = (float)(v / a.scale);
-        a.base[row] = fu;
-        a.base[row + 3] = fv;
+        a.base[row] = u / a.scale;
+        a.base[row + 3] = v / a.scale;
     }
 }
 
@@ -588,6 +565,49 @@ __global__ void node_rows_kernel(const float *state, int grid_w, int grid_h, int
     row[3] = s0.w / translation_scale - bv;
     row[4] = s1.x * gradient_scale;
     row[5] = s1.y * gradient_scale;
+}
+
+// Direct 3x3 stride-2 convolution of the 2-channel input layer with 32
+// outputs, bias and ReLU, for inference: one output pixel per thread, the 18
+// input taps in registers and the weights as constant operands of the FMAs
+// (kernel parameters), so the layer reads its input once and writes its BF16
+// output once, with no im2col operand and none of the GEMM's K padding.
+// FP32 accumulation over k = (ky, kx, ci) in order, bias added after the sum,
+// as the GEMM epilogue does.
+__global__ void __launch_bounds__(256) conv_c2_direct_kernel(NnConvShape s, const uint32_t *__restrict__ x,
+                                                             NnConv1Weights p, uint4 *__restrict__ y) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= s.B * s.OH * s.OW) return;
+    const int ox = m % s.OW, t = m / s.OW, oy = t % s.OH, b = t / s.OH;
+    float in[18];
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
+        const int ky = tap / 3, kx = tap - 3 * ky;
+        const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
+        const uint32_t v = (iy >= 0 && iy < s.H && ix >= 0 && ix < s.W) ? __ldg(x + ((size_t)b * s.H + iy) * s.W + ix) : 0u;
+        in[2 * tap] = __uint_as_float(v << 16);             // channel 0 (low half)
+        in[2 * tap + 1] = __uint_as_float(v & 0xffff0000u);  // channel 1 (high half)
+    }
+    uint4 *row = y + (size_t)m * 4;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint32_t packed[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            float r[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int co = q * 8 + h * 2 + e;
+                float acc = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 18; ++k) acc = fmaf(p.w[co][k], in[k], acc);
+                r[e] = fmaxf(acc + p.bias[co], 0.0f);
+            }
+            const __nv_bfloat162 v2 = __floats2bfloat162_rn(r[0], r[1]);
+            packed[h] = *reinterpret_cast<const uint32_t *>(&v2);
+        }
+        row[q] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    }
 }
 
 unsigned blocks(long long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -714,6 +734,15 @@ cudaError_t launch_nn_node_rows(const float *state, int grid_w, int grid_h, int 
     if (n <= 0) return cudaSuccess;
     node_rows_kernel<<<blocks(n, 256), 256, 0, s>>>(state, grid_w, grid_h, step, lattice_w, lattice_h, pred, base, ldp,
                                                    translation_scale, gradient_scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_conv_c2_direct(const NnConvShape &sh, const void *x, const NnConv1Weights &w, void *y,
+                                     cudaStream_t s) {
+    const long long rows = (long long)sh.B * sh.OH * sh.OW;
+    if (rows <= 0) return cudaSuccess;
+    conv_c2_direct_kernel<<<blocks(rows, 256), 256, 0, s>>>(sh, static_cast<const uint32_t *>(x), w,
+                                                            static_cast<uint4 *>(y));
     return cudaGetLastError();
 }
 

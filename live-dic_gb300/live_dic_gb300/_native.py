@@ -210,6 +210,7 @@ _SIGNATURES = {
     "gbdic_nn_regression_loss": (C.c_int, [P, I32, P, I32, I32, P, P, I32, P, P]),
     "gbdic_reduce_half": (C.c_int, [P, I32, I32, P, P]),
     "gbdic_nn_lattice_seeds": (C.c_int, [P, P, I32, I32, I32, I32, I32, I32, I32, C.c_float, C.c_float, P, P, P]),
+    "gbdic_nn_conv_c2_direct": (C.c_int, [C.POINTER(NnConvShape), P, P, P, P, P]),
     "gbdic_nn_consensus": (C.c_int, [P, P, I32, I32, P, P, I32, P, I32, P, I32, P, I32, C.c_float, P]),
     "gbdic_nn_reseed_select": (C.c_int, [P, I32, P, I32, P, P, P, P]),
     "gbdic_nn_merge_rows": (C.c_int, [P, P, I32, I32, P, P]),

@@ -165,11 +165,29 @@ class SeedNet:
         _call(self.lib, "gbdic_nn_transpose", _ptr(self.w6b), OUT_PAD, self.features, self.features, _ptr(self.w6t),
               LOSS_PAD, self.features, stream)
 
+    def use_direct_first_layer(self) -> None:
+        """Inference copies: run the 2-channel input layer as one direct
+        convolution (gbdic_nn_conv_c2_direct) with the current BF16 weights,
+        read to the host once here; later weight updates are not seen, and
+        the layer's im2col operand (needed by backward) is not written."""
+        torch = _torch()
+        c = self.convs[0]
+        w = self.w[0][:, :9 * c.cin].to(torch.bfloat16).float().cpu().numpy()
+        self._direct = (np.ascontiguousarray(w, dtype=np.float32),
+                        np.ascontiguousarray(self.b[0].cpu().numpy(), dtype=np.float32))
+
     # ------------------------------------------------------------ forward
     def forward(self, stream=None):
         """self.x0 (B x 64 x 64 x 2 BF16) -> self.out (B x 16 FP32, first 6 used)."""
         x = self.x0
+        direct = getattr(self, "_direct", None)
         for i, c in enumerate(self.convs):
+            if i == 0 and direct is not None:
+                _call(self.lib, "gbdic_nn_conv_c2_direct", C.byref(self._shape(0)), _ptr(x),
+                      direct[0].ctypes.data_as(C.c_void_p), direct[1].ctypes.data_as(C.c_void_p), _ptr(self.y[0]),
+                      stream)
+                x = self.y[0]
+                continue
             _call(self.lib, "gbdic_nn_im2col", C.byref(self._shape(i)), _ptr(x), _ptr(self.a[i]), stream)
             self._gemm(self.a[i], self.wb[i], c.M, c.cout, c.kp, d_bf16=self.y[i], bias=self.b[i], relu=True,
                        stream=stream)
@@ -279,6 +297,8 @@ class SeedNet:
         for n, p in zip(names, self.params, strict=True):
             p.copy_(torch.as_tensor(state[n], device=self.device))
         self.pack()
+        if getattr(self, "_direct", None) is not None:
+            self.use_direct_first_layer()
 
 
 # ---------------------------------------------------------------- training data
@@ -521,6 +541,7 @@ class LearnedSeeder:
         # forward per pass.
         self.inet = SeedNet(batch=_pad(self.lattice, 128), device=net.device.index or 0)
         self.inet.load_state_dict(net.state_dict())
+        self.inet.use_direct_first_layer()
         self.batches = 1
         # One non-default stream carries the network, the engine's kernels and
         # the mask arithmetic in order (a NULL stream would select the

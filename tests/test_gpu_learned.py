@@ -212,3 +212,23 @@ def test_resolve_reuses_the_prefiltered_frame():
         torch.cuda.synchronize()
         np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
         assert (a.view(-1, 8)[:, 6].cpu().numpy()[active == 1] >= 1).mean() > 0.9
+
+
+def test_direct_first_layer_matches_the_gemm_path():
+    """The inference form of the input layer (direct convolution, weights as
+    constant operands) against im2col + tcgen05 GEMM on the same patches:
+    identical up to the FP32 summation order before BF16 rounding."""
+    gemm = learned.SeedNet(batch=128, seed=3)
+    direct = learned.SeedNet(batch=128, seed=3)
+    direct.use_direct_first_layer()
+    rng = np.random.default_rng(9)
+    x = torch.from_numpy(rng.normal(size=(128, 64, 64, 2)).astype(np.float32)).to(torch.bfloat16).cuda()
+    gemm.x0.copy_(x)
+    direct.x0.copy_(x)
+    gemm.forward()
+    direct.forward()
+    torch.cuda.synchronize()
+    y0, y1 = gemm.y[0].float(), direct.y[0].float()
+    close = (y0 - y1).abs() <= 1e-2 * y0.abs() + 1e-3
+    assert close.float().mean().item() > 0.999
+    np.testing.assert_allclose(direct.out[:, :6].cpu().numpy(), gemm.out[:, :6].cpu().numpy(), rtol=2e-2, atol=2e-2)
