@@ -51,6 +51,7 @@ LOSS_PAD = 64         # K padding of the output gradient
 TRANSLATION_SCALE = 16.0
 GRADIENT_SCALE = 20.0
 CONSENSUS_TOLERANCES = (8.0, 6.0, 4.0, 3.0)   # px: hypothesis scoring, then refits
+NODE_ITERATIONS = 8   # Gauss-Newton iterations of the lattice-node solve
 NORMALISATION = np.array([1 / TRANSLATION_SCALE, GRADIENT_SCALE, GRADIENT_SCALE, 1 / TRANSLATION_SCALE,
                           GRADIENT_SCALE, GRADIENT_SCALE], np.float32)
 
@@ -685,8 +686,13 @@ class LearnedSeeder:
             # network's proposals; their solved warps replace the network rows
             # and the interpolated seeds of every subset come from them.  The
             # full solve then reuses the node solve's B-spline coefficients.
+            # The node solve is latency-bound (a few hundred subsets), so its
+            # iterations are capped at NODE_ITERATIONS: a node that needs more
+            # keeps the network's warp.
+            node_cfg = eng._cfg(eng._config)
+            node_cfg.iterations = min(int(node_cfg.iterations), NODE_ITERATIONS)
             _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self._node_active),
-                         cfg, _ptr(self.state), stream)
+                         C.byref(node_cfg), _ptr(self.state), stream)
             _call(self.lib, "gbdic_nn_node_rows", _ptr(self.state), self.gw, self.gh, self.step, self.lw, self.lh,
                   _ptr(self.pred), _ptr(self.base) if self._shifted else None, OUT_PAD, C.c_float(TRANSLATION_SCALE),
                   C.c_float(GRADIENT_SCALE), stream)
