@@ -160,17 +160,48 @@ __global__ void gradient_kernel(const float *__restrict__ intensity, const float
 }
 
 // ---------------------------------------------------------------- stage 4
-template <int MODEL>
-struct Moments {
-    static constexpr int nm = MODEL == kModelQuadratic ? 6 : (MODEL == kModelTranslation ? 1 : 3);
-    static constexpr int pairs = nm * (nm + 1) / 2;
-    static constexpr int count = 1 + 4 * nm + 3 * pairs;  // 8, 31, 88
-};
-
 // Pair index (i <= j) -> position in the upper-triangular list.
 __host__ __device__ constexpr int pair_index(int nm, int i, int j) {
     return i * nm - i * (i - 1) / 2 + (j - i);
 }
+
+// Quadratic Hessian moments by monomial: the products m_i m_j of the six
+// monomials (1, x, y, x^2/2, xy, y^2/2) are c x^a y^b with a + b <= 4, 15
+// distinct monomials, so each gradient product needs 15 sums instead of 21
+// (c is 1, 1/2 or 1/4, exact).  x, y are integer or half-integer offsets, so
+// every monomial of a window up to 41 px is an exact binary32 value.
+__host__ __device__ constexpr int mono_exp_x(int i) { return i == 1 ? 1 : i == 3 ? 2 : i == 4 ? 1 : 0; }
+__host__ __device__ constexpr int mono_exp_y(int i) { return i == 2 ? 1 : i == 4 ? 1 : i == 5 ? 2 : 0; }
+// index of x^a y^b in (1, x, y, x^2, xy, y^2, x^3, x^2y, xy^2, y^3, x^4, ...)
+__host__ __device__ constexpr int monomial_index(int a, int b) {
+    return (a + b) * (a + b + 1) / 2 + b;
+}
+__host__ __device__ constexpr float pair_scale(int i, int j) {
+    return (i == 3 || i == 5 ? 0.5f : 1.0f) * (j == 3 || j == 5 ? 0.5f : 1.0f);
+}
+
+template <int MODEL>
+struct Moments {
+    static constexpr int nm = MODEL == kModelQuadratic ? 6 : (MODEL == kModelTranslation ? 1 : 3);
+    static constexpr int pairs = nm * (nm + 1) / 2;
+    // Hessian sums per gradient product: pairs of monomials, or for the
+    // quadratic model the 15 monomials of degree <= 4
+    static constexpr int hess = MODEL == kModelQuadratic ? 15 : pairs;
+    static constexpr int count = 1 + 4 * nm + 3 * hess;  // 8, 31, 70
+};
+
+// Position of Hessian entry (i <= j) among a gradient product's sums, and
+// its scale.
+template <int MODEL>
+__host__ __device__ constexpr int hess_index(int i, int j) {
+    return MODEL == kModelQuadratic ? monomial_index(mono_exp_x(i) + mono_exp_x(j), mono_exp_y(i) + mono_exp_y(j))
+                                    : pair_index(Moments<MODEL>::nm, i, j);
+}
+template <int MODEL>
+__host__ __device__ constexpr float hess_scale(int i, int j) {
+    return MODEL == kModelQuadratic ? pair_scale(i, j) : 1.0f;
+}
+
 
 // All moments of one pixel in the order of Moments (f^2; gx f m; gy f m;
 // gx m; gy m; then gx^2, gx gy, gy^2 times m_i m_j for i <= j), with
@@ -189,14 +220,27 @@ __device__ __forceinline__ void moment_values(float w, float f, float gx, float 
         out[1 + 3 * nm + q] = wgy * m[q];
     }
     int k = 1 + 4 * nm;
+    if constexpr (MODEL == kModelQuadratic) {
+        // x = m[1], y = m[2]: the 15 monomials x^a y^b (a + b <= 4), exact
+        const float x = m[1], y = m[2], x2 = x * x, xy = x * y, y2 = y * y;
+        const float mono[15] = {1.0f, x, y, x2, xy, y2, x2 * x, x2 * y, x * y2, y2 * y,
+                                x2 * x2, x2 * xy, x2 * y2, xy * y2, y2 * y2};
 #pragma unroll
-    for (int block = 0; block < 3; ++block) {
-        const float wg = w * (block == 0 ? gx * gx : (block == 1 ? gx * gy : gy * gy));
+        for (int block = 0; block < 3; ++block) {
+            const float wg = w * (block == 0 ? gx * gx : (block == 1 ? gx * gy : gy * gy));
 #pragma unroll
-        for (int i = 0; i < nm; ++i) {
-            const float wgi = wg * m[i];
+            for (int q = 0; q < 15; ++q) out[k++] = wg * mono[q];
+        }
+    } else {
 #pragma unroll
-            for (int j = i; j < nm; ++j) out[k++] = wgi * m[j];
+        for (int block = 0; block < 3; ++block) {
+            const float wg = w * (block == 0 ? gx * gx : (block == 1 ? gx * gy : gy * gy));
+#pragma unroll
+            for (int i = 0; i < nm; ++i) {
+                const float wgi = wg * m[i];
+#pragma unroll
+                for (int j = i; j < nm; ++j) out[k++] = wgi * m[j];
+            }
         }
     }
 }
@@ -358,8 +402,8 @@ template <int MODEL>
 __global__ void __launch_bounds__(128) subset_prep_kernel(PrepArgs a) {
     using T = typename std::conditional<MODEL == kModelQuadratic, double, float>::type;
     constexpr int n = parameter_count(MODEL);
-    constexpr int nm = Moments<MODEL>::nm, P = Moments<MODEL>::pairs, NM = Moments<MODEL>::count;
-    constexpr int kChunkM = MODEL == kModelTranslation ? 8 : 32;
+    constexpr int nm = Moments<MODEL>::nm, P = Moments<MODEL>::hess, NM = Moments<MODEL>::count;
+    constexpr int kChunkM = MODEL == kModelTranslation ? 8 : (MODEL == kModelQuadratic ? 36 : 32);
     __shared__ float s_tot[4][NM];
     __shared__ T s_A[4][n * n];
     __shared__ T s_X[4][n * n];
@@ -480,7 +524,7 @@ __global__ void __launch_bounds__(128) subset_prep_kernel(PrepArgs a) {
             for (int r = 0; r < n; ++r) {
                 const int br = blk(r), ir = mono(r);
                 const int lo = iq < ir ? iq : ir, hi = iq < ir ? ir : iq;
-                A[lane * n + r] = (T)t[1 + 4 * nm + (bq + br) * P + pair_index(nm, lo, hi)];
+                A[lane * n + r] = (T)(hess_scale<MODEL>(lo, hi) * t[1 + 4 * nm + (bq + br) * P + hess_index<MODEL>(lo, hi)]);
             }
         }
         __syncwarp();
