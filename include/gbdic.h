@@ -184,7 +184,9 @@ int gbdic_set_partial_support(gbdic_engine *engine, int32_t count, const int32_t
 int gbdic_register_seeded_device(gbdic_engine *engine, const uint8_t *device_frame, const float *device_seed,
                                  const uint32_t *device_active, const gbdic_solver_cfg *cfg, float *device_state,
                                  void *stream);
-/* Second seeded solve of the same device frame as the previous
+/* Second seeded solve (new here; the learned seeding's retry, nearest
+ * reference component the selective retry wgpu_backend.py:1893-2036) of the
+ * same device frame as the previous
  * gbdic_register_seeded_device call (its B-spline coefficients are reused,
  * not recomputed): typically only a few subsets active after a reseeding
  * search.  Calling it with another frame solves against stale coefficients. */
@@ -442,8 +444,9 @@ int gbdic_fourier_destroy(gbdic_fourier *fourier);
 const char *gbdic_fourier_last_error(const gbdic_fourier *fourier);
 int gbdic_fourier_estimate(gbdic_fourier *fourier, const uint8_t *frame, int64_t row_stride, int32_t height,
                            int32_t x, int32_t y, int32_t device_frame, double *out);
-/* Stream-ordered phase correlation of a device frame's window (no host
- * synchronisation) that writes the accepted integer shift into rows of affine
+/* Stream-ordered phase correlation (new here; the computation of
+ * FourierInitializer.estimate, fourier.py:59-111) of a device frame's window
+ * (no host synchronisation) that writes the accepted integer shift into rows of affine
  * parameters: rows[i * pitch] = dx * multiplier, rows[i * pitch + 3] =
  * dy * multiplier for i < count.  Accepted when the window's standard
  * deviation is >= 1, the peak score >= 8 and the overlap >= 0.25, else zero
