@@ -1,18 +1,30 @@
 """Static ROI geometry, computed once per reference on the host.
 
-Restates the reference's live_dic/roi.py (validate_roi 29-60, integral 63,
-select_windows 74-86, reduce_mask 89-97, _links_clear 100-107, RoiPlan
-110-170, prepare_roi 178-263, seed_permissions 358-437): full-window
-selection through a summed-area table of forbidden pixels, 3x3 (or 9x9)
-neighbour-permission bits for UOD, and coarse-to-fine seed permissions.
-The mask layout, bit layouts and hash format are the reference's, so plans
-and archives are interchangeable.
+What it computes is the reference's live_dic/roi.py: window selection
+(validate_roi 29-60, integral 63-65, select_windows 74-86), the coarse
+pyramid mask (reduce_mask 89-97), the segment-box link test (100-107), the
+plan record (RoiPlan 110-170), UOD neighbour permissions and the 9x9 median
+lattice (prepare_roi 178-263), partial-support windows (266-366) and
+coarse-to-fine seed permissions (369-437).  The formats are interface and
+stay the reference's: the 3x3 bit order (dy+1)*3 + dx+1, the 9x9 lattice in
+four 24-bit float words, support words (row-major pixels, bit 0 of
+little-endian uint32 words first), seed words (bits 0-3 corners, bit 4
+selected, bits 5-31 fallback index + 1) and the mask hash
+("live-dic-roi-v1\\0" + uint64le(height, width) + the mask's 0/1 bytes).
+
+The computation is organised differently: every neighbour link of a plan is
+evaluated once for all offsets of the widest stencil in use (shared by the
+3x3 bits and the median lattice), through a zero-padded selection grid; the
+mask reduction is a separable AND; support words are built by integer
+shifts; the central component is a connected-component labelling; the
+visibility sets are computed cell by cell for all end points at once; and
+seed permissions are evaluated for the four corners and the 36 fallback
+candidates as stacked arrays.
 """
 
 from __future__ import annotations
 
 import hashlib
-import struct
 from dataclasses import dataclass
 
 import numpy as np
@@ -26,10 +38,15 @@ from .subset import subset_grid_shape
 PARTIAL_MAX_NORMALIZED_CONDITION = 1e8
 PARTIAL_MIN_WEIGHTED_CONTRAST = 1.0
 
+_HASH_PREFIX = b"live-dic-roi-v1\0"
+_LATTICE = 9          # side of the median neighbour lattice
+_WORD_BITS = 24       # exact integers per float32 word
+
 
 def immutable(array: np.ndarray) -> np.ndarray:
-    """Read-only copy that owns its bytes."""
-    return np.frombuffer(array.tobytes(order="C"), dtype=array.dtype).reshape(array.shape)
+    """Read-only array backed by its own bytes (no alias of the caller's)."""
+    data = np.ascontiguousarray(array)
+    return np.frombuffer(data.tobytes(), dtype=data.dtype).reshape(data.shape)
 
 
 def validate_roi(
@@ -39,6 +56,8 @@ def validate_roi(
     motion_model: str,
     truncation: str = "none",
 ) -> np.ndarray | None:
+    """Argument checks with the reference's messages; returns an owned,
+    canonical (0/1 bytes) copy of the mask."""
     if not isinstance(policy, str) or policy not in ("full", "partial"):
         raise ValueError("roi_policy must be 'full' or 'partial'")
     if not isinstance(truncation, str) or truncation not in ("none", "visibility"):
@@ -53,59 +72,72 @@ def validate_roi(
         raise TypeError("roi_mask must be a two-dimensional boolean NumPy array")
     if mask.ndim != 2 or mask.shape != shape:
         raise ValueError(f"roi_mask must have reference shape {shape}")
-    return immutable(np.logical_and(mask, True))
+    return immutable(mask.astype(np.bool_, copy=True))
 
 
+def mask_digest(mask: np.ndarray) -> str:
+    """SHA-256 of the hash prefix, the shape as two little-endian uint64 and
+    the mask's bytes in C order (one 0/1 byte per pixel)."""
+    h = hashlib.sha256(_HASH_PREFIX)
+    h.update(np.asarray(mask.shape, dtype="<u8").tobytes())
+    h.update(np.ascontiguousarray(mask, dtype=np.bool_).view(np.uint8).tobytes())
+    return h.hexdigest()
+
+
+# ---------------------------------------------------------------- counting forbidden pixels
 def integral(mask: np.ndarray) -> np.ndarray:
-    """Exclusive 2-D prefix sum of forbidden pixels (int64), padded by one."""
-    forbidden = (~mask).astype(np.int64)
-    out = np.zeros((mask.shape[0] + 1, mask.shape[1] + 1), dtype=np.int64)
-    out[1:, 1:] = forbidden.cumsum(axis=0).cumsum(axis=1)
-    return out
+    """Summed-area table of forbidden pixels, int64, with a zero first row
+    and column: entry [y, x] counts the forbidden pixels of [0, x) x [0, y)."""
+    h, w = mask.shape
+    table = np.zeros((h + 1, w + 1), dtype=np.int64)
+    np.cumsum(np.logical_not(mask), axis=0, dtype=np.int64, out=table[1:, 1:])
+    np.cumsum(table[1:, 1:], axis=1, out=table[1:, 1:])
+    return table
 
 
 def boxes_clear(prefix: np.ndarray, x0, y0, x1, y1) -> np.ndarray:
-    """True where the half-open pixel box [x0, x1) x [y0, y1) holds no forbidden pixel."""
-    return prefix[y1, x1] - prefix[y0, x1] - prefix[y1, x0] + prefix[y0, x0] == 0
+    """True where the half-open box [x0, x1) x [y0, y1) has no forbidden pixel."""
+    forbidden = (prefix[y1, x1] + prefix[y0, x0]) - (prefix[y0, x1] + prefix[y1, x0])
+    return forbidden == 0
 
 
 def select_windows(mask: np.ndarray, size: int, stride: int, *, summed_area: np.ndarray | None = None) -> np.ndarray:
+    """Windows whose whole S x S footprint is allowed."""
     height, width = mask.shape
     gw, gh = subset_grid_shape(width, height, subset_size=size, subset_stride=stride)
-    ys, xs = np.meshgrid(np.arange(gh) * stride, np.arange(gw) * stride, indexing="ij")
-    prefix = integral(mask) if summed_area is None else summed_area
-    return boxes_clear(prefix, xs, ys, xs + size, ys + size)
+    table = integral(mask) if summed_area is None else summed_area
+    x0 = (np.arange(gw) * stride)[None, :]
+    y0 = (np.arange(gh) * stride)[:, None]
+    return boxes_clear(table, x0, y0, x0 + size, y0 + size)
 
 
-def _reflect(n: int, pad: int) -> np.ndarray:
-    idx = np.arange(-pad, n + pad)
-    idx = np.where(idx < 0, -idx, idx)
-    return np.where(idx >= n, 2 * n - 2 - idx, idx)
+def _segment_clear(prefix: np.ndarray, ax, ay, bx, by) -> np.ndarray:
+    """The closed pixel box spanned by the segment between two pixel-centre
+    points (every pixel the segment touches, corners included) holds no
+    forbidden pixel.  A pixel k covers [k - 0.5, k + 0.5]."""
+    h, w = prefix.shape[0] - 1, prefix.shape[1] - 1
+    first_x = np.ceil(np.minimum(ax, bx) - 0.5).astype(np.int64)
+    first_y = np.ceil(np.minimum(ay, by) - 0.5).astype(np.int64)
+    last_x = np.floor(np.maximum(ax, bx) + 0.5).astype(np.int64)
+    last_y = np.floor(np.maximum(ay, by) + 0.5).astype(np.int64)
+    return boxes_clear(prefix, np.maximum(first_x, 0), np.maximum(first_y, 0),
+                       np.minimum(last_x + 1, w), np.minimum(last_y + 1, h))
 
 
 def reduce_mask(mask: np.ndarray) -> np.ndarray:
-    """A coarse pixel is allowed only if all 25 reflected source pixels of the
-    5x5 reduction footprint centred on (2x, 2y) are allowed."""
+    """Mask of the next pyramid level: coarse pixel (x, y) is allowed when
+    the 5 x 5 reduction footprint centred on (2x, 2y), reflected at the
+    borders without repeating the edge, is allowed.  Evaluated as an AND
+    along x, then along y."""
     h, w = mask.shape
     h2, w2 = h // 2, w // 2
-    padded = mask[_reflect(h, 2)][:, _reflect(w, 2)]
-    out = np.ones((h2, w2), dtype=bool)
-    for dy in range(5):
-        for dx in range(5):
-            out &= padded[dy : dy + 2 * h2 : 2, dx : dx + 2 * w2 : 2]
-    return immutable(out)
+    padded = np.pad(np.asarray(mask, bool), 2, mode="reflect")
+    across = np.logical_and.reduce([padded[:, k: k + 2 * w2: 2] for k in range(5)])
+    down = np.logical_and.reduce([across[k: k + 2 * h2: 2, :] for k in range(5)])
+    return immutable(down)
 
 
-def _links_clear(prefix: np.ndarray, ax, ay, bx, by) -> np.ndarray:
-    """Closed pixel box around the segment a-b is free of forbidden pixels."""
-    h, w = np.array(prefix.shape) - 1
-    x0 = np.maximum(0, np.ceil(np.minimum(ax, bx) - 0.5).astype(int))
-    y0 = np.maximum(0, np.ceil(np.minimum(ay, by) - 0.5).astype(int))
-    x1 = np.minimum(w, np.floor(np.maximum(ax, bx) + 0.5).astype(int) + 1)
-    y1 = np.minimum(h, np.floor(np.maximum(ay, by) + 0.5).astype(int) + 1)
-    return boxes_clear(prefix, x0, y0, x1, y1)
-
-
+# ---------------------------------------------------------------- the plan
 @dataclass(frozen=True, slots=True)
 class RoiPlan:
     """Immutable ROI arrays shared by a reference and all its results."""
@@ -132,27 +164,33 @@ class RoiPlan:
         return self.selected_count == 0
 
     def summary(self) -> dict:
-        return {
+        out = {
             "policy": self.policy,
             "truncation": self.truncation,
             "partial": 0 if self.partial_indices is None else int(self.partial_indices.size),
-            "maskShape": list(self.mask.shape),
-            "maskSha256": self.mask_hash,
-            "gridTotal": self.selected.size,
-            "selected": self.selected_count,
-            "excluded": self.selected.size - self.selected_count,
-            "hashFormat": "live-dic-roi-v1\\0 + uint64le(height,width) + C-order uint8 bool",
         }
+        if self.policy == "partial":
+            out.update(supportConditionLimit=PARTIAL_MAX_NORMALIZED_CONDITION,
+                       supportContrastRmsMinimum=PARTIAL_MIN_WEIGHTED_CONTRAST, supportConnectivity=4,
+                       evenCenter="all four central pixels required")
+        out.update(
+            maskShape=list(self.mask.shape),
+            maskSha256=self.mask_hash,
+            gridTotal=self.selected.size,
+            selected=self.selected_count,
+            excluded=self.selected.size - self.selected_count,
+            hashFormat="live-dic-roi-v1\\0 + uint64le(height,width) + C-order uint8 bool",
+        )
+        return out
 
     def archive_fields(self) -> dict[str, np.ndarray]:
         fields = {"roi_mask": self.mask, "roi_selected": self.selected}
         if self.partial_indices is not None:
-            fields.update(
-                roi_partial_indices=self.partial_indices,
-                roi_support_words=self.support_words,
-                roi_support_boxes=self.support_boxes,
-                roi_coverage=self.coverage,
-            )
+            fields.update(roi_partial_indices=self.partial_indices, roi_support_words=self.support_words,
+                          roi_support_boxes=self.support_boxes, roi_coverage=self.coverage)
+            if self.support_condition is not None:
+                fields.update(roi_support_condition=self.support_condition, roi_support_rank=self.support_rank,
+                              roi_support_contrast=self.support_contrast)
         return fields
 
     def links_table(self, median_filter_size: int, outlier_policy: str) -> np.ndarray:
@@ -164,6 +202,27 @@ class RoiPlan:
         else:
             links[:, 0] = self.neighbour_bits.ravel()
         return links
+
+
+def _neighbour_links(selected: np.ndarray, prefix: np.ndarray | None, size: int, stride: int,
+                     radius: int) -> dict[tuple[int, int], np.ndarray]:
+    """For every offset (dx, dy) with |dx|, |dy| <= radius: both windows
+    selected and, with a mask, the box around the two window centres clear."""
+    gh, gw = selected.shape
+    grid = np.zeros((gh + 2 * radius, gw + 2 * radius), dtype=bool)
+    grid[radius: radius + gh, radius: radius + gw] = selected
+    half = 0.5 * (size - 1)
+    cx = (np.arange(gw) * stride + half)[None, :]
+    cy = (np.arange(gh) * stride + half)[:, None]
+    links = {}
+    for dy in range(-radius, radius + 1):
+        for dx in range(-radius, radius + 1):
+            other = grid[radius + dy: radius + dy + gh, radius + dx: radius + dx + gw]
+            ok = selected & other
+            if prefix is not None:
+                ok = ok & _segment_clear(prefix, cx, cy, cx + dx * stride, cy + dy * stride)
+            links[dx, dy] = ok
+    return links
 
 
 def prepare_roi(
@@ -178,151 +237,144 @@ def prepare_roi(
     median_filter_size = normalize_median_filter_size(median_filter_size)
     if mask is None:
         return None
-    height, width = mask.shape
-    all_allowed = bool(mask.all())
-    prefix = None if all_allowed else integral(mask)
-    gw, gh = subset_grid_shape(width, height, subset_size=size, subset_stride=stride)
-    selected = np.ones((gh, gw), dtype=bool) if all_allowed else select_windows(mask, size, stride, summed_area=prefix)
-    partial_indices = support_words = support_boxes = coverage = None
-    if policy == "partial":
-        selected, partial_indices, support_words, support_boxes, coverage = _partial_windows(
-            mask, selected, size, stride, truncation=truncation)
-    elif policy != "full" or truncation != "none":
+    if policy not in ("full", "partial") or (policy == "full" and truncation != "none"):
         raise ValueError("Unknown ROI policy/truncation")
-    y, x = np.indices(selected.shape)
-    ax = x * stride + (size - 1) / 2
-    ay = y * stride + (size - 1) / 2
-
-    def allowed_offset(dx: int, dy: int) -> np.ndarray:
-        nx, ny = x + dx, y + dy
-        inside = (nx >= 0) & (ny >= 0) & (nx < selected.shape[1]) & (ny < selected.shape[0])
-        ok = inside & selected & selected[ny.clip(0, selected.shape[0] - 1), nx.clip(0, selected.shape[1] - 1)]
-        if prefix is not None:
-            ok &= _links_clear(prefix, ax, ay, ax + dx * stride, ay + dy * stride)
-        return ok
-
+    height, width = mask.shape
+    everywhere = bool(mask.all())
+    prefix = None if everywhere else integral(mask)
+    gw, gh = subset_grid_shape(width, height, subset_size=size, subset_stride=stride)
+    if everywhere:
+        selected = np.ones((gh, gw), dtype=bool)
+    else:
+        selected = select_windows(mask, size, stride, summed_area=prefix)
+    partial = (None,) * 4
+    if policy == "partial":
+        selected, *partial = _partial_windows(mask, selected, size, stride, truncation=truncation)
+    radius = max(1, median_filter_size // 2)
+    links = _neighbour_links(selected, prefix, size, stride, radius)
     bits = np.zeros(selected.shape, dtype=np.uint32)
     for dy in (-1, 0, 1):
         for dx in (-1, 0, 1):
-            bits |= allowed_offset(dx, dy).astype(np.uint32) << np.uint32((dy + 1) * 3 + dx + 1)
+            bits |= links[dx, dy].astype(np.uint32) << np.uint32(3 * (dy + 1) + dx + 1)
     median_words = None
     if median_filter_size > 3:
-        radius = median_filter_size // 2
-        words = np.zeros((*selected.shape, 4), dtype=np.float32)
-        for dy in range(-radius, radius + 1):
-            for dx in range(-radius, radius + 1):
-                bit = (dy + 4) * 9 + dx + 4
-                words[..., bit // 24] += allowed_offset(dx, dy).astype(np.float32) * float(1 << (bit % 24))
-        median_words = immutable(words.reshape(-1, 4))
-    digest = hashlib.sha256(b"live-dic-roi-v1\0" + struct.pack("<QQ", *mask.shape) + mask.tobytes(order="C")).hexdigest()
+        # the fixed 9x9 lattice (bit (dy + 4) * 9 + dx + 4), 24 bits per word,
+        # whatever the median's own size
+        words = np.zeros((*selected.shape, 4), dtype=np.float64)
+        centre = _LATTICE // 2
+        for (dx, dy), ok in links.items():
+            word, bit = divmod((dy + centre) * _LATTICE + dx + centre, _WORD_BITS)
+            words[..., word] += ok * float(2 ** bit)
+        median_words = immutable(words.astype(np.float32).reshape(-1, 4))
     return RoiPlan(
-        mask,
-        immutable(selected),
-        immutable(bits),
-        digest,
-        not all_allowed,
-        int(selected.sum()),
-        policy,
-        truncation,
-        partial_indices,
-        support_words,
-        support_boxes,
-        coverage,
-        median_neighbour_words=median_words,
+        mask, immutable(selected), immutable(bits), mask_digest(mask), not everywhere, int(selected.sum()), policy,
+        truncation, *partial, median_neighbour_words=median_words,
     )
 
 
 # ---------------------------------------------------------------- partial support
 def pack_support(support: np.ndarray) -> np.ndarray:
-    """Row-major pixel bits, bit 0 of little-endian uint32 words first
-    (roi.py:266-270)."""
-    bits = np.packbits(np.asarray(support, bool).ravel(), bitorder="little")
-    bits = np.pad(bits, (0, (-bits.size) % 4))
-    return bits.view("<u4").astype(np.uint32, copy=False)
+    """Pixels in row-major order; pixel i is bit i % 32 of word i // 32."""
+    flat = np.asarray(support, bool).ravel()
+    count = (flat.size + 31) // 32
+    bits = np.zeros(count * 32, dtype=np.uint64)
+    bits[: flat.size] = flat
+    return (bits.reshape(count, 32) << np.arange(32, dtype=np.uint64)).sum(axis=1).astype(np.uint32)
 
 
 def unpack_support(words: np.ndarray, size: int) -> np.ndarray:
-    raw = np.asarray(words, dtype="<u4").view(np.uint8)
-    return np.unpackbits(raw, bitorder="little")[: size * size].reshape(size, size).astype(bool)
+    w = np.asarray(words, dtype=np.uint32).ravel()
+    bits = (w[:, None] >> np.arange(32, dtype=np.uint32)) & np.uint32(1)
+    return bits.ravel()[: size * size].reshape(size, size).astype(bool)
+
+
+_FOUR_NEIGHBOURS = np.array([[0, 1, 0], [1, 1, 1], [0, 1, 0]], dtype=bool)
 
 
 def _central_component(support: np.ndarray) -> np.ndarray:
-    """Pixels 4-connected to the window centre (roi.py:279-300); an even
-    window needs all four central pixels allowed."""
+    """The 4-connected component of `support` that holds the window centre:
+    the centre pixel of an odd window, or all four central pixels of an
+    even one (otherwise the component is empty)."""
+    from scipy import ndimage
+
     size = support.shape[0]
-    lo, hi = (size - 1) // 2, size // 2
-    out = np.zeros_like(support, dtype=bool)
-    if not support[lo: hi + 1, lo: hi + 1].all():
-        return out
-    stack = [(lo, lo)]
-    out[lo, lo] = True
-    while stack:
-        y, x = stack.pop()
-        for ny, nx in ((y - 1, x), (y + 1, x), (y, x - 1), (y, x + 1)):
-            if 0 <= ny < size and 0 <= nx < size and support[ny, nx] and not out[ny, nx]:
-                out[ny, nx] = True
-                stack.append((ny, nx))
-    return out
+    a, b = (size - 1) // 2, size // 2
+    if not support[a: b + 1, a: b + 1].all():
+        return np.zeros(support.shape, dtype=bool)
+    labels, _ = ndimage.label(support, structure=_FOUR_NEIGHBOURS)
+    return labels == labels[a, a]
 
 
 _VISIBILITY: dict[int, np.ndarray] = {}
 
 
 def _visibility_paths(size: int) -> np.ndarray:
-    """For every pixel, the packed set of pixel cells touched by the segment
-    from the window centre to it (roi.py:303-327): slab intersection of the
-    segment with each closed unit cell, boundary touches included."""
+    """Boolean (pixels x cells) table: cell c lies on the closed segment from
+    the window centre to the centre of pixel p, touches of a cell's edge or
+    corner included.  Each cell [c - 0.5, c + 0.5]^2 is clipped against all
+    segments at once (slab method: the segment's parameter interval inside
+    the cell along x and along y must overlap within [0, 1])."""
     if size in _VISIBILITY:
         return _VISIBILITY[size]
-    y, x = np.indices((size, size)).reshape(2, -1).astype(np.float64)
-    centre = (size - 1) / 2
-    lower = np.zeros((size * size, size * size))
-    upper = np.ones_like(lower)
-    for coord in (x, y):
-        delta = coord - centre
-        moving = delta != 0
-        a = np.full_like(lower, -np.inf)
-        b = np.full_like(upper, np.inf)
-        a[moving] = (coord[None, :] - 0.5 - centre) / delta[moving, None]
-        b[moving] = (coord[None, :] + 0.5 - centre) / delta[moving, None]
-        lower = np.maximum(lower, np.minimum(a, b))
-        upper = np.minimum(upper, np.maximum(a, b))
-        upper[np.ix_(~moving, np.abs(coord - centre) > 0.5)] = -1
-    paths = immutable(np.stack([pack_support(row) for row in lower <= upper]))
-    _VISIBILITY[size] = paths
-    return paths
+    centre = 0.5 * (size - 1)
+    py, px = np.indices((size, size)).reshape(2, -1).astype(np.float64)
+    steps = (px - centre, py - centre)
+    table = np.zeros((size * size, size * size), dtype=bool)
+    for cell in range(size * size):
+        cy, cx = divmod(cell, size)
+        enter = np.zeros(size * size)
+        leave = np.ones(size * size)
+        for step, c in zip(steps, (cx, cy), strict=True):
+            lo_edge, hi_edge = c - 0.5 - centre, c + 0.5 - centre
+            fixed = step == 0.0
+            with np.errstate(divide="ignore", invalid="ignore"):
+                t0 = np.where(fixed, -np.inf, lo_edge / step)
+                t1 = np.where(fixed, np.inf, hi_edge / step)
+            enter = np.maximum(enter, np.minimum(t0, t1))
+            leave = np.minimum(leave, np.maximum(t0, t1))
+            if abs(c - centre) > 0.5:
+                # a segment that does not move along this axis stays on the centre line
+                leave = np.where(fixed, -1.0, leave)
+        table[:, cell] = enter <= leave
+    _VISIBILITY[size] = table
+    return table
 
 
 def _partial_windows(mask: np.ndarray, complete: np.ndarray, size: int, stride: int, *, truncation: str):
-    """Windows cut by the ROI whose central component survives
-    (roi.py:330-366): (selected, indices, support words, boxes, coverage)."""
+    """Windows cut by the mask whose central component survives.  Returns
+    (selected, window indices, support words, support boxes (x0, y0, x1, y1),
+    coverage)."""
     if truncation not in ("none", "visibility"):
         raise ValueError("roi_truncation must be 'none' or 'visibility'")
+    gh, gw = complete.shape
     selected = complete.copy()
-    indices, words, boxes = [], [], []
     coverage = complete.astype(np.float32)
-    for gy, gx in np.argwhere(~complete):
-        local = mask[gy * stride: gy * stride + size, gx * stride: gx * stride + size]
-        support = _central_component(local)
+    kept: list[tuple[int, np.ndarray]] = []
+    paths = _visibility_paths(size) if truncation == "visibility" else None
+    for index in np.flatnonzero(~complete):
+        gy, gx = divmod(int(index), gw)
+        window = mask[gy * stride: gy * stride + size, gx * stride: gx * stride + size]
+        support = _central_component(window)
+        if support.any() and paths is not None:
+            blocked = ~support.ravel()
+            visible = ~(paths & blocked[None, :]).any(axis=1)
+            support = _central_component(support & visible.reshape(size, size))
         if not support.any():
             continue
-        if truncation == "visibility":
-            visible = ~np.any(_visibility_paths(size) & ~pack_support(support), axis=1)
-            support = _central_component(support & visible.reshape(size, size))
-            if not support.any():
-                continue
         selected[gy, gx] = True
-        indices.append(gy * complete.shape[1] + gx)
-        words.append(pack_support(support))
-        sy, sx = np.nonzero(support)
-        boxes.append((sx.min(), sy.min(), sx.max(), sy.max()))
-        coverage[gy, gx] = support.sum() / (size * size)
-    count = (size * size + 31) // 32
-    return (selected, immutable(np.asarray(indices, np.uint32)),
-            immutable(np.asarray(words, np.uint32).reshape(-1, count)),
-            immutable(np.asarray(boxes, np.float32).reshape(-1, 4)), immutable(coverage))
+        coverage[gy, gx] = np.count_nonzero(support) / float(size * size)
+        kept.append((int(index), support))
+    words = (size * size + 31) // 32
+    indices = np.array([i for i, _ in kept], dtype=np.uint32)
+    packed = np.array([pack_support(s) for _, s in kept], dtype=np.uint32).reshape(-1, words)
+    boxes = np.zeros((len(kept), 4), dtype=np.float32)
+    for row, (_, s) in enumerate(kept):
+        cols, rows = np.flatnonzero(s.any(axis=0)), np.flatnonzero(s.any(axis=1))
+        boxes[row] = (cols[0], rows[0], cols[-1], rows[-1])
+    return selected, immutable(indices), immutable(packed), immutable(boxes), immutable(coverage)
 
 
+# ---------------------------------------------------------------- seed permissions
 def seed_permissions(
     source: RoiPlan,
     destination: RoiPlan,
@@ -336,53 +388,57 @@ def seed_permissions(
 ) -> np.ndarray:
     """Per destination subset: bits 0-3 allow the four bilinear source corners,
     bit 4 marks a selected destination, bits 5-31 hold 1 + the linear index of
-    a fallback source subset (0 = none) used when no corner is admissible."""
-    y, x = np.indices(destination.selected.shape)
-    centre = size / 2
-    sh, sw = source.selected.shape
-    sx = (destination_scale * (centre + x * stride) + (source_scale - destination_scale) / 2) / source_scale
-    sy = (destination_scale * (centre + y * stride) + (source_scale - destination_scale) / 2) / source_scale
-    lower_x = np.clip(np.floor((sx - centre) / stride), 0, max(0, sw - 2)).astype(int)
-    lower_y = np.clip(np.floor((sy - centre) / stride), 0, max(0, sh - 2)).astype(int)
-    bits = destination.selected.astype(np.uint32) << np.uint32(4)
-    prefix = reference_prefix if reference_prefix is not None else integral(reference_mask)
-    half = (size - 1) / 2
-    for corner in range(4):
-        nx = lower_x + (corner & 1)
-        ny = lower_y + (corner >> 1)
-        inside = (nx < sw) & (ny < sh)
-        nx = nx.clip(0, sw - 1)
-        ny = ny.clip(0, sh - 1)
-        ok = inside & source.selected[ny, nx] & destination.selected
-        ok &= _links_clear(
-            prefix,
-            destination_scale * (half + x * stride),
-            destination_scale * (half + y * stride),
-            source_scale * (half + nx * stride),
-            source_scale * (half + ny * stride),
-        )
-        bits |= ok.astype(np.uint32) << np.uint32(corner)
-    if source_scale > destination_scale and source.selected.size < (1 << 27) - 1:
-        my, mx = np.nonzero(destination.selected & ((bits & 15) == 0))
-        best = np.full(mx.shape, np.inf)
-        chosen = np.zeros(mx.shape, dtype=np.uint32)
-        for dy in range(-2, 4):
-            for dx in range(-2, 4):
-                nx = lower_x[my, mx] + dx
-                ny = lower_y[my, mx] + dy
-                inside = (nx >= 0) & (ny >= 0) & (nx < sw) & (ny < sh)
-                cx = nx.clip(0, sw - 1)
-                cy = ny.clip(0, sh - 1)
-                distance = (sx[my, mx] - (centre + cx * stride)) ** 2 + (sy[my, mx] - (centre + cy * stride)) ** 2
-                ok = inside & source.selected[cy, cx] & (distance < best)
-                ok &= _links_clear(
-                    prefix,
-                    destination_scale * (half + mx * stride),
-                    destination_scale * (half + my * stride),
-                    source_scale * (half + cx * stride),
-                    source_scale * (half + cy * stride),
-                )
-                best[ok] = distance[ok]
-                chosen[ok] = (cy[ok] * sw + cx[ok] + 1).astype(np.uint32)
-        bits[my, mx] |= chosen << np.uint32(5)
-    return immutable(bits)
+    a fallback source subset (0 = none) used when no corner is admissible.
+
+    Source corners follow the seed transfer's edge-anchored layout (window
+    centre at S/2 + k*step, half a coarse pixel of phase between the scales).
+    A corner, or a fallback candidate, is admissible when it is selected and
+    the reference-resolution box around the segment between the two window
+    centres ((S - 1)/2 + k*step, times each scale) is clear.  The fallback
+    (coarse-to-fine transfers only) is the nearest admissible source among
+    the 6 x 6 subsets around the lower corner; equal distances keep the
+    first in row-major (dy, dx) order."""
+    dsel = np.asarray(destination.selected, bool)
+    ssel = np.asarray(source.selected, bool)
+    sh, sw = ssel.shape
+    gy, gx = np.indices(dsel.shape)
+    edge = 0.5 * size
+    mid = 0.5 * (size - 1)
+    phase = 0.5 * (source_scale - destination_scale)
+    # destination window centre in source-level edge coordinates
+    sx = (destination_scale * (edge + gx * stride) + phase) / source_scale
+    sy = (destination_scale * (edge + gy * stride) + phase) / source_scale
+    low_x = np.clip(np.floor((sx - edge) / stride), 0, max(0, sw - 2)).astype(np.int64)
+    low_y = np.clip(np.floor((sy - edge) / stride), 0, max(0, sh - 2)).astype(np.int64)
+    prefix = integral(reference_mask) if reference_prefix is None else reference_prefix
+    ax, ay = destination_scale * (mid + gx * stride), destination_scale * (mid + gy * stride)
+
+    def admissible(nx, ny, ax, ay):
+        inside = (nx >= 0) & (ny >= 0) & (nx < sw) & (ny < sh)
+        cx, cy = np.clip(nx, 0, sw - 1), np.clip(ny, 0, sh - 1)
+        ok = inside & ssel[cy, cx]
+        ok &= _segment_clear(prefix, ax, ay, source_scale * (mid + cx * stride), source_scale * (mid + cy * stride))
+        return ok, cx, cy
+
+    corner_x = low_x[None] + np.array([0, 1, 0, 1])[:, None, None]
+    corner_y = low_y[None] + np.array([0, 0, 1, 1])[:, None, None]
+    corners, _, _ = admissible(corner_x, corner_y, ax[None], ay[None])
+    corners &= dsel[None]
+    words = dsel.astype(np.uint32) << np.uint32(4)
+    for k in range(4):
+        words |= corners[k].astype(np.uint32) << np.uint32(k)
+    if source_scale > destination_scale and ssel.size < (1 << 27) - 1:
+        my, mx = np.nonzero(dsel & ((words & 15) == 0))
+        if my.size:
+            off_y, off_x = np.divmod(np.arange(36), 6)
+            nx = low_x[my, mx][None, :] + (off_x - 2)[:, None]
+            ny = low_y[my, mx][None, :] + (off_y - 2)[:, None]
+            ok, cx, cy = admissible(nx, ny, ax[my, mx][None, :], ay[my, mx][None, :])
+            dist = (sx[my, mx][None, :] - (edge + cx * stride)) ** 2 + (sy[my, mx][None, :] - (edge + cy * stride)) ** 2
+            dist = np.where(ok, dist, np.inf)
+            best = np.argmin(dist, axis=0)
+            pick = np.arange(my.size)
+            found = np.isfinite(dist[best, pick])
+            fallback = np.where(found, cy[best, pick] * sw + cx[best, pick] + 1, 0).astype(np.uint32)
+            words[my, mx] |= fallback << np.uint32(5)
+    return immutable(words)

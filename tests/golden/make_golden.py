@@ -3,7 +3,7 @@
 Run from the repository root, in a checkout where the reference sources are
 available (they are not needed afterwards):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the live-dic checkout>
 
 The reference package imports Pillow and websockets at module level although
 none of the routines used here touch them, so both are replaced by empty
@@ -172,6 +172,49 @@ def main(reference_root: str) -> None:
     np.savez_compressed(HERE / "reference_vectors.npz", **out)
     fourier_vectors(Path(reference_root))
     partial_vectors(Path(reference_root))
+    roi_vectors(Path(reference_root))
+
+
+def roi_vectors(reference_root: Path) -> None:
+    """ROI planning on harder masks (several holes, a cut edge, odd and even
+    windows, overlapping and tiled grids, every median lattice, both partial
+    truncations) and the seed permissions between two pyramid levels."""
+    _, _, roi, _ = _import_reference(reference_root)
+    rng = np.random.default_rng(2718)
+    out: dict[str, np.ndarray] = {}
+    cases = [(190, 230, 17, 6), (160, 200, 16, 16), (210, 170, 24, 9)]
+    for k, (h, w, size, stride) in enumerate(cases):
+        yy, xx = np.mgrid[:h, :w]
+        mask = np.ones((h, w), dtype=bool)
+        for _ in range(3):
+            cx, cy, r = rng.uniform(0, w), rng.uniform(0, h), rng.uniform(8, 30)
+            mask &= (xx - cx) ** 2 + (yy - cy) ** 2 >= r * r
+        mask[: int(rng.integers(3, 15))] = False
+        mask[:, w - int(rng.integers(3, 15)):] = False
+        out[f"roi{k}_mask"] = mask
+        out[f"roi{k}_geometry"] = np.array([size, stride])
+        for median in (3, 5, 7, 9):
+            plan = roi.prepare_roi(mask, size, stride, median_filter_size=median)
+            if median == 3:
+                out[f"roi{k}_selected"] = plan.selected
+                out[f"roi{k}_bits"] = plan.neighbour_bits
+                out[f"roi{k}_hash"] = np.frombuffer(plan.mask_hash.encode(), np.uint8)
+            else:
+                out[f"roi{k}_median{median}"] = plan.median_neighbour_words
+        for truncation in ("none", "visibility"):
+            plan = roi.prepare_roi(mask, size, stride, policy="partial", truncation=truncation)
+            for name in ("selected", "partial_indices", "support_words", "support_boxes", "coverage",
+                         "neighbour_bits"):
+                out[f"roi{k}_partial_{truncation}_{name}"] = getattr(plan, name)
+        fine = roi.prepare_roi(mask, size, stride)
+        coarse_mask = roi.reduce_mask(mask)
+        out[f"roi{k}_reduced"] = coarse_mask
+        coarse = roi.prepare_roi(coarse_mask, size, stride)
+        out[f"roi{k}_down"] = roi.seed_permissions(coarse, fine, source_scale=2, destination_scale=1, size=size,
+                                                   stride=stride, reference_mask=mask)
+        out[f"roi{k}_up"] = roi.seed_permissions(fine, coarse, source_scale=1, destination_scale=2, size=size,
+                                                 stride=stride, reference_mask=mask)
+    np.savez_compressed(HERE / "roi_vectors.npz", **out)
 
 
 def partial_vectors(reference_root: Path) -> None:
@@ -246,4 +289,6 @@ def fourier_vectors(reference_root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit(f"usage: python {sys.argv[0]} <path of the live-dic checkout>")
+    main(sys.argv[1])

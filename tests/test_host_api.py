@@ -316,3 +316,35 @@ def test_register_pair_argument_errors():
         register_pair(image, image, roi_policy="partial")
     with pytest.raises(ICGNError, match="CUDA engine"):
         register_pair(image, image, backend="regl")
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_roi_planning_matches_reference_on_harder_masks(case):
+    """Several holes and cut edges, odd and even windows, overlapping and
+    tiled grids: selection, 3x3 bits, every median lattice, the mask hash,
+    both partial truncations, the reduced mask and the seed permissions in
+    both directions, against the reference's own outputs."""
+    g = np.load(ROOT / "tests" / "golden" / "roi_vectors.npz")
+    k = f"roi{case}"
+    mask = g[f"{k}_mask"]
+    size, stride = (int(v) for v in g[f"{k}_geometry"])
+    plan = roi.prepare_roi(mask, size, stride)
+    np.testing.assert_array_equal(plan.selected, g[f"{k}_selected"])
+    np.testing.assert_array_equal(plan.neighbour_bits, g[f"{k}_bits"])
+    assert plan.mask_hash == bytes(g[f"{k}_hash"]).decode()
+    for median in (5, 7, 9):
+        np.testing.assert_array_equal(roi.prepare_roi(mask, size, stride, median_filter_size=median)
+                                      .median_neighbour_words, g[f"{k}_median{median}"])
+    for truncation in ("none", "visibility"):
+        partial = roi.prepare_roi(mask, size, stride, policy="partial", truncation=truncation)
+        for name in ("selected", "partial_indices", "support_words", "support_boxes", "coverage", "neighbour_bits"):
+            got, want = getattr(partial, name), g[f"{k}_partial_{truncation}_{name}"]
+            assert got.dtype == want.dtype, name
+            np.testing.assert_array_equal(got, want, err_msg=name)
+    coarse_mask = roi.reduce_mask(mask)
+    np.testing.assert_array_equal(coarse_mask, g[f"{k}_reduced"])
+    coarse = roi.prepare_roi(coarse_mask, size, stride)
+    np.testing.assert_array_equal(roi.seed_permissions(coarse, plan, source_scale=2, destination_scale=1, size=size,
+                                                       stride=stride, reference_mask=mask), g[f"{k}_down"])
+    np.testing.assert_array_equal(roi.seed_permissions(plan, coarse, source_scale=1, destination_scale=2, size=size,
+                                                       stride=stride, reference_mask=mask), g[f"{k}_up"])
