@@ -25,7 +25,7 @@ rendered from the full frame by the reference's own fractional_shift.
 
 Run from the repository root where the reference checkout is available:
 
-    python tests/golden/make_uhd_fixtures.py /root/reference
+    python tests/golden/make_uhd_fixtures.py <path of the live-dic checkout>
 
 PNG decoding is restated here (8-bit greyscale, non-interlaced: zlib inflate
 plus the five scanline filters of the PNG specification) because Pillow is
@@ -162,4 +162,6 @@ def main(reference_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit(f"usage: python {sys.argv[0]} <path of the live-dic checkout>")
+    main(sys.argv[1])
