@@ -299,8 +299,10 @@ def temporal_save_previous(history: np.ndarray, ages: np.ndarray, raw: np.ndarra
 def seed_search(reference: np.ndarray, target: np.ndarray, *, subset_size: int, subset_stride: int, radius: int,
                 model: str = "affine", seed: np.ndarray | None = None, only_missing: bool = False,
                 selected: np.ndarray | None = None, centered: bool = False,
-                mask: np.ndarray | None = None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
-    """Exhaustive integer ZNCC search; returns (seed states, activity, best scores)."""
+                mask: np.ndarray | None = None,
+                active: np.ndarray | None = None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Exhaustive integer ZNCC search; returns (seed states, activity, best scores).
+    `active` (or all ones) is the activity that subsets left unsearched keep."""
     ref = np.ascontiguousarray(reference, dtype=np.uint8)
     tgt = np.ascontiguousarray(target, dtype=np.uint8)
     h, w = ref.shape
@@ -308,7 +310,7 @@ def seed_search(reference: np.ndarray, target: np.ndarray, *, subset_size: int, 
     gh = 1 + (h - subset_size) // subset_stride
     stride = 16 if model == "quadratic" else 8
     seeds = np.zeros((gh * gw, stride), np.float32) if seed is None else np.ascontiguousarray(seed, np.float32).copy()
-    active = np.ones(gh * gw, np.uint32)
+    active = np.ones(gh * gw, np.uint32) if active is None else np.ascontiguousarray(active, np.uint32).ravel().copy()
     score = np.full(gh * gw, -3.0, np.float32)
     sel = None if selected is None else np.ascontiguousarray(selected, dtype=np.uint8).ravel()
     msk = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8).ravel()

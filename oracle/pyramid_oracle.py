@@ -11,6 +11,14 @@ correction.  The per-level reference arrays are taken as given (the GPU
 engine's exported plane / metadata / inverse), so a comparison covers the
 per-frame path bit for bit.  Counters: [projected, accepted updates,
 velocity-predicted, expired (adaptive policy only)].
+
+ROI (`rois`, one LevelRoi per level, plus `temporal_links`): the solver's
+status -3 propagation, the UOD neighbour permissions, the coarse-to-fine and
+temporal seed permissions (bits 0-3 corners, bit 4 selected, bits 5-31 the
+fallback source; full_pyramid.wgsl:397-450).  `search_radius` > 0: the
+integer ZNCC search at the coarsest level (every subset, or with temporal
+seeding only those the projection left without a seed, whose status the
+projection marks -1), on `reference_levels[-1]`.
 """
 
 from __future__ import annotations
@@ -21,6 +29,13 @@ import numpy as np
 
 from . import oracle as oc
 from . import reference_prep as rp
+
+
+@dataclass
+class LevelRoi:
+    selected: np.ndarray            # uint8 per subset
+    links: np.ndarray               # float32 (count, 4): UOD neighbour permissions
+    seed_links: np.ndarray | None   # uint32 per subset: transfer from the next coarser level
 
 
 @dataclass
@@ -40,8 +55,14 @@ class PyramidOracle:
                  model: str = "affine", interpolation: str = "bspline", lanes: int = 32,
                  outlier_policy: str = "replace", median_size: int = 3, temporal: bool = False,
                  velocity: bool = False, fine_correction: bool = False, adaptive: bool = False,
-                 max_age: int = 0xFFFFFFFE, divergence_patience: int = 0, divergence_min_iterations: int = 4):
+                 max_age: int = 0xFFFFFFFE, divergence_patience: int = 0, divergence_min_iterations: int = 4,
+                 rois: list[LevelRoi] | None = None, temporal_links: np.ndarray | None = None,
+                 search_radius: int = 0, reference_levels: list[np.ndarray] | None = None):
         self.levels = levels
+        self.rois, self.temporal_links = rois, temporal_links
+        self.search_radius, self.reference_levels = search_radius, reference_levels
+        if search_radius and reference_levels is None:
+            raise ValueError("the seed search needs the reference image of every level")
         self.L = len(levels)
         self.S, self.s = subset_size, subset_stride
         self.iterations, self.tolerances, self.zncc_min = iterations, tolerances, zncc_min
@@ -80,12 +101,13 @@ class PyramidOracle:
                        iterations=self.iterations[schedule], tolerance=self.tolerances[schedule],
                        zncc_min=self.zncc_min, seed_state=seed, active=active,
                        divergence_patience=self.patience if level == 0 else 0,
-                       divergence_min_iterations=self.min_iterations)
+                       divergence_min_iterations=self.min_iterations, roi_enabled=self.rois is not None)
         if self.policy == "disabled":
             return raw, raw
         out = oc.uod(raw, lv.metadata, grid=self._grid(level), subset_stride=self.s, model=self.model,
                      policy=self.policy, median_size=self.median_size,
-                     seed_mode=self.policy == "median" and level > 0)
+                     seed_mode=self.policy == "median" and level > 0,
+                     permissions=None if self.rois is None else self.rois[level].links)
         return raw, out
 
     def register(self, frame: np.ndarray, levels_used: int | None = None) -> tuple[np.ndarray, list[int]]:
@@ -101,26 +123,39 @@ class PyramidOracle:
             if self.velocity:
                 source, counters[2] = oc.temporal_predict(self.history, self.prev_history, self.ages,
                                                           self.prev_ages, model=self.model)
+            links = self.temporal_links if c == self.L - 1 else None
             seed, active, weights = oc.transfer_seed(
                 source, source_grid=self._grid(0), destination_grid=self._grid(c), source_scale=1.0,
                 destination_scale=float(1 << c), subset_size=self.S, subset_stride=self.s, model=self.model,
-                track_availability=self.fine_correction, return_weights=True)
+                track_availability=self.fine_correction, return_weights=True, permissions=links)
             projected = weights > 0.0
+            if links is not None:
+                projected &= (np.asarray(links, np.uint32).ravel() & 16) != 0
             counters[0] = int(projected.sum())
+            if self.search_radius:
+                seed[weights == 0.0, self.status_at] = -1.0
             if self.fine_correction:
                 seed[~projected, self.status_at] = -1.0
+        if self.search_radius and c == self.L - 1:
+            selected = None if self.rois is None else self.rois[c].selected
+            seed, active, _ = oc.seed_search(
+                self.reference_levels[c], frames[c], subset_size=self.S, subset_stride=self.s,
+                radius=self.search_radius, model=self.model, seed=seed, only_missing=self.temporal,
+                selected=selected, active=active)
         raws, outs = {}, {}
         raws[c], outs[c] = self._solve_level(c, frames[c], seed, active)
         for level in range(L - 2, -1, -1):
             seed, active = oc.transfer_seed(
                 outs[level + 1], source_grid=self._grid(level + 1), destination_grid=self._grid(level),
                 source_scale=float(1 << (level + 1)), destination_scale=float(1 << level), subset_size=self.S,
-                subset_stride=self.s, model=self.model, track_availability=self.fine_correction)
+                subset_stride=self.s, model=self.model, track_availability=self.fine_correction,
+                permissions=None if self.rois is None else self.rois[level].seed_links)
             if level == 0 and self.temporal and self.fine_correction:
                 seed = oc.refine_temporal_seed(
                     seed, active, self.coarse_history, self.coarse_ages, self.history, self.ages,
                     source_grid=self._grid(1), destination_grid=self._grid(0), source_scale=2.0,
-                    subset_size=self.S, subset_stride=self.s, model=self.model, max_age=self.max_age)
+                    subset_size=self.S, subset_stride=self.s, model=self.model, max_age=self.max_age,
+                    permissions=None if self.rois is None else self.rois[0].seed_links)
             raws[level], outs[level] = self._solve_level(level, frames[level], seed, active)
         if self.temporal:
             use_filtered = self.policy == "replace" and not self.velocity

@@ -1,0 +1,245 @@
+"""Parity at the geometry of the headline workloads.
+
+* UHD plate-with-hole sequence (subset 31 / step 8, 3-level pyramid, a
+  circular ROI hole, ZNCC integer search on the first frame, temporal
+  seeding with velocity prediction afterwards, UOD replace): a 1024x768
+  crop with a hole of radius 150 px and the Kirsch field ramped to a 2 px
+  peak over 6 frames, every frame bit for bit against the pipeline oracle
+  (oracle/pyramid_oracle.py) fed the engine's per-level reference arrays
+  and the host ROI tables.
+* Quadratic consecutive pairs (subset 41 / step 10, GPU reference
+  preparation every pair): the 12x12 preparation against the float64
+  restatement of _reference_arrays (the reference's own GPU-preparation
+  tolerances, test_gpu_reference.py:107-124, for every first-order
+  quantity; the second-order moments stage by stage), then the engine's GPU
+  preparation + GPU solve against float64 preparation + oracle solve at
+  the parity tolerances (identical statuses except threshold borderline
+  windows, |du| <= 1e-3 px, |grad u| <= 1e-5), and the reference's accuracy
+  gate for the quadratic model against the imposed sinusoid field
+  (test_gpu_regressions.py:730-793: displacement RMSE < 0.02 px, curvature
+  RMSE < 2e-4).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from live_dic_gb300 import ICGNWGPU, ICGNWGPUFullPyramid, _native, synthetic
+from live_dic_gb300.roi import integral, prepare_roi, reduce_mask, seed_permissions
+from oracle import oracle as oracle_c
+from oracle import reference_prep as rp
+from oracle.pyramid_oracle import LevelArrays, LevelRoi, PyramidOracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _packed(result):
+    return np.concatenate([result.parameters, result.status[..., None], result.iterations[..., None]], -1)
+
+
+# ------------------------------------------------------------------ plate-with-hole sequence
+PW, PH, HOLE, S1, ST1, LEVELS, RADIUS = 1024, 768, 150.0, 31, 8, 3, 4
+
+
+def _roi_tables(mask, size, stride, levels, policy="replace"):
+    """The host ROI tables the full-pyramid engine uploads (per-level
+    selection and UOD links, coarse-to-fine and temporal seed permissions)."""
+    masks = [mask]
+    for _ in range(1, levels):
+        masks.append(reduce_mask(masks[-1]))
+    plans = [prepare_roi(m, size, stride) for m in masks]
+    prefix = integral(mask)
+    rois = []
+    for level, plan in enumerate(plans):
+        seed_links = None
+        if level < levels - 1:
+            seed_links = np.ascontiguousarray(seed_permissions(
+                plans[level + 1], plan, source_scale=1 << (level + 1), destination_scale=1 << level, size=size,
+                stride=stride, reference_mask=mask, reference_prefix=prefix), dtype=np.uint32).ravel()
+        rois.append(LevelRoi(np.ascontiguousarray(plan.selected, np.uint8).ravel(),
+                             np.ascontiguousarray(plan.links_table(3, policy)), seed_links))
+    temporal = np.ascontiguousarray(seed_permissions(
+        plans[0], plans[-1], source_scale=1, destination_scale=1 << (levels - 1), size=size, stride=stride,
+        reference_mask=mask, reference_prefix=prefix), dtype=np.uint32).ravel()
+    return plans, rois, temporal
+
+
+def test_plate_with_hole_sequence_bit_exact():
+    ref, sp = synthetic.reference_image(PW, PH, seed=1201, device="cuda")
+    field = synthetic.KirschField(PW, PH, HOLE, peak=2.0)
+    mask = synthetic.hole_mask(PW, PH, HOLE)
+    count = 6
+    frames = [synthetic.deformed_image(sp, field.torch_field(k / count), noise_seed=1300 + k, device="cuda")
+              for k in range(1, count + 1)]
+    plans, rois, temporal = _roi_tables(mask, S1, ST1, LEVELS)
+    refs = [ref]
+    for _ in range(1, LEVELS):
+        refs.append(oracle_c.reduce(refs[-1]))
+    with ICGNWGPUFullPyramid(pyramid_levels=LEVELS, subset_size=S1, subset_stride=ST1, initialization="temporal",
+                             temporal_prediction="velocity", seed_search_radius=RADIUS) as engine:
+        info = engine.set_reference(ref, roi_mask=mask)
+        np.testing.assert_array_equal(info.roi.selected, plans[0].selected)
+        levels = []
+        for level in range(LEVELS):
+            gw, gh = engine.level_grid(level)
+            w, h = PW >> level, PH >> level
+            levels.append(LevelArrays(
+                w, h, gw, gh,
+                engine.export_level(level, _native.EXPORT_PLANE, np.float32, (h * w * 4,)),
+                engine.export_level(level, _native.EXPORT_METADATA, np.float32, (gw * gh * 16,)),
+                engine.export_level(level, _native.EXPORT_INVERSE, np.float32, (gw * gh * 36,))))
+        oracle = PyramidOracle(levels, subset_size=S1, subset_stride=ST1, iterations=engine.iterations_per_level,
+                               tolerances=engine.tolerance_per_level, outlier_policy=engine.outlier_policy,
+                               lanes=engine.solver_workgroup_size, temporal=True, velocity=True, rois=rois,
+                               temporal_links=temporal, search_radius=RADIUS, reference_levels=refs)
+        selected = plans[0].selected
+        cx, cy = synthetic.subset_centres(PW, PH, S1, ST1)
+        for k, frame in enumerate(frames):
+            result = engine.register(frame)
+            state, counters = oracle.register(frame)
+            got = _packed(result)
+            np.testing.assert_array_equal(got, state.reshape(got.shape), err_msg=f"frame {k}")
+            assert result.timing["temporallySeededCoarseSubsets"] == counters[0]
+            assert result.timing["temporalAcceptedUpdates"] == counters[1]
+            assert result.timing["velocityPredictedSubsets"] == counters[2]
+            assert np.all(result.status[~selected] == -3)
+            ok = result.status >= 1
+            assert ok[selected].mean() > 0.95, (k, ok[selected].mean())
+            truth = field.truth(cx, cy, load=(k + 1) / count)
+            err = result.displacement[ok] - truth[ok]
+            rmse = float(np.sqrt(np.mean(np.sum(err * err, axis=1))))
+            assert rmse < 0.02, (k, rmse)
+        assert counters[0] > 0 and counters[2] > 0
+
+
+# ------------------------------------------------------------------ quadratic pairs
+QW, QH, S2, ST2 = 640, 480, 41, 10
+
+
+@pytest.fixture(scope="module")
+def quadratic_pair():
+    ref, sp = synthetic.reference_image(QW, QH, seed=1401, device="cuda")
+    field = synthetic.sinusoid_field()
+    tgt = synthetic.deformed_image(sp, field, noise_seed=1402, device="cuda")
+    return ref, tgt, field
+
+
+def _sinusoid_parameters(cx, cy):
+    """u = 2 sin(kx x) cos(ky y), v = 1.5 cos(kv x): the 12 quadratic
+    parameters [u, ux, uy, v, vx, vy, uxx, uxy, uyy, vxx, vxy, vyy]."""
+    kx, ky, kv = 2 * np.pi / 400.0, 2 * np.pi / 600.0, 2 * np.pi / 500.0
+    sx, cxx = np.sin(kx * cx), np.cos(kx * cx)
+    sy, cyy = np.sin(ky * cy), np.cos(ky * cy)
+    sv, cv = np.sin(kv * cx), np.cos(kv * cx)
+    zero = np.zeros_like(cx)
+    return np.stack([
+        2 * sx * cyy, 2 * kx * cxx * cyy, -2 * ky * sx * sy,
+        1.5 * cv, -1.5 * kv * sv, zero,
+        -2 * kx * kx * sx * cyy, -2 * kx * ky * cxx * sy, -2 * ky * ky * sx * cyy,
+        -1.5 * kv * kv * cv, zero, zero], -1)
+
+
+def _float64_moments(plane: np.ndarray, width: int, height: int, size: int, stride: int):
+    """J^T f and sum J of the 12 quadratic Jacobian columns, summed in
+    float64 over a given reference plane (f, gx, gy, 0), with the absolute
+    sums of their terms."""
+    p = plane.reshape(height, width, 4).astype(np.float64)
+    gw, gh = 1 + (width - size) // stride, 1 + (height - size) // stride
+    c = np.arange(size) - 0.5 * (size - 1)
+    ly, lx = np.meshgrid(c, c, indexing="ij")
+    mono = np.stack([np.ones_like(lx), lx, ly, 0.5 * lx * lx, lx * ly, 0.5 * ly * ly]).reshape(6, -1)
+    order = [0, 1, 2, 6, 7, 8, 3, 4, 5, 9, 10, 11]   # [gx*m0..2, gy*m0..2, gx*m3..5, gy*m3..5]
+    jtf = np.zeros((gh * gw, 12))
+    sj = np.zeros_like(jtf)
+    jtf_abs = np.zeros_like(jtf)
+    sj_abs = np.zeros_like(jtf)
+    win = np.lib.stride_tricks.sliding_window_view
+    for gy in range(gh):
+        rows = win(p[gy * stride: gy * stride + size], (size, size, 4))[0, ::stride, 0][:gw]
+        rows = rows.reshape(gw, size * size, 4)
+        f = rows[..., 0] - rows[..., 0].mean(axis=1, keepdims=True)
+        cols = np.concatenate([rows[..., 1:2] * mono.T[None], rows[..., 2:3] * mono.T[None]], -1)[..., order]
+        sl = slice(gy * gw, (gy + 1) * gw)
+        jtf[sl] = np.einsum("gpk,gp->gk", cols, f)
+        jtf_abs[sl] = np.einsum("gpk,gp->gk", np.abs(cols), np.abs(f))
+        sj[sl] = cols.sum(axis=1)
+        sj_abs[sl] = np.abs(cols).sum(axis=1)
+    return jtf, sj, jtf_abs, sj_abs
+
+
+def test_quadratic_preparation_matches_float64_oracle(quadratic_pair):
+    """The reference's GPU-preparation tolerances exist for its first-order
+    models only (its GPU preparation rejects the quadratic model,
+    reference.wgsl:22).  Here the plane, validity, the first-order rows and
+    the 12x12 inverse are held to them; the six second-order rows of J^T f
+    and sum J, whose window weights reach (S-1)^2/4 = 400 at S41 and whose
+    sums cancel, are checked stage by stage instead: the FP32 sums against
+    float64 sums over the same (GPU) plane within 1e-6 of the absolute sum
+    of their terms, the plane itself against the float64 oracle as above.
+    The solution parity test below shows the combined effect."""
+    ref, _, _ = quadratic_pair
+    plane, inverse, metadata = rp.reference_arrays(ref, motion_model="quadratic", subset_size=S2, subset_stride=ST2)
+    with ICGNWGPU(motion_model="quadratic", subset_size=S2, subset_stride=ST2) as engine:
+        engine.set_reference(ref)
+        g_plane, g_inverse, g_meta = engine.export_reference()
+        valid = engine.reference_valid
+    n, ms = 12, 28
+    err = np.abs(g_plane - plane)
+    assert np.all(err <= 3e-4 + 3e-6 * np.abs(plane)), float(err.max())
+    meta, gm = metadata.reshape(-1, ms), g_meta.reshape(-1, ms)
+    np.testing.assert_array_equal(gm[:, 1], meta[:, 1])
+    np.testing.assert_array_equal(valid.ravel(), meta[:, 1] > 0.5)
+    ok = meta[:, 1] > 0.5
+    assert ok.all()
+    second_order = set(range(2 + 6, 2 + n)) | set(range(2 + n + 6, 2 + 2 * n))
+    for comp in range(ms):
+        if comp in second_order:
+            continue
+        a, b = gm[ok, comp], meta[ok, comp]
+        if 2 <= comp < 2 + n:
+            tol = 0.1 + 1e-4 * np.abs(b)
+        elif 2 + n <= comp < 2 + 2 * n:
+            tol = 0.003 + 1e-4 * np.abs(b)
+        else:
+            tol = 0.001 + 1e-5 * np.abs(b)
+        assert np.all(np.abs(a - b) <= tol), (comp, float(np.abs(a - b).max()))
+    jtf, sj, jtf_abs, sj_abs = _float64_moments(g_plane, QW, QH, S2, ST2)
+    for k in range(6, 12):
+        e = np.abs(gm[:, 2 + k] - jtf[:, k])
+        assert np.all(e <= 1e-6 * jtf_abs[:, k] + 1e-3), (k, float((e / jtf_abs[:, k]).max()))
+        e = np.abs(gm[:, 2 + n + k] - sj[:, k])
+        assert np.all(e <= 1e-6 * sj_abs[:, k] + 1e-3), (k, float((e / sj_abs[:, k]).max()))
+    inv, ginv = inverse.reshape(-1, n * n)[ok], g_inverse.reshape(-1, n * n)[ok]
+    scale = np.abs(inv).max(axis=1, keepdims=True)
+    assert np.all(np.abs(ginv - inv) <= 5e-9 + 5e-4 * np.maximum(np.abs(inv), 1e-3 * scale))
+
+
+def test_quadratic_pair_parity_and_curvature_accuracy(quadratic_pair):
+    ref, tgt, _ = quadratic_pair
+    with ICGNWGPU(motion_model="quadratic", subset_size=S2, subset_stride=ST2, outlier_policy="disabled") as engine:
+        engine.set_reference(ref, tolerance=1e-4)
+        result = engine.register(tgt)
+    plane, inverse, metadata = rp.reference_arrays(ref, motion_model="quadratic", subset_size=S2, subset_stride=ST2)
+    coef = oracle_c.prefilter(tgt, rp.runtime_fir_taps())
+    expected = oracle_c.solve(tgt, coef, plane, metadata, inverse, subset_size=S2, subset_stride=ST2,
+                              model="quadratic", lanes=16, tolerance=1e-4)
+    expected = expected.reshape(result.parameters.shape[:2] + (16,))
+    status, estatus = result.status, expected[..., 12]
+    mismatch = status != estatus
+    assert mismatch.sum() <= max(1, int(0.002 * status.size)), int(mismatch.sum())
+    both = (status == 1) & (estatus == 1)
+    assert both.mean() > 0.95
+    d = np.abs(result.parameters[both] - expected[..., :12][both])
+    assert d[:, [0, 3]].max() <= 1e-3, float(d[:, [0, 3]].max())
+    assert d[:, [1, 2, 4, 5]].max() <= 1e-5, float(d[:, [1, 2, 4, 5]].max())
+    # the curvature terms: the gradient bound over half a subset
+    assert d[:, 6:].max() <= 1e-5 / ((S2 - 1) / 2), float(d[:, 6:].max())
+    cx, cy = synthetic.subset_centres(QW, QH, S2, ST2)
+    truth = _sinusoid_parameters(cx, cy)
+    ok = status == 1
+    error = result.parameters.astype(np.float64) - truth
+    displacement_rmse = float(np.sqrt(np.mean(np.sum(error[..., (0, 3)][ok] ** 2, axis=1))))
+    curvature_rmse = float(np.sqrt(np.mean(error[..., 6:][ok] ** 2)))
+    assert displacement_rmse < 0.02, displacement_rmse
+    assert curvature_rmse < 2e-4, curvature_rmse

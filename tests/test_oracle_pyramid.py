@@ -64,3 +64,52 @@ def test_pyramid_oracle_recovers_a_translation_sequence(sequence):
         assert float(np.sqrt(np.mean(err ** 2))) < 0.02, k
         if k > 1:
             assert counters[0] > 0 and counters[1] > 0
+
+
+def test_pyramid_oracle_with_roi_hole_and_first_frame_search(sequence):
+    """The ROI and seed-search paths of the composed oracle: a circular hole
+    excluded from every level (status -3, UOD and seed permissions from the
+    host ROI plan), the integer ZNCC search on the coarsest level for the
+    first frame and for windows the temporal projection leaves unseeded."""
+    from live_dic_gb300.roi import integral, prepare_roi, reduce_mask, seed_permissions
+    from oracle.pyramid_oracle import LevelRoi
+
+    oc.build()
+    ref, frames = sequence
+    yy, xx = np.ogrid[:H, :W]
+    mask = (xx - W / 2) ** 2 + (yy - H / 2) ** 2 >= 30.0 ** 2
+    masks = [mask, reduce_mask(mask)]
+    plans = [prepare_roi(m, S, ST) for m in masks]
+    levels = _levels(ref, 2)
+    for lv, plan in zip(levels, plans, strict=True):
+        meta = lv.metadata.reshape(lv.grid_w * lv.grid_h, -1)
+        meta[~plan.selected.ravel(), 1] = -3.0
+    prefix = integral(mask)
+    links0 = seed_permissions(plans[1], plans[0], source_scale=2, destination_scale=1, size=S, stride=ST,
+                              reference_mask=mask, reference_prefix=prefix)
+    temporal = seed_permissions(plans[0], plans[1], source_scale=1, destination_scale=2, size=S, stride=ST,
+                                reference_mask=mask, reference_prefix=prefix)
+    rois = [LevelRoi(plans[0].selected.astype(np.uint8).ravel(), plans[0].links_table(3, "replace"),
+                     np.asarray(links0, np.uint32).ravel()),
+            LevelRoi(plans[1].selected.astype(np.uint8).ravel(), plans[1].links_table(3, "replace"), None)]
+    oracle = PyramidOracle(levels, subset_size=S, subset_stride=ST, iterations=(8, 16), tolerances=(5e-3, 5e-3),
+                           lanes=16, temporal=True, velocity=True, rois=rois,
+                           temporal_links=np.asarray(temporal, np.uint32).ravel(), search_radius=3,
+                           reference_levels=[ref, oc.reduce(ref)])
+    gw, gh = levels[0].grid_w, levels[0].grid_h
+    selected = plans[0].selected
+    assert not selected.all() and selected.mean() > 0.6
+    for k, frame in enumerate(frames, start=1):
+        state, counters = oracle.register(frame)
+        state = state.reshape(gh, gw, -1)
+        assert np.all(state[..., 6][~selected] == -3.0)
+        inner = np.zeros_like(selected)
+        inner[1:-1, 1:-1] = True
+        ok = (state[..., 6] >= 1) & inner & selected
+        assert ok.sum() > 0.9 * (inner & selected).sum(), (k, ok.sum())
+        err = np.hypot(state[..., 0] - 0.4 * k, state[..., 3] + 0.25 * k)[ok]
+        assert float(np.sqrt(np.mean(err ** 2))) < 0.02, k
+        if k == 1:
+            assert counters[0] == 0
+        else:
+            assert counters[0] > 0 and counters[1] > 0
