@@ -217,7 +217,13 @@ int gbdic_export(gbdic_engine *engine, int32_t what, void *host_out, int64_t byt
  * ones return GBDIC_EINVAL), held by every GPU that loads the library until
  * exit and shared by all calls: calls that overlap on the GPU race.  The first
  * call on a device sets that device up and should come before any stream
- * capture.  Errors: message in gbdic_last_error(NULL). */
+ * capture; the device address it caches does not survive cudaDeviceReset, so
+ * the entry point must not be used on a device after a reset.  Only complete
+ * windows are solved: partial-support windows (metadata validity -4, prepared
+ * with roi_policy "partial") come back with status -4 (roi_enabled) or -1 and
+ * zero parameters, and the stagnation stop (divergence_patience) is off, so
+ * results equal gbdic_register only on an engine without partial windows and
+ * with divergence_patience 0.  Errors: message in gbdic_last_error(NULL). */
 typedef struct {
     const uint8_t *frame;      /* width*height target bytes, dense rows */
     const float *plane;        /* width*height*4 floats */

@@ -21,6 +21,14 @@
 // The first call on a device, with that device current, resolves the
 // array's device address with cudaGetSymbolAddress and uploads the FIR taps
 // to constant memory; that first call should come before any stream capture.
+// The cached address and taps belong to the device's context: after a
+// cudaDeviceReset they are stale, so the entry point must not be used on a
+// device that has been reset.
+//
+// Only complete windows are solved.  Partial-support windows (metadata
+// validity -4) keep the status the solver gives invalid windows (-4 with
+// roi_enabled, else -1) and zero parameters, and the stagnation stop is off
+// (divergence_patience 0).
 #include <cstring>
 #include <mutex>
 #include <string>

@@ -67,7 +67,7 @@ void validate_options(const gbdic_options &o) {
     if (o.median_filter_scope < 0 || o.median_filter_scope > 1) fail(GBDIC_EINVAL, "median_filter_scope must be 'rejected' or 'all'");
     if (o.threads_per_subset != 16 && o.threads_per_subset != 32 && o.threads_per_subset != 64 && o.threads_per_subset != 128)
         fail(GBDIC_EINVAL, "threads_per_subset must be 16, 32, 64, or 128");
-    if (o.divergence_patience < 0 || o.divergence_patience > 30) fail(GBDIC_EINVAL, "divergence_patience must be an integer from 1 to 30");
+    if (o.divergence_patience < 0 || o.divergence_patience > 30) fail(GBDIC_EINVAL, "divergence_patience must be an integer from 0 to 30");
     if (o.divergence_min_iterations < 1 || o.divergence_min_iterations > 30)
         fail(GBDIC_EINVAL, "divergence_min_iterations must be an integer from 1 to 30");
     if (o.pipeline_slots < 1 || o.pipeline_slots > 64) fail(GBDIC_EINVAL, "pipeline_depth must be a positive integer");
