@@ -17,6 +17,10 @@
 //     with tcgen05.ld and apply the epilogue.
 // Every mbarrier wait is bounded: on expiry the CTA records an error code and
 // carries on, so a fault of the pipeline ends the kernel instead of hanging.
+// Before a failed CTA frees its tensor memory and exits, it waits (bounded
+// again) for the copies of every stage the producer armed but the MMA issuer
+// never consumed, and for the MMAs it did issue, so no bulk copy or MMA is
+// left writing into the CTA's shared or tensor memory.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -100,6 +104,7 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
     __shared__ uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
     __shared__ uint32_t tmem_slot;
     __shared__ int failed;
+    __shared__ int issued_kb, consumed_kb;  // K blocks whose loads were issued / consumed
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -115,6 +120,8 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
         }
         mbar_init(&done_bar, 1);
         failed = 0;
+        issued_kb = 0;
+        consumed_kb = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -129,7 +136,8 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
 
     if (warp == 0 && lane == 0) {
         // TMA producer.
-        for (int kb = 0; kb < num_kb; ++kb) {
+        int kb = 0;
+        for (; kb < num_kb; ++kb) {
             const int s = kb % kStages;
             if (kb >= kStages && !mbar_wait(&empty_bar[s], ((kb / kStages) - 1) & 1)) {
                 atomicExch(&failed, 1);
@@ -142,10 +150,12 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
             tma_load_2d(sa, &map_a, &full_bar[s], kx, m0);
             tma_load_2d(sb, &map_b, &full_bar[s], kx, n0);
         }
+        issued_kb = kb;
     } else if (warp == 1 && lane == 0) {
         // MMA issuer.
         constexpr uint32_t idesc = instr_desc(kBM, BN);
-        for (int kb = 0; kb < num_kb; ++kb) {
+        int kb = 0;
+        for (; kb < num_kb; ++kb) {
             const int s = kb % kStages;
             if (!mbar_wait(&full_bar[s], (kb / kStages) & 1)) {
                 atomicExch(&failed, 1);
@@ -169,6 +179,7 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
                              smem_u32(&empty_bar[s]))
                          : "memory");
         }
+        consumed_kb = kb;
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                          smem_u32(&done_bar))
                      : "memory");
@@ -220,6 +231,14 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
+        if (lane == 0 && failed) {
+            // The producer runs at most kStages K blocks ahead of the issuer,
+            // so the unconsumed blocks occupy distinct stages.
+            for (int kb = consumed_kb; kb < issued_kb; ++kb) mbar_wait(&full_bar[kb % kStages], (kb / kStages) & 1);
+            mbar_wait(&done_bar, 0);
+        }
+        __syncwarp();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
     }
     if (tid == 0 && failed && args.error) atomicExch(args.error, 1);
