@@ -1,6 +1,6 @@
 // Shared device helpers and kernel argument blocks for the gbdic library.
 //
-// Rounding contract: the library is compiled with --fmad=false, so a*b+c is
+// Rounding contract: the bit-exact units are compiled with --fmad=false, so a*b+c is
 // only fused where the source writes fmaf(); every other float operation is
 // one IEEE binary32 operation rounded to nearest (no fast-math, IEEE
 // division and square root).  The arithmetic order of each kernel is fixed
