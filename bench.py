@@ -57,6 +57,8 @@ def parse_args() -> argparse.Namespace:
     ap.add_argument("--peak", type=float, default=2.0)
     ap.add_argument("--lanes", type=int, default=16)
     ap.add_argument("--persistent", action="store_true")
+    ap.add_argument("--solver-mode", choices=("exact", "fast"), default="exact",
+                    help="IC-GN pixel loop: the reference's order, or the sliding-window sampler")
     ap.add_argument("--autotune", action="store_true", help="pick lanes/persistence with the solver autotuner")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -254,6 +256,7 @@ def workload_config(args) -> dict:
         "pyramid_levels": args.levels,
         "lanes_per_subset": args.lanes,
         "persistent": bool(args.persistent),
+        "solver_mode": args.solver_mode,
         "parallelism": "replicas",
         "l2": "no flush: per-step working set (finest reference plane 133 MB + coefficient planes + states) exceeds "
               "the 129 MB L2",
@@ -703,9 +706,10 @@ def main() -> None:
         pyramid_levels=args.levels, subset_size=args.subset, subset_stride=args.stride,
         initialization="temporal", temporal_prediction="velocity", solver_workgroup_size=args.lanes,
         device=local, pipeline_slots=2, persistent=args.persistent, autotune=args.autotune,
+        solver_mode=args.solver_mode,
     )
     info = engine.set_reference(ref, roi_mask=mask)
-    args.lanes, args.persistent = engine.solver_workgroup_size, engine._persistent
+    args.lanes, args.persistent, args.solver_mode = engine.solver_workgroup_size, engine._persistent, engine.solver_mode
     gw, gh = info.grid
     state = torch.zeros(gw * gh * 8, dtype=torch.float32, device=device)
     stream = torch.cuda.Stream(device=device)

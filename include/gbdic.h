@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define GBDIC_ABI_VERSION 1
+#define GBDIC_ABI_VERSION 2
 
 enum {
     GBDIC_OK = 0,
@@ -49,6 +49,12 @@ enum {
 
 enum { GBDIC_MODEL_AFFINE = 0, GBDIC_MODEL_TRANSLATION = 1, GBDIC_MODEL_QUADRATIC = 2 };
 enum { GBDIC_INTERP_BSPLINE = 0, GBDIC_INTERP_LINEAR = 1, GBDIC_INTERP_KEYS = 2 };
+/* IC-GN pixel loop: EXACT keeps the reference's pixel-to-lane order and
+ * summation (bit-exact against the oracle); FAST walks column runs with a
+ * sliding register window of B-spline taps (translation and affine models,
+ * B-spline interpolation, 16 or 32 lanes; every other configuration runs the
+ * exact loop), within the parity tolerances of the exact one. */
+enum { GBDIC_SOLVER_EXACT = 0, GBDIC_SOLVER_FAST = 1 };
 enum { GBDIC_OUTLIER_FLAG = 0, GBDIC_OUTLIER_REPLACE = 1, GBDIC_OUTLIER_DISABLED = 2,
        GBDIC_OUTLIER_MEDIAN = 3 };
 enum { GBDIC_EXPORT_COEFFICIENTS = 0, GBDIC_EXPORT_PLANE = 1, GBDIC_EXPORT_METADATA = 2,
@@ -76,6 +82,7 @@ typedef struct {
     int32_t divergence_min_iterations; /* >= 1 */
     int32_t pipeline_slots;            /* frames that may be in flight, >= 1 */
     int32_t persistent;                /* 1: one persistent launch over a work queue */
+    int32_t solver_mode;               /* GBDIC_SOLVER_* (no reference counterpart) */
 } gbdic_options;
 
 /* Per-call solver controls; mirrors _validated_config (wgpu_backend.py:504-524). */
@@ -357,6 +364,10 @@ int gbdic_field_summary(const float *packed, int64_t count, int32_t stride, int3
  * wgpu_backend.py:2213-2296, which switches between solver pipelines). */
 int gbdic_set_solver_variant(gbdic_engine *engine, int32_t threads_per_subset, int32_t persistent);
 int gbdic_pyramid_set_solver_variant(gbdic_pyramid *pyramid, int32_t threads_per_subset, int32_t persistent);
+/* Switch the pixel loop (GBDIC_SOLVER_*) of a prepared handle; no reference
+ * counterpart (the autotuner's third axis). */
+int gbdic_set_solver_mode(gbdic_engine *engine, int32_t mode);
+int gbdic_pyramid_set_solver_mode(gbdic_pyramid *pyramid, int32_t mode);
 
 /* Global translation seed (full-resolution pixels) of the next frame run on
  * `slot` (0 for gbdic_pyramid_register / register_device) when the pyramid

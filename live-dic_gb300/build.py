@@ -30,11 +30,13 @@ INCLUDE = ROOT.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(INCLUDE)]
 # Units whose results are checked against a tolerance, not bit for bit.
-CONTRACTED = {"refprep", "fourier", "nn_ops", "nn_api", "tc_gemm"}
+CONTRACTED = {"refprep", "fourier", "nn_ops", "nn_api", "tc_gemm", "solver_fast"}
 
 
 def unit_flags(unit: Path) -> list[str]:
-    return ["--fmad=true" if unit.stem in CONTRACTED else "--fmad=false"]
+    # GBDIC_NVCC_DEFINES: extra -D tuning macros (e.g. GBDIC_FAST_MIN_BLOCKS), for sweeps
+    extra = os.environ.get("GBDIC_NVCC_DEFINES", "").split()
+    return ["--fmad=true" if unit.stem in CONTRACTED else "--fmad=false", *extra]
 
 
 def nvcc() -> str:

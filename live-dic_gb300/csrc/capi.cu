@@ -666,6 +666,17 @@ int gbdic_set_solver_variant(gbdic_engine *e, int32_t threads_per_subset, int32_
     });
 }
 
+int gbdic_set_solver_mode(gbdic_engine *e, int32_t mode) {
+    return guarded(e, [&] {
+        check_cuda(cudaStreamSynchronize(e->rt->stream()), "pending work");
+        e->rt->set_mode(mode);
+        for (auto &h : e->host) {
+            if (h.graph) cudaGraphExecDestroy(h.graph);
+            h.graph = nullptr;
+        }
+    });
+}
+
 int gbdic_profile(gbdic_engine *e, int32_t enable) {
     return guarded(e, [&] {
         check_cuda(cudaStreamSynchronize(e->rt->stream()), "pending work");

@@ -147,6 +147,10 @@ class Runtime {
     int persistent_grid(int lanes);
     // Switch the solver variant (lanes per subset, persistent queue).
     void set_variant(int lanes, bool persistent);
+    // Switch the pixel loop (GBDIC_SOLVER_*).
+    void set_mode(int mode);
+    // The fast loop runs for this configuration.
+    bool fast_active() const;
     const DeviceBuffer &weights() const { return weights_; }
     // Solver profiling: CUDA events around every solver launch (outside graph
     // capture) and a device counter of executed Gauss-Newton iterations.
@@ -163,6 +167,7 @@ class Runtime {
     int device_ = 0;
     int persistent_grid_ = 0;
     int persistent_lanes_ = 0;
+    bool persistent_fast_ = false;
     bool profiling_ = false;
     std::vector<cudaEvent_t> profile_begin_, profile_end_;
     int profile_used_ = 0;

@@ -160,6 +160,9 @@ struct SolveArgs {
     const uint32_t *support;
     const float4 *support_box;
     int support_words;
+    // Fast pixel loop (solver_fast.cu): row segments per column, or 0 for the
+    // exact loop.
+    int fast_segments;
 };
 
 }  // namespace gbdic

@@ -23,6 +23,14 @@ int icgn_grid(int count, int lanes);
 int icgn_occupancy(int model, int interp, int lanes, bool gauss);
 cudaError_t launch_icgn(const SolveArgs &a, int model, int interp, int lanes, bool gauss,
                         int persistent_grid, cudaStream_t stream);
+// Sliding-window ("fast") pixel loop: supported configurations, the row
+// segments per column that minimise its steps, its launcher (grid as for
+// launch_icgn; with occupancy_only set, the resident CTAs per SM instead).
+bool icgn_fast_supported(int model, int interp, int lanes);
+int icgn_fast_segments(int S, int lanes);
+cudaError_t launch_icgn_fast(const SolveArgs &a, int model, int lanes, bool gauss, int grid, cudaStream_t stream,
+                             int *occupancy_only);
+int icgn_fast_occupancy(int model, int lanes, bool gauss);
 
 // Partial-support windows (a.count = number of partial windows; a.partial_index,
 // a.support, a.support_box, a.support_words set); translation and affine.

@@ -682,6 +682,16 @@ int gbdic_pyramid_set_solver_variant(gbdic_pyramid *p, int32_t threads_per_subse
     });
 }
 
+int gbdic_pyramid_set_solver_mode(gbdic_pyramid *p, int32_t mode) {
+    return pguarded(p, [&] {
+        for (auto &s : p->slots)
+            if (s.pending) fail(GBDIC_ESTATE, "retire every slot before switching the solver mode");
+        check_cuda(cudaStreamSynchronize(p->rt->stream()), "pending work");
+        p->rt->set_mode(mode);
+        for (auto &s : p->slots) s.drop_graphs();
+    });
+}
+
 int gbdic_pyramid_profile(gbdic_pyramid *p, int32_t enable) {
     return pguarded(p, [&] {
         check_cuda(cudaStreamSynchronize(p->rt->stream()), "pending work");

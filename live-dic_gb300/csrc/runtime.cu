@@ -71,6 +71,8 @@ void validate_options(const gbdic_options &o) {
     if (o.divergence_min_iterations < 1 || o.divergence_min_iterations > 30)
         fail(GBDIC_EINVAL, "divergence_min_iterations must be an integer from 1 to 30");
     if (o.pipeline_slots < 1 || o.pipeline_slots > 64) fail(GBDIC_EINVAL, "pipeline_depth must be a positive integer");
+    if (o.solver_mode != GBDIC_SOLVER_EXACT && o.solver_mode != GBDIC_SOLVER_FAST)
+        fail(GBDIC_EINVAL, "solver_mode must be 'exact' or 'fast'");
 }
 
 void validate_cfg(const gbdic_solver_cfg *c) {
@@ -170,6 +172,17 @@ Runtime::~Runtime() {
     for (auto ev : profile_end_) cudaEventDestroy(ev);
 }
 
+bool Runtime::fast_active() const {
+    return opt_.o.solver_mode == GBDIC_SOLVER_FAST &&
+           icgn_fast_supported(opt_.o.motion_model, opt_.o.interpolation, opt_.lanes);
+}
+
+void Runtime::set_mode(int mode) {
+    if (mode != GBDIC_SOLVER_EXACT && mode != GBDIC_SOLVER_FAST) fail(GBDIC_EINVAL, "solver_mode must be 'exact' or 'fast'");
+    opt_.o.solver_mode = mode;
+    if (opt_.o.persistent) persistent_grid(opt_.lanes);
+}
+
 void Runtime::set_variant(int lanes, bool persistent) {
     if (lanes != 16 && lanes != 32 && lanes != 64 && lanes != 128)
         fail(GBDIC_EINVAL, "threads_per_subset must be 16, 32, 64, or 128");
@@ -181,10 +194,15 @@ void Runtime::set_variant(int lanes, bool persistent) {
 
 int Runtime::persistent_grid(int lanes) {
     // Queried once per lane count outside any stream capture, then cached.
-    if (lanes != persistent_lanes_ || persistent_grid_ <= 0) {
-        const int per_sm = icgn_occupancy(opt_.o.motion_model, opt_.o.interpolation, lanes, opt_.o.spatial_weighting == 1);
+    const bool fast = opt_.o.solver_mode == GBDIC_SOLVER_FAST &&
+                      icgn_fast_supported(opt_.o.motion_model, opt_.o.interpolation, lanes);
+    if (lanes != persistent_lanes_ || fast != persistent_fast_ || persistent_grid_ <= 0) {
+        const bool gauss = opt_.o.spatial_weighting == 1;
+        const int per_sm = fast ? icgn_fast_occupancy(opt_.o.motion_model, lanes, gauss)
+                                : icgn_occupancy(opt_.o.motion_model, opt_.o.interpolation, lanes, gauss);
         persistent_grid_ = std::max(1, per_sm) * sm_count_;
         persistent_lanes_ = lanes;
+        persistent_fast_ = fast;
     }
     return persistent_grid_;
 }
@@ -401,6 +419,7 @@ SolveArgs Runtime::solve_args(Level &level, LevelSlot &slot, const gbdic_solver_
     a.div_patience = level.divergence ? opt_.o.divergence_patience : 0;
     a.div_min = opt_.o.divergence_min_iterations;
     a.persistent = opt_.o.persistent;
+    a.fast_segments = fast_active() ? icgn_fast_segments(opt_.o.subset_size, opt_.lanes) : 0;
     return a;
 }
 

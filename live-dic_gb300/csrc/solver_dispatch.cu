@@ -37,11 +37,20 @@ int icgn_occupancy(int model, int interp, int lanes, bool gauss) {
     return blocks;
 }
 
+int icgn_fast_occupancy(int model, int lanes, bool gauss) {
+    SolveArgs unused{};
+    int blocks = 0;
+    if (launch_icgn_fast(unused, model, lanes, gauss, 0, nullptr, &blocks) != cudaSuccess) return 0;
+    return blocks;
+}
+
 cudaError_t launch_icgn(const SolveArgs &a, int model, int interp, int lanes, bool gauss,
                         int persistent_grid, cudaStream_t stream) {
     if (a.count <= 0) return cudaSuccess;
     const int grid = a.persistent ? persistent_grid : icgn_grid(a.count, lanes);
     if (grid <= 0) return cudaErrorInvalidConfiguration;
+    if (a.fast_segments > 0 && icgn_fast_supported(model, interp, lanes))
+        return launch_icgn_fast(a, model, lanes, gauss, grid, stream, nullptr);
     return dispatch(a, model, interp, lanes, gauss, grid, stream, nullptr);
 }
 

@@ -39,7 +39,11 @@ class Options(C.Structure):
         ("divergence_min_iterations", C.c_int32),
         ("pipeline_slots", C.c_int32),
         ("persistent", C.c_int32),
+        ("solver_mode", C.c_int32),
     ]
+
+
+SOLVER_MODES = {"exact": 0, "fast": 1}
 
 
 class SolverCfg(C.Structure):
@@ -186,6 +190,8 @@ _SIGNATURES = {
     "gbdic_register_noalloc": (C.c_int, [C.POINTER(NoAllocFrame), P, P]),
     "gbdic_set_solver_variant": (C.c_int, [P, I32, I32]),
     "gbdic_pyramid_set_solver_variant": (C.c_int, [P, I32, I32]),
+    "gbdic_set_solver_mode": (C.c_int, [P, I32]),
+    "gbdic_pyramid_set_solver_mode": (C.c_int, [P, I32]),
     "gbdic_batch_create": (C.c_int, [I32, C.POINTER(P)]),
     "gbdic_batch_destroy": (C.c_int, [P]),
     "gbdic_batch_last_error": (C.c_char_p, [P]),

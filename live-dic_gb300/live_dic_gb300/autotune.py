@@ -1,4 +1,5 @@
-"""Solver autotuner: picks lanes per subset and the work distribution.
+"""Solver autotuner: picks lanes per subset, the work distribution and the
+pixel loop.
 
 Follows the reference's _autotune_solver (wgpu_backend.py:2213-2296): run the
 baseline variant and every candidate on one representative target (the
@@ -6,8 +7,12 @@ reference shifted by (-1, +2) pixels), reject candidates whose field disagrees
 with the baseline under the reference's acceptance rule
 (_compare_solver_outputs, 222-299: accepted-mask mismatch <= 0.5 % of the
 grid, parameter RMSE <= 2e-3, max |difference| <= 2e-2), time the rest and
-keep the fastest.  Candidates: 16, 32, 64 or 128 lanes per subset, each as a
-grid launch or as a persistent grid over the work queue.
+keep the fastest.  Candidates: 16, 32, 64 or 128 lanes per subset with the
+exact pixel loop (the reference's pixel-to-lane order), and 16 or 32 lanes
+with the sliding-window loop (column runs sharing B-spline taps in
+registers; the engine runs it for B-spline translation / affine windows and
+falls back to the exact loop elsewhere), each as a grid launch or as a
+persistent grid over the work queue.
 """
 
 from __future__ import annotations
@@ -18,7 +23,8 @@ from statistics import median
 
 import numpy as np
 
-CANDIDATES = tuple((lanes, persistent) for persistent in (False, True) for lanes in (16, 32, 64, 128))
+CANDIDATES = tuple((lanes, persistent, "exact") for persistent in (False, True) for lanes in (16, 32, 64, 128)) + \
+    tuple((lanes, persistent, "fast") for persistent in (False, True) for lanes in (16, 32))
 
 
 def compare_solver_outputs(portable: np.ndarray, candidate: np.ndarray) -> dict:
@@ -62,42 +68,44 @@ def compare_solver_outputs(portable: np.ndarray, candidate: np.ndarray) -> dict:
     return out
 
 
-def variant_name(lanes: int, persistent: bool) -> str:
-    return f"{lanes}-lane {'persistent-queue' if persistent else 'grid'}"
+def variant_name(lanes: int, persistent: bool, mode: str = "exact") -> str:
+    name = f"{lanes}-lane {'persistent-queue' if persistent else 'grid'}"
+    return name if mode == "exact" else f"{name} {mode}"
 
 
 def autotune(
-    set_variant: Callable[[int, bool], None],
+    set_variant: Callable[[int, bool, str], None],
     run: Callable[[], tuple[np.ndarray, float]],
     *,
-    baseline: tuple[int, bool] = (32, False),
+    baseline: tuple[int, bool, str] = (32, False, "exact"),
     candidates=CANDIDATES,
     repeats: int = 3,
-) -> tuple[tuple[int, bool], dict[str, float], dict[str, dict]]:
+) -> tuple[tuple[int, bool, str], dict[str, float], dict[str, dict]]:
     """Returns (best variant, median device ms per variant, validation per variant).
-    `run()` registers the tuning target and returns (packed field, device ms)."""
+    A variant is (lanes, persistent, pixel loop).  `run()` registers the
+    tuning target and returns (packed field, device ms)."""
     set_variant(*baseline)
     run()
     reference_field, _ = run()
     timings: dict[str, list[float]] = {}
     validation: dict[str, dict] = {}
     valid = []
-    for lanes, persistent in candidates:
-        name = variant_name(lanes, persistent)
-        set_variant(lanes, persistent)
+    for variant in candidates:
+        name = variant_name(*variant)
+        set_variant(*variant)
         field, _ = run()
         check = compare_solver_outputs(reference_field, field)
         validation[name] = check
         if check["valid"]:
-            valid.append((lanes, persistent))
+            valid.append(variant)
     if baseline not in valid:
         valid.insert(0, baseline)
     for repetition in range(repeats):
         order = valid if repetition % 2 == 0 else list(reversed(valid))
-        for lanes, persistent in order:
-            set_variant(lanes, persistent)
+        for variant in order:
+            set_variant(*variant)
             _, ms = run()
-            timings.setdefault(variant_name(lanes, persistent), []).append(ms)
+            timings.setdefault(variant_name(*variant), []).append(ms)
     tuning = {name: float(median(values)) for name, values in timings.items()}
     best = min(valid, key=lambda v: tuning[variant_name(*v)])
     set_variant(*best)

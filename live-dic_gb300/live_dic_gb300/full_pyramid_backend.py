@@ -27,7 +27,8 @@ from .engine import ICGNError, ImageInput, ReferenceInfo, RegistrationResult, _a
 from .fourier import FourierInitializer
 from .interpolation import normalize_interpolation
 from .motion import normalize_motion_model, parameter_count, state_float_count
-from .native_backend import DEFAULT_IN_FLIGHT_FRAMES, _normalize_device_type, _normalize_solver_workgroup_size, _validated_config, native_options
+from .native_backend import (DEFAULT_IN_FLIGHT_FRAMES, _normalize_device_type, _normalize_solver_workgroup_size,
+                             _validated_config, native_options, normalize_solver_mode)
 from .outlier import normalize_median_filter_scope, normalize_median_filter_size, normalize_outlier_policy
 from .roi import immutable, integral, prepare_roi, reduce_mask, seed_permissions, validate_roi
 from .subset import DEFAULT_SUBSET_SIZE, normalize_subset_size, normalize_subset_stride, subset_grid_shape
@@ -111,7 +112,9 @@ class ICGNWGPUFullPyramid:
         persistent: bool = False,
         seed_search_radius: int | None = None,
         autotune: bool = False,
+        solver_mode: str = "exact",
     ) -> None:
+        self.solver_mode = normalize_solver_mode(solver_mode)
         self._autotune = bool(autotune)
         self.solver_tuning_ms: dict[str, float] = {}
         self.solver_validation: dict[str, dict] = {}
@@ -231,7 +234,7 @@ class ICGNWGPUFullPyramid:
         self._handle = self._create(device)
         self.device_index = int(device)
         self.device_name = f"CUDA device {self.device_index} (gbdic sm_103a)"
-        self.solver = _tuning.variant_name(self.solver_workgroup_size, self._persistent)
+        self.solver = _tuning.variant_name(self.solver_workgroup_size, self._persistent, self.solver_mode)
         self.execution_device_type = "gpu"
         self._reference_ready = False
         self.roi = None
@@ -256,6 +259,7 @@ class ICGNWGPUFullPyramid:
             persistent=self._persistent,
             divergence_patience=self.divergence_patience or 0,
             divergence_min_iterations=self.divergence_min_iterations,
+            solver_mode=self.solver_mode,
         )
         po.levels = self.pyramid_levels
         for i in range(self.pyramid_levels):
@@ -434,6 +438,7 @@ class ICGNWGPUFullPyramid:
             "subsetStride": self.subset_stride,
             "spatialWeighting": self.spatial_weighting,
             "solverWorkgroupSize": self.solver_workgroup_size,
+            "solverMode": self.solver_mode,
             "gaussianSigma": self.gaussian_sigma,
         }
         if self.pyramid_policy == "adaptive":
@@ -666,13 +671,23 @@ class ICGNWGPUFullPyramid:
         self._check(self._lib.gbdic_pyramid_register_device(
             self._handle, C.c_void_p(device_frame), C.c_void_p(device_state), C.c_void_p(stream or 0)))
 
-    def set_solver_variant(self, lanes: int, persistent: bool = False) -> None:
-        """Select the solver variant of every level (lanes per subset, grid or persistent queue)."""
+    def set_solver_variant(self, lanes: int, persistent: bool = False, mode: str | None = None) -> None:
+        """Select the solver variant of every level (lanes per subset, grid or
+        persistent queue, and optionally the pixel loop)."""
         self._check(self._lib.gbdic_pyramid_set_solver_variant(
             self._handle, _normalize_solver_workgroup_size(lanes), int(bool(persistent))))
         self.solver_workgroup_size = int(lanes)
         self._persistent = bool(persistent)
-        self.solver = _tuning.variant_name(int(lanes), bool(persistent))
+        if mode is not None:
+            self.set_solver_mode(mode)
+        self.solver = _tuning.variant_name(int(lanes), bool(persistent), self.solver_mode)
+
+    def set_solver_mode(self, mode: str) -> None:
+        """Select the pixel loop ('exact' or 'fast') of every level."""
+        mode = normalize_solver_mode(mode)
+        self._check(self._lib.gbdic_pyramid_set_solver_mode(self._handle, _native.SOLVER_MODES[mode]))
+        self.solver_mode = mode
+        self.solver = _tuning.variant_name(self.solver_workgroup_size, self._persistent, mode)
 
     def _autotune_solver(self, reference: np.ndarray) -> None:
         """Fastest validated variant on the reference shifted by (-1, +2) px;

@@ -71,6 +71,16 @@ def _normalize_solver_workgroup_size(value: int) -> int:
     return size
 
 
+def normalize_solver_mode(value: str) -> str:
+    """Pixel loop of the IC-GN solver (no reference counterpart): 'exact'
+    keeps the reference's pixel-to-lane order and summation, 'fast' runs the
+    sliding-window loop for B-spline translation / affine windows (other
+    configurations keep the exact loop)."""
+    if not isinstance(value, str) or value not in _native.SOLVER_MODES:
+        raise ValueError("solver_mode must be 'exact' or 'fast'")
+    return value
+
+
 def _exclusive_call(method):
     """One registration at a time per engine (wgpu_backend.py:826-838)."""
 
@@ -118,6 +128,7 @@ def native_options(
     persistent: bool,
     divergence_patience: int = 0,
     divergence_min_iterations: int = 4,
+    solver_mode: str = "exact",
 ) -> _native.Options:
     o = _native.Options()
     o.device = device
@@ -135,6 +146,7 @@ def native_options(
     o.divergence_min_iterations = divergence_min_iterations
     o.pipeline_slots = pipeline_slots
     o.persistent = int(persistent)
+    o.solver_mode = _native.SOLVER_MODES[solver_mode]
     return o
 
 
@@ -147,7 +159,10 @@ class ICGNWGPU:
     FIR prefilter, the IC-GN solve and the UOD pass, and returns the packed
     field as zero-copy NumPy views.  ``solver_workgroup_size`` is the number
     of CUDA lanes that share one subset (16, 32, 64 or 128); results at
-    different widths differ only by float reduction order.
+    different widths differ only by float reduction order.  ``solver_mode``
+    (an extension) selects the pixel loop: 'exact' (the reference's order)
+    or 'fast' (sliding-window B-spline sampling, within the parity
+    tolerances of the exact loop); the autotuner considers both.
     ``device_type='cpu'`` is rejected: there is no CPU execution path.
     """
 
@@ -175,8 +190,10 @@ class ICGNWGPU:
         pipeline_slots: int = DEFAULT_IN_FLIGHT_FRAMES,
         persistent: bool = False,
         autotune: bool = False,
+        solver_mode: str = "exact",
     ) -> None:
         self.device_type = _normalize_device_type(device_type)
+        self.solver_mode = normalize_solver_mode(solver_mode)
         if power_preference not in ("high-performance", "low-power"):
             raise ValueError("power_preference must be 'high-performance' or 'low-power'")
         self.interpolation = normalize_interpolation(interpolation)
@@ -242,13 +259,14 @@ class ICGNWGPU:
             lanes=self.solver_workgroup_size,
             pipeline_slots=slots,
             persistent=self._persistent,
+            solver_mode=self.solver_mode,
         )
         code = self._lib.gbdic_create(C.byref(options), C.byref(handle))
         _native.check(code, self._lib.gbdic_last_error(None))
         self._handle = handle
         self.device_index = int(device)
         self.device_name = f"CUDA device {self.device_index} (gbdic sm_103a)"
-        self.solver = _tuning.variant_name(self.solver_workgroup_size, self._persistent)
+        self.solver = _tuning.variant_name(self.solver_workgroup_size, self._persistent, self.solver_mode)
         self.execution_device_type = "gpu"
         self.width = self.height = self.grid_width = self.grid_height = 0
         self._reference_ready = False
@@ -264,13 +282,23 @@ class ICGNWGPU:
         if code != _native.OK:
             _native.check(code, self._lib.gbdic_last_error(self._handle))
 
-    def set_solver_variant(self, lanes: int, persistent: bool = False) -> None:
-        """Select the solver variant: lanes per subset and grid or persistent queue."""
+    def set_solver_variant(self, lanes: int, persistent: bool = False, mode: str | None = None) -> None:
+        """Select the solver variant: lanes per subset, grid or persistent
+        queue, and (optionally) the pixel loop."""
         self._check(self._lib.gbdic_set_solver_variant(self._handle, _normalize_solver_workgroup_size(lanes),
                                                        int(bool(persistent))))
         self.solver_workgroup_size = int(lanes)
         self._persistent = bool(persistent)
-        self.solver = _tuning.variant_name(int(lanes), bool(persistent))
+        if mode is not None:
+            self.set_solver_mode(mode)
+        self.solver = _tuning.variant_name(int(lanes), bool(persistent), self.solver_mode)
+
+    def set_solver_mode(self, mode: str) -> None:
+        """Select the pixel loop ('exact' or 'fast') without re-preparing the reference."""
+        mode = normalize_solver_mode(mode)
+        self._check(self._lib.gbdic_set_solver_mode(self._handle, _native.SOLVER_MODES[mode]))
+        self.solver_mode = mode
+        self.solver = _tuning.variant_name(self.solver_workgroup_size, self._persistent, mode)
 
     def _autotune_solver(self, reference: np.ndarray) -> None:
         """Choose the fastest validated variant on the reference shifted by
@@ -321,6 +349,7 @@ class ICGNWGPU:
             "subsetStride": self.subset_stride,
             "spatialWeighting": self.spatial_weighting,
             "solverWorkgroupSize": self.solver_workgroup_size,
+            "solverMode": self.solver_mode,
             "gaussianSigma": self.gaussian_sigma,
         }
         if self.roi is not None:

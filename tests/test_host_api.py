@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
     for name in sorted(declared):
         assert hasattr(lib, name), name
     assert declared == set(_native.EXPORTED_SYMBOLS)
-    assert _native.load().gbdic_abi_version() == 1
+    assert _native.load().gbdic_abi_version() == 2
 
 
 @pytest.mark.parametrize(
