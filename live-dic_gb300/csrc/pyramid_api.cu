@@ -93,9 +93,11 @@ struct gbdic_pyramid {
     }
     int L() const { return (int)levels.size(); }
     bool temporal() const { return po.initialization == 1; }
-    // ZNCC integer seed search at the coarsest level: initialization 2, or
-    // temporal initialization with a search radius (subsets without history).
-    bool search() const { return po.seed_search_radius > 0 && (po.initialization == 2 || po.initialization == 1); }
+    // ZNCC integer seed search at the coarsest level: initialization 2;
+    // temporal initialization with a search radius (subsets without
+    // history); or Fourier initialization with a search radius (shifts
+    // centred on the global translation, the residual of a non-rigid field).
+    bool search() const { return po.seed_search_radius > 0 && po.initialization >= 1 && po.initialization <= 3; }
     bool velocity() const { return po.temporal_prediction == 1; }
     bool fine_correction() const { return po.temporal_fine_correction != 0; }
     // Global translation seed of the coarsest level (Fourier initialization).
@@ -237,7 +239,8 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
     }
     if (p->search() && c == p->L() - 1) {
         // ZNCC integer search at the coarsest level: every subset (zncc
-        // initialization) or only those without a temporal seed.
+        // initialization), only those without a temporal seed, or every
+        // subset around the global translation seed (Fourier).
         gbdic::SearchArgs q{};
         q.ref = coarse.ref_image.as<uint8_t>();
         q.tgt = cframe ? cframe : cslot.frame.as<uint8_t>();
@@ -250,6 +253,7 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
         q.radius = p->po.seed_search_radius;
         q.model = model;
         q.only_missing = p->temporal() ? 1 : 0;
+        q.centered = p->global() ? 1 : 0;
         check_cuda(gbdic::launch_zncc_search(q, s), "seed search launch");
         seeded = true;
     }

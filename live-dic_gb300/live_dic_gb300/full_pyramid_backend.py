@@ -150,8 +150,8 @@ class ICGNWGPUFullPyramid:
                 raise ValueError("seed_search_radius must be an integer from 1 to 64") from error
             if isinstance(seed_search_radius, bool) or not 1 <= radius <= 64:
                 raise ValueError("seed_search_radius must be an integer from 1 to 64")
-            if initialization not in ("zncc", "temporal"):
-                raise ValueError("seed_search_radius requires initialization='zncc' or 'temporal'")
+            if initialization not in ("zncc", "temporal", "fourier"):
+                raise ValueError("seed_search_radius requires initialization='zncc', 'temporal' or 'fourier'")
             seed_search_radius = radius
         elif initialization == "zncc":
             seed_search_radius = 8
@@ -662,11 +662,21 @@ class ICGNWGPUFullPyramid:
                 self._lib.gbdic_pyramid_retire(self._handle, slot, None, None, None)
             self._registration_lock.release()
 
-    def register_device(self, device_frame: int, device_state: int, *, stream: int | None = None) -> None:
-        """Resident registration of a device frame into a device state buffer."""
+    def register_device(self, device_frame: int, device_state: int, *, stream: int | None = None,
+                        translation: tuple[float, float] | None = None) -> None:
+        """Resident registration of a device frame into a device state buffer.
+        With Fourier initialization, `translation` (dx, dy) replaces the
+        initializer's own estimate as the global seed (e.g. one computed on
+        the device from another window)."""
         if not self._reference_ready:
             raise ICGNError("Call set_reference() before register().")
-        self._global_translation(0, device_frame=device_frame, row_stride=self.width)
+        if translation is not None:
+            if self.initialization != "fourier":
+                raise ValueError("translation requires initialization='fourier'")
+            self._check(self._lib.gbdic_pyramid_set_translation(self._handle, 0, float(translation[0]),
+                                                                float(translation[1])))
+        else:
+            self._global_translation(0, device_frame=device_frame, row_stride=self.width)
         self._begin_frame()
         self._check(self._lib.gbdic_pyramid_register_device(
             self._handle, C.c_void_p(device_frame), C.c_void_p(device_state), C.c_void_p(stream or 0)))

@@ -492,6 +492,86 @@ def fit_consensus(translations: np.ndarray, xy: np.ndarray, tables, tolerances=C
     return A @ fit_coef
 
 
+class HalfResolutionShift:
+    """Global translation of a frame by GPU phase correlation of a 256-pixel
+    window at the centre of its half-resolution level (a 512-pixel region of
+    the frame; the shift is resolved to 2 frame pixels), the computation of
+    FourierInitializer.estimate (fourier.py:59-111) run in stream order on
+    the device without host synchronisation (gbdic_fourier_shift_device).
+    The learned seeder removes it before its first network pass; a plain
+    pyramid can take it as its global seed."""
+
+    def __init__(self, width: int, height: int, *, device: int = 0) -> None:
+        torch = _torch()
+        self.W, self.H = int(width), int(height)
+        self.lib = _native.load()
+        self.device = torch.device("cuda", device)
+        self.tgt_half = torch.empty(self.H // 2, self.W // 2, dtype=torch.uint8, device=self.device)
+        self.fourier = None
+        self.window = None
+
+    def set_reference_half(self, half: np.ndarray) -> None:
+        """The reference's half-resolution level (host bytes)."""
+        from .fourier import FourierInitializer
+
+        self.close()
+        hh, hw = half.shape
+        side = min(256, hh, hw)
+        x0, y0 = (hw - side) // 2, (hh - side) // 2
+        try:
+            self.fourier = FourierInitializer(np.ascontiguousarray(half[y0:y0 + side, x0:x0 + side]),
+                                              device=self.device.index or 0)
+        except ValueError:
+            self.fourier = None
+        if self.fourier is not None:
+            win = self.fourier.window
+            self.window = (x0 + win["x"], y0 + win["y"])
+
+    def set_reference_frame(self, frame) -> None:
+        """The reference as a device frame (uint8 H x W)."""
+        torch = _torch()
+        half = torch.empty_like(self.tgt_half)
+        _call(self.lib, "gbdic_reduce_half", _ptr(frame), self.W, self.H, _ptr(half), None)
+        torch.cuda.synchronize(self.device)
+        self.set_reference_half(half.cpu().numpy())
+
+    @property
+    def available(self) -> bool:
+        return self.fourier is not None
+
+    def write(self, frame_half_ptr: int, rows_ptr: int, count: int, pitch: int, multiplier: float, stream) -> None:
+        """Writes dx * multiplier and dy * multiplier (dx, dy in half-level
+        pixels) into rows[i * pitch] and rows[i * pitch + 3], i < count; zero
+        when the estimate is not accepted."""
+        fx, fy = self.window
+        code = self.lib.gbdic_fourier_shift_device(
+            self.fourier._handle, C.c_void_p(frame_half_ptr), self.W // 2, self.H // 2, fx, fy,
+            C.c_float(multiplier), C.c_void_p(rows_ptr), count, pitch, stream)
+        _native.check(code, self.lib.gbdic_fourier_last_error(self.fourier._handle))
+
+    def shift_of(self, frame, stream=None) -> tuple[float, float]:
+        """(dx, dy) in frame pixels of device frame `frame` (uint8 H x W),
+        computed on `stream` (a torch.cuda.Stream; None: the current one),
+        which is synchronised to read it; (0, 0) when not accepted."""
+        torch = _torch()
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        handle = C.c_void_p(s.cuda_stream)
+        with torch.cuda.stream(s):
+            rows = torch.zeros(8, device=self.device)
+        _call(self.lib, "gbdic_reduce_half", _ptr(frame), self.W, self.H, _ptr(self.tgt_half), handle)
+        if self.available:
+            self.write(self.tgt_half.data_ptr(), rows.data_ptr(), 1, 8, 2.0, handle)
+        s.synchronize()
+        values = rows.cpu()
+        return float(values[0]), float(values[3])
+
+    def close(self) -> None:
+        if self.fourier is not None:
+            self.fourier.close()
+        self.fourier = None
+        self.window = None
+
+
 class LearnedSeeder:
     """Learned-seed registration for one fixed reference on the single-scale
     engine: the global translation by GPU phase correlation, network
@@ -510,7 +590,6 @@ class LearnedSeeder:
         self.passes = max(1, int(passes))
         self.global_alignment = bool(global_alignment)
         self.refine_nodes = bool(refine_nodes)
-        self.fourier = None
         self.lib = _native.load()
         dev = net.device
         W, H = engine.width, engine.height
@@ -528,6 +607,7 @@ class LearnedSeeder:
         self.ref_ptrs = torch.tensor([self.ref_half.data_ptr()], dtype=torch.int64, device=dev)
         self.tgt_ptrs = torch.tensor([self.tgt_half.data_ptr()], dtype=torch.int64, device=dev)
         self._ref_full = torch.empty(H, W, dtype=torch.uint8, device=dev)
+        self.global_shift = HalfResolutionShift(W, H, device=dev.index or 0)
         usable = np.asarray(engine.reference_valid, dtype=bool)
         if engine.roi is not None:
             usable = usable & np.asarray(engine.roi.selected, dtype=bool)
@@ -566,7 +646,6 @@ class LearnedSeeder:
         self._node_active = torch.from_numpy(node_active.ravel()).to(dev)
         self._shifted = False
         self.reseed_count = torch.zeros(1, dtype=torch.int32, device=dev)
-        self._fourier_window = None
 
     def set_reference_image(self, reference: np.ndarray) -> None:
         """Half-resolution reference for the network (the engine keeps its own),
@@ -575,26 +654,12 @@ class LearnedSeeder:
         half-resolution reference (a 512-pixel region of the frame; the shift
         is resolved to 4 frame pixels, well inside the network's range)."""
         torch = _torch()
-        from .fourier import FourierInitializer
 
         self._ref_full.copy_(torch.from_numpy(np.ascontiguousarray(reference, dtype=np.uint8)))
         _call(self.lib, "gbdic_reduce_half", _ptr(self._ref_full), self.W, self.H, _ptr(self.ref_half), None)
-        if self.fourier is not None:
-            self.fourier.close()
-        self.fourier = None
-        self._fourier_window = None
+        self.global_shift.close()
         if self.global_alignment:
-            half = self.ref_half.cpu().numpy()
-            hh, hw = half.shape
-            side = min(256, hh, hw)
-            x0, y0 = (hw - side) // 2, (hh - side) // 2
-            try:
-                self.fourier = FourierInitializer(half[y0:y0 + side, x0:x0 + side], device=self.net.device.index or 0)
-            except ValueError:
-                self.fourier = None
-            if self.fourier is not None:
-                win = self.fourier.window
-                self._fourier_window = (x0 + win["x"], y0 + win["y"])
+            self.global_shift.set_reference_half(self.ref_half.cpu().numpy())
     def propose(self, frame) -> None:
         """Network proposals for device frame `frame` (uint8 H x W) -> self.seeds
         (on self.stream)."""
@@ -642,12 +707,9 @@ class LearnedSeeder:
         # device, in stream order.
         _call(self.lib, "gbdic_reduce_half", _ptr(frame), self.W, self.H, _ptr(self.tgt_half), stream)
         shift = None
-        if self.fourier is not None:
-            fx, fy = self._fourier_window
-            code = self.lib.gbdic_fourier_shift_device(
-                self.fourier._handle, _ptr(self.tgt_half), self.W // 2, self.H // 2, fx, fy,
-                C.c_float(2.0 / TRANSLATION_SCALE), _ptr(self.base), self.lattice, OUT_PAD, stream)
-            _native.check(code, self.lib.gbdic_fourier_last_error(self.fourier._handle))
+        if self.global_shift.available:
+            self.global_shift.write(self.tgt_half.data_ptr(), self.base.data_ptr(), self.lattice, OUT_PAD,
+                                    2.0 / TRANSLATION_SCALE, stream)
             shift = self.base
         for p in range(self.passes):
             self._network_pass(self.pred, shift, stream)

@@ -18,7 +18,11 @@ temporal seed permissions (bits 0-3 corners, bit 4 selected, bits 5-31 the
 fallback source; full_pyramid.wgsl:397-450).  `search_radius` > 0: the
 integer ZNCC search at the coarsest level (every subset, or with temporal
 seeding only those the projection left without a seed, whose status the
-projection marks -1), on `reference_levels[-1]`.
+projection marks -1), on `reference_levels[-1]`.  `global_shift`: the
+Fourier initialization, whose uniform coarsest seed (dx, dy) / 2^(levels-1)
+for every selected subset (full_pyramid_backend.py:1704-1714) takes the
+frame's estimate `register(frame, shift=(dx, dy))`, followed with a search
+radius by the search centred on it.
 """
 
 from __future__ import annotations
@@ -57,10 +61,12 @@ class PyramidOracle:
                  velocity: bool = False, fine_correction: bool = False, adaptive: bool = False,
                  max_age: int = 0xFFFFFFFE, divergence_patience: int = 0, divergence_min_iterations: int = 4,
                  rois: list[LevelRoi] | None = None, temporal_links: np.ndarray | None = None,
-                 search_radius: int = 0, reference_levels: list[np.ndarray] | None = None):
+                 search_radius: int = 0, reference_levels: list[np.ndarray] | None = None,
+                 global_shift: bool = False):
         self.levels = levels
         self.rois, self.temporal_links = rois, temporal_links
         self.search_radius, self.reference_levels = search_radius, reference_levels
+        self.global_shift = global_shift
         if search_radius and reference_levels is None:
             raise ValueError("the seed search needs the reference image of every level")
         self.L = len(levels)
@@ -110,7 +116,10 @@ class PyramidOracle:
                      permissions=None if self.rois is None else self.rois[level].links)
         return raw, out
 
-    def register(self, frame: np.ndarray, levels_used: int | None = None) -> tuple[np.ndarray, list[int]]:
+    def register(self, frame: np.ndarray, levels_used: int | None = None,
+                 shift: tuple[float, float] | None = None) -> tuple[np.ndarray, list[int]]:
+        """One frame; `shift` = the frame's global translation (Fourier
+        initialization)."""
         L = levels_used or self.L
         frames = [np.ascontiguousarray(frame, dtype=np.uint8)]
         for _ in range(1, L):
@@ -136,12 +145,19 @@ class PyramidOracle:
                 seed[weights == 0.0, self.status_at] = -1.0
             if self.fine_correction:
                 seed[~projected, self.status_at] = -1.0
+        selected = None if self.rois is None else self.rois[c].selected
+        if self.global_shift:
+            count = self.levels[c].grid_w * self.levels[c].grid_h
+            seed = np.zeros((count, self.ss), np.float32)
+            inv = np.float32(1.0 / (1 << c))
+            seed[:, 0] = np.float32(shift[0]) * inv
+            seed[:, 3] = np.float32(shift[1]) * inv
+            active = np.ones(count, np.uint32) if selected is None else (selected != 0).astype(np.uint32)
         if self.search_radius and c == self.L - 1:
-            selected = None if self.rois is None else self.rois[c].selected
             seed, active, _ = oc.seed_search(
                 self.reference_levels[c], frames[c], subset_size=self.S, subset_stride=self.s,
                 radius=self.search_radius, model=self.model, seed=seed, only_missing=self.temporal,
-                selected=selected, active=active)
+                selected=selected, active=active, centered=self.global_shift)
         raws, outs = {}, {}
         raws[c], outs[c] = self._solve_level(c, frames[c], seed, active)
         for level in range(L - 2, -1, -1):
@@ -175,3 +191,55 @@ class PyramidOracle:
                 oc.temporal_merge(self.coarse_history, self.coarse_ages, raw_top, out_top, model=self.model,
                                   max_age=self.max_age, use_filtered=use_filtered)
         return outs[0], counters
+
+
+def roi_tables(mask: np.ndarray | None, *, subset_size: int, subset_stride: int, levels: int,
+               median_filter_size: int = 3, outlier_policy: str = "replace"):
+    """The host ROI tables a full-pyramid engine uploads for `mask` (per-level
+    selection, UOD links, coarse-to-fine seed permissions, and the temporal
+    projection's permissions), from the package's ROI planner (whose plans
+    are pinned to the reference's).  Returns (plans, rois, temporal_links),
+    or (None, None, None) without a mask."""
+    from live_dic_gb300.roi import integral, prepare_roi, reduce_mask, seed_permissions
+
+    if mask is None:
+        return None, None, None
+    masks = [mask]
+    for _ in range(1, levels):
+        masks.append(reduce_mask(masks[-1]))
+    plans = [prepare_roi(m, subset_size, subset_stride, median_filter_size=median_filter_size) for m in masks]
+    prefix = integral(mask)
+    rois = []
+    for level, plan in enumerate(plans):
+        links = None
+        if level < levels - 1:
+            links = np.ascontiguousarray(seed_permissions(
+                plans[level + 1], plan, source_scale=1 << (level + 1), destination_scale=1 << level,
+                size=subset_size, stride=subset_stride, reference_mask=mask, reference_prefix=prefix),
+                dtype=np.uint32).ravel()
+        rois.append(LevelRoi(np.ascontiguousarray(plan.selected, np.uint8).ravel(),
+                             np.ascontiguousarray(plan.links_table(median_filter_size, outlier_policy)), links))
+    temporal = np.ascontiguousarray(seed_permissions(
+        plans[0], plans[-1], source_scale=1, destination_scale=1 << (levels - 1), size=subset_size,
+        stride=subset_stride, reference_mask=mask, reference_prefix=prefix), dtype=np.uint32).ravel()
+    return plans, rois, temporal
+
+
+def float64_levels(reference: np.ndarray, *, subset_size: int, subset_stride: int, levels: int,
+                   plans=None) -> tuple[list[LevelArrays], list[np.ndarray]]:
+    """Per-level reference arrays from the float64 restatement of
+    _reference_arrays on the integer pyramid of `reference` (windows a plan
+    excludes get validity -3), and the level images."""
+    images = [np.ascontiguousarray(reference, dtype=np.uint8)]
+    for _ in range(1, levels):
+        images.append(oc.reduce(images[-1]))
+    out = []
+    for level, img in enumerate(images):
+        plane, inverse, metadata = rp.reference_arrays(img, subset_size=subset_size, subset_stride=subset_stride)
+        h, w = img.shape
+        gw, gh = 1 + (w - subset_size) // subset_stride, 1 + (h - subset_size) // subset_stride
+        if plans is not None:
+            meta = metadata.reshape(gw * gh, -1)
+            meta[~plans[level].selected.ravel(), 1] = -3.0
+        out.append(LevelArrays(w, h, gw, gh, plane, metadata, inverse))
+    return out, images

@@ -26,10 +26,9 @@ import numpy as np
 import pytest
 
 from live_dic_gb300 import ICGNWGPU, ICGNWGPUFullPyramid, _native, synthetic
-from live_dic_gb300.roi import integral, prepare_roi, reduce_mask, seed_permissions
 from oracle import oracle as oracle_c
 from oracle import reference_prep as rp
-from oracle.pyramid_oracle import LevelArrays, LevelRoi, PyramidOracle
+from oracle.pyramid_oracle import LevelArrays, PyramidOracle, roi_tables
 
 pytestmark = pytest.mark.gpu
 
@@ -42,29 +41,6 @@ def _packed(result):
 PW, PH, HOLE, S1, ST1, LEVELS, RADIUS = 1024, 768, 150.0, 31, 8, 3, 4
 
 
-def _roi_tables(mask, size, stride, levels, policy="replace"):
-    """The host ROI tables the full-pyramid engine uploads (per-level
-    selection and UOD links, coarse-to-fine and temporal seed permissions)."""
-    masks = [mask]
-    for _ in range(1, levels):
-        masks.append(reduce_mask(masks[-1]))
-    plans = [prepare_roi(m, size, stride) for m in masks]
-    prefix = integral(mask)
-    rois = []
-    for level, plan in enumerate(plans):
-        seed_links = None
-        if level < levels - 1:
-            seed_links = np.ascontiguousarray(seed_permissions(
-                plans[level + 1], plan, source_scale=1 << (level + 1), destination_scale=1 << level, size=size,
-                stride=stride, reference_mask=mask, reference_prefix=prefix), dtype=np.uint32).ravel()
-        rois.append(LevelRoi(np.ascontiguousarray(plan.selected, np.uint8).ravel(),
-                             np.ascontiguousarray(plan.links_table(3, policy)), seed_links))
-    temporal = np.ascontiguousarray(seed_permissions(
-        plans[0], plans[-1], source_scale=1, destination_scale=1 << (levels - 1), size=size, stride=stride,
-        reference_mask=mask, reference_prefix=prefix), dtype=np.uint32).ravel()
-    return plans, rois, temporal
-
-
 def test_plate_with_hole_sequence_bit_exact():
     ref, sp = synthetic.reference_image(PW, PH, seed=1201, device="cuda")
     field = synthetic.KirschField(PW, PH, HOLE, peak=2.0)
@@ -72,7 +48,7 @@ def test_plate_with_hole_sequence_bit_exact():
     count = 6
     frames = [synthetic.deformed_image(sp, field.torch_field(k / count), noise_seed=1300 + k, device="cuda")
               for k in range(1, count + 1)]
-    plans, rois, temporal = _roi_tables(mask, S1, ST1, LEVELS)
+    plans, rois, temporal = roi_tables(mask, subset_size=S1, subset_stride=ST1, levels=LEVELS)
     refs = [ref]
     for _ in range(1, LEVELS):
         refs.append(oracle_c.reduce(refs[-1]))
@@ -243,3 +219,60 @@ def test_quadratic_pair_parity_and_curvature_accuracy(quadratic_pair):
     curvature_rmse = float(np.sqrt(np.mean(error[..., 6:][ok] ** 2)))
     assert displacement_rmse < 0.02, displacement_rmse
     assert curvature_rmse < 2e-4, curvature_rmse
+
+
+# ------------------------------------------------------------------ large motion, Fourier-seeded search
+def test_fourier_seeded_search_pyramid_bit_exact():
+    """The plain comparator of the learned seeding at its geometry (subset 31
+    / step 8, 3 levels) on a 1024x768 crop: rigid translations of 20-30 px
+    plus strain and shear of 1-2 %.  The Fourier initialization's global
+    translation seeds the coarsest level and the integer ZNCC search,
+    centred on it, absorbs the strain's residual; every frame is compared bit
+    for bit with the pipeline oracle given the engine's translation
+    estimate."""
+    W, H, radius = 1024, 768, 6
+    ref, sp = synthetic.reference_image(W, H, seed=1501, device="cuda")
+    c = (0.5 * (W - 1), 0.5 * (H - 1))
+    cases = [((24.3, -17.6), (0.02, -0.015, 0.01)), ((-28.1, 9.4), (-0.018, 0.02, -0.012))]
+    refs = [ref]
+    for _ in range(2):
+        refs.append(oracle_c.reduce(refs[-1]))
+    cx, cy = synthetic.subset_centres(W, H, S1, ST1)
+    with ICGNWGPUFullPyramid(pyramid_levels=3, subset_size=S1, subset_stride=ST1, initialization="fourier",
+                             seed_search_radius=radius) as engine:
+        engine.set_reference(ref)
+        levels = []
+        for level in range(3):
+            gw, gh = engine.level_grid(level)
+            w, h = W >> level, H >> level
+            levels.append(LevelArrays(
+                w, h, gw, gh,
+                engine.export_level(level, _native.EXPORT_PLANE, np.float32, (h * w * 4,)),
+                engine.export_level(level, _native.EXPORT_METADATA, np.float32, (gw * gh * 16,)),
+                engine.export_level(level, _native.EXPORT_INVERSE, np.float32, (gw * gh * 36,))))
+        oracle = PyramidOracle(levels, subset_size=S1, subset_stride=ST1, iterations=engine.iterations_per_level,
+                               tolerances=engine.tolerance_per_level, outlier_policy=engine.outlier_policy,
+                               lanes=engine.solver_workgroup_size, search_radius=radius, reference_levels=refs,
+                               global_shift=True)
+        for k, (t, e) in enumerate(cases):
+            def field(X, Y, t=t, e=e):
+                return (t[0] + e[0] * (X - c[0]) + e[2] * (Y - c[1]), t[1] + e[2] * (X - c[0]) + e[1] * (Y - c[1]))
+
+            frame = synthetic.deformed_image(sp, field, noise_seed=1510 + k, device="cuda")
+            result = engine.register(frame)
+            shift = result.config["globalTranslation"]
+            assert abs(shift["dx"] - t[0]) <= 2.0 and abs(shift["dy"] - t[1]) <= 2.0
+            state, _ = oracle.register(frame, shift=(shift["dx"], shift["dy"]))
+            got = _packed(result)
+            np.testing.assert_array_equal(got, state.reshape(got.shape), err_msg=f"frame {k}")
+            u, v = field(cx, cy)
+            # Coarse windows pushed off the image fail, and the transfer
+            # hands their seeds to a band about one coarse window wide
+            # (31 x 4 px) along the leading edges; accuracy is measured
+            # inside it.
+            m = 2 * S1
+            inside = (cx - 15 + u > m) & (cx + 15 + u < W - m) & (cy - 15 + v > m) & (cy + 15 + v < H - m)
+            ok = result.status >= 1
+            assert ok[inside].mean() > 0.95, ok[inside].mean()
+            err = np.hypot(result.displacement[..., 0] - u, result.displacement[..., 1] - v)[ok & inside]
+            assert float(np.sqrt(np.mean(err ** 2))) < 0.02
