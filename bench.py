@@ -1,12 +1,15 @@
 #!/usr/bin/env python
 """UHD DIC throughput benchmark (frames/s and subsets/s).
 
-Workload (one step = one target frame through the whole per-frame path):
-3840x2160 synthetic speckle reference, 60 targets deformed by the plane-strain
-Kirsch field of a circular hole (radius 300 px at the centre, masked out of
-the ROI), scaled to a 2 px peak and ramped linearly over the 60 frames;
-affine IC-GN with subset 31, step 8, B-spline interpolation, 3-level GPU
-pyramid, temporal seeding with velocity prediction, UOD replace.
+Headline workload (one step = one target frame through the whole per-frame
+path): 3840x2160 synthetic speckle reference and a 60-frame sequence deformed
+by the plane-strain Kirsch field of a circular hole (radius 300 px at the
+centre, masked out of the ROI), scaled to a 2 px peak and ramped linearly
+over the 60 frames; affine IC-GN with subset 31, step 8, B-spline
+interpolation, 3-level GPU pyramid, integer ZNCC seed search on the first
+frame, temporal seeding with velocity prediction afterwards, UOD replace.
+The warm-up and timed frames are the last W + K frames of the ramp, so the
+last timed frame is at the 2 px peak.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -14,7 +17,10 @@ pyramid, temporal seeding with velocity prediction, UOD replace.
 resident C-ABI entry, CUDA events on the launching stream); `e2e` runs the
 public register_stream API on host NumPy frames (host->device upload and
 device->host readback inside the timed region).  With N > 1 (torchrun) every
-rank runs an independent replica on its own GPU and frame sequence.
+rank runs an independent replica on its own GPU and frame sequence.  At
+N = 1 the line also carries the two other headline measurements: quadratic
+pairs with the reference rebuilt every pair, and learned versus ZNCC-seeded
+IC-GN on large-motion frames (`--no-extras` leaves them out).
 """
 
 from __future__ import annotations
@@ -52,24 +58,34 @@ def parse_args() -> argparse.Namespace:
     ap.add_argument("--subset", type=int, default=31)
     ap.add_argument("--stride", type=int, default=8)
     ap.add_argument("--levels", type=int, default=3)
-    ap.add_argument("--frames", type=int, default=60)
+    ap.add_argument("--frames", type=int, default=60, help="length of the load ramp")
     ap.add_argument("--hole", type=float, default=300.0)
     ap.add_argument("--peak", type=float, default=2.0)
+    ap.add_argument("--search-radius", type=int, default=4,
+                    help="ZNCC integer search radius at the coarsest level (first frame, unseeded windows)")
     ap.add_argument("--lanes", type=int, default=16)
     ap.add_argument("--persistent", action="store_true")
     ap.add_argument("--solver-mode", choices=("exact", "fast"), default="exact",
                     help="IC-GN pixel loop: the reference's order, or the sliding-window sampler")
-    ap.add_argument("--autotune", action="store_true", help="pick lanes/persistence with the solver autotuner")
+    ap.add_argument("--autotune", action="store_true", help="pick lanes/persistence/pixel loop with the autotuner")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-frames", type=int, default=4, help="timed frames of the CPU pipeline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline workload only (no quadratic-pairs and learned-seeding measurements)")
     ap.add_argument("--workload", choices=("uhd-plate", "batch", "learned", "quadratic-pairs"), default="uhd-plate",
                     help="uhd-plate: the headline UHD sequence; batch: 16 uneven pairs in one batched step; "
-                         "learned: learned-seed vs pyramid+ZNCC seeding on large-translation UHD frames")
-    ap.add_argument("--train-images", type=int, default=512, help="learned workload: training images (320x320)")
+                         "learned: learned-seed vs Fourier + pyramid + ZNCC seeding on large-motion UHD frames; "
+                         "quadratic-pairs: UHD quadratic pairs with the reference rebuilt every pair")
+    ap.add_argument("--train-images", type=int, default=400, help="learned workload: training images")
+    ap.add_argument("--train-size", type=int, default=640, help="learned workload: training image side (px)")
     ap.add_argument("--train-steps", type=int, default=8000, help="learned workload: Adam steps (batch 512)")
     ap.add_argument("--lattice", type=int, default=16, help="learned workload: network on every n-th subset")
-    ap.add_argument("--plain-radius", type=int, default=18,
-                    help="learned workload: ZNCC search radius of the plain path at the coarsest level")
+    ap.add_argument("--plain-radius", type=int, default=17,
+                    help="learned workload: ZNCC search radius of the plain path at the coarsest level, centred on "
+                         "the global translation (covers the strain residual at the frame corners)")
+    ap.add_argument("--learned-steps", type=int, default=20, help="timed frames of the learned-seeding comparison")
+    ap.add_argument("--pair-steps", type=int, default=10, help="timed pairs of the quadratic-pairs measurement")
     ap.add_argument("--pairs", type=int, default=16, help="batch workload: number of image pairs")
     return ap.parse_args()
 
@@ -141,6 +157,10 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
 
+    def line(self) -> dict:
+        s = self.summary()
+        return {"sm_mhz": s["sm_mhz"], "sm_max_mhz": s["sm_max_mhz"], "reasons": s["reasons"]}
+
 
 def make_workload(args, rank: int, device: str):
     from live_dic_gb300 import synthetic
@@ -152,72 +172,88 @@ def make_workload(args, rank: int, device: str):
     return ref, sp, field, mask, seed
 
 
+def ramp_loads(args, count: int) -> list[float]:
+    """Load factors of the last `count` frames of the ramp (frame k of a ramp
+    of n frames has load k / n; the ramp is lengthened to `count` frames if
+    it is shorter)."""
+    total = max(args.frames, count)
+    return [(total - count + k + 1) / total for k in range(count)]
+
+
 def render_frames(args, sp, field, seed: int, count: int, device: str):
     import torch
 
     from live_dic_gb300 import synthetic
 
-    frames = []
-    for k in range(count):
-        load = (k + 1) / args.frames
-        img = synthetic.deformed_image(sp, field.torch_field(load), noise_seed=seed + 100 + k, device=device)
-        frames.append(torch.from_numpy(img))
-    return frames
+    return [torch.from_numpy(synthetic.deformed_image(sp, field.torch_field(load), noise_seed=seed + 100 + k,
+                                                      device=device))
+            for k, load in enumerate(ramp_loads(args, count))]
 
 
-def cpu_sample_frame_time(args, frame: np.ndarray, plane, metadata, inverse, rows: int) -> tuple[float, dict]:
-    """Oracle port on the host cores: full-frame FIR prefilter plus the
-    finest-level IC-GN (zero seed) on `rows` subset rows; returns the
-    extrapolated seconds per frame."""
-    from oracle import oracle as oracle_c
-    from oracle import reference_prep as rp
+def pipeline_oracle(args, levels, rois, temporal, refs):
+    """The CPU pipeline of one headline frame: the C oracle's prefilter,
+    seeded IC-GN, UOD, pyramid reductions, coarse-to-fine transfers, ZNCC
+    search, temporal projection with velocity prediction and history merges
+    (oracle/pyramid_oracle.py), with the pyramid's default per-level
+    schedule (full_pyramid_backend.py:51-62 of the reference)."""
+    from live_dic_gb300.full_pyramid_backend import (_DEFAULT_ITERATION_SCHEDULES, _DEFAULT_TOLERANCES,
+                                                     _FOUR_LEVEL_TOLERANCES)
+    from oracle.pyramid_oracle import PyramidOracle
 
-    S, st = args.subset, args.stride
-    gw = 1 + (args.width - S) // st
-    gh = 1 + (args.height - S) // st
-    rows = max(1, min(rows, gh))
-    start = (gh - rows) // 2
-    subsets = np.arange(start * gw, (start + rows) * gw, dtype=np.int32)
+    tolerances = (_FOUR_LEVEL_TOLERANCES if args.levels == 4 else _DEFAULT_TOLERANCES)[-args.levels:]
+    return PyramidOracle(levels, subset_size=args.subset, subset_stride=args.stride,
+                         iterations=_DEFAULT_ITERATION_SCHEDULES[args.levels], tolerances=tolerances,
+                         lanes=args.lanes, temporal=True, velocity=True, rois=rois, temporal_links=temporal,
+                         search_radius=args.search_radius, reference_levels=refs)
+
+
+def cpu_pipeline_time(oracle, frames: list[np.ndarray], warmup: int, steps: int) -> float:
+    """Seconds per frame of the CPU pipeline over `steps` consecutive frames
+    after `warmup` untimed ones (the first frame runs the ZNCC search)."""
+    for k in range(warmup):
+        oracle.register(frames[k])
     t0 = time.perf_counter()
-    coef = oracle_c.prefilter(frame, rp.runtime_fir_taps())
-    t1 = time.perf_counter()
-    state = np.zeros((gh * gw, 8), np.float32)
-    oracle_c.solve(frame, coef, plane, metadata, inverse, subset_size=S, subset_stride=st, lanes=32,
-                   iterations=16, tolerance=5e-3, subsets=subsets, state=state, roi_enabled=True)
-    t2 = time.perf_counter()
-    per_frame = (t1 - t0) + (t2 - t1) * gh / rows
-    return per_frame, {"prefilter_s": t1 - t0, "solve_s": t2 - t1, "rows": rows, "subsets": int(subsets.size)}
+    for k in range(warmup, warmup + steps):
+        oracle.register(frames[k])
+    return (time.perf_counter() - t0) / steps
+
+
+def cpu_sample_text(args, steps: int, arrays: str) -> str:
+    cores = os.cpu_count()
+    return (f"whole frames through the oracle C port of the per-frame path with {cores} OpenMP threads: "
+            f"{args.levels}-level pyramid (integer reductions, FIR prefilters, seeded IC-GN, UOD replace, "
+            f"coarse-to-fine transfers), ZNCC search on the first frame, temporal projection with velocity "
+            f"prediction and history merges, ROI hole; {steps} consecutive timed frames of the sequence after "
+            f"its first; {arrays}; the reference's own GPU path (WGSL via wgpu) cannot run here: no graphics "
+            "stack or software renderer on this box")
 
 
 def run_reference_arm(args) -> None:
+    """The reference arm: the path's CPU implementation (the oracle port of
+    the reference's per-frame WGSL path, with the float64 restatement of
+    its _reference_arrays for the reference preparation) on the host cores,
+    on the headline workload, frames through the whole pipeline."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import torch
 
     from oracle import oracle as oracle_c
-    from oracle import reference_prep as rp
+    from oracle.pyramid_oracle import float64_levels, roi_tables
 
     oracle_c.build()
     device = "cuda" if torch.cuda.is_available() else "cpu"
     ref, sp, field, mask, seed = make_workload(args, 0, device)
-    frames = [f.numpy() for f in render_frames(args, sp, field, seed, 4, device)]
-    plane, inverse, metadata = rp.reference_arrays(ref, subset_size=args.subset, subset_stride=args.stride)
-    from live_dic_gb300.roi import prepare_roi
-
-    plan = prepare_roi(mask, args.subset, args.stride)
-    meta = metadata.reshape(-1, 16).copy()
-    meta[~plan.selected.ravel(), 1] = -3.0
-    gh = 1 + (args.height - args.subset) // args.stride
-    rows = max(4, gh // 8)
-    for k in range(args.warmup if args.warmup < 2 else 1):
-        cpu_sample_frame_time(args, frames[k % len(frames)], plane, meta, inverse, rows)
-    times = []
-    for k in range(args.steps):
-        t, info = cpu_sample_frame_time(args, frames[k % len(frames)], plane, meta, inverse, rows)
-        times.append(t)
-    total = sum(times)
-    value = args.steps / total
+    count = args.warmup + args.steps
+    frames = [f.numpy() for f in render_frames(args, sp, field, seed, count, device)]
+    plans, rois, temporal = roi_tables(mask, subset_size=args.subset, subset_stride=args.stride, levels=args.levels)
+    t0 = time.perf_counter()
+    levels, refs = float64_levels(ref, subset_size=args.subset, subset_stride=args.stride, levels=args.levels,
+                                  plans=plans)
+    prep_s = time.perf_counter() - t0
+    oracle = pipeline_oracle(args, levels, rois, temporal, refs)
+    per_frame = cpu_pipeline_time(oracle, frames, args.warmup, args.steps)
+    value = 1.0 / per_frame
     cores = os.cpu_count()
     line = {
         "impl": "reference",
@@ -227,33 +263,36 @@ def run_reference_arm(args) -> None:
         "n_gpus": args.gpus,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": 1e3 * total / args.steps,
+        "ms_per_step": 1e3 * per_frame,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
         "config": workload_config(args),
+        "reference_preparation_s": prep_s,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"oracle C port (OpenMP, {cores} threads): full-frame FIR prefilter + finest-level "
-                                   f"affine IC-GN from zero seed on {info['rows']} of {gh} subset rows per step, "
-                                   "extrapolated to the frame; the reference's own GPU path (WGSL via wgpu) cannot run "
-                                   "here: no graphics stack or software renderer on this box"},
+                         "sample": cpu_sample_text(args, args.steps, "float64 reference preparation of every level")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
 def workload_config(args) -> dict:
+    loads = ramp_loads(args, args.warmup + args.steps)
     return {
         "workload": f"{args.width}x{args.height} plate-with-hole (Kirsch, ROI hole r={args.hole:g} px, peak "
-                    f"{args.peak:g} px ramped over {args.frames} frames), affine IC-GN S{args.subset}/s{args.stride}, "
-                    f"bspline, {args.levels}-level GPU pyramid, temporal+velocity seeding, UOD replace",
+                    f"{args.peak:g} px ramped over {max(args.frames, args.warmup + args.steps)} frames; warm-up and "
+                    f"timed frames are its last {args.warmup + args.steps}, loads {loads[0]:.3f}-{loads[-1]:.3f}), "
+                    f"affine IC-GN S{args.subset}/s{args.stride}, bspline, {args.levels}-level GPU pyramid, ZNCC "
+                    f"search (radius {args.search_radius}) on the first frame, temporal+velocity seeding, UOD "
+                    "replace",
         "width": args.width,
         "height": args.height,
         "subset_size": args.subset,
         "subset_stride": args.stride,
         "pyramid_levels": args.levels,
+        "seed_search_radius": args.search_radius,
         "lanes_per_subset": args.lanes,
         "persistent": bool(args.persistent),
         "solver_mode": args.solver_mode,
@@ -387,37 +426,44 @@ def run_batch_workload(args) -> None:
         dist.destroy_process_group()
 
 
-def run_quadratic_workload(args) -> None:
+
+
+def sinusoid_parameters(cx, cy) -> np.ndarray:
+    """u = 2 sin(2 pi x / 400) cos(2 pi y / 600), v = 1.5 cos(2 pi x / 500):
+    the 12 quadratic parameters [u, ux, uy, v, vx, vy, uxx, uxy, uyy, vxx,
+    vxy, vyy] at (cx, cy)."""
+    kx, ky, kv = 2 * math.pi / 400.0, 2 * math.pi / 600.0, 2 * math.pi / 500.0
+    sx, cxx, sy, cyy = np.sin(kx * cx), np.cos(kx * cx), np.sin(ky * cy), np.cos(ky * cy)
+    sv, cv = np.sin(kv * cx), np.cos(kv * cx)
+    zero = np.zeros_like(cx)
+    return np.stack([2 * sx * cyy, 2 * kx * cxx * cyy, -2 * ky * sx * sy, 1.5 * cv, -1.5 * kv * sv, zero,
+                     -2 * kx * kx * sx * cyy, -2 * kx * ky * cxx * sy, -2 * ky * ky * sx * cyy, -1.5 * kv * kv * cv,
+                     zero, zero], -1)
+
+
+def measure_quadratic(args, local: int, world: int, dist, *, steps: int, warmup: int, cpu_reference: bool) -> dict:
     """UHD pairs, quadratic IC-GN S41/s10 with the reference rebuilt for every
     pair (GPU reference preparation: B-spline, gradients, 12x12 Hessians,
-    FP64 Cholesky inverses), sinusoid field u = 2 sin(2 pi x/400)
-    cos(2 pi y/600), v = 1.5 cos(2 pi x/500); value = pairs/s with both
-    images resident (set_reference_device + register_device per pair, host
-    clock around synchronised steps because preparation waits on the device);
-    e2e = set_reference + register on host NumPy images."""
+    FP64 Cholesky inverses), sinusoid field; pairs/s with both images
+    resident (set_reference_device + register_device per pair, host clock
+    around synchronised steps because preparation waits on the device), and
+    end to end through set_reference + register on host images."""
     import ctypes
 
     import torch
 
     from live_dic_gb300 import ICGNWGPU, _native, synthetic
 
-    rank, world, local = dist_env()
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
     device = f"cuda:{local}"
+    rank = dist_env()[0]
     S, st = 41, 10
     distinct = 4
     field = synthetic.sinusoid_field()
     refs, tgts = [], []
     for k in range(distinct):
         ref, sp = synthetic.reference_image(args.width, args.height, seed=5000 + 31 * k + 7 * rank, device=device)
-        tgt = synthetic.deformed_image(sp, field, noise_seed=6000 + 31 * k + 7 * rank, device=device)
         refs.append(ref)
-        tgts.append(tgt)
+        tgts.append(synthetic.deformed_image(sp, field, noise_seed=6000 + 31 * k + 7 * rank, device=device))
     dev_refs = [torch.from_numpy(r).to(device) for r in refs]
     dev_tgts = [torch.from_numpy(t).to(device) for t in tgts]
     engine = ICGNWGPU(subset_size=S, subset_stride=st, motion_model="quadratic", solver_workgroup_size=args.lanes,
@@ -431,7 +477,7 @@ def run_quadratic_workload(args) -> None:
         engine.register_device(dev_tgts[k % distinct].data_ptr(), state.data_ptr())
         return prep
 
-    for k in range(args.warmup):
+    for k in range(warmup):
         step(k)
     torch.cuda.synchronize()
     if dist:
@@ -440,104 +486,97 @@ def run_quadratic_workload(args) -> None:
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        prep_ms = [step(k) for k in range(args.steps)]
+        prep_ms = [step(k) for k in range(steps)]
         torch.cuda.synchronize()
         t1 = time.perf_counter()
     profile = engine.read_profile()
     engine.set_profiling(False)
-    local_ms = (t1 - t0) * 1e3
-    ms_max = slowest_ms(local_ms, world, dist, device)
-    value = world * args.steps / (ms_max / 1e3)
+    ms_max = slowest_ms((t1 - t0) * 1e3, world, dist, device)
+    value = world * steps / (ms_max / 1e3)
     final = state.view(gh, gw, 16).cpu().numpy()
     cx, cy = synthetic.subset_centres(args.width, args.height, S, st)
-    gx, gy = np.meshgrid(cx, cy) if np.ndim(cx) == 1 else (cx, cy)
-    u, v = field(np.asarray(gx, np.float64), np.asarray(gy, np.float64))
-    truth = np.stack([u, v], -1)
+    truth = sinusoid_parameters(np.asarray(cx, np.float64), np.asarray(cy, np.float64))
     ok = final[..., 12] >= 1.0
-    err = final[..., [0, 3]][ok] - truth[ok]
-    rmse = float(np.sqrt(np.mean(np.sum(err * err, axis=1)))) if ok.any() else None
-    # end to end through the public API on host images
+    error = final[..., :12].astype(np.float64) - truth
+    rmse = float(np.sqrt(np.mean(np.sum(error[..., (0, 3)][ok] ** 2, axis=1)))) if ok.any() else None
+    curvature_rmse = float(np.sqrt(np.mean(error[..., 6:][ok] ** 2))) if ok.any() else None
     for k in range(2):
         engine.set_reference(refs[k % distinct])
         engine.register(tgts[k % distinct])
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = max(3, steps // 2)
     t0 = time.perf_counter()
     for k in range(e2e_steps):
         engine.set_reference(refs[k % distinct])
         engine.register(tgts[k % distinct])
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if rank != 0:
-        engine.close()
-        if dist:
-            dist.destroy_process_group()
-        return
+    engine.close()
     lib = _native.load()
     peak = ctypes.c_double()
     _native.check(lib.gbdic_fp32_peak_probe(local, ctypes.byref(peak)), b"FP32 probe failed")
     iters = float(profile["iterations"])
     flops = 120.0 * S * S * iters + 900.0 * iters
     achieved = flops / (profile["solver_ms"] / 1e3) / 1e12 if profile["solver_ms"] > 0 else None
-    summary = clocks.summary()
-    line = {
+    out = {
         "metric": "UHD quadratic pairs/s with the reference rebuilt every pair",
         "value": value,
         "unit": "pairs/s",
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": ms_max / args.steps,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32",
-        "data": "synthetic",
-        "config": {
-            "workload": f"{args.width}x{args.height} speckle pairs ({distinct} distinct, cycled), quadratic IC-GN "
-                        f"S{S}/s{st}, bspline, sinusoid field (2 px / 1.5 px), reference rebuilt every pair",
-            "subsets_per_pair": gw * gh,
-            "lanes_per_subset": args.lanes,
-            "l2": "no flush: the reference plane (133 MB), metadata + inverses (55 MB) and coefficient plane exceed "
-                  "the 129 MB L2",
-        },
+        "steps": steps,
+        "warmup": warmup,
+        "ms_per_step": ms_max / steps,
+        "workload": f"{args.width}x{args.height} speckle pairs ({distinct} distinct, cycled), quadratic IC-GN "
+                    f"S{S}/s{st}, bspline, sinusoid field (2 px / 1.5 px), GPU reference preparation every pair",
+        "subsets_per_pair": gw * gh,
         "reference_prep_ms_median": float(statistics.median(prep_ms)),
         "displacement_rmse_px": rmse,
+        "curvature_rmse": curvature_rmse,
         "accepted_fraction": float(ok.mean()),
-        "clocks": {"sm_mhz": summary["sm_mhz"], "sm_max_mhz": summary["sm_max_mhz"], "reasons": summary["reasons"]},
+        "accuracy_pair": "the last timed pair, against the FP64 sinusoid field",
+        "clocks": clocks.line(),
         "gpu_launches": profile["launches"],
         "roofline": {"bound": "fp32", "kernel": f"icgn_kernel<quadratic,bspline,{args.lanes} lanes>",
                      "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                      "frac": None if achieved is None else achieved / peak.value,
-                     "solver_ms_per_pair": profile["solver_ms"] / max(1, args.steps), "traffic": None},
-        "e2e": {"value": 1.0 / e2e_s, "unit": "pairs/s",
-                "h2d_bytes_per_step": 2 * args.width * args.height,
-                "d2h_bytes_per_step": gw * gh * 16 * 4,
-                "api": "ICGNWGPU.set_reference + register (host NumPy images)"},
-        "cpu_baseline": None,
+                     "solver_ms_per_pair": profile["solver_ms"] / max(1, steps)},
+        "e2e": {"value": 1.0 / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": 2 * args.width * args.height,
+                "d2h_bytes_per_step": gw * gh * 16 * 4, "api": "ICGNWGPU.set_reference + register (host NumPy images)"},
     }
-    print(json.dumps(line), flush=True)
-    engine.close()
-    if dist:
-        dist.destroy_process_group()
+    if cpu_reference:
+        # The reference prepares a quadratic reference on the CPU in float64
+        # (wgpu_backend.py:589-823); its restatement, timed on one UHD image.
+        from oracle import reference_prep as rp
+
+        t0 = time.perf_counter()
+        rp.reference_arrays(refs[0], motion_model="quadratic", subset_size=S, subset_stride=st)
+        out["cpu_reference_preparation"] = {
+            "seconds_per_pair": time.perf_counter() - t0, "kind": "port", "cores": 1,
+            "sample": "float64 NumPy restatement of _reference_arrays (12x12 Hessians, np.linalg.inv) on one "
+                      f"{args.width}x{args.height} reference, S{S}/s{st}: the reference's own CPU preparation path"}
+    return out
 
 
-def run_learned_workload(args) -> None:
-    """UHD frames under rigid translations of 15-30 px plus +-2 % strain,
-    subset 31 / step 8.  Plain method: 3-level GPU pyramid with the integer
-    ZNCC seed search at the coarsest level, IC-GN at every level.  Learned
-    method: the seed network (trained here on engine-generated pairs) on a
-    lattice of subsets after a GPU phase correlation, IC-GN at the lattice
-    nodes, every subset seeded from the node warps and solved at full
-    resolution with the plain path's finest-level settings, failed or
-    low-ZNCC subsets reseeded by the ZNCC search and solved again."""
+def measure_learned(args, local: int, *, steps: int, warmup: int) -> dict:
+    """UHD frames under rigid translations of 15-30 px plus strain and shear
+    within +-2 % about the centre, subset 31 / step 8.  Plain method (the
+    reference's large-motion path, with the integer search this project
+    adds): the global translation by the same GPU phase correlation the
+    learned method uses (a 256-pixel window at the centre of the
+    half-resolution frame; the reference's own 1024-pixel window fails its
+    acceptance rule under this strain) seeds the coarsest level of a 3-level
+    pyramid (Fourier initialization), an integer ZNCC search centred on it
+    absorbs the strain residual, IC-GN at every level.  Learned method: the
+    seed network (trained here on engine-generated pairs) on a lattice of
+    subsets after the same phase correlation, IC-GN at the lattice nodes,
+    every subset seeded from the node warps and solved at full resolution
+    with the plain path's finest-level settings, failed or low-ZNCC subsets
+    reseeded by the ZNCC search and solved again."""
     import torch
 
     from live_dic_gb300 import ICGNWGPU, ICGNWGPUFullPyramid, learned, synthetic
 
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
     device = f"cuda:{local}"
+    rank = dist_env()[0]
     t0 = time.perf_counter()
-    data = learned.training_pairs(args.train_images, size=320, seed=11 + rank, device=local)
+    data = learned.training_pairs(args.train_images, size=args.train_size, seed=11 + rank, device=local)
     gen_s = time.perf_counter() - t0
     net = learned.SeedNet(batch=512, device=local, seed=rank)
     t0 = time.perf_counter()
@@ -548,7 +587,7 @@ def run_learned_workload(args) -> None:
     rng = np.random.default_rng(77 + rank)
     ref, sp = synthetic.reference_image(W, H, seed=4242 + rank, device=device)
     c = (0.5 * (W - 1), 0.5 * (H - 1))
-    count = args.warmup + args.steps
+    count = warmup + steps
     warps, frames = [], []
     for k in range(count):
         ang, r = rng.uniform(0, 2 * math.pi), rng.uniform(15.0, 30.0)
@@ -570,18 +609,19 @@ def run_learned_workload(args) -> None:
         s = state.view(gh, gw, 8).cpu().numpy()
         ok = s[..., 6] >= 1
         tr = truth_of(k)
-        inside = (cx + tr[..., 0] >= 4) & (cx + S + tr[..., 0] <= W - 4) & (cy + tr[..., 1] >= 4) & (cy + S + tr[..., 1] <= H - 4)
+        inside = ((cx - S // 2 + tr[..., 0] >= 4) & (cx + S // 2 + tr[..., 0] <= W - 5) &
+                  (cy - S // 2 + tr[..., 1] >= 4) & (cy + S // 2 + tr[..., 1] <= H - 5))
         err = np.linalg.norm(s[..., [0, 3]][ok & inside] - tr[ok & inside], axis=-1)
         good = err <= 0.5
         return (float((ok & inside).sum() / inside.sum()), float(np.sqrt(np.mean(err[good] ** 2))),
                 float(1.0 - good.mean()) if err.size else 0.0)
 
     def run(step_fn, gh, gw, after=None):
-        for k in range(args.warmup):
+        for k in range(warmup):
             step_fn(k)
         torch.cuda.synchronize()
         times, acc = [], []
-        for k in range(args.warmup, count):
+        for k in range(warmup, count):
             t1 = time.perf_counter()
             state = step_fn(k)
             torch.cuda.synchronize()
@@ -592,26 +632,27 @@ def run_learned_workload(args) -> None:
         return times, acc
 
     with ClockSampler(local) as clocks:
-        # plain: pyramid + ZNCC search
-        plain = ICGNWGPUFullPyramid(pyramid_levels=3, subset_size=S, subset_stride=st, initialization="zncc",
+        plain = ICGNWGPUFullPyramid(pyramid_levels=3, subset_size=S, subset_stride=st, initialization="fourier",
                                     seed_search_radius=args.plain_radius, device=local)
         info = plain.set_reference(ref)
         gw, gh = info.grid
         pstate = torch.zeros(gw * gh * 8, device=device)
         pstream = torch.cuda.Stream(device=device)
+        shifter = learned.HalfResolutionShift(W, H, device=local)
+        shifter.set_reference_frame(torch.from_numpy(ref).to(device))
 
         def plain_step(k):
+            shift = shifter.shift_of(frames[k], pstream)
             with torch.cuda.stream(pstream):
-                plain.register_device(frames[k].data_ptr(), pstate.data_ptr(), stream=pstream.cuda_stream)
+                plain.register_device(frames[k].data_ptr(), pstate.data_ptr(), stream=pstream.cuda_stream,
+                                      translation=shift)
             pstream.synchronize()
             return pstate
 
         plain_times, plain_acc = run(plain_step, gh, gw)
-        plain_schedule = (plain.iterations_per_level[-1], plain.tolerance_per_level[-1])
+        fine_iterations, fine_tolerance = plain.iterations_per_level[-1], plain.tolerance_per_level[-1]
         plain.close()
-        # learned
-        # the same IC-GN settings as the plain path's full-resolution level
-        fine_iterations, fine_tolerance = plain_schedule
+        shifter.close()
         engine = ICGNWGPU(subset_size=S, subset_stride=st, device=local, solver_workgroup_size=args.lanes)
         engine.set_reference(ref, iterations=fine_iterations, tolerance=fine_tolerance)
         seeder = learned.LearnedSeeder(engine, net, step=args.lattice)
@@ -627,33 +668,21 @@ def run_learned_workload(args) -> None:
 
         learned_times, learned_acc = run(learned_step, engine.grid_height, engine.grid_width, learned_count)
         engine.close()
-    if rank != 0:
-        return
     lt, pt = float(np.mean(learned_times)), float(np.mean(plain_times))
-    summary = clocks.summary()
-    line = {
+    return {
         "metric": "learned- vs ZNCC-seeded IC-GN frames/s at equal RMSE (UHD, 15-30 px translation + 2 % strain)",
         "value": 1.0 / lt,
         "unit": "frames/s",
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
+        "steps": steps,
+        "warmup": warmup,
         "ms_per_step": 1e3 * lt,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32 solver, bf16 network (fp32 accumulate)",
-        "data": "synthetic",
-        "config": {"workload": f"{W}x{H}, S{S}/s{st}, rigid translation 15-30 px + uniform strain within 2 % about "
-                               f"the frame centre, network on every {args.lattice}-th subset (Fourier global "
-                               f"shift, 2 passes with an affine consensus), IC-GN at the lattice nodes, interpolated "
-                               f"seeds for every subset, IC-GN ({plain_schedule[0]} iterations, tolerance "
-                               f"{plain_schedule[1]:g} as the plain path's finest level), ZNCC reseeding of failures; "
-                               f"plain = 3-level pyramid + ZNCC search radius {args.plain_radius} at the coarsest "
-                               "level",
-                   "train_pairs": data.size, "train_images": args.train_images, "train_steps": args.train_steps,
-                   "train_batch": 512, "pair_generation_s": gen_s, "training_s": train_s,
-                   "loss_first_last": [losses[0], losses[-1]]},
+        "workload": f"{W}x{H}, S{S}/s{st}, rigid translation 15-30 px + strain and shear within 2 % about the "
+                    f"frame centre; learned: network on every {args.lattice}-th subset (GPU phase-correlation "
+                    "global shift, 2 passes with an affine consensus), IC-GN at the lattice nodes, interpolated "
+                    f"seeds for every subset, IC-GN ({fine_iterations} iterations, tolerance {fine_tolerance:g}, "
+                    "as the plain path's finest level), ZNCC reseeding of failures; plain: the same GPU phase "
+                    "correlation as global translation (Fourier initialization), 3-level pyramid, ZNCC search "
+                    f"radius {args.plain_radius} centred on it at the coarsest level",
         "plain_frames_per_s": 1.0 / pt,
         "speedup_vs_plain": pt / lt,
         "learned_accepted": float(np.mean([a for a, _, _ in learned_acc])),
@@ -662,12 +691,57 @@ def run_learned_workload(args) -> None:
         "plain_rmse_px": float(np.mean([r for _, r, _ in plain_acc])),
         "learned_outliers": float(np.mean([o for _, _, o in learned_acc])),
         "plain_outliers": float(np.mean([o for _, _, o in plain_acc])),
-        "accuracy_note": "accepted = status >= 1 among windows whose displaced footprint stays in the frame; "
-                         "rmse over accepted windows within 0.5 px of the FP64 field, outliers = the rest",
+        "accuracy_note": "per timed frame against the FP64 field: accepted = status >= 1 among windows whose "
+                         "displaced footprint stays in the frame; rmse over accepted windows within 0.5 px of the "
+                         "field, outliers = the accepted rest",
         "reseeded_per_frame": float(np.mean(reseeded)) if reseeded else None,
-        "clocks": {"sm_mhz": summary["sm_mhz"], "sm_max_mhz": summary["sm_max_mhz"], "reasons": summary["reasons"]},
+        "timing": "host clock around each synchronised frame (both methods include their host-side steps)",
+        "train_pairs": int(data.size), "train_images": args.train_images, "train_image_size": args.train_size,
+        "train_steps": args.train_steps, "train_batch": 512, "pair_generation_s": gen_s, "training_s": train_s,
+        "loss_first_last": [losses[0], losses[-1]],
+        "clocks": clocks.line(),
     }
-    print(json.dumps(line), flush=True)
+
+
+def run_quadratic_workload(args) -> None:
+    import torch
+
+    rank, world, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    out = measure_quadratic(args, local, world, dist, steps=args.steps, warmup=args.warmup,
+                            cpu_reference=rank == 0 and world == 1 and not args.no_cpu_baseline)
+    if rank == 0:
+        line = {"metric": out.pop("metric"), "value": out.pop("value"), "unit": out.pop("unit"), "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": out.pop("ms_per_step"),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": out.pop("workload"), "subsets_per_pair": out.pop("subsets_per_pair"),
+                           "lanes_per_subset": args.lanes,
+                           "l2": "no flush: the reference plane (133 MB), metadata + inverses (55 MB) and "
+                                 "coefficient plane exceed the 129 MB L2"},
+                **out}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_learned_workload(args) -> None:
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    out = measure_learned(args, local, steps=args.steps, warmup=args.warmup)
+    if rank == 0:
+        line = {"metric": out.pop("metric"), "value": out.pop("value"), "unit": out.pop("unit"), "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": out.pop("ms_per_step"),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 solver, bf16 network (fp32 accumulate)", "data": "synthetic",
+                "config": {"workload": out.pop("workload")}, **out}
+        print(json.dumps(line), flush=True)
 
 
 def main() -> None:
@@ -697,16 +771,16 @@ def main() -> None:
 
     from live_dic_gb300 import ICGNWGPUFullPyramid, _native
 
-    if args.warmup + args.steps > args.frames:
-        args.frames = args.warmup + args.steps
+    count = args.warmup + args.steps
     ref, sp, field, mask, seed = make_workload(args, rank, device)
-    frames = render_frames(args, sp, field, seed, args.frames, device)
+    frames = render_frames(args, sp, field, seed, count, device)
+    loads = ramp_loads(args, count)
     dev_frames = torch.stack(frames).to(device).contiguous()
     engine = ICGNWGPUFullPyramid(
         pyramid_levels=args.levels, subset_size=args.subset, subset_stride=args.stride,
-        initialization="temporal", temporal_prediction="velocity", solver_workgroup_size=args.lanes,
-        device=local, pipeline_slots=2, persistent=args.persistent, autotune=args.autotune,
-        solver_mode=args.solver_mode,
+        initialization="temporal", temporal_prediction="velocity", seed_search_radius=args.search_radius,
+        solver_workgroup_size=args.lanes, device=local, pipeline_slots=2, persistent=args.persistent,
+        autotune=args.autotune, solver_mode=args.solver_mode,
     )
     info = engine.set_reference(ref, roi_mask=mask)
     args.lanes, args.persistent, args.solver_mode = engine.solver_workgroup_size, engine._persistent, engine.solver_mode
@@ -727,7 +801,7 @@ def main() -> None:
         torch.cuda.synchronize()
         with torch.cuda.stream(stream):
             start.record(stream)
-            for k in range(args.warmup, args.warmup + args.steps):
+            for k in range(args.warmup, count):
                 engine.register_device(dev_frames[k].data_ptr(), state.data_ptr(), stream=stream.cuda_stream)
             end.record(stream)
         torch.cuda.synchronize()
@@ -740,16 +814,16 @@ def main() -> None:
     ms_max = slowest_ms(ms, world, dist, device)
     value = job_throughput(steps=args.steps, local_ms=ms, world=world, dist=dist, device=device)
 
-    # ---------------- accuracy of the last timed frame against the FP64 field
+    # ---------------- accuracy of the last timed frame (the ramp's peak) against the FP64 field
     from live_dic_gb300 import synthetic
 
     cx, cy = synthetic.subset_centres(args.width, args.height, args.subset, args.stride)
-    last = args.warmup + args.steps - 1
-    truth = field.truth(cx, cy, load=(last + 1) / args.frames)
+    truth = field.truth(cx, cy, load=loads[-1])
     ok = final_state[..., 6] >= 1.0
     err = final_state[..., [0, 3]][ok] - truth[ok]
     rmse = float(np.sqrt(np.mean(np.sum(err * err, axis=1)))) if ok.any() else None
     selected = int(info.roi.selected.sum()) if info.roi is not None else gw * gh
+    peak_px = float(np.hypot(truth[..., 0], truth[..., 1])[info.roi.selected].max()) if info.roi is not None else None
 
     # ---------------- end to end through the public API (host frames)
     e2e = None
@@ -762,7 +836,7 @@ def main() -> None:
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
-        results = list(engine.register_stream(host_frames[args.warmup: args.warmup + args.steps], pipeline_depth=2))
+        results = list(engine.register_stream(host_frames[args.warmup: count], pipeline_depth=2))
         t1 = time.perf_counter()
         e2e_s = slowest_ms((t1 - t0) * 1e3, world, dist, device) / 1e3
         age = [r.timing["resultAgeWallMs"] for r in results]
@@ -807,6 +881,8 @@ def main() -> None:
         "peak_source": "measured in this run by gbdic_fp32_peak_probe (FMA chains on every SM); "
                        "MEASURED_PEAKS.json has no FP32 figure",
         "traffic": traffic,
+        "traffic_source": "profiles/traffic_per_launch.json (one ncu capture of the finest level, scaled by units "
+                          "processed to the average launch)",
         "flops_per_launch": flops / launches,
         "avg_launch_ms": profile["solver_ms"] / launches,
         "solver_share_of_step": profile["solver_ms"] / ms if ms > 0 else None,
@@ -816,27 +892,41 @@ def main() -> None:
     cpu_baseline = None
     if world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as oracle_c
+        from oracle.pyramid_oracle import LevelArrays, roi_tables
 
         oracle_c.build()
-        plane = engine.export_level(0, _native.EXPORT_PLANE, np.float32, (args.height * args.width * 4,))
-        meta = engine.export_level(0, _native.EXPORT_METADATA, np.float32, (gw * gh * 16,))
-        inv = engine.export_level(0, _native.EXPORT_INVERSE, np.float32, (gw * gh * 36,))
-        frame = frames[last].numpy()
-        rows = max(4, gh // 4)
-        per_frame, sample = cpu_sample_frame_time(args, frame, plane, meta, inv, rows)
-        cores = os.cpu_count()
+        plans, rois, temporal = roi_tables(mask, subset_size=args.subset, subset_stride=args.stride,
+                                           levels=args.levels)
+        levels, refs = [], [ref]
+        for level in range(args.levels):
+            lw, lh = engine.level_grid(level)
+            w, h = args.width >> level, args.height >> level
+            levels.append(LevelArrays(
+                w, h, lw, lh,
+                engine.export_level(level, _native.EXPORT_PLANE, np.float32, (h * w * 4,)),
+                engine.export_level(level, _native.EXPORT_METADATA, np.float32, (lw * lh * 16,)),
+                engine.export_level(level, _native.EXPORT_INVERSE, np.float32, (lw * lh * 36,))))
+            if level:
+                refs.append(oracle_c.reduce(refs[-1]))
+        oracle = pipeline_oracle(args, levels, rois, temporal, refs)
+        cpu_steps = max(1, min(args.cpu_frames, count - 1))
+        per_frame = cpu_pipeline_time(oracle, [f.numpy() for f in frames], 1, cpu_steps)
         cpu_baseline = {
             "value": 1.0 / per_frame,
             "unit": UNIT,
-            "cores": cores,
+            "cores": os.cpu_count(),
             "kind": "port",
-            "sample": f"oracle C port with {cores} OpenMP threads: full-frame FIR prefilter ({sample['prefilter_s']:.2f} s) "
-                      f"+ finest-level affine IC-GN on {sample['rows']} of {gh} subset rows ({sample['subsets']} subsets, "
-                      f"{sample['solve_s']:.2f} s), extrapolated to one frame; GPU-prepared reference arrays",
+            "sample": cpu_sample_text(args, cpu_steps, "the reference arrays this run prepared on the GPU"),
         }
+    engine.close()
 
-    summary = clocks.summary()
-    kernels_per_frame = (args.levels - 1) + 2 + 3 + 4 * (args.levels - 1) + 2
+    extras = {}
+    if world == 1 and not args.no_extras:
+        extras["quadratic_pairs"] = measure_quadratic(args, local, world, dist, steps=args.pair_steps, warmup=3,
+                                                      cpu_reference=not args.no_cpu_baseline)
+        extras["learned_seeding"] = measure_learned(args, local, steps=args.learned_steps, warmup=3)
+
+    kernels_per_frame = 5 * args.levels + 3
     line = {
         "metric": METRIC,
         "value": value,
@@ -856,15 +946,17 @@ def main() -> None:
         "subsets_per_s": value * selected,
         "subsets_per_frame": selected,
         "displacement_rmse_px": rmse,
+        "accuracy_frame": {"load": loads[-1], "peak_displacement_px": peak_px,
+                           "note": "the last timed frame, at the ramp's 2 px peak"},
         "accepted_fraction": float(ok.sum() / max(1, selected)),
-        "clocks": {"sm_mhz": summary["sm_mhz"], "sm_max_mhz": summary["sm_max_mhz"], "reasons": summary["reasons"]},
+        "clocks": clocks.line(),
         "gpu_launches": kernels_per_frame * args.steps,
         "roofline": roofline,
         "cpu_baseline": cpu_baseline,
         "e2e": e2e,
+        **extras,
     }
     print(json.dumps(line), flush=True)
-    engine.close()
     if dist:
         dist.destroy_process_group()
 
