@@ -150,6 +150,18 @@ int gbdic_register_seeded(gbdic_engine *engine, const uint8_t *frame, int64_t ro
                           const float *seed_state, const uint32_t *active,
                           const gbdic_solver_cfg *cfg, float *out_state, gbdic_timing *timing);
 
+/* Selective pyramid recovery on the device (wgpu_backend.py:2038-2197, whose
+ * per-level targets are _reduce_half of the frame, 318-334): the target held
+ * in `finer`'s slot, reduced by one pyramid level (the exact integer 5x5
+ * reduction, full_pyramid.wgsl:218-249) into this engine's slot 0, whose
+ * reference must be width // 2 x height // 2 of the finer one's; ordered
+ * after the finer engine's queued work. */
+int gbdic_reduce_frame(gbdic_engine *engine, const gbdic_engine *finer, int32_t finer_slot);
+/* register_seeded() of the target already in slot 0 (gbdic_reduce_frame or
+ * an earlier upload): prefilter, seeded IC-GN, UOD, readback. */
+int gbdic_register_seeded_resident(gbdic_engine *engine, const float *seed_state, const uint32_t *active,
+                                   const gbdic_solver_cfg *cfg, float *out_state, gbdic_timing *timing);
+
 /* ICGNWGPU._retry_seeded (wgpu_backend.py:1893-1949): re-solve active
  * subsets on the target resident in `slot` (0 after gbdic_register; a
  * retired stream slot before its next submit), keeping inactive subsets'

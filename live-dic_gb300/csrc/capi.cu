@@ -282,6 +282,51 @@ int gbdic_register_seeded(gbdic_engine *e, const uint8_t *frame, int64_t row_str
     });
 }
 
+int gbdic_reduce_frame(gbdic_engine *e, const gbdic_engine *finer, int32_t finer_slot) {
+    return guarded(e, [&] {
+        e->require_ready("reduce_frame");
+        if (!finer || !finer->ready) fail(GBDIC_ESTATE, "the finer engine has no prepared reference");
+        finer->check_slot(finer_slot);
+        if (finer->device != e->device) fail(GBDIC_EINVAL, "both engines must use the same device");
+        if (e->level.W != finer->level.W / 2 || e->level.H != finer->level.H / 2)
+            fail(GBDIC_EINVAL, "this engine's frame must be half the finer engine's (width // 2, height // 2)");
+        cudaStream_t s = e->rt->stream();
+        // The finer engine's work on its frame precedes the reduction.
+        cudaEvent_t done = nullptr;
+        check_cuda(cudaEventCreateWithFlags(&done, cudaEventDisableTiming), "event");
+        cudaError_t err = cudaEventRecord(done, finer->rt->stream());
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(s, done, 0);
+        cudaEventDestroy(done);
+        check_cuda(err, "stream order");
+        check_cuda(gbdic::launch_reduce_half(finer->level.slots[finer_slot]->frame.as<uint8_t>(), finer->level.W,
+                                             finer->level.H, e->level.slots[0]->frame.as<uint8_t>(), s),
+                   "reduction launch");
+    });
+}
+
+int gbdic_register_seeded_resident(gbdic_engine *e, const float *seed_state, const uint32_t *active,
+                                   const gbdic_solver_cfg *cfg, float *out_state, gbdic_timing *timing) {
+    return guarded(e, [&] {
+        e->require_ready("register_seeded");
+        gbdic::validate_cfg(cfg);
+        if (!seed_state || !active) fail(GBDIC_EINVAL, "seed_state and active are required");
+        if (e->host[0].pending) fail(GBDIC_ESTATE, "slot is still in flight; retire it first");
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        auto &h = e->host[0];
+        const auto s = e->rt->stream();
+        h.submitted = std::chrono::steady_clock::now();
+        const size_t sb = (size_t)lvl.count * gbdic::state_stride(e->rt->opts().o.motion_model) * sizeof(float);
+        check_cuda(cudaMemcpyAsync(slot.seed.get(), seed_state, sb, cudaMemcpyHostToDevice, s), "seed upload");
+        check_cuda(cudaMemcpyAsync(slot.active.get(), active, (size_t)lvl.count * sizeof(uint32_t), cudaMemcpyHostToDevice, s),
+                   "activity upload");
+        h.upload_ms = gbdic::ms_since(h.submitted);
+        const auto t_exec = std::chrono::steady_clock::now();
+        enqueue_frame(e, 0, *cfg, true, false, true);
+        readback(e, 0, out_state, timing, t_exec);
+    });
+}
+
 int gbdic_retry_seeded(gbdic_engine *e, int32_t slot_index, const float *seed_state, const uint32_t *active,
                        const gbdic_solver_cfg *cfg, float *out_state, gbdic_timing *timing) {
     return guarded(e, [&] {

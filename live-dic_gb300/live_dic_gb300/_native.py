@@ -191,6 +191,8 @@ _SIGNATURES = {
     "gbdic_set_solver_variant": (C.c_int, [P, I32, I32]),
     "gbdic_pyramid_set_solver_variant": (C.c_int, [P, I32, I32]),
     "gbdic_set_solver_mode": (C.c_int, [P, I32]),
+    "gbdic_reduce_frame": (C.c_int, [P, P, I32]),
+    "gbdic_register_seeded_resident": (C.c_int, [P, P, P, C.POINTER(SolverCfg), P, C.POINTER(Timing)]),
     "gbdic_pyramid_set_solver_mode": (C.c_int, [P, I32]),
     "gbdic_batch_create": (C.c_int, [I32, C.POINTER(P)]),
     "gbdic_batch_destroy": (C.c_int, [P]),

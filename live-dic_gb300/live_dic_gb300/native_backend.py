@@ -706,6 +706,20 @@ class ICGNWGPU:
         self._target_ready = True
         return packed
 
+    def _register_seeded_resident(self, seeds: np.ndarray, active: np.ndarray) -> np.ndarray:
+        """_register_seeded_states on the target already resident in slot 0
+        (put there by gbdic_reduce_frame)."""
+        packed = self._new_packed()
+        timing = _native.Timing()
+        act = np.ascontiguousarray(active, dtype=np.uint32)
+        if self.roi is not None:
+            act = act * self.roi.selected.astype(np.uint32)
+        self._check(self._lib.gbdic_register_seeded_resident(
+            self._handle, _native.ptr(np.ascontiguousarray(seeds)), _native.ptr(np.ascontiguousarray(act)),
+            C.byref(self._cfg(self._config)), _native.ptr(packed), C.byref(timing)))
+        self._target_ready = True
+        return packed
+
     def _recover_pyramid(self, slot: int, frame: np.ndarray, fine_packed: np.ndarray,
                          fine_result: RegistrationResult) -> RegistrationResult:
         """Re-solve failed fine subsets from coarse-to-fine seeds
@@ -720,11 +734,13 @@ class ICGNWGPU:
         if failed_count == 0:
             return fine_result
         started = time.perf_counter()
-        reduced_targets = []
-        reduced = frame
-        for _ in self._pyramid_engines:
-            reduced = reduce_half(reduced)
-            reduced_targets.append(reduced)
+        # The coarser targets are reduced on the device from the frame this
+        # engine holds in `slot`, level by level (bit-identical to
+        # _reduce_half, wgpu_backend.py:318-334).
+        finer, finer_slot = self, int(slot)
+        for engine in self._pyramid_engines:
+            engine._check(engine._lib.gbdic_reduce_frame(engine._handle, finer._handle, finer_slot))
+            finer, finer_slot = engine, 0
         requested_by_level = []
         requested = failed
         destination_scale = 1
@@ -755,7 +771,7 @@ class ICGNWGPU:
                     destination_grid=(engine.grid_width, engine.grid_height), requested=level_requested,
                     subset_size=self.subset_size, subset_stride=self.subset_stride,
                     permissions=engine._roi_seed_permissions)
-            level_packed = engine._register_seeded_states(reduced_targets[level_index], seeds, active)
+            level_packed = engine._register_seeded_resident(seeds, active)
             source = (level_packed[..., :n], level_packed[..., n], level_requested, level_scale)
         seeds, active = transfer_pyramid_seed(
             source[0], source[1], motion_model=self.motion_model, source_available=source[2],

@@ -178,6 +178,16 @@ def test_selective_pyramid_recovery_of_failed_subsets():
     with ICGNWGPU(subset_size=31, subset_stride=8, pyramid_levels=3) as engine:
         info = engine.set_reference(ref, roi_mask=mask)
         result = engine.register(tgt)
+        # the coarser targets were reduced on the device, bit for bit as
+        # the reference's _reduce_half (restated in pyramid_recovery)
+        from live_dic_gb300 import _native
+        from live_dic_gb300.pyramid_recovery import reduce_half
+
+        expected = tgt
+        for child in engine._pyramid_engines:
+            expected = reduce_half(expected)
+            got = child._export(_native.EXPORT_FRAME, np.uint8, expected.shape)
+            np.testing.assert_array_equal(got, expected)
         streamed = list(engine.register_stream([tgt, tgt], pipeline_depth=2))
     inside = info.roi.selected
     assert (result.status[~inside] == -3).all()
