@@ -511,6 +511,7 @@ typedef struct {
 } gbdic_nn_gemm_desc;
 int gbdic_nn_gemm(const gbdic_nn_gemm_desc *desc, int32_t *device_error, void *stream);
 
+
 /* 64x64 reference/target patch pairs around `centres` ((x, y) per patch,
  * image pixels) of uint8 images W x H: refs / tgts are device arrays of
  * device image pointers, image_index (or NULL) selects the image of each
@@ -526,6 +527,17 @@ int gbdic_nn_patches(const uint8_t *const *refs, const uint8_t *const *tgts, con
 typedef struct {
     int32_t B, H, W, C, OH, OW, Cout, Kp;
 } gbdic_nn_conv_shape;
+
+/* The same GEMM with operand A gathered in the kernel from an NHWC BF16
+ * tensor (implicit GEMM; desc->a is that tensor, not a matrix):
+ * mode 1, A[m][k] = the im2col row of the input, as gbdic_nn_im2col writes
+ * it (M = B*OH*OW, K = Kp, C % 8 == 0); mode 2, A[m][k] = the data-gradient
+ * gather of the output gradient, as gbdic_nn_dgrad_gather writes it
+ * (M = B*H*W, K = 9*Cout, Cout % 8 == 0).  k_split must be 1.  Results are
+ * those of gbdic_nn_gemm on the materialised matrix, which is never
+ * written. */
+int gbdic_nn_conv_gemm(const gbdic_nn_gemm_desc *desc, int32_t mode, const gbdic_nn_conv_shape *shape,
+                       int32_t *device_error, void *stream);
 /* Forward GEMM operand A[(b, oy, ox)][(ky, kx, ci)] (zero beyond 9 C). */
 int gbdic_nn_im2col(const gbdic_nn_conv_shape *shape, const void *x, void *a, void *stream);
 /* Inference form of the 2-channel input layer (Cout 32): the 3x3 stride-2

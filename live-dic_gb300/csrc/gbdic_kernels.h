@@ -167,6 +167,16 @@ struct ChooseArgs {
 cudaError_t launch_spatial_choose(const ChooseArgs &a, cudaStream_t stream);
 
 // ------------------------------------------------------------ learned seeds
+struct NnConvShape {
+    int B, H, W, C;       // input NHWC
+    int OH, OW, Cout;     // 3x3 stride-2 pad-1 output
+    int Kp;               // padded reduction length of the forward GEMM (>= 9 C)
+};
+
+// Operand A of a convolution GEMM gathered from an NHWC tensor in the
+// kernel (implicit GEMM) instead of read from a materialised matrix.
+enum { kGatherNone = 0, kGatherIm2col = 1, kGatherDgrad = 2 };
+
 // D (+)= A B^T on the tensor cores: A M x K, B N x K, BF16 row-major (K
 // contiguous); M % 128 == 0, N % 16 == 0, K % (64 k_split) == 0.
 struct TcGemmArgs {
@@ -179,6 +189,11 @@ struct TcGemmArgs {
     const float *bias;        // per column, or nullptr
     int relu, accumulate;     // accumulate: D_f32 += result
     int *error;               // set to 1 when a pipeline wait expired
+    // kGatherIm2col: A[m][k] = im2col of the input `a` (rows B*OH*OW, K = Kp);
+    // kGatherDgrad: A[m][k] = the data-gradient gather of the output
+    // gradient `a` (rows B*H*W, K = 9 Cout).  k_split 1.
+    int gather;
+    NnConvShape conv;
 };
 int tc_gemm_tile_n(int N);
 cudaError_t launch_tc_gemm(const TcGemmArgs &a, cudaStream_t stream);
@@ -193,11 +208,6 @@ struct NnPatchArgs {
     const float *shift;           // per patch predictions displacing the target window, or nullptr
     int shift_ld;                 // row stride of `shift` (translation at columns 0 and 3)
     float shift_scale;            // prediction units -> image pixels
-};
-struct NnConvShape {
-    int B, H, W, C;       // input NHWC
-    int OH, OW, Cout;     // 3x3 stride-2 pad-1 output
-    int Kp;               // padded reduction length of the forward GEMM (>= 9 C)
 };
 struct NnAdamArgs {
     float *param;

@@ -45,6 +45,22 @@ int gbdic_nn_gemm(const gbdic_nn_gemm_desc *d, int32_t *device_error, void *stre
               "tensor-core GEMM (M % 128, N % 16, K % (64 k_split), 16-byte aligned operands, ldd % 4)");
 }
 
+int gbdic_nn_conv_gemm(const gbdic_nn_gemm_desc *d, int32_t mode, const gbdic_nn_conv_shape *s,
+                       int32_t *device_error, void *stream) {
+    if (!d || !valid_shape(s)) return invalid("gemm descriptor and convolution shape are required");
+    if (mode != gbdic::kGatherIm2col && mode != gbdic::kGatherDgrad) return invalid("unknown gather mode");
+    gbdic::TcGemmArgs a{};
+    a.a = d->a; a.b = d->b;
+    a.M = d->M; a.N = d->N; a.K = d->K; a.k_split = d->k_split;
+    a.d_f32 = d->d_f32; a.d_bf16 = d->d_bf16; a.ldd = d->ldd; a.split_stride = d->split_stride;
+    a.bias = d->bias; a.relu = d->relu; a.accumulate = d->accumulate;
+    a.error = device_error;
+    a.gather = mode;
+    a.conv = shape_of(s);
+    return rc(gbdic::launch_tc_gemm(a, as_stream(stream)),
+              "implicit convolution GEMM (rows and K of the convolution, C or Cout % 8, k_split 1)");
+}
+
 int gbdic_nn_patches(const uint8_t *const *refs, const uint8_t *const *tgts, const int32_t *image_index,
                      const float *centres, int32_t count, int32_t width, int32_t height, void *out,
                      const float *shift, int32_t shift_ld, float shift_scale, void *stream) {

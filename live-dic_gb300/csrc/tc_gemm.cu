@@ -15,6 +15,14 @@
 //     each stage with tcgen05.commit on its empty barrier;
 //   * after the last commit all four warps read their 32 accumulator lanes
 //     with tcgen05.ld and apply the epilogue.
+// Convolution GEMMs can gather operand A in the kernel (implicit GEMM):
+// warps 2 and 3 then fill each stage's A tile with 16-byte cp.async copies
+// straight from the NHWC tensor (an im2col row of the forward, or the
+// data-gradient gather of the output gradient; zero-filled outside the
+// image), at the positions the 128-byte swizzle gives them, and each warp
+// arrives on the stage's full barrier after its copies landed and were
+// fenced to the async proxy that tcgen05.mma reads through; TMA still
+// loads B.  The 9x-expanded im2col matrix is never written or read.
 // Every mbarrier wait is bounded: on expiry the CTA records an error code and
 // carries on, so a fault of the pipeline ends the kernel instead of hanging.
 // Before a failed CTA frees its tensor memory and exits, it waits (bounded
@@ -66,6 +74,38 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     return false;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// 16 bytes from global to shared memory; src_bytes 0 writes zeros.
+__device__ __forceinline__ void cp_async_16(uint32_t dst, const void *src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+
+// Chunk q (K elements 8q .. 8q+7) of row m of the gathered operand, or
+// nullptr where it is zero.  Same mapping as im2col_vec_kernel /
+// dgrad_gather_vec_kernel (nn_ops.cu): C (Cout) % 8 == 0, so a chunk never
+// straddles two taps.
+__device__ __forceinline__ const uint4 *gather_chunk(const TcGemmArgs &a, int m, int q) {
+    const NnConvShape &s = a.conv;
+    const uint4 *src = static_cast<const uint4 *>(a.a);
+    const int k0 = 8 * q;
+    if (a.gather == kGatherIm2col) {
+        if (k0 >= 9 * s.C) return nullptr;
+        const int tap = k0 / s.C, ci0 = k0 - tap * s.C, ky = tap / 3, kx = tap - 3 * ky;
+        const int ox = m % s.OW, t = m / s.OW, oy = t % s.OH, b = t / s.OH;
+        const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
+        if (iy < 0 || iy >= s.H || ix < 0 || ix >= s.W) return nullptr;
+        return src + ((((size_t)b * s.H + iy) * s.W + ix) * s.C + ci0) / 8;
+    }
+    const int tap = k0 / s.Cout, co0 = k0 - tap * s.Cout, ky = tap / 3, kx = tap - 3 * ky;
+    const int ix = m % s.W, t = m / s.W, iy = t % s.H, b = t / s.H;
+    const int ty = iy + 1 - ky, tx = ix + 1 - kx;
+    if (ty < 0 || tx < 0 || (ty & 1) || (tx & 1) || (ty >> 1) >= s.OH || (tx >> 1) >= s.OW) return nullptr;
+    return src + ((((size_t)b * s.OH + (ty >> 1)) * s.OW + (tx >> 1)) * s.Cout + co0) / 8;
+}
+
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
@@ -114,8 +154,11 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
     const int num_kb = k_len / kBK;
 
     if (tid == 0) {
+        // Full barriers: the TMA producer's arrive (with the stage's bytes),
+        // plus one arrive per gathering warp in gather mode.
+        const uint32_t full_count = args.gather ? 3u : 1u;
         for (int s = 0; s < kStages; ++s) {
-            mbar_init(&full_bar[s], 1);
+            mbar_init(&full_bar[s], full_count);
             mbar_init(&empty_bar[s], 1);
         }
         mbar_init(&done_bar, 1);
@@ -145,9 +188,9 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
             }
             uint8_t *sa = smem + s * kStageBytes;
             uint8_t *sb = sa + kBytesA;
-            mbar_expect_tx(&full_bar[s], kStageBytes);
+            mbar_expect_tx(&full_bar[s], args.gather ? kBytesB : kStageBytes);
             const int kx = k_begin + kb * kBK;
-            tma_load_2d(sa, &map_a, &full_bar[s], kx, m0);
+            if (!args.gather) tma_load_2d(sa, &map_a, &full_bar[s], kx, m0);
             tma_load_2d(sb, &map_b, &full_bar[s], kx, n0);
         }
         issued_kb = kb;
@@ -183,6 +226,38 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                          smem_u32(&done_bar))
                      : "memory");
+    }
+    if (args.gather && warp >= 2) {
+        // Operand A producers: 64 threads, thread g copies chunk g % 8 of
+        // rows g / 8 + 8 i (i < 16) of the 128 x 64 tile, so eight threads
+        // read one row's 128 contiguous bytes.  Row r, chunk j lands at byte
+        // r * 128 + ((j ^ (r % 8)) * 16) of the 1024-byte-aligned stage, the
+        // 128-byte swizzle of the TMA loads it replaces.
+        const int g = tid - 64, j = g & 7;
+        for (int kb = 0; kb < num_kb; ++kb) {
+            const int s = kb % kStages;
+            if (kb >= kStages) {
+                int ok = 1;
+                if (lane == 0) ok = mbar_wait(&empty_bar[s], ((kb / kStages) - 1) & 1) ? 1 : 0;
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (!ok) {
+                    if (lane == 0) atomicExch(&failed, 1);
+                    break;
+                }
+            }
+            const uint32_t sa = smem_u32(smem + s * kStageBytes);
+            const int q = (k_begin + kb * kBK) / 8 + j;
+#pragma unroll 4
+            for (int i = 0; i < 16; ++i) {
+                const int r = (g >> 3) + 8 * i;
+                const uint4 *src = gather_chunk(args, m0 + r, q);
+                cp_async_16(sa + (uint32_t)(r * 128 + ((j ^ (r & 7)) << 4)), src ? src : args.a, src ? 16u : 0u);
+            }
+            asm volatile("cp.async.wait_all;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full_bar[s]);
+        }
     }
     __syncwarp();
     if (!mbar_wait(&done_bar, 0)) atomicExch(&failed, 1);
@@ -309,8 +384,28 @@ cudaError_t launch_tc_gemm(const TcGemmArgs &a, cudaStream_t stream) {
         (!a.d_f32 && !a.d_bf16) || (a.accumulate && !a.d_f32) || (a.k_split > 1 && a.bias))
         return cudaErrorInvalidValue;
     if ((reinterpret_cast<uintptr_t>(a.a) | reinterpret_cast<uintptr_t>(a.b)) & 15u) return cudaErrorMisalignedAddress;
+    if (a.gather != kGatherNone) {
+        // The gathered operand's rows and reduction length must be the
+        // convolution's exactly (every row and chunk maps into the tensor).
+        const NnConvShape &s = a.conv;
+        if (a.k_split != 1 || s.B < 1 || s.H < 1 || s.W < 1 || s.OH != (s.H + 1) / 2 || s.OW != (s.W + 1) / 2)
+            return cudaErrorInvalidValue;
+        if (a.gather == kGatherIm2col) {
+            if (s.C < 8 || s.C % 8 || a.M != s.B * s.OH * s.OW || a.K != s.Kp || s.Kp < 9 * s.C)
+                return cudaErrorInvalidValue;
+        } else if (a.gather == kGatherDgrad) {
+            if (s.Cout < 8 || s.Cout % 8 || a.M != s.B * s.H * s.W || a.K != 9 * s.Cout) return cudaErrorInvalidValue;
+        } else {
+            return cudaErrorInvalidValue;
+        }
+    }
     CUtensorMap ma, mb;
-    if (!make_map(&ma, a.a, a.M, a.K, kBM) || !make_map(&mb, a.b, a.N, a.K, bn)) return cudaErrorInvalidValue;
+    if (!make_map(&mb, a.b, a.N, a.K, bn)) return cudaErrorInvalidValue;
+    if (a.gather == kGatherNone) {
+        if (!make_map(&ma, a.a, a.M, a.K, kBM)) return cudaErrorInvalidValue;
+    } else {
+        ma = mb;  // not read: operand A is gathered
+    }
     switch (bn) {
     case 128: return launch_bn<128>(ma, mb, a, stream);
     case 64: return launch_bn<64>(ma, mb, a, stream);

@@ -206,6 +206,7 @@ _SIGNATURES = {
     "gbdic_affine_frontier": (C.c_int, [P, P, P, P, P]),
     "gbdic_spatial_choose": (C.c_int, [P, P, P, P, C.POINTER(ChooseCfg), P, P, P]),
     "gbdic_nn_gemm": (C.c_int, [C.POINTER(NnGemmDesc), P, P]),
+    "gbdic_nn_conv_gemm": (C.c_int, [C.POINTER(NnGemmDesc), I32, C.POINTER(NnConvShape), P, P]),
     "gbdic_nn_patches": (C.c_int, [P, P, P, P, I32, I32, I32, P, P, I32, C.c_float, P]),
     "gbdic_nn_im2col": (C.c_int, [C.POINTER(NnConvShape), P, P, P]),
     "gbdic_nn_dgrad_gather": (C.c_int, [C.POINTER(NnConvShape), P, P, P]),

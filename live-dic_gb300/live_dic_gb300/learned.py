@@ -8,11 +8,13 @@ the library's own kernels:
 
 * ``SeedNet`` -- five 3x3 stride-2 convolutions with ReLU (channels 32, 64,
   128, 128, 64) and a linear layer to 6 outputs (315,878 parameters) on
-  64 x 64 x 2 patches.  Forward and backward run as implicit GEMMs on the
-  tcgen05 tensor cores (BF16 operands, FP32 accumulation in tensor memory):
-  im2col -> GEMM(+bias, ReLU) forward; gathered output gradients x
-  transposed weights for data gradients; transposed im2col x transposed
-  output gradients (split-K, fixed-order reduction) for weight gradients.
+  64 x 64 x 2 patches.  Forward and backward run as GEMMs on the tcgen05
+  tensor cores (BF16 operands, FP32 accumulation in tensor memory): the
+  im2col rows of the forward and the gathered output gradients of the data
+  gradient are built inside the GEMM kernel from the NHWC tensors (implicit
+  GEMM, gbdic_nn_conv_gemm; the 2-channel input layer keeps a materialised
+  im2col), then GEMM(+bias, ReLU); weight gradients are transposed im2col x
+  transposed output gradients (split-K, fixed-order reduction).
   FP32 master weights, Adam.  PyTorch only allocates the device buffers and
   owns the stream.
 * ``training_pairs`` -- subset pairs the engine generates itself: seeded
@@ -145,12 +147,18 @@ class SeedNet:
 
     # ------------------------------------------------------------ kernels
     def _gemm(self, a, b, M, N, K, *, d_f32=None, d_bf16=None, ldd=None, bias=None, relu=False, k_split=1,
-              split_stride=0, stream=None):
+              split_stride=0, stream=None, gather: int = 0, shape=None):
+        """D = A B^T on the tensor cores; with `gather` (1 im2col of the
+        input `a`, 2 data-gradient gather of the output gradient `a`) operand
+        A is gathered in the kernel from the NHWC tensor `a` of `shape`."""
         desc = _native.NnGemmDesc(a.data_ptr(), b.data_ptr(), M, N, K, k_split,
                                   d_f32.data_ptr() if d_f32 is not None else None,
                                   d_bf16.data_ptr() if d_bf16 is not None else None, ldd or N, split_stride,
                                   bias.data_ptr() if bias is not None else None, int(relu), 0)
-        _call(self.lib, "gbdic_nn_gemm", C.byref(desc), _ptr(self.err), stream)
+        if gather:
+            _call(self.lib, "gbdic_nn_conv_gemm", C.byref(desc), gather, C.byref(shape), _ptr(self.err), stream)
+        else:
+            _call(self.lib, "gbdic_nn_gemm", C.byref(desc), _ptr(self.err), stream)
 
     def _shape(self, i: int) -> _native.NnConvShape:
         c = self.convs[i]
@@ -189,9 +197,14 @@ class SeedNet:
                       stream)
                 x = self.y[0]
                 continue
-            _call(self.lib, "gbdic_nn_im2col", C.byref(self._shape(i)), _ptr(x), _ptr(self.a[i]), stream)
-            self._gemm(self.a[i], self.wb[i], c.M, c.cout, c.kp, d_bf16=self.y[i], bias=self.b[i], relu=True,
-                       stream=stream)
+            if c.cin % 8 == 0:
+                # implicit GEMM: the im2col rows are gathered in the kernel
+                self._gemm(x, self.wb[i], c.M, c.cout, c.kp, d_bf16=self.y[i], bias=self.b[i], relu=True,
+                           stream=stream, gather=1, shape=self._shape(i))
+            else:
+                _call(self.lib, "gbdic_nn_im2col", C.byref(self._shape(i)), _ptr(x), _ptr(self.a[i]), stream)
+                self._gemm(self.a[i], self.wb[i], c.M, c.cout, c.kp, d_bf16=self.y[i], bias=self.b[i], relu=True,
+                           stream=stream)
             x = self.y[i]
         self._gemm(self.y[-1], self.w6b, self.B, OUT_PAD, self.features, d_f32=self.out, bias=self.b6, stream=stream)
         return self.out
@@ -211,7 +224,6 @@ class SeedNet:
             "dz": [torch.zeros(c.M, c.cout, dtype=bf16, device=dev) for c in self.convs],
             "dzT": [torch.zeros(c.cout, c.M, dtype=bf16, device=dev) for c in self.convs],
             "aT": [torch.zeros(c.kp_rows, c.M, dtype=bf16, device=dev) for c in self.convs],
-            "g": [None] + [torch.zeros(c.Min, c.kt, dtype=bf16, device=dev) for c in self.convs[1:]],
         }
         bufs["splits"] = [self._splits(c) for c in self.convs]
         bufs["partial"] = [torch.zeros(s, c.kp_rows, c.cout, dtype=f32, device=dev)
@@ -255,7 +267,11 @@ class SeedNet:
             _call(lib, "gbdic_nn_relu_backward", _ptr(dy), c.cout, _ptr(self.y[i]), _ptr(dz), c.M, c.cout, stream)
             _call(lib, "gbdic_nn_bias_grad", _ptr(dy), c.cout, _ptr(self.y[i]), c.M, c.cout,
                   _ptr(self.grads[nconv + i]), stream)
-            # weight gradient: dW^T[k][co] = sum_m A[m][k] dZ[m][co]
+            # weight gradient: dW^T[k][co] = sum_m A[m][k] dZ[m][co] (the
+            # forward of an implicit-GEMM layer left A unwritten)
+            if c.cin % 8 == 0:
+                x = self.x0 if i == 0 else self.y[i - 1]
+                _call(lib, "gbdic_nn_im2col", C.byref(self._shape(i)), _ptr(x), _ptr(self.a[i]), stream)
             _call(lib, "gbdic_nn_transpose", _ptr(self.a[i]), c.M, c.kp, c.kp, _ptr(b["aT"][i]), c.M, c.kp_rows,
                   stream)
             _call(lib, "gbdic_nn_transpose", _ptr(dz), c.M, c.cout, c.cout, _ptr(b["dzT"][i]), c.M, c.cout, stream)
@@ -265,9 +281,10 @@ class SeedNet:
             _call(lib, "gbdic_nn_splitk_reduce", _ptr(b["partial"][i]), splits, c.kp_rows, c.cout, c.kp,
                   _ptr(self.grads[i]), stream)
             if i > 0:
-                # data gradient: dY_{i-1}[m][ci] = sum_(ky,kx,co) G[m][.] Wt[ci][.]
-                _call(lib, "gbdic_nn_dgrad_gather", C.byref(self._shape(i)), _ptr(dz), _ptr(b["g"][i]), stream)
-                self._gemm(b["g"][i], self.wt[i], c.Min, c.cin, c.kt, d_f32=b["dy"][i - 1], stream=stream)
+                # data gradient: dY_{i-1}[m][ci] = sum_(ky,kx,co) G[m][.] Wt[ci][.],
+                # G gathered from dZ in the kernel (implicit GEMM)
+                self._gemm(dz, self.wt[i], c.Min, c.cin, c.kt, d_f32=b["dy"][i - 1], stream=stream, gather=2,
+                           shape=self._shape(i))
 
     def adam_step(self, lr: float = 1e-3, *, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
                   weight_decay: float = 0.0, stream=None) -> None:

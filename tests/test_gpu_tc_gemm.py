@@ -80,3 +80,75 @@ def test_gemm_rejects_unpadded_shapes():
     out = torch.empty(128, 16, device="cuda")
     with pytest.raises(ValueError, match="tensor-core GEMM"):
         _gemm(a[:100], b, d_f32=out)
+
+
+def _conv_gemm(src, b, mode, shape, M, K, d_f32):
+    lib = _native.load()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    desc = _native.NnGemmDesc(src.data_ptr(), b.data_ptr(), M, b.shape[0], K, 1, d_f32.data_ptr(), None,
+                              b.shape[0], 0, None, 0, 0)
+    code = lib.gbdic_nn_conv_gemm(C.byref(desc), mode, C.byref(shape), C.c_void_p(err.data_ptr()), None)
+    _native.check(code, lib.gbdic_last_error(None))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+
+
+def _conv_case(B, H, Cin, Cout, seed):
+    OH = (H + 1) // 2
+    return _native.NnConvShape(B, H, H, Cin, OH, OH, Cout, -(-9 * Cin // 64) * 64), torch.Generator(
+        device="cuda").manual_seed(seed)
+
+
+@pytest.mark.parametrize("B,H,Cin,Cout", [(8, 32, 32, 64), (4, 16, 64, 128), (16, 8, 128, 32), (2, 32, 16, 16),
+                                        (2, 16, 8, 64), (1, 31, 32, 64)])
+def test_implicit_im2col_gemm_equals_materialised_operand(B, H, Cin, Cout):
+    """Operand A gathered in the kernel as im2col rows of the NHWC input
+    gives the GEMM of the materialised im2col matrix bit for bit: the same
+    operand values reach the tensor cores in the same K order (zero taps at
+    the border and in the K padding beyond 9 C)."""
+    lib = _native.load()
+    shape, g = _conv_case(B, H, Cin, Cout, B * H + Cin)
+    M = B * shape.OH * shape.OW
+    if M % 128:
+        pytest.skip("rows must fill 128-row tiles")
+    x = torch.randn(B, H, H, Cin, generator=g, device="cuda").to(torch.bfloat16)
+    w = torch.randn(Cout, shape.Kp, generator=g, device="cuda").to(torch.bfloat16)
+    a = torch.empty(M, shape.Kp, dtype=torch.bfloat16, device="cuda")
+    _native.check(lib.gbdic_nn_im2col(C.byref(shape), C.c_void_p(x.data_ptr()), C.c_void_p(a.data_ptr()), None),
+                  lib.gbdic_last_error(None))
+    want = torch.empty(M, Cout, device="cuda")
+    _gemm(a, w, d_f32=want)
+    got = torch.empty(M, Cout, device="cuda")
+    _conv_gemm(x, w, 1, shape, M, shape.Kp, got)
+    assert torch.equal(got, want)
+
+
+@pytest.mark.parametrize("B,H,Cin,Cout", [(8, 32, 32, 64), (4, 16, 64, 128), (16, 8, 128, 64), (2, 32, 16, 64),
+                                        (1, 32, 64, 192)])
+def test_implicit_dgrad_gemm_equals_materialised_operand(B, H, Cin, Cout):
+    """Operand A gathered in the kernel as the data-gradient rows of the
+    output gradient (stride-2 transposed taps) gives the GEMM of the
+    materialised gather matrix bit for bit."""
+    lib = _native.load()
+    shape, g = _conv_case(B, H, Cin, Cout, B * H + Cout)
+    OH = shape.OH
+    dz = torch.randn(B, OH, OH, Cout, generator=g, device="cuda").to(torch.bfloat16)
+    wt = torch.randn(Cin, 9 * Cout, generator=g, device="cuda").to(torch.bfloat16)
+    Min = B * H * H
+    gmat = torch.empty(Min, 9 * Cout, dtype=torch.bfloat16, device="cuda")
+    _native.check(lib.gbdic_nn_dgrad_gather(C.byref(shape), C.c_void_p(dz.data_ptr()), C.c_void_p(gmat.data_ptr()),
+                                            None), lib.gbdic_last_error(None))
+    want = torch.empty(Min, Cin, device="cuda")
+    _gemm(gmat, wt, d_f32=want)
+    got = torch.empty(Min, Cin, device="cuda")
+    _conv_gemm(dz, wt, 2, shape, Min, 9 * Cout, got)
+    assert torch.equal(got, want)
+
+
+def test_implicit_conv_gemm_rejects_mismatched_shapes():
+    x = torch.zeros(2, 16, 16, 32, dtype=torch.bfloat16, device="cuda")
+    w = torch.zeros(64, 320, dtype=torch.bfloat16, device="cuda")
+    out = torch.empty(128, 64, device="cuda")
+    shape = _native.NnConvShape(2, 16, 16, 32, 8, 8, 64, 320)
+    with pytest.raises(ValueError, match="implicit convolution GEMM"):
+        _conv_gemm(x, w, 1, shape, 256, 320, out)   # rows are 2 * 8 * 8 = 128
