@@ -557,6 +557,18 @@ int gbdic_nn_relu_backward(const float *dy, int32_t ld, const void *y, void *dz,
 /* db[c] = sum_r dY[r][c] (masked by Y > 0 when y != NULL). */
 int gbdic_nn_bias_grad(const float *dy, int32_t ld, const void *y, int64_t rows, int32_t cols, float *db,
                        void *stream);
+/* ReLU backward, bias gradient and transposed output gradient in one pass:
+ * dz (BF16, rows x cols) = dY (FP32, row stride ld) where Y > 0 (everywhere
+ * when y == NULL); dz_t (BF16, cols x rows, or NULL) its transpose; db[c] =
+ * sum_r dz[r][c] before rounding, in a fixed order.  partial: device scratch
+ * of cols * ceil(rows / 64) floats.  cols a power of two from 4 to 256,
+ * ld % 4 == 0, rows % 8 == 0 when dz_t != NULL. */
+int gbdic_nn_relu_bias_backward(const float *dy, int32_t ld, const void *y, int64_t rows, int32_t cols, void *dz,
+                                void *dz_t, float *partial, float *db, void *stream);
+/* a_t (rows_padded x B*OH*OW) = the im2col operand of x (gbdic_nn_im2col)
+ * transposed, zero in rows >= 9 C, without writing the operand itself
+ * (the weight-gradient GEMM's A); rows_padded % 64 == 0, B*OH*OW % 8 == 0. */
+int gbdic_nn_im2col_t(const gbdic_nn_conv_shape *shape, const void *x, void *a_t, int32_t rows_padded, void *stream);
 /* out[n][k] = sum_s partial[s][k][n] for k < Kp (partials Kp_rows x N). */
 int gbdic_nn_splitk_reduce(const float *partial, int32_t splits, int32_t kp_rows, int32_t n, int32_t kp, float *out,
                            void *stream);

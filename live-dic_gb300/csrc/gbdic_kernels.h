@@ -175,7 +175,10 @@ struct NnConvShape {
 
 // Operand A of a convolution GEMM gathered from an NHWC tensor in the
 // kernel (implicit GEMM) instead of read from a materialised matrix.
-enum { kGatherNone = 0, kGatherIm2col = 1, kGatherDgrad = 2 };
+// kGatherDgradClasses is the launcher's internal form of kGatherDgrad for
+// even H, W and Cout % 64 == 0: rows ordered by the input pixel's parity
+// class, K blocks of the taps that are zero for a tile's class skipped.
+enum { kGatherNone = 0, kGatherIm2col = 1, kGatherDgrad = 2, kGatherDgradClasses = 3 };
 
 // D (+)= A B^T on the tensor cores: A M x K, B N x K, BF16 row-major (K
 // contiguous); M % 128 == 0, N % 16 == 0, K % (64 k_split) == 0.
@@ -220,6 +223,12 @@ cudaError_t launch_nn_patches(const NnPatchArgs &a, cudaStream_t s);
 cudaError_t launch_nn_im2col(const NnConvShape &sh, const void *x, void *A, cudaStream_t s);
 cudaError_t launch_nn_dgrad_gather(const NnConvShape &sh, const void *dz, void *G, cudaStream_t s);
 cudaError_t launch_nn_transpose(const void *src, int R, int C, int ld_src, void *dst, int Rp, int Cp, cudaStream_t s);
+// dZ = masked dY (BF16, and transposed when dzt != nullptr) and db = its
+// column sums; partial: C x ceil(rows / 64) FP32 scratch.
+cudaError_t launch_nn_relu_bias_backward(const float *dy, int ld, const void *y, long long rows, int C, void *dz,
+                                        void *dzt, float *partial, float *db, cudaStream_t s);
+// At (Kt x M) = the im2col operand of x transposed, without writing it.
+cudaError_t launch_nn_im2col_t(const NnConvShape &sh, const void *x, void *At, int Kt, cudaStream_t s);
 cudaError_t launch_nn_relu_backward(const float *dy, int ld, const void *y, void *dz, long long rows, int C,
                                     cudaStream_t s);
 cudaError_t launch_nn_bias_grad(const float *dy, int ld, const void *y, long long rows, int C, float *db,

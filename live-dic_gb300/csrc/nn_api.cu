@@ -115,6 +115,20 @@ int gbdic_nn_bias_grad(const float *dy, int32_t ld, const void *y, int64_t rows,
     return rc(gbdic::launch_nn_bias_grad(dy, ld, y, rows, cols, db, as_stream(stream)), "bias gradient");
 }
 
+int gbdic_nn_relu_bias_backward(const float *dy, int32_t ld, const void *y, int64_t rows, int32_t cols, void *dz,
+                                void *dz_t, float *partial, float *db, void *stream) {
+    if (!dy || !dz || !partial || !db || ld < cols || rows <= 0 || cols <= 0)
+        return invalid("invalid ReLU/bias backward arguments");
+    return rc(gbdic::launch_nn_relu_bias_backward(dy, ld, y, rows, cols, dz, dz_t, partial, db, as_stream(stream)),
+              "ReLU/bias backward (cols a power of two 4..256, ld % 4 == 0, rows % 8 == 0 with dz_t, aligned)");
+}
+
+int gbdic_nn_im2col_t(const gbdic_nn_conv_shape *s, const void *x, void *a_t, int32_t rows_padded, void *stream) {
+    if (!valid_shape(s) || !x || !a_t || rows_padded < s->Kp) return invalid("invalid convolution shape or pointers");
+    return rc(gbdic::launch_nn_im2col_t(shape_of(s), x, a_t, rows_padded, as_stream(stream)),
+              "transposed im2col (B*OH*OW % 8 == 0, rows_padded % 64 == 0, 16-byte aligned)");
+}
+
 int gbdic_nn_splitk_reduce(const float *partial, int32_t splits, int32_t kp_rows, int32_t n, int32_t kp, float *out,
                            void *stream) {
     if (!partial || !out || splits < 1 || kp > kp_rows || n <= 0 || kp <= 0) return invalid("invalid split-K reduction");

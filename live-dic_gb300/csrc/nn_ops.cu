@@ -2,10 +2,11 @@
 // contractions (convolutions as implicit GEMMs, the final linear layer and
 // all their gradients) run on the tensor cores in tc_gemm.cu; everything here
 // is HBM-bound glue around them:
-//   patch extraction and normalisation, 3x3 stride-2 im2col, the gather of
-//   output gradients for the data gradient, BF16 transposes, ReLU backward,
-//   bias gradients, split-K reduction of weight gradients, Adam, weight
-//   packing and the regression loss.
+//   patch extraction and normalisation, 3x3 stride-2 im2col (and its
+//   transpose for the weight gradient), the gather of output gradients for
+//   the data gradient, BF16 transposes, ReLU backward fused with the bias
+//   gradient and the output-gradient transpose, split-K reduction of weight
+//   gradients, Adam, weight packing and the regression loss.
 // Activations are NHWC BF16 (rows = pixels, channels contiguous); weights are
 // [Cout][(ky, kx, ci)] with the reduction index padded to the GEMM tile.
 #include <cuda_bf16.h>
@@ -219,6 +220,133 @@ __global__ void __launch_bounds__(256) bias_grad_kernel(const float *dy, int ld,
     if (threadIdx.x == 0) db[c] = red[0];
 }
 
+// ReLU backward, bias gradient and the transposed output gradient in one
+// pass over dY: dZ = dY where Y > 0 (everywhere when y == nullptr), written
+// BF16 as [rows][C] and, when dzt != nullptr, as [C][rows]; the FP32 column
+// sums of each 64-row tile go to partial[c * tiles + tile] (rows ascending
+// per thread, then the threads of a column in order).  256 threads, C a
+// power of two from 4 to 256; the reads (float4 of dY) and both writes are
+// contiguous, the transpose staged in shared memory.
+__global__ void __launch_bounds__(256) relu_bias_backward_kernel(const float *dy, int ld, const __nv_bfloat16 *y,
+                                                                 long long rows, int C, __nv_bfloat16 *dz,
+                                                                 __nv_bfloat16 *dzt, float *partial, int tiles) {
+    extern __shared__ __align__(16) uint8_t nn_smem[];
+    float4 *red = reinterpret_cast<float4 *>(nn_smem);                       // [256]
+    __nv_bfloat16 *tile = reinterpret_cast<__nv_bfloat16 *>(nn_smem + 256 * sizeof(float4));  // [C][72]
+    const int t = threadIdx.x, groups = C / 4, c4 = t % groups, rstep = 256 / groups;
+    const long long r0 = (long long)blockIdx.x * 64;
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int r = t / groups; r < 64 && r0 + r < rows; r += rstep) {
+        const long long row = r0 + r;
+        float4 g = *reinterpret_cast<const float4 *>(dy + row * ld + 4 * c4);
+        if (y != nullptr) {
+            const uint2 yy = *reinterpret_cast<const uint2 *>(y + row * C + 4 * c4);
+            const __nv_bfloat162 y01 = *reinterpret_cast<const __nv_bfloat162 *>(&yy.x);
+            const __nv_bfloat162 y23 = *reinterpret_cast<const __nv_bfloat162 *>(&yy.y);
+            if (!(bf(y01.x) > 0.0f)) g.x = 0.0f;
+            if (!(bf(y01.y) > 0.0f)) g.y = 0.0f;
+            if (!(bf(y23.x) > 0.0f)) g.z = 0.0f;
+            if (!(bf(y23.y) > 0.0f)) g.w = 0.0f;
+        }
+        acc.x += g.x; acc.y += g.y; acc.z += g.z; acc.w += g.w;
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(g.x, g.y), hi = __floats2bfloat162_rn(g.z, g.w);
+        uint2 out;
+        out.x = *reinterpret_cast<const uint32_t *>(&lo);
+        out.y = *reinterpret_cast<const uint32_t *>(&hi);
+        *reinterpret_cast<uint2 *>(dz + row * C + 4 * c4) = out;
+        if (dzt != nullptr) {
+            tile[(4 * c4 + 0) * 72 + r] = lo.x;
+            tile[(4 * c4 + 1) * 72 + r] = lo.y;
+            tile[(4 * c4 + 2) * 72 + r] = hi.x;
+            tile[(4 * c4 + 3) * 72 + r] = hi.y;
+        }
+    }
+    red[t] = acc;
+    __syncthreads();
+    if (t < groups) {
+        float4 sum = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (int q = t; q < 256; q += groups) {
+            const float4 v = red[q];
+            sum.x += v.x; sum.y += v.y; sum.z += v.z; sum.w += v.w;
+        }
+        partial[(size_t)(4 * t + 0) * tiles + blockIdx.x] = sum.x;
+        partial[(size_t)(4 * t + 1) * tiles + blockIdx.x] = sum.y;
+        partial[(size_t)(4 * t + 2) * tiles + blockIdx.x] = sum.z;
+        partial[(size_t)(4 * t + 3) * tiles + blockIdx.x] = sum.w;
+    }
+    if (dzt != nullptr) {
+        // rows % 8 == 0: every 8-row chunk is complete or absent
+        for (int idx = t; idx < C * 8; idx += 256) {
+            const int c = idx >> 3, ch = idx & 7;
+            if (r0 + 8 * ch >= rows) continue;
+            *reinterpret_cast<uint4 *>(dzt + (size_t)c * rows + r0 + 8 * ch) =
+                *reinterpret_cast<const uint4 *>(tile + c * 72 + 8 * ch);
+        }
+    }
+}
+
+// db[c] = sum over tiles of partial[c * tiles + tile]: one CTA per column,
+// thread t the tiles t, t + 256, ... in order, then a fixed tree.
+__global__ void __launch_bounds__(256) bias_reduce_kernel(const float *partial, int tiles, float *db) {
+    const int c = blockIdx.x;
+    float acc = 0.0f;
+    for (int i = threadIdx.x; i < tiles; i += 256) acc += partial[(size_t)c * tiles + i];
+    __shared__ float red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int off = 128; off > 0; off >>= 1) {
+        if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[c] = red[0];
+}
+
+// Transposed im2col At[k][m] = A[m][k] (A as im2col_kernel writes it, zero
+// for k >= 9 C) for k < Kt, m < M = B OH OW: one CTA per 64 k x 64 m tile,
+// staged in shared memory so that the reads (a pixel's channels) and the
+// writes (64 consecutive m of one k, 128 bytes) are both contiguous.  The
+// weight-gradient GEMM reads At; A itself is never written.
+__global__ void __launch_bounds__(256) im2col_t_kernel(NnConvShape s, const __nv_bfloat16 *x, __nv_bfloat16 *At,
+                                                       int Kt) {
+    __shared__ __align__(16) __nv_bfloat16 tile[64 * 72];  // [k][m], rows padded to 72
+    const int M = s.B * s.OH * s.OW;
+    const int m0 = blockIdx.x * 64, k0 = blockIdx.y * 64, t = threadIdx.x;
+    if (s.C % 8 == 0) {
+        for (int i = 0; i < 2; ++i) {
+            const int j = t & 7, ml = (t >> 3) + 32 * i, m = m0 + ml, k = k0 + 8 * j;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (m < M && k < 9 * s.C) {
+                const int tap = k / s.C, ci0 = k - tap * s.C, ky = tap / 3, kx = tap - 3 * ky;
+                const int ox = m % s.OW, tt = m / s.OW, oy = tt % s.OH, b = tt / s.OH;
+                const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
+                if (iy >= 0 && iy < s.H && ix >= 0 && ix < s.W)
+                    v = __ldg(reinterpret_cast<const uint4 *>(x + (((size_t)b * s.H + iy) * s.W + ix) * s.C + ci0));
+            }
+            const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) tile[(8 * j + q) * 72 + ml] = e[q];
+        }
+    } else {
+        for (int i = 0; i < 16; ++i) {
+            const int kl = t & 63, ml = (t >> 6) + 4 * i, m = m0 + ml, k = k0 + kl;
+            __nv_bfloat16 v = __float2bfloat16(0.0f);
+            if (m < M && k < 9 * s.C) {
+                const int tap = k / s.C, ci = k - tap * s.C, ky = tap / 3, kx = tap - 3 * ky;
+                const int ox = m % s.OW, tt = m / s.OW, oy = tt % s.OH, b = tt / s.OH;
+                const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
+                if (iy >= 0 && iy < s.H && ix >= 0 && ix < s.W) v = x[(((size_t)b * s.H + iy) * s.W + ix) * s.C + ci];
+            }
+            tile[kl * 72 + ml] = v;
+        }
+    }
+    __syncthreads();
+    for (int i = 0; i < 2; ++i) {
+        const int ch = t & 7, kl = (t >> 3) + 32 * i, k = k0 + kl, m = m0 + 8 * ch;
+        if (k < Kt && m < M)
+            *reinterpret_cast<uint4 *>(At + (size_t)k * M + m) = *reinterpret_cast<const uint4 *>(tile + kl * 72 + 8 * ch);
+    }
+}
+
 // out[n][k] = sum_s partial[s][k][n] (s ascending) for k < Kp, n < N.
 __global__ void splitk_reduce_kernel(const float *partial, int splits, int Kp_rows, int N, int Kp, float *out) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -257,11 +385,11 @@ __global__ void pack_weights_kernel(const float *w, int Cout, int Cin, int Kp, _
 
 // Loss 0.5 / B sum (pred - target)^2 over the first `outputs` columns and
 // its gradient (pred - target) / B as BF16 [B][ldg] (zero elsewhere); one CTA.
-__global__ void __launch_bounds__(256) regression_loss_kernel(const float *pred, int ldp, const float *target,
-                                                              int outputs, int B, __nv_bfloat16 *grad,
-                                                              float *grad_f32, int ldg, float *loss) {
+__global__ void __launch_bounds__(1024) regression_loss_kernel(const float *pred, int ldp, const float *target,
+                                                               int outputs, int B, __nv_bfloat16 *grad,
+                                                               float *grad_f32, int ldg, float *loss) {
     float acc = 0.0f;
-    for (int i = threadIdx.x; i < B * ldg; i += 256) {
+    for (int i = threadIdx.x; i < B * ldg; i += 1024) {
         const int b = i / ldg, j = i % ldg;
         float g = 0.0f;
         if (j < outputs) {
@@ -272,10 +400,10 @@ __global__ void __launch_bounds__(256) regression_loss_kernel(const float *pred,
         grad[i] = __float2bfloat16(g);
         if (grad_f32) grad_f32[i] = g;
     }
-    __shared__ float red[256];
+    __shared__ float red[1024];
     red[threadIdx.x] = acc;
     __syncthreads();
-    for (int off = 128; off > 0; off >>= 1) {
+    for (int off = 512; off > 0; off >>= 1) {
         if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
         __syncthreads();
     }
@@ -669,6 +797,46 @@ cudaError_t launch_nn_bias_grad(const float *dy, int ld, const void *y, long lon
     return cudaGetLastError();
 }
 
+cudaError_t launch_nn_relu_bias_backward(const float *dy, int ld, const void *y, long long rows, int C, void *dz,
+                                        void *dzt, float *partial, float *db, cudaStream_t s) {
+    const bool pow2 = C >= 4 && C <= 256 && (C & (C - 1)) == 0;
+    const long long tiles = (rows + 63) / 64;
+    if (!pow2 || rows <= 0 || ld < C || ld % 4 || !dy || !dz || !partial || !db || (dzt && rows % 8) ||
+        tiles >= (1ll << 31) || ((reinterpret_cast<uintptr_t>(dy) | reinterpret_cast<uintptr_t>(dzt)) & 15) ||
+        ((reinterpret_cast<uintptr_t>(y) | reinterpret_cast<uintptr_t>(dz)) & 7))
+        return cudaErrorInvalidValue;
+    const size_t smem = 256 * sizeof(float4) + (size_t)C * 72 * sizeof(__nv_bfloat16);
+    static thread_local int configured_device = -1;
+    int device = 0;
+    cudaError_t err = cudaGetDevice(&device);
+    if (err != cudaSuccess) return err;
+    if (configured_device != device) {
+        err = cudaFuncSetAttribute(relu_bias_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(256 * sizeof(float4) + 256 * 72 * sizeof(__nv_bfloat16)));
+        if (err != cudaSuccess) return err;
+        configured_device = device;
+    }
+    relu_bias_backward_kernel<<<(unsigned)tiles, 256, smem, s>>>(dy, ld, static_cast<const __nv_bfloat16 *>(y), rows,
+                                                                 C, static_cast<__nv_bfloat16 *>(dz),
+                                                                 static_cast<__nv_bfloat16 *>(dzt), partial,
+                                                                 (int)tiles);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    bias_reduce_kernel<<<C, 256, 0, s>>>(partial, (int)tiles, db);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_im2col_t(const NnConvShape &sh, const void *x, void *At, int Kt, cudaStream_t s) {
+    const long long M = (long long)sh.B * sh.OH * sh.OW;
+    if (M <= 0 || M % 8 || Kt <= 0 || Kt % 64 || M >= (1ll << 31) || (long long)Kt * M >= (1ll << 40) ||
+        ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(At)) & 15))
+        return cudaErrorInvalidValue;
+    dim3 grid((unsigned)((M + 63) / 64), (unsigned)(Kt / 64));
+    im2col_t_kernel<<<grid, 256, 0, s>>>(sh, static_cast<const __nv_bfloat16 *>(x), static_cast<__nv_bfloat16 *>(At),
+                                         Kt);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_nn_splitk_reduce(const float *partial, int splits, int Kp_rows, int N, int Kp, float *out,
                                     cudaStream_t s) {
     splitk_reduce_kernel<<<blocks((long long)N * Kp, 256), 256, 0, s>>>(partial, splits, Kp_rows, N, Kp, out);
@@ -689,7 +857,7 @@ cudaError_t launch_nn_pack_weights(const float *w, int Cout, int Cin, int Kp, vo
 
 cudaError_t launch_nn_regression_loss(const float *pred, int ldp, const float *target, int outputs, int B, void *grad,
                                       float *grad_f32, int ldg, float *loss, cudaStream_t s) {
-    regression_loss_kernel<<<1, 256, 0, s>>>(pred, ldp, target, outputs, B, static_cast<__nv_bfloat16 *>(grad),
+    regression_loss_kernel<<<1, 1024, 0, s>>>(pred, ldp, target, outputs, B, static_cast<__nv_bfloat16 *>(grad),
                                              grad_f32, ldg, loss);
     return cudaGetLastError();
 }

@@ -16,13 +16,20 @@
 //   * after the last commit all four warps read their 32 accumulator lanes
 //     with tcgen05.ld and apply the epilogue.
 // Convolution GEMMs can gather operand A in the kernel (implicit GEMM):
-// warps 2 and 3 then fill each stage's A tile with 16-byte cp.async copies
+// the CTA then has 64 + 32 kGatherWarps threads, and warps 2 and up fill
+// each stage's A tile with 16-byte cp.async copies
 // straight from the NHWC tensor (an im2col row of the forward, or the
 // data-gradient gather of the output gradient; zero-filled outside the
-// image), at the positions the 128-byte swizzle gives them, and each warp
-// arrives on the stage's full barrier after its copies landed and were
-// fenced to the async proxy that tcgen05.mma reads through; TMA still
-// loads B.  The 9x-expanded im2col matrix is never written or read.
+// image), at the positions the 128-byte swizzle gives them, from a table of
+// the tile's 128 row origins built once per CTA; each warp keeps two stages
+// of copies in flight and arrives on a stage's full barrier as soon as that
+// stage's copies landed and were fenced to the async proxy that tcgen05.mma
+// reads through; TMA still loads B.  The 9x-expanded im2col matrix is never
+// written or read.  The data-gradient GEMM orders its rows by the input
+// pixel's stride-2 parity class and skips the K blocks of the taps that are
+// zero for the tile's class (9 of the 36 class-tap pairs remain).  The
+// ring has min(4, K blocks) stages, so a 64-deep K loop needs one stage of
+// shared memory and more CTAs stay resident.
 // Every mbarrier wait is bounded: on expiry the CTA records an error code and
 // carries on, so a fault of the pipeline ends the kernel instead of hanging.
 // Before a failed CTA frees its tensor memory and exits, it waits (bounded
@@ -39,7 +46,21 @@
 namespace gbdic {
 namespace {
 
-constexpr int kStages = 4;
+#ifndef GBDIC_GEMM_STAGES
+#define GBDIC_GEMM_STAGES 4
+#endif
+#ifndef GBDIC_GATHER_AHEAD
+#define GBDIC_GATHER_AHEAD 2
+#endif
+#ifndef GBDIC_GATHER_WARPS
+#define GBDIC_GATHER_WARPS 8
+#endif
+constexpr int kStages = GBDIC_GEMM_STAGES;
+// Gather mode: warps 2 .. 2 + kGatherWarps - 1 fill operand A.
+constexpr int kGatherWarps = GBDIC_GATHER_WARPS;
+constexpr int kGatherThreads = 32 * kGatherWarps;
+constexpr int kMaxThreads = 64 + kGatherThreads;
+static_assert(kGatherWarps == 2 || kGatherWarps == 4 || kGatherWarps == 8, "1024 chunks per stage split evenly");
 constexpr int kBM = 128;
 constexpr int kBK = 64;
 constexpr uint32_t kSpinLimit = 1u << 22;
@@ -83,27 +104,101 @@ __device__ __forceinline__ void cp_async_16(uint32_t dst, const void *src, uint3
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
 }
 
-// Chunk q (K elements 8q .. 8q+7) of row m of the gathered operand, or
-// nullptr where it is zero.  Same mapping as im2col_vec_kernel /
-// dgrad_gather_vec_kernel (nn_ops.cu): C (Cout) % 8 == 0, so a chunk never
-// straddles two taps.
-__device__ __forceinline__ const uint4 *gather_chunk(const TcGemmArgs &a, int m, int q) {
+// Row descriptor of the gathered operand, built once per CTA: the chunk
+// (8-element) offset of the row's pixel origin in the NHWC source and the
+// origin's coordinates.  im2col row m = (b, oy, ox): origin (2 oy - 1,
+// 2 ox - 1) of input image b, tap (ky, kx) reads pixel (y + ky, x + kx).
+// Data-gradient row m = (b, iy, ix): origin (iy + 1, ix + 1), tap (ky, kx)
+// reads output-gradient pixel ((y - ky) / 2, (x - kx) / 2) when both are
+// even and inside the OH x OW grid.  Same mapping as im2col_vec_kernel /
+// dgrad_gather_vec_kernel (nn_ops.cu).
+//
+// Parity classes (kGatherDgradClasses, even H and W): the rows are ordered
+// by class c = 2 py + px of the input pixel (iy, ix) = (2u + py, 2v + px),
+// then by (b, u, v); a class holds B OH OW rows (a multiple of 128), so a
+// tile never mixes classes.  In class (py, px) the tap (ky, kx) is nonzero
+// only for ky = 1 (py = 0) or ky in {0, 2} (py = 1), likewise kx, and reads
+// output-gradient pixel (u + dy, v + dx), dy = 1 for (py, ky) = (1, 0), else
+// 0.  The other taps' K blocks are zero for every row of the tile and are
+// skipped: they would add exact zeros to the accumulator.
+__device__ __forceinline__ int4 gather_row(const TcGemmArgs &a, int m) {
+    const NnConvShape &s = a.conv;
+    if (a.gather == kGatherIm2col) {
+        const int ox = m % s.OW, t = m / s.OW, oy = t % s.OH, b = t / s.OH;
+        const int y = 2 * oy - 1, x = 2 * ox - 1;
+        return make_int4(((b * s.H + y) * s.W + x) * (s.C / 8), y, x, 0);
+    }
+    if (a.gather == kGatherDgradClasses) {
+        const int local = m % (s.B * s.OH * s.OW);
+        const int v = local % s.OW, t = local / s.OW, u = t % s.OH, b = t / s.OH;
+        return make_int4(((b * s.OH + u) * s.OW + v) * (s.Cout / 8), u, v, 0);
+    }
+    const int ix = m % s.W, t = m / s.W, iy = t % s.H, b = t / s.H;
+    return make_int4(b * s.OH * s.OW * (s.Cout / 8), iy + 1, ix + 1, 0);
+}
+
+// Parity class of the tile starting at row m0 (class mode), else 0.
+__device__ __forceinline__ int gather_class(const TcGemmArgs &a, int m0) {
+    return a.gather == kGatherDgradClasses ? m0 / (a.conv.B * a.conv.OH * a.conv.OW) : 0;
+}
+
+// K blocks of one CTA: all of its split, or in class mode those of the
+// class's nonzero taps (Cout / 64 blocks per tap).
+__device__ __forceinline__ int kblock_count(const TcGemmArgs &a, int k_len, int cls) {
+    if (a.gather != kGatherDgradClasses) return k_len / kBK;
+    return ((cls >> 1) ? 2 : 1) * ((cls & 1) ? 2 : 1) * (a.conv.Cout / kBK);
+}
+
+// First K element of the CTA's kb-th K block.
+__device__ __forceinline__ int kblock_offset(const TcGemmArgs &a, int kb, int k_begin, int cls) {
+    if (a.gather != kGatherDgradClasses) return k_begin + kb * kBK;
+    const int per_tap = a.conv.Cout / kBK, t = kb / per_tap, within = kb - t * per_tap;
+    const int nx = (cls & 1) ? 2 : 1, ty = t / nx, tx = t - ty * nx;
+    const int ky = (cls >> 1) ? 2 * ty : 1, kx = (cls & 1) ? 2 * tx : 1;
+    return (ky * 3 + kx) * a.conv.Cout + within * kBK;
+}
+
+// Tap of the chunk starting at K element k0: C (Cout) % 8 == 0, so a chunk
+// never straddles two taps.  im2col: (ky, kx, the tap's chunk offset, 0 for
+// the K padding beyond 9 C); data gradient: (ky, kx, channel chunk, 1);
+// class mode: (dy, dx, chunk offset of pixel (dy, dx) and channel, 1).
+__device__ __forceinline__ int4 gather_tap(const TcGemmArgs &a, int k0, int cls) {
+    const NnConvShape &s = a.conv;
+    const int per_tap = (a.gather == kGatherIm2col ? s.C : s.Cout) / 8;
+    const int q = k0 / 8, tap = q / per_tap, c8 = q - tap * per_tap, ky = tap / 3, kx = tap - 3 * ky;
+    if (a.gather == kGatherIm2col) return make_int4(ky, kx, (ky * s.W + kx) * per_tap + c8, tap < 9 ? 1 : 0);
+    if (a.gather == kGatherDgradClasses) {
+        const int dy = ((cls >> 1) && ky == 0) ? 1 : 0, dx = ((cls & 1) && kx == 0) ? 1 : 0;
+        return make_int4(dy, dx, (dy * s.OW + dx) * per_tap + c8, 1);
+    }
+    return make_int4(ky, kx, c8, 1);
+}
+
+// Source chunk of (row, tap), or nullptr where the operand is zero.
+__device__ __forceinline__ const uint4 *gather_src(const TcGemmArgs &a, int4 row, int4 tap) {
     const NnConvShape &s = a.conv;
     const uint4 *src = static_cast<const uint4 *>(a.a);
-    const int k0 = 8 * q;
     if (a.gather == kGatherIm2col) {
-        if (k0 >= 9 * s.C) return nullptr;
-        const int tap = k0 / s.C, ci0 = k0 - tap * s.C, ky = tap / 3, kx = tap - 3 * ky;
-        const int ox = m % s.OW, t = m / s.OW, oy = t % s.OH, b = t / s.OH;
-        const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
-        if (iy < 0 || iy >= s.H || ix < 0 || ix >= s.W) return nullptr;
-        return src + ((((size_t)b * s.H + iy) * s.W + ix) * s.C + ci0) / 8;
+        const int yy = row.y + tap.x, xx = row.z + tap.y;
+        if (!tap.w || (unsigned)yy >= (unsigned)s.H || (unsigned)xx >= (unsigned)s.W) return nullptr;
+        return src + (row.x + tap.z);
     }
-    const int tap = k0 / s.Cout, co0 = k0 - tap * s.Cout, ky = tap / 3, kx = tap - 3 * ky;
-    const int ix = m % s.W, t = m / s.W, iy = t % s.H, b = t / s.H;
-    const int ty = iy + 1 - ky, tx = ix + 1 - kx;
-    if (ty < 0 || tx < 0 || (ty & 1) || (tx & 1) || (ty >> 1) >= s.OH || (tx >> 1) >= s.OW) return nullptr;
-    return src + ((((size_t)b * s.OH + (ty >> 1)) * s.OW + (tx >> 1)) * s.Cout + co0) / 8;
+    if (a.gather == kGatherDgradClasses) {
+        if (row.y + tap.x >= s.OH || row.z + tap.y >= s.OW) return nullptr;
+        return src + (row.x + tap.z);
+    }
+    const int ty = row.y - tap.x, tx = row.z - tap.y;
+    if (((ty | tx) & 1) || (unsigned)ty >= (unsigned)(2 * s.OH) || (unsigned)tx >= (unsigned)(2 * s.OW)) return nullptr;
+    return src + (row.x + ((ty >> 1) * s.OW + (tx >> 1)) * (s.Cout / 8) + tap.z);
+}
+
+// Output row of accumulator row m (class mode: back to (b, iy, ix) order).
+__device__ __forceinline__ int output_row(const TcGemmArgs &a, int m, int cls) {
+    if (a.gather != kGatherDgradClasses) return m;
+    const NnConvShape &s = a.conv;
+    const int local = m - cls * (s.B * s.OH * s.OW);
+    const int v = local % s.OW, t = local / s.OW, u = t % s.OH, b = t / s.OH;
+    return (b * s.H + 2 * u + (cls >> 1)) * s.W + 2 * v + (cls & 1);
 }
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
@@ -133,7 +228,7 @@ __host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
 }
 
 template <int BN>
-__global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap map_a,
+__global__ void __launch_bounds__(kMaxThreads, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap map_a,
                                                          const __grid_constant__ CUtensorMap map_b,
                                                          TcGemmArgs args) {
     constexpr uint32_t kBytesA = kBM * kBK * 2;
@@ -145,19 +240,26 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
     __shared__ uint32_t tmem_slot;
     __shared__ int failed;
     __shared__ int issued_kb, consumed_kb;  // K blocks whose loads were issued / consumed
+    __shared__ int4 row_tab[kBM];           // gather mode: descriptors of the tile's rows
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int n0 = blockIdx.x * BN, m0 = blockIdx.y * kBM;
     const int k_len = args.K / args.k_split;
     const int k_begin = blockIdx.z * k_len;
-    const int num_kb = k_len / kBK;
+    const int cls = gather_class(args, m0);
+    const int num_kb = kblock_count(args, k_len, cls);
+    // The ring holds min(4, K blocks) stages (launch_bn sizes the dynamic
+    // shared memory the same way), so short K loops leave room for more
+    // resident CTAs.
+    const int nst = num_kb < kStages ? num_kb : kStages;
 
+    if (args.gather && tid < kBM) row_tab[tid] = gather_row(args, m0 + tid);
     if (tid == 0) {
         // Full barriers: the TMA producer's arrive (with the stage's bytes),
         // plus one arrive per gathering warp in gather mode.
-        const uint32_t full_count = args.gather ? 3u : 1u;
-        for (int s = 0; s < kStages; ++s) {
+        const uint32_t full_count = args.gather ? 1u + (uint32_t)kGatherWarps : 1u;
+        for (int s = 0; s < nst; ++s) {
             mbar_init(&full_bar[s], full_count);
             mbar_init(&empty_bar[s], 1);
         }
@@ -181,15 +283,15 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
         // TMA producer.
         int kb = 0;
         for (; kb < num_kb; ++kb) {
-            const int s = kb % kStages;
-            if (kb >= kStages && !mbar_wait(&empty_bar[s], ((kb / kStages) - 1) & 1)) {
+            const int s = kb % nst;
+            if (kb >= nst && !mbar_wait(&empty_bar[s], ((kb / nst) - 1) & 1)) {
                 atomicExch(&failed, 1);
                 break;
             }
             uint8_t *sa = smem + s * kStageBytes;
             uint8_t *sb = sa + kBytesA;
             mbar_expect_tx(&full_bar[s], args.gather ? kBytesB : kStageBytes);
-            const int kx = k_begin + kb * kBK;
+            const int kx = kblock_offset(args, kb, k_begin, cls);
             if (!args.gather) tma_load_2d(sa, &map_a, &full_bar[s], kx, m0);
             tma_load_2d(sb, &map_b, &full_bar[s], kx, n0);
         }
@@ -199,8 +301,8 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
         constexpr uint32_t idesc = instr_desc(kBM, BN);
         int kb = 0;
         for (; kb < num_kb; ++kb) {
-            const int s = kb % kStages;
-            if (!mbar_wait(&full_bar[s], (kb / kStages) & 1)) {
+            const int s = kb % nst;
+            if (!mbar_wait(&full_bar[s], (kb / nst) & 1)) {
                 atomicExch(&failed, 1);
                 break;
             }
@@ -228,17 +330,38 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
                      : "memory");
     }
     if (args.gather && warp >= 2) {
-        // Operand A producers: 64 threads, thread g copies chunk g % 8 of
-        // rows g / 8 + 8 i (i < 16) of the 128 x 64 tile, so eight threads
-        // read one row's 128 contiguous bytes.  Row r, chunk j lands at byte
-        // r * 128 + ((j ^ (r % 8)) * 16) of the 1024-byte-aligned stage, the
-        // 128-byte swizzle of the TMA loads it replaces.
-        const int g = tid - 64, j = g & 7;
-        for (int kb = 0; kb < num_kb; ++kb) {
-            const int s = kb % kStages;
-            if (kb >= kStages) {
+        // Operand A producers: kGatherThreads threads, thread g copies chunk
+        // j = g % 8 of rows g / 8 + (kGatherThreads / 8) i of the 128 x 64
+        // tile, so eight threads read one row's 128 contiguous bytes (one
+        // tap, or two for C = 32).
+        // Row r, chunk j lands at byte r * 128 + ((j ^ (r % 8)) * 16) of the
+        // 1024-byte-aligned stage, the 128-byte swizzle of the TMA loads it
+        // replaces.  Each stage's copies form one cp.async group; a warp
+        // keeps up to kAhead groups in flight.  At the top of each iteration
+        // the oldest group is waited for, fenced to the async proxy that
+        // tcgen05.mma reads through and arrived on its full barrier, before
+        // the warp waits for the next ring slot, so the slot's release (by
+        // the MMAs of a stage arrived kAhead iterations earlier) is never
+        // held up by the warp's own arrivals.
+        // kAhead <= kStages - 1: the slot waited for at iteration kb belongs to
+        // stage kb - nst, arrived at iteration kb - nst + kAhead < kb.
+        constexpr int kAhead = GBDIC_GATHER_AHEAD;
+        static_assert(kAhead >= 1 && kAhead < kStages, "gather look-ahead must leave a ring slot");
+        constexpr int kRowStep = kGatherThreads / 8, kRowsPerThread = kBM / kRowStep;
+        const int g = tid - 64, j = g & 7, r0 = g >> 3;
+        int kb = 0, arrived = 0;
+        for (; kb < num_kb; ++kb) {
+            const int s = kb % nst;
+            if (kb - arrived == kAhead) {
+                asm volatile("cp.async.wait_group %0;" ::"n"(kAhead - 1) : "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full_bar[arrived % nst]);
+                ++arrived;
+            }
+            if (kb >= nst) {
                 int ok = 1;
-                if (lane == 0) ok = mbar_wait(&empty_bar[s], ((kb / kStages) - 1) & 1) ? 1 : 0;
+                if (lane == 0) ok = mbar_wait(&empty_bar[s], ((kb / nst) - 1) & 1) ? 1 : 0;
                 ok = __shfl_sync(0xffffffffu, ok, 0);
                 if (!ok) {
                     if (lane == 0) atomicExch(&failed, 1);
@@ -246,29 +369,33 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
                 }
             }
             const uint32_t sa = smem_u32(smem + s * kStageBytes);
-            const int q = (k_begin + kb * kBK) / 8 + j;
-#pragma unroll 4
-            for (int i = 0; i < 16; ++i) {
-                const int r = (g >> 3) + 8 * i;
-                const uint4 *src = gather_chunk(args, m0 + r, q);
+            const int4 tap = gather_tap(args, kblock_offset(args, kb, k_begin, cls) + 8 * j, cls);
+#pragma unroll
+            for (int i = 0; i < kRowsPerThread; ++i) {
+                const int r = r0 + kRowStep * i;
+                const uint4 *src = gather_src(args, row_tab[r], tap);
                 cp_async_16(sa + (uint32_t)(r * 128 + ((j ^ (r & 7)) << 4)), src ? src : args.a, src ? 16u : 0u);
             }
-            asm volatile("cp.async.wait_all;" ::: "memory");
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&full_bar[s]);
+            asm volatile("cp.async.commit_group;" ::: "memory");
         }
+        // Drain: every issued copy lands before the warp moves on (also after
+        // a failed wait, so no copy is left writing into shared memory).
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        for (; arrived < kb; ++arrived)
+            if (lane == 0) mbar_arrive(&full_bar[arrived % nst]);
     }
     __syncwarp();
     if (!mbar_wait(&done_bar, 0)) atomicExch(&failed, 1);
     __syncwarp();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-    // Epilogue: warp w owns accumulator lanes (rows) 32w .. 32w + 31.
-    const int row = m0 + warp * 32 + lane;
+    // Epilogue: warp w < 4 owns accumulator lanes (rows) 32w .. 32w + 31.
+    const int row = output_row(args, m0 + warp * 32 + lane, cls);
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
 #pragma unroll 1
-    for (int c = 0; c < BN; c += 16) {
+    for (int c = 0; c < (warp < 4 ? BN : 0); c += 16) {
         uint32_t r[16];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
@@ -309,7 +436,7 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
         if (lane == 0 && failed) {
             // The producer runs at most kStages K blocks ahead of the issuer,
             // so the unconsumed blocks occupy distinct stages.
-            for (int kb = consumed_kb; kb < issued_kb; ++kb) mbar_wait(&full_bar[kb % kStages], (kb / kStages) & 1);
+            for (int kb = consumed_kb; kb < issued_kb; ++kb) mbar_wait(&full_bar[kb % nst], (kb / nst) & 1);
             mbar_wait(&done_bar, 0);
         }
         __syncwarp();
@@ -351,19 +478,22 @@ bool make_map(CUtensorMap *map, const void *ptr, int rows, int cols, int box_row
 
 template <int BN>
 cudaError_t launch_bn(const CUtensorMap &ma, const CUtensorMap &mb, const TcGemmArgs &a, cudaStream_t stream) {
-    const size_t smem = (size_t)kStages * (kBM * kBK * 2 + BN * kBK * 2) + 1024;
+    const int num_kb = a.K / a.k_split / kBK;
+    const int nst = num_kb < kStages ? num_kb : kStages;
+    const size_t smem = (size_t)nst * (kBM * kBK * 2 + BN * kBK * 2) + 1024;
+    const size_t smem_max = (size_t)kStages * (kBM * kBK * 2 + BN * kBK * 2) + 1024;
     // The attribute is per device; set it once per device and tile width.
     static thread_local int configured_device = -1;
     int device = 0;
     cudaError_t err = cudaGetDevice(&device);
     if (err != cudaSuccess) return err;
     if (configured_device != device) {
-        err = cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        err = cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
         if (err != cudaSuccess) return err;
         configured_device = device;
     }
     dim3 grid(a.N / BN, a.M / kBM, a.k_split);
-    tc_gemm_kernel<BN><<<grid, 128, smem, stream>>>(ma, mb, a);
+    tc_gemm_kernel<BN><<<grid, a.gather ? kMaxThreads : 128, smem, stream>>>(ma, mb, a);
     return cudaGetLastError();
 }
 
@@ -390,27 +520,41 @@ cudaError_t launch_tc_gemm(const TcGemmArgs &a, cudaStream_t stream) {
         const NnConvShape &s = a.conv;
         if (a.k_split != 1 || s.B < 1 || s.H < 1 || s.W < 1 || s.OH != (s.H + 1) / 2 || s.OW != (s.W + 1) / 2)
             return cudaErrorInvalidValue;
+        // chunk offsets are 32-bit in the kernel
         if (a.gather == kGatherIm2col) {
-            if (s.C < 8 || s.C % 8 || a.M != s.B * s.OH * s.OW || a.K != s.Kp || s.Kp < 9 * s.C)
+            if (s.C < 8 || s.C % 8 || a.M != s.B * s.OH * s.OW || a.K != s.Kp || s.Kp < 9 * s.C ||
+                (long long)s.B * s.H * s.W * (s.C / 8) >= (1ll << 31))
                 return cudaErrorInvalidValue;
         } else if (a.gather == kGatherDgrad) {
-            if (s.Cout < 8 || s.Cout % 8 || a.M != s.B * s.H * s.W || a.K != 9 * s.Cout) return cudaErrorInvalidValue;
+            if (s.Cout < 8 || s.Cout % 8 || a.M != s.B * s.H * s.W || a.K != 9 * s.Cout ||
+                (long long)s.B * s.OH * s.OW * (s.Cout / 8) >= (1ll << 31))
+                return cudaErrorInvalidValue;
         } else {
             return cudaErrorInvalidValue;
         }
     }
+    TcGemmArgs args = a;
+    if (a.gather == kGatherDgrad) {
+        // Rows by parity class, zero taps skipped: same sums (the skipped K
+        // blocks are exact zeros), a quarter of the gathers and MMAs.
+        const NnConvShape &s = a.conv;
+        if (s.H == 2 * s.OH && s.W == 2 * s.OW && s.Cout % kBK == 0 && (s.B * s.OH * s.OW) % kBM == 0)
+            args.gather = kGatherDgradClasses;
+    } else if (a.gather != kGatherNone && a.gather != kGatherIm2col) {
+        return cudaErrorInvalidValue;
+    }
     CUtensorMap ma, mb;
-    if (!make_map(&mb, a.b, a.N, a.K, bn)) return cudaErrorInvalidValue;
-    if (a.gather == kGatherNone) {
-        if (!make_map(&ma, a.a, a.M, a.K, kBM)) return cudaErrorInvalidValue;
+    if (!make_map(&mb, args.b, args.N, args.K, bn)) return cudaErrorInvalidValue;
+    if (args.gather == kGatherNone) {
+        if (!make_map(&ma, args.a, args.M, args.K, kBM)) return cudaErrorInvalidValue;
     } else {
         ma = mb;  // not read: operand A is gathered
     }
     switch (bn) {
-    case 128: return launch_bn<128>(ma, mb, a, stream);
-    case 64: return launch_bn<64>(ma, mb, a, stream);
-    case 32: return launch_bn<32>(ma, mb, a, stream);
-    default: return launch_bn<16>(ma, mb, a, stream);
+    case 128: return launch_bn<128>(ma, mb, args, stream);
+    case 64: return launch_bn<64>(ma, mb, args, stream);
+    case 32: return launch_bn<32>(ma, mb, args, stream);
+    default: return launch_bn<16>(ma, mb, args, stream);
     }
 }
 

@@ -207,6 +207,8 @@ _SIGNATURES = {
     "gbdic_spatial_choose": (C.c_int, [P, P, P, P, C.POINTER(ChooseCfg), P, P, P]),
     "gbdic_nn_gemm": (C.c_int, [C.POINTER(NnGemmDesc), P, P]),
     "gbdic_nn_conv_gemm": (C.c_int, [C.POINTER(NnGemmDesc), I32, C.POINTER(NnConvShape), P, P]),
+    "gbdic_nn_relu_bias_backward": (C.c_int, [P, I32, P, I64, I32, P, P, P, P, P]),
+    "gbdic_nn_im2col_t": (C.c_int, [C.POINTER(NnConvShape), P, P, I32, P]),
     "gbdic_nn_patches": (C.c_int, [P, P, P, P, I32, I32, I32, P, P, I32, C.c_float, P]),
     "gbdic_nn_im2col": (C.c_int, [C.POINTER(NnConvShape), P, P, P]),
     "gbdic_nn_dgrad_gather": (C.c_int, [C.POINTER(NnConvShape), P, P, P]),

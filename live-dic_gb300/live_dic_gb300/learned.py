@@ -13,8 +13,10 @@ the library's own kernels:
   im2col rows of the forward and the gathered output gradients of the data
   gradient are built inside the GEMM kernel from the NHWC tensors (implicit
   GEMM, gbdic_nn_conv_gemm; the 2-channel input layer keeps a materialised
-  im2col), then GEMM(+bias, ReLU); weight gradients are transposed im2col x
-  transposed output gradients (split-K, fixed-order reduction).
+  im2col), then GEMM(+bias, ReLU); weight gradients are transposed im2col
+  (written straight from the layer input) x transposed output gradients
+  (written by the one-pass ReLU/bias backward), split-K with a fixed-order
+  reduction.
   FP32 master weights, Adam.  PyTorch only allocates the device buffers and
   owns the stream.
 * ``training_pairs`` -- subset pairs the engine generates itself: seeded
@@ -136,7 +138,10 @@ class SeedNet:
         self.w6t = torch.zeros(self.features, LOSS_PAD, dtype=bf16, device=dev)
         # activations
         self.x0 = torch.zeros(batch, PATCH, PATCH, 2, dtype=bf16, device=dev)
-        self.a = [torch.zeros(c.M, c.kp, dtype=bf16, device=dev) for c in self.convs]
+        # materialised im2col operand only for layers whose channel count is
+        # not a multiple of 8 (the 2-channel input layer); the others gather
+        # it inside the GEMM
+        self.a = [torch.zeros(c.M, c.kp, dtype=bf16, device=dev) if c.cin % 8 else None for c in self.convs]
         self.y = [torch.zeros(c.M, c.cout, dtype=bf16, device=dev) for c in self.convs]
         self.out = torch.zeros(batch, OUT_PAD, dtype=f32, device=dev)
         # backward buffers (allocated on first backward)
@@ -222,6 +227,7 @@ class SeedNet:
             "dw6T": torch.zeros(self.features, OUT_PAD, dtype=f32, device=dev),
             "dy": [torch.zeros(c.M, c.cout, dtype=f32, device=dev) for c in self.convs],
             "dz": [torch.zeros(c.M, c.cout, dtype=bf16, device=dev) for c in self.convs],
+            "db_partial": [torch.zeros(c.cout * ((c.M + 63) // 64), dtype=f32, device=dev) for c in self.convs],
             "dzT": [torch.zeros(c.cout, c.M, dtype=bf16, device=dev) for c in self.convs],
             "aT": [torch.zeros(c.kp_rows, c.M, dtype=bf16, device=dev) for c in self.convs],
         }
@@ -264,17 +270,13 @@ class SeedNet:
         for i in range(nconv - 1, -1, -1):
             c = self.convs[i]
             dy, dz = b["dy"][i], b["dz"][i]
-            _call(lib, "gbdic_nn_relu_backward", _ptr(dy), c.cout, _ptr(self.y[i]), _ptr(dz), c.M, c.cout, stream)
-            _call(lib, "gbdic_nn_bias_grad", _ptr(dy), c.cout, _ptr(self.y[i]), c.M, c.cout,
-                  _ptr(self.grads[nconv + i]), stream)
-            # weight gradient: dW^T[k][co] = sum_m A[m][k] dZ[m][co] (the
-            # forward of an implicit-GEMM layer left A unwritten)
-            if c.cin % 8 == 0:
-                x = self.x0 if i == 0 else self.y[i - 1]
-                _call(lib, "gbdic_nn_im2col", C.byref(self._shape(i)), _ptr(x), _ptr(self.a[i]), stream)
-            _call(lib, "gbdic_nn_transpose", _ptr(self.a[i]), c.M, c.kp, c.kp, _ptr(b["aT"][i]), c.M, c.kp_rows,
-                  stream)
-            _call(lib, "gbdic_nn_transpose", _ptr(dz), c.M, c.cout, c.cout, _ptr(b["dzT"][i]), c.M, c.cout, stream)
+            # dZ, its transpose and the bias gradient in one pass over dY
+            _call(lib, "gbdic_nn_relu_bias_backward", _ptr(dy), c.cout, _ptr(self.y[i]), c.M, c.cout, _ptr(dz),
+                  _ptr(b["dzT"][i]), _ptr(b["db_partial"][i]), _ptr(self.grads[nconv + i]), stream)
+            # weight gradient: dW^T[k][co] = sum_m A[m][k] dZ[m][co], with A^T
+            # written straight from the layer input (A is never materialised)
+            x = self.x0 if i == 0 else self.y[i - 1]
+            _call(lib, "gbdic_nn_im2col_t", C.byref(self._shape(i)), _ptr(x), _ptr(b["aT"][i]), c.kp_rows, stream)
             splits = b["splits"][i]
             self._gemm(b["aT"][i], b["dzT"][i], c.kp_rows, c.cout, c.M, d_f32=b["partial"][i], k_split=splits,
                        split_stride=c.kp_rows * c.cout, stream=stream)

@@ -124,11 +124,14 @@ def test_implicit_im2col_gemm_equals_materialised_operand(B, H, Cin, Cout):
 
 
 @pytest.mark.parametrize("B,H,Cin,Cout", [(8, 32, 32, 64), (4, 16, 64, 128), (16, 8, 128, 64), (2, 32, 16, 64),
-                                        (1, 32, 64, 192)])
+                                        (1, 32, 64, 192), (1, 16, 32, 64), (128, 15, 16, 64)])
 def test_implicit_dgrad_gemm_equals_materialised_operand(B, H, Cin, Cout):
     """Operand A gathered in the kernel as the data-gradient rows of the
     output gradient (stride-2 transposed taps) gives the GEMM of the
-    materialised gather matrix bit for bit."""
+    materialised gather matrix bit for bit.  The first five shapes take the
+    parity-class form (rows by the input pixel's parity, zero tap blocks
+    skipped); B 1 x 16^2 (a class of 64 rows) and the odd side 15 take the
+    plain gather."""
     lib = _native.load()
     shape, g = _conv_case(B, H, Cin, Cout, B * H + Cout)
     OH = shape.OH
