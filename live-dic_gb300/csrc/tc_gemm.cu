@@ -21,14 +21,15 @@
 // straight from the NHWC tensor (an im2col row of the forward, or the
 // data-gradient gather of the output gradient; zero-filled outside the
 // image), at the positions the 128-byte swizzle gives them, from a table of
-// the tile's 128 row origins built once per CTA; each warp keeps two stages
-// of copies in flight and arrives on a stage's full barrier as soon as that
-// stage's copies landed and were fenced to the async proxy that tcgen05.mma
-// reads through; TMA still loads B.  The 9x-expanded im2col matrix is never
+// the tile's 128 row origins built once per CTA; each warp arrives on a
+// stage's full barrier once that stage's copies landed and were fenced to
+// the async proxy that tcgen05.mma reads through, while its next stage's
+// copies are in flight; TMA still loads B.  The 9x-expanded im2col matrix is never
 // written or read.  The data-gradient GEMM orders its rows by the input
 // pixel's stride-2 parity class and skips the K blocks of the taps that are
 // zero for the tile's class (9 of the 36 class-tap pairs remain).  The
-// ring has min(4, K blocks) stages, so a 64-deep K loop needs one stage of
+// ring has min(4, K blocks) stages (2 in gather mode, where the copies, not
+// the ring, set the pace), so short K loops and gathering CTAs need little
 // shared memory and more CTAs stay resident.
 // Every mbarrier wait is bounded: on expiry the CTA records an error code and
 // carries on, so a fault of the pipeline ends the kernel instead of hanging.
@@ -50,12 +51,19 @@ namespace {
 #define GBDIC_GEMM_STAGES 4
 #endif
 #ifndef GBDIC_GATHER_AHEAD
-#define GBDIC_GATHER_AHEAD 2
+#define GBDIC_GATHER_AHEAD 1
 #endif
 #ifndef GBDIC_GATHER_WARPS
 #define GBDIC_GATHER_WARPS 8
 #endif
+#ifndef GBDIC_GATHER_STAGES
+#define GBDIC_GATHER_STAGES 2
+#endif
 constexpr int kStages = GBDIC_GEMM_STAGES;
+// Ring depth in gather mode (<= kStages): the gathers keep only a few
+// stages in flight, so a shallower ring leaves room for more resident CTAs.
+constexpr int kGatherStages = GBDIC_GATHER_STAGES;
+static_assert(kGatherStages >= 2 && kGatherStages <= kStages, "gather ring depth");
 // Gather mode: warps 2 .. 2 + kGatherWarps - 1 fill operand A.
 constexpr int kGatherWarps = GBDIC_GATHER_WARPS;
 constexpr int kGatherThreads = 32 * kGatherWarps;
@@ -252,7 +260,8 @@ __global__ void __launch_bounds__(kMaxThreads, 1) tc_gemm_kernel(const __grid_co
     // The ring holds min(4, K blocks) stages (launch_bn sizes the dynamic
     // shared memory the same way), so short K loops leave room for more
     // resident CTAs.
-    const int nst = num_kb < kStages ? num_kb : kStages;
+    const int ring = args.gather ? kGatherStages : kStages;
+    const int nst = num_kb < ring ? num_kb : ring;
 
     if (args.gather && tid < kBM) row_tab[tid] = gather_row(args, m0 + tid);
     if (tid == 0) {
@@ -343,10 +352,10 @@ __global__ void __launch_bounds__(kMaxThreads, 1) tc_gemm_kernel(const __grid_co
         // the warp waits for the next ring slot, so the slot's release (by
         // the MMAs of a stage arrived kAhead iterations earlier) is never
         // held up by the warp's own arrivals.
-        // kAhead <= kStages - 1: the slot waited for at iteration kb belongs to
-        // stage kb - nst, arrived at iteration kb - nst + kAhead < kb.
+        // kAhead <= ring depth: the slot waited for at iteration kb belongs to
+        // stage kb - nst, arrived at the top of iteration kb - nst + kAhead <= kb.
         constexpr int kAhead = GBDIC_GATHER_AHEAD;
-        static_assert(kAhead >= 1 && kAhead < kStages, "gather look-ahead must leave a ring slot");
+        static_assert(kAhead >= 1 && kAhead <= kGatherStages, "gather look-ahead must stay within the ring");
         constexpr int kRowStep = kGatherThreads / 8, kRowsPerThread = kBM / kRowStep;
         const int g = tid - 64, j = g & 7, r0 = g >> 3;
         int kb = 0, arrived = 0;
@@ -479,7 +488,8 @@ bool make_map(CUtensorMap *map, const void *ptr, int rows, int cols, int box_row
 template <int BN>
 cudaError_t launch_bn(const CUtensorMap &ma, const CUtensorMap &mb, const TcGemmArgs &a, cudaStream_t stream) {
     const int num_kb = a.K / a.k_split / kBK;
-    const int nst = num_kb < kStages ? num_kb : kStages;
+    const int ring = a.gather ? kGatherStages : kStages;
+    const int nst = num_kb < ring ? num_kb : ring;
     const size_t smem = (size_t)nst * (kBM * kBK * 2 + BN * kBK * 2) + 1024;
     const size_t smem_max = (size_t)kStages * (kBM * kBK * 2 + BN * kBK * 2) + 1024;
     // The attribute is per device; set it once per device and tile width.
