@@ -65,8 +65,9 @@ def parse_args() -> argparse.Namespace:
                     help="ZNCC integer search radius at the coarsest level (first frame, unseeded windows)")
     ap.add_argument("--lanes", type=int, default=16)
     ap.add_argument("--persistent", action="store_true")
-    ap.add_argument("--solver-mode", choices=("exact", "fast"), default="exact",
-                    help="IC-GN pixel loop: the reference's order, or the sliding-window sampler")
+    ap.add_argument("--solver-mode", choices=("exact", "fast", "staged", "staged-wide"), default="exact",
+                    help="IC-GN pixel loop: the reference's order, the sliding-window sampler, or the reference's "
+                         "order on TMA-staged shared-memory tiles (compact or wide)")
     ap.add_argument("--autotune", action="store_true", help="pick lanes/persistence/pixel loop with the autotuner")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frames", type=int, default=4, help="timed frames of the CPU pipeline sample")

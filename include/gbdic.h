@@ -53,8 +53,12 @@ enum { GBDIC_INTERP_BSPLINE = 0, GBDIC_INTERP_LINEAR = 1, GBDIC_INTERP_KEYS = 2 
  * summation (bit-exact against the oracle); FAST walks column runs with a
  * sliding register window of B-spline taps (translation and affine models,
  * B-spline interpolation, 16 or 32 lanes; every other configuration runs the
- * exact loop), within the parity tolerances of the exact one. */
-enum { GBDIC_SOLVER_EXACT = 0, GBDIC_SOLVER_FAST = 1 };
+ * exact loop), within the parity tolerances of the exact one.  STAGED and
+ * STAGED_WIDE run the exact loop on B-spline taps staged per warp in a
+ * shared-memory tile by TMA (56 x 44 or 72 x 56 floats), bit-identical to
+ * EXACT (translation and affine, B-spline, 16 or 32 lanes, image width a
+ * multiple of 4; elsewhere the exact loop). */
+enum { GBDIC_SOLVER_EXACT = 0, GBDIC_SOLVER_FAST = 1, GBDIC_SOLVER_STAGED = 2, GBDIC_SOLVER_STAGED_WIDE = 3 };
 enum { GBDIC_OUTLIER_FLAG = 0, GBDIC_OUTLIER_REPLACE = 1, GBDIC_OUTLIER_DISABLED = 2,
        GBDIC_OUTLIER_MEDIAN = 3 };
 enum { GBDIC_EXPORT_COEFFICIENTS = 0, GBDIC_EXPORT_PLANE = 1, GBDIC_EXPORT_METADATA = 2,

@@ -167,7 +167,7 @@ class Runtime {
     int device_ = 0;
     int persistent_grid_ = 0;
     int persistent_lanes_ = 0;
-    bool persistent_fast_ = false;
+    int persistent_variant_ = 0;  // 0 exact, 1 fast, 2 / 3 staged tile 1 / 2
     bool profiling_ = false;
     std::vector<cudaEvent_t> profile_begin_, profile_end_;
     int profile_used_ = 0;

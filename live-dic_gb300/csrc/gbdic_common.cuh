@@ -163,6 +163,9 @@ struct SolveArgs {
     // Fast pixel loop (solver_fast.cu): row segments per column, or 0 for the
     // exact loop.
     int fast_segments;
+    // Staged tiles (solver_staged.cu): 0 off, 1 compact (56 x 44 floats per
+    // warp), 2 wide (72 x 56).
+    int staged_tile;
 };
 
 }  // namespace gbdic

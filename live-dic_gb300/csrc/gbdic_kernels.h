@@ -31,6 +31,12 @@ int icgn_fast_segments(int S, int lanes);
 cudaError_t launch_icgn_fast(const SolveArgs &a, int model, int lanes, bool gauss, int grid, cudaStream_t stream,
                              int *occupancy_only);
 int icgn_fast_occupancy(int model, int lanes, bool gauss);
+// TMA-staged coefficient tiles (solver_staged.cu): tile 1 compact (56 x 44),
+// 2 wide (72 x 56); bit-identical to the exact loop.
+bool icgn_staged_supported(int model, int interp, int lanes, int W);
+cudaError_t launch_icgn_staged(const SolveArgs &a, int model, int lanes, bool gauss, int tile, int grid,
+                               cudaStream_t stream, int *occupancy_only);
+int icgn_staged_occupancy(int model, int lanes, bool gauss, int tile);
 
 // Partial-support windows (a.count = number of partial windows; a.partial_index,
 // a.support, a.support_box, a.support_words set); translation and affine.

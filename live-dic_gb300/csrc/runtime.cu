@@ -71,8 +71,8 @@ void validate_options(const gbdic_options &o) {
     if (o.divergence_min_iterations < 1 || o.divergence_min_iterations > 30)
         fail(GBDIC_EINVAL, "divergence_min_iterations must be an integer from 1 to 30");
     if (o.pipeline_slots < 1 || o.pipeline_slots > 64) fail(GBDIC_EINVAL, "pipeline_depth must be a positive integer");
-    if (o.solver_mode != GBDIC_SOLVER_EXACT && o.solver_mode != GBDIC_SOLVER_FAST)
-        fail(GBDIC_EINVAL, "solver_mode must be 'exact' or 'fast'");
+    if (o.solver_mode < GBDIC_SOLVER_EXACT || o.solver_mode > GBDIC_SOLVER_STAGED_WIDE)
+        fail(GBDIC_EINVAL, "solver_mode must be 'exact', 'fast', 'staged' or 'staged-wide'");
 }
 
 void validate_cfg(const gbdic_solver_cfg *c) {
@@ -178,7 +178,8 @@ bool Runtime::fast_active() const {
 }
 
 void Runtime::set_mode(int mode) {
-    if (mode != GBDIC_SOLVER_EXACT && mode != GBDIC_SOLVER_FAST) fail(GBDIC_EINVAL, "solver_mode must be 'exact' or 'fast'");
+    if (mode < GBDIC_SOLVER_EXACT || mode > GBDIC_SOLVER_STAGED_WIDE)
+        fail(GBDIC_EINVAL, "solver_mode must be 'exact', 'fast', 'staged' or 'staged-wide'");
     opt_.o.solver_mode = mode;
     if (opt_.o.persistent) persistent_grid(opt_.lanes);
 }
@@ -196,13 +197,21 @@ int Runtime::persistent_grid(int lanes) {
     // Queried once per lane count outside any stream capture, then cached.
     const bool fast = opt_.o.solver_mode == GBDIC_SOLVER_FAST &&
                       icgn_fast_supported(opt_.o.motion_model, opt_.o.interpolation, lanes);
-    if (lanes != persistent_lanes_ || fast != persistent_fast_ || persistent_grid_ <= 0) {
+    // Staged tiles: occupancy of the widest-level variant (the engine's
+    // levels differ in width only by factors of two).
+    const int tile = (opt_.o.solver_mode == GBDIC_SOLVER_STAGED || opt_.o.solver_mode == GBDIC_SOLVER_STAGED_WIDE) &&
+                             icgn_staged_supported(opt_.o.motion_model, opt_.o.interpolation, lanes, 4)
+                         ? opt_.o.solver_mode - GBDIC_SOLVER_STAGED + 1
+                         : 0;
+    const int variant = fast ? 1 : (tile ? 1 + tile : 0);
+    if (lanes != persistent_lanes_ || variant != persistent_variant_ || persistent_grid_ <= 0) {
         const bool gauss = opt_.o.spatial_weighting == 1;
-        const int per_sm = fast ? icgn_fast_occupancy(opt_.o.motion_model, lanes, gauss)
-                                : icgn_occupancy(opt_.o.motion_model, opt_.o.interpolation, lanes, gauss);
+        const int per_sm = fast   ? icgn_fast_occupancy(opt_.o.motion_model, lanes, gauss)
+                           : tile ? icgn_staged_occupancy(opt_.o.motion_model, lanes, gauss, tile)
+                                  : icgn_occupancy(opt_.o.motion_model, opt_.o.interpolation, lanes, gauss);
         persistent_grid_ = std::max(1, per_sm) * sm_count_;
         persistent_lanes_ = lanes;
-        persistent_fast_ = fast;
+        persistent_variant_ = variant;
     }
     return persistent_grid_;
 }
@@ -420,6 +429,9 @@ SolveArgs Runtime::solve_args(Level &level, LevelSlot &slot, const gbdic_solver_
     a.div_min = opt_.o.divergence_min_iterations;
     a.persistent = opt_.o.persistent;
     a.fast_segments = fast_active() ? icgn_fast_segments(opt_.o.subset_size, opt_.lanes) : 0;
+    a.staged_tile = opt_.o.solver_mode == GBDIC_SOLVER_STAGED        ? 1
+                    : opt_.o.solver_mode == GBDIC_SOLVER_STAGED_WIDE ? 2
+                                                                     : 0;
     return a;
 }
 

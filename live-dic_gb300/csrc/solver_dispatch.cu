@@ -51,6 +51,8 @@ cudaError_t launch_icgn(const SolveArgs &a, int model, int interp, int lanes, bo
     if (grid <= 0) return cudaErrorInvalidConfiguration;
     if (a.fast_segments > 0 && icgn_fast_supported(model, interp, lanes))
         return launch_icgn_fast(a, model, lanes, gauss, grid, stream, nullptr);
+    if (a.staged_tile > 0 && icgn_staged_supported(model, interp, lanes, a.W))
+        return launch_icgn_staged(a, model, lanes, gauss, a.staged_tile, grid, stream, nullptr);
     return dispatch(a, model, interp, lanes, gauss, grid, stream, nullptr);
 }
 

@@ -471,9 +471,171 @@ __device__ __forceinline__ float2 sample_bspline_pair(const float *__restrict__ 
     return value;
 }
 
-template <int MODEL, int INTERP, int LANES, bool GAUSS, bool PART = false>
+// ---------------------------------------------------------------- staged tiles
+// Staged solver modes: each warp keeps one shared-memory tile of the
+// coefficient plane, TW x TH floats loaded by TMA (cp.async.bulk.tensor),
+// that covers the tap footprints of its subsets; the pixel loop samples from
+// the tile instead of global memory.  The tile is reloaded only when a
+// subset's footprint leaves it, so over a subset's iterations (whose warps
+// move by fractions of a pixel) it is usually loaded once.  A subset whose
+// footprint does not fit the tile samples from global memory that
+// iteration.  Values and arithmetic are those of the exact loop: results are
+// bit-identical to it.
+struct StageTile {
+    const void *map;  // CUtensorMap of the coefficient plane (box TW x TH)
+    float *tile;      // the warp's tile, TW x TH row-major, 128-byte aligned
+    uint64_t *bar;    // its mbarrier (one arrival + the tile's bytes)
+};
+struct StageState {
+    int tx0, ty0;     // tile origin (tx0 % 4 == 0: 16-byte TMA coordinate)
+    unsigned phase;   // parity of the next load's completion
+    bool valid;       // the tile holds the plane at (tx0, ty0)
+    bool broken;      // a load's wait expired: no further staging in this warp
+    bool pending;     // a load may still be landing (after an expired wait)
+};
+constexpr uint32_t kStageSpinLimit = 1u << 22;
+
+__device__ __forceinline__ bool stage_wait(uint64_t *bar, unsigned parity) {
+    const uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+    for (uint32_t i = 0; i < kStageSpinLimit; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Taps a subset's samples can touch under warp w, with a one-pixel margin:
+// x in [b0, b1], y in [b2, b3] (b0 > b1 when `none`).  The sample positions
+// are origin + (lx, ly) + displacement over |lx|, |ly| <= half.
+template <int MODEL>
+__device__ __forceinline__ void stage_box(const Warp &w, float ox, float oy, float half, bool none, int (&b)[4]) {
+    b[0] = 1 << 29; b[1] = -(1 << 29); b[2] = 1 << 29; b[3] = -(1 << 29);
+    if (none) return;
+    const float ex = half * (fabsf(1.0f + w.l0) + fabsf(w.l1));
+    const float ey = half * (fabsf(w.l2) + fabsf(1.0f + w.l3));
+    const float cx = ox + w.t0, cy = oy + w.t1;
+    const float x0 = floorf(cx - ex) - 2.0f, x1 = floorf(cx + ex) + 3.0f;
+    const float y0 = floorf(cy - ey) - 2.0f, y1 = floorf(cy + ey) + 3.0f;
+    if (!(x0 > -1e6f && x1 < 1e6f && y0 > -1e6f && y1 < 1e6f)) {
+        b[0] = -(1 << 29); b[1] = 1 << 29;  // never fits: sampled from global memory
+        b[2] = -(1 << 29); b[3] = 1 << 29;
+        return;
+    }
+    b[0] = (int)x0; b[1] = (int)x1; b[2] = (int)y0; b[3] = (int)y1;
+}
+
+// Tile origin for box b, or false when b does not fit a TW x TH tile.
+template <int TW, int TH>
+__device__ __forceinline__ bool stage_origin(const int (&b)[4], int &tx0, int &ty0) {
+    if (b[1] - b[0] + 1 > TW || b[3] - b[2] + 1 > TH) return false;
+    const int cx = b[0] - (TW - (b[1] - b[0] + 1)) / 2;
+    tx0 = cx - (((cx % 4) + 4) % 4);
+    ty0 = b[2] - (TH - (b[3] - b[2] + 1)) / 2;
+    return b[0] >= tx0 && b[1] < tx0 + TW;
+}
+
+template <int TW, int TH>
+__device__ __forceinline__ bool stage_contains(const StageState &ss, const int (&b)[4]) {
+    return ss.valid && b[0] >= ss.tx0 && b[1] < ss.tx0 + TW && b[2] >= ss.ty0 && b[3] < ss.ty0 + TH;
+}
+
+// Warp-uniform tile update at the top of an iteration: gathers the warp's
+// subset boxes (two per warp for 16 lanes), reloads the tile when a live
+// subset's box is outside it (over the union of the boxes when that fits,
+// else the first live subset's box) and returns whether this lane's subset
+// samples from the tile.
+template <int LANES, int TW, int TH>
+__device__ __forceinline__ bool stage_update(const StageTile &st, StageState &ss, const int (&b)[4],
+                                             int lane_in_warp) {
+    int A[4], B[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int o = LANES == 16 ? __shfl_xor_sync(kFullMask, b[k], 16) : b[k];
+        const bool upper = LANES == 16 && (lane_in_warp & 16);
+        A[k] = upper ? o : b[k];
+        B[k] = upper ? b[k] : o;
+    }
+    const bool liveA = A[0] <= A[1], liveB = LANES == 16 && B[0] <= B[1];
+    const bool need = (liveA && !stage_contains<TW, TH>(ss, A)) || (liveB && !stage_contains<TW, TH>(ss, B));
+    if (need && !ss.broken) {
+        int U[4] = {min(A[0], B[0]), max(A[1], B[1]), min(A[2], B[2]), max(A[3], B[3])};
+        if (!liveA) { U[0] = B[0]; U[1] = B[1]; U[2] = B[2]; U[3] = B[3]; }
+        if (!liveB) { U[0] = A[0]; U[1] = A[1]; U[2] = A[2]; U[3] = A[3]; }
+        int tx0 = 0, ty0 = 0;
+        bool ok = stage_origin<TW, TH>(U, tx0, ty0);
+        if (!ok && liveA) ok = stage_origin<TW, TH>(A, tx0, ty0);
+        if (!ok && liveB) ok = stage_origin<TW, TH>(B, tx0, ty0);
+        if (ok) {
+            // Every lane's reads of the old tile precede the asynchronous
+            // writes of the new one.
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            const uint32_t bar = static_cast<uint32_t>(__cvta_generic_to_shared(st.bar));
+            if (lane_in_warp == 0) {
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                             "r"((uint32_t)(TW * TH * 4))
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+                    "%4}], [%2];" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(st.tile))),
+                    "l"(reinterpret_cast<uint64_t>(st.map)), "r"(bar), "r"(tx0), "r"(ty0)
+                    : "memory");
+            }
+            int landed = 0;
+            if (lane_in_warp == 0) landed = stage_wait(st.bar, ss.phase) ? 1 : 0;
+            landed = __shfl_sync(kFullMask, landed, 0);
+            __syncwarp();
+            if (landed) {
+                ss.phase ^= 1u;
+                ss.valid = true;
+                ss.tx0 = tx0;
+                ss.ty0 = ty0;
+            } else {
+                ss.valid = false;
+                ss.broken = true;
+                ss.pending = true;
+            }
+        }
+        // else: no box fits; this iteration samples from global memory and
+        // the tile is kept for later subsets
+    }
+    return b[0] <= b[1] && stage_contains<TW, TH>(ss, b);
+}
+
+// sample_bspline_pair<false> from a staged tile whose origin is (tx0, ty0):
+// the same taps at tile-relative addresses, the same arithmetic.
+template <int TW>
+__device__ __forceinline__ float2 sample_bspline_pair_tile(const float *tile, int tx0, int ty0, float2 px, float2 py) {
+    const float fxa = floorf(px.x), fxb = floorf(px.y), fya = floorf(py.x), fyb = floorf(py.y);
+    const float2 m1 = pair(-1.0f);
+    float2 wx[4], wy[4];
+    bspline_weights2(fma2(make_float2(fxa, fxb), m1, px), wx);
+    bspline_weights2(fma2(make_float2(fya, fyb), m1, py), wy);
+    const float *ra = tile + ((int)fya - 1 - ty0) * TW + ((int)fxa - 1 - tx0);
+    const float *rb = tile + ((int)fyb - 1 - ty0) * TW + ((int)fxb - 1 - tx0);
+    float2 value = pair(0.0f);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float2 row = pair(0.0f);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) row = fma2(wx[i], make_float2(ra[i], rb[i]), row);
+        value = fma2(wy[j], row, value);
+        ra += TW;
+        rb += TW;
+    }
+    return value;
+}
+
+template <int MODEL, int INTERP, int LANES, bool GAUSS, bool PART = false, int TW = 0, int TH = 0>
 __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int glane, int lane_in_warp,
-                                            float *red) {
+                                            float *red, const StageTile *st = nullptr, StageState *ss = nullptr) {
     constexpr int N = SumCount<MODEL>::value;
     constexpr bool kBlock = LANES > 32;
     constexpr bool kClamp = MODEL == kModelQuadratic;
@@ -549,6 +711,14 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int g
         } else {
             if (__all_sync(kFullMask, done)) break;
         }
+        // Staged modes: the warp's tile covers this subset's taps this
+        // iteration (warp-uniform update; complete windows only).
+        bool staged = false;
+        if constexpr (TW > 0) {
+            int box[4];
+            stage_box<MODEL>(w, ox, oy, half, done, box);
+            staged = stage_update<LANES, TW, TH>(*st, *ss, box, lane_in_warp);
+        }
         float s[N];
 #pragma unroll
         for (int k = 0; k < N; ++k) s[k] = 0.0f;
@@ -583,8 +753,14 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int g
                         dx = add2(dx, fma2(pair(w.c0), hx2, fma2(pair(w.c1), xy, mul2(pair(w.c2), hy2))));
                         dy = add2(dy, fma2(pair(w.c3), hx2, fma2(pair(w.c4), xy, mul2(pair(w.c5), hy2))));
                     }
-                    const float2 g = sample_bspline_pair<kClamp>(a.coef, W, H, add2(add2(ox2, lx), dx),
-                                                                 add2(add2(oy2, ly), dy));
+                    const float2 spx = add2(add2(ox2, lx), dx), spy = add2(add2(oy2, ly), dy);
+                    float2 g;
+                    if constexpr (TW > 0) {
+                        g = staged ? sample_bspline_pair_tile<TW>(st->tile, ss->tx0, ss->ty0, spx, spy)
+                                   : sample_bspline_pair<kClamp>(a.coef, W, H, spx, spy);
+                    } else {
+                        g = sample_bspline_pair<kClamp>(a.coef, W, H, spx, spy);
+                    }
                     accumulate_pixel<MODEL, GAUSS, N>(s, a, g.x, ridx, p, lx.x, ly.x, ref_mean, hx2.x, xy.x, hy2.x);
                     accumulate_pixel<MODEL, GAUSS, N>(s, a, g.y, ridxb, p + LANES, lx.y, ly.y, ref_mean, hx2.y, xy.y,
                                                       hy2.y);

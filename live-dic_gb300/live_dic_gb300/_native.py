@@ -43,7 +43,7 @@ class Options(C.Structure):
     ]
 
 
-SOLVER_MODES = {"exact": 0, "fast": 1}
+SOLVER_MODES = {"exact": 0, "fast": 1, "staged": 2, "staged-wide": 3}
 
 
 class SolverCfg(C.Structure):

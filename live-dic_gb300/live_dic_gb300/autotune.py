@@ -10,9 +10,12 @@ grid, parameter RMSE <= 2e-3, max |difference| <= 2e-2), time the rest and
 keep the fastest.  Candidates: 16, 32, 64 or 128 lanes per subset with the
 exact pixel loop (the reference's pixel-to-lane order), and 16 or 32 lanes
 with the sliding-window loop (column runs sharing B-spline taps in
-registers; the engine runs it for B-spline translation / affine windows and
-falls back to the exact loop elsewhere), each as a grid launch or as a
-persistent grid over the work queue.
+registers) or with the exact loop on TMA-staged shared-memory tiles of the
+coefficient plane (staging axis; tile shape 56 x 44 or, "staged-wide",
+72 x 56 floats per warp); the engine runs the last two for B-spline
+translation / affine windows and falls back to the exact loop elsewhere.
+Each runs as a grid launch or as a persistent grid over the work queue
+(the wide tile as a grid launch only).
 """
 
 from __future__ import annotations
@@ -24,7 +27,9 @@ from statistics import median
 import numpy as np
 
 CANDIDATES = tuple((lanes, persistent, "exact") for persistent in (False, True) for lanes in (16, 32, 64, 128)) + \
-    tuple((lanes, persistent, "fast") for persistent in (False, True) for lanes in (16, 32))
+    tuple((lanes, persistent, "fast") for persistent in (False, True) for lanes in (16, 32)) + \
+    tuple((lanes, persistent, "staged") for persistent in (False, True) for lanes in (16, 32)) + \
+    tuple((lanes, False, "staged-wide") for lanes in (16, 32))
 
 
 def compare_solver_outputs(portable: np.ndarray, candidate: np.ndarray) -> dict:

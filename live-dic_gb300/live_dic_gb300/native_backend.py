@@ -74,10 +74,12 @@ def _normalize_solver_workgroup_size(value: int) -> int:
 def normalize_solver_mode(value: str) -> str:
     """Pixel loop of the IC-GN solver (no reference counterpart): 'exact'
     keeps the reference's pixel-to-lane order and summation, 'fast' runs the
-    sliding-window loop for B-spline translation / affine windows (other
-    configurations keep the exact loop)."""
+    sliding-window loop for B-spline translation / affine windows, 'staged'
+    and 'staged-wide' run the exact loop on taps staged by TMA in a per-warp
+    shared-memory tile (56 x 44 or 72 x 56 floats; bit-identical to 'exact').
+    Configurations a mode does not cover keep the exact loop."""
     if not isinstance(value, str) or value not in _native.SOLVER_MODES:
-        raise ValueError("solver_mode must be 'exact' or 'fast'")
+        raise ValueError("solver_mode must be 'exact', 'fast', 'staged' or 'staged-wide'")
     return value
 
 
