@@ -874,7 +874,9 @@ def main() -> None:
         traffic = json.loads(traffic_file.read_text()).get("icgn_solver_dram_bytes_per_launch")
     roofline = {
         "bound": "fp32",
-        "kernel": f"icgn_kernel<affine,bspline,{args.lanes} lanes> (all pyramid levels)",
+        "kernel": {"exact": "icgn_kernel", "fast": "icgn_fast_kernel", "staged": "icgn_staged_kernel",
+                   "staged-wide": "icgn_staged_kernel"}[args.solver_mode]
+        + f"<affine,bspline,{args.lanes} lanes> (all pyramid levels)",
         "achieved": achieved,
         "peak": peak.value,
         "unit": "TFLOP/s",
