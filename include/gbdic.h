@@ -428,7 +428,10 @@ typedef struct {
 
 /* Step modes: one persistent launch per class over the shared work queue, or
  * one grid launch per job in job order (the per-pair baseline). */
-enum { GBDIC_BATCH_PERSISTENT = 0, GBDIC_BATCH_PER_JOB = 1 };
+/* Step modes: PERSISTENT, one persistent launch per shape-function class
+ * (affine + translation, quadratic) on two graph branches; PER_JOB, one
+ * grid launch per job; SINGLE, one persistent launch over every job. */
+enum { GBDIC_BATCH_PERSISTENT = 0, GBDIC_BATCH_PER_JOB = 1, GBDIC_BATCH_SINGLE = 2 };
 
 int gbdic_batch_create(int32_t device, gbdic_batch **out);
 int gbdic_batch_destroy(gbdic_batch *batch);

@@ -42,8 +42,8 @@ struct gbdic_batch {
                 solve_end = nullptr;
     std::string error;
     std::vector<std::unique_ptr<BatchJobHost>> jobs;
-    int lanes = 16, mode = GBDIC_BATCH_PERSISTENT, ctas_per_sm = 0;
-    ClassQueue light, heavy;
+    int lanes = 16, mode = GBDIC_BATCH_SINGLE, ctas_per_sm = 0;
+    ClassQueue light, heavy, all;  // per-class queues, and the single queue
     gbdic::HostBuffer in, out;
     size_t in_bytes = 0, out_bytes = 0;
     cudaGraphExec_t host_graph = nullptr, device_graph = nullptr;
@@ -77,14 +77,24 @@ struct gbdic_batch {
     void rebuild() {
         if (!dirty) return;
         const int units = gbdic::batch_units(lanes);
-        for (int cls = 0; cls < 2; ++cls) {
-            ClassQueue &q = cls ? heavy : light;
+        // Queue 0: light class, 1: quadratic class, 2: every job (SINGLE).
+        for (int cls = 0; cls < 3; ++cls) {
+            ClassQueue &q = cls == 0 ? light : cls == 1 ? heavy : all;
             q.order.clear();
+            if ((cls == 2) != (mode == GBDIC_BATCH_SINGLE)) {
+                q.grid = 0;
+                continue;
+            }
             for (int j = 0; j < (int)jobs.size(); ++j)
-                if (is_quadratic(*jobs[j]) == (cls == 1)) q.order.push_back(j);
-            // Costliest subsets first so the cheap ones fill the tail.
+                if (cls == 2 || is_quadratic(*jobs[j]) == (cls == 1)) q.order.push_back(j);
+            // Costliest subsets first so the cheap ones fill the tail (a
+            // quadratic subset costs about 1.5 affine ones of its size).
             std::stable_sort(q.order.begin(), q.order.end(), [&](int a, int b) {
-                return jobs[a]->desc.subset_size > jobs[b]->desc.subset_size;
+                const double ca = (is_quadratic(*jobs[a]) ? 1.5 : 1.0) * jobs[a]->desc.subset_size *
+                                  jobs[a]->desc.subset_size;
+                const double cb = (is_quadratic(*jobs[b]) ? 1.5 : 1.0) * jobs[b]->desc.subset_size *
+                                  jobs[b]->desc.subset_size;
+                return ca > cb;
             });
             if (q.order.empty()) {
                 q.grid = 0;
@@ -112,7 +122,8 @@ struct gbdic_batch {
                        "batch table");
             check_cuda(cudaMemcpy(q.first.get(), first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice),
                        "batch table");
-            const int resident = gbdic::icgn_batch_occupancy(lanes, cls == 1);
+            const int resident =
+                cls == 2 ? gbdic::icgn_batch_any_occupancy(lanes) : gbdic::icgn_batch_occupancy(lanes, cls == 1);
             if (resident <= 0) fail(GBDIC_ECUDA, "batch solver occupancy query failed");
             const int per_sm = ctas_per_sm > 0 ? std::min(ctas_per_sm, resident) : resident;
             q.grid = per_sm * sm_count;
@@ -131,7 +142,8 @@ struct gbdic_batch {
         dirty = false;
     }
 
-    void launch_class(ClassQueue &q, bool quadratic, cudaStream_t s) {
+    // quadratic: 0 light class, 1 quadratic class, 2 every job.
+    void launch_class(ClassQueue &q, int quadratic, cudaStream_t s) {
         if (q.order.empty()) return;
         gbdic::BatchSolveArgs b{};
         b.args = q.args.as<gbdic::SolveArgs>();
@@ -140,7 +152,9 @@ struct gbdic_batch {
         b.work_counter = q.counter.as<unsigned>();
         b.jobs = (int)q.order.size();
         check_cuda(cudaMemsetAsync(q.counter.get(), 0, sizeof(unsigned), s), "queue reset");
-        check_cuda(gbdic::launch_icgn_batch(b, lanes, quadratic, q.grid, s), "batch solver launch");
+        check_cuda(quadratic == 2 ? gbdic::launch_icgn_batch_any(b, lanes, q.grid, s)
+                                  : gbdic::launch_icgn_batch(b, lanes, quadratic == 1, q.grid, s),
+                   "batch solver launch");
     }
 
     // Prefilter -> solver launches -> outlier passes on `s`; with `timed`,
@@ -151,18 +165,20 @@ struct gbdic_batch {
         if (mode == GBDIC_BATCH_PER_JOB) {
             for (auto &jp : jobs)
                 jp->rt->enqueue_solve(jp->level, *jp->level.slots[0], jp->desc.cfg, false, false, nullptr, nullptr, s);
+        } else if (mode == GBDIC_BATCH_SINGLE) {
+            launch_class(all, 2, s);
         } else {
             const bool both = !light.order.empty() && !heavy.order.empty();
             if (both) {
                 check_cuda(cudaEventRecord(fork, s), "fork");
                 check_cuda(cudaStreamWaitEvent(side, fork, 0), "fork");
-                launch_class(heavy, true, side);
-                launch_class(light, false, s);
+                launch_class(heavy, 1, side);
+                launch_class(light, 0, s);
                 check_cuda(cudaEventRecord(join, side), "join");
                 check_cuda(cudaStreamWaitEvent(s, join, 0), "join");
             } else {
-                launch_class(heavy, true, s);
-                launch_class(light, false, s);
+                launch_class(heavy, 1, s);
+                launch_class(light, 0, s);
             }
         }
         if (timed) check_cuda(cudaEventRecord(solve_end, s), "event");
@@ -329,7 +345,8 @@ int gbdic_batch_set_variant(gbdic_batch *b, int32_t lanes, int32_t mode, int32_t
     return guarded(b, [&] {
         if (lanes != 16 && lanes != 32 && lanes != 64 && lanes != 128)
             fail(GBDIC_EINVAL, "threads_per_subset must be 16, 32, 64, or 128");
-        if (mode != GBDIC_BATCH_PERSISTENT && mode != GBDIC_BATCH_PER_JOB) fail(GBDIC_EINVAL, "unknown batch mode");
+        if (mode != GBDIC_BATCH_PERSISTENT && mode != GBDIC_BATCH_PER_JOB && mode != GBDIC_BATCH_SINGLE)
+            fail(GBDIC_EINVAL, "unknown batch mode");
         if (ctas_per_sm < 0 || ctas_per_sm > 32) fail(GBDIC_EINVAL, "ctas_per_sm must be in [0, 32]");
         check_cuda(cudaStreamSynchronize(b->stream), "pending work");
         b->lanes = lanes;

@@ -57,6 +57,9 @@ int batch_units(int lanes);
 // Launches of the affine/translation class or of the quadratic class.
 int icgn_batch_occupancy(int lanes, bool quadratic);
 cudaError_t launch_icgn_batch(const BatchSolveArgs &b, int lanes, bool quadratic, int grid, cudaStream_t stream);
+// One launch over every class (the shape function dispatched per job).
+int icgn_batch_any_occupancy(int lanes);
+cudaError_t launch_icgn_batch_any(const BatchSolveArgs &b, int lanes, int grid, cudaStream_t stream);
 
 // ------------------------------------------------------------ UOD
 struct UodArgs {

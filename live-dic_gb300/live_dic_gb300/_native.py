@@ -126,7 +126,7 @@ class BatchJob(C.Structure):
     ]
 
 
-BATCH_PERSISTENT, BATCH_PER_JOB = 0, 1
+BATCH_PERSISTENT, BATCH_PER_JOB, BATCH_SINGLE = 0, 1, 2
 
 
 class ChooseCfg(C.Structure):

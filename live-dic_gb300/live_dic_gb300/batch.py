@@ -6,7 +6,9 @@ so its analogue of a batch is a loop of per-pair calls.  Here every job keeps
 the arithmetic of ICGNWGPU.register (B-spline interpolation, uniform
 weighting, zero seed, the job's outlier pass) and a step runs all jobs as one
 CUDA graph: every target's prefilter, one persistent IC-GN launch per
-shape-function class over a device work queue, then the outlier passes.
+shape-function class over a device work queue ("persistent"), or one
+persistent launch over every job with the shape function dispatched per job
+("single"), then the outlier passes.
 A job's result is bit-identical to ICGNWGPU.register with the same lanes per
 subset.
 
@@ -34,7 +36,7 @@ from .roi import prepare_roi, validate_roi
 from .subset import normalize_subset_size, normalize_subset_stride, subset_grid_shape
 
 _POLICY = {"disabled": 0, "replace": 1, "flag": 2}
-_MODES = {"persistent": _native.BATCH_PERSISTENT, "per-job": _native.BATCH_PER_JOB}
+_MODES = {"persistent": _native.BATCH_PERSISTENT, "per-job": _native.BATCH_PER_JOB, "single": _native.BATCH_SINGLE}
 LANE_CHOICES = (16, 32, 64, 128)
 
 
@@ -61,7 +63,7 @@ class ICGNBatch:
     """Many registration jobs of uneven image size, subset size and shape
     function, registered together."""
 
-    def __init__(self, *, device: int = 0, solver_workgroup_size: int = 16, mode: str = "persistent",
+    def __init__(self, *, device: int = 0, solver_workgroup_size: int = 16, mode: str = "single",
                  ctas_per_sm: int = 0) -> None:
         self._check_variant(solver_workgroup_size, mode, ctas_per_sm)
         self._lib = _native.load()
@@ -143,9 +145,11 @@ class ICGNBatch:
                               "tolerance": float(tolerance), "znccMin": float(zncc_min)})
         return int(index.value)
 
-    def set_variant(self, lanes: int, mode: str = "persistent", ctas_per_sm: int = 0) -> None:
-        """Lanes per subset, step mode ('persistent' queue or 'per-job'
-        launches) and persistent CTAs per SM (0: all resident)."""
+    def set_variant(self, lanes: int, mode: str = "single", ctas_per_sm: int = 0) -> None:
+        """Lanes per subset, step mode ('persistent': a persistent queue per
+        shape-function class, 'single': one persistent queue over every job,
+        'per-job': one launch per job) and persistent CTAs per SM (0: all
+        resident)."""
         self._require_open()
         self._check_variant(lanes, mode, ctas_per_sm)
         self._check(self._lib.gbdic_batch_set_variant(self._handle, int(lanes), _MODES[mode], int(ctas_per_sm)))
@@ -154,7 +158,7 @@ class ICGNBatch:
     @property
     def variant_name(self) -> str:
         lanes, mode, ctas = self.variant
-        return f"{lanes}-lane {mode}" + (f" {ctas}/SM" if ctas and mode == "persistent" else "")
+        return f"{lanes}-lane {mode}" + (f" {ctas}/SM" if ctas and mode != "per-job" else "")
 
     # ------------------------------------------------------------ steps
     def _register_packed(self, targets) -> tuple[list[np.ndarray], dict[str, float]]:
@@ -223,7 +227,8 @@ class ICGNBatch:
         whose fields pass the reference's solver acceptance rule
         (wgpu_backend.py:222-299) against the per-job 32-lane baseline."""
         if candidates is None:
-            candidates = [(lanes, "persistent", ctas) for lanes in LANE_CHOICES for ctas in (0, 2)]
+            candidates = [(lanes, mode, ctas) for mode in ("persistent", "single") for lanes in LANE_CHOICES
+                          for ctas in (0, 2)]
             candidates += [(lanes, "per-job", 0) for lanes in LANE_CHOICES]
         self.set_variant(32, "per-job", 0)
         baseline, _ = self._register_packed(targets)

@@ -1,8 +1,8 @@
 """Batched registration of uneven jobs: every job's field must be
 bit-identical to a solo ICGNWGPU.register with the same lanes per subset,
 whatever the step mode (one persistent launch per shape-function class over
-the work queue, or one launch per job), and the resident path must agree
-with the host path."""
+the work queue, one persistent launch over every job, or one launch per
+job), and the resident path must agree with the host path."""
 
 from __future__ import annotations
 
@@ -52,15 +52,23 @@ def _packed(result):
 def test_batch_matches_solo_engines(pairs, lanes):
     expected = [_solo(job, lanes) for job in pairs]
     with _batch(pairs, solver_workgroup_size=lanes) as batch:
+        assert batch.variant[1] == "single"
+        batch.set_variant(lanes, "persistent")
         persistent = batch.register([j["target"] for j in pairs])
         batch.set_variant(lanes, "per-job")
         per_job = batch.register([j["target"] for j in pairs])
         batch.set_variant(lanes, "persistent", 1)
         one_cta = batch.register([j["target"] for j in pairs])
+        batch.set_variant(lanes, "single")
+        single = batch.register([j["target"] for j in pairs])
+        batch.set_variant(lanes, "single", 1)
+        single_one_cta = batch.register([j["target"] for j in pairs])
     for k, job in enumerate(pairs):
         np.testing.assert_array_equal(_packed(persistent[k]), expected[k], err_msg=f"job {k} ({job['motion_model']})")
         np.testing.assert_array_equal(_packed(per_job[k]), expected[k])
         np.testing.assert_array_equal(_packed(one_cta[k]), expected[k])
+        np.testing.assert_array_equal(_packed(single[k]), expected[k], err_msg=f"job {k} ({job['motion_model']})")
+        np.testing.assert_array_equal(_packed(single_one_cta[k]), expected[k])
 
 
 def test_batch_accuracy_and_roi(pairs):
@@ -104,7 +112,8 @@ def test_batch_autotuner_keeps_a_valid_variant(pairs):
         best = batch.autotune([j["target"] for j in pairs], repeats=1)
         assert batch.validation[batch.variant_name]["valid"]
         assert best == batch.variant
-        assert len(batch.tuning_ms) == 12  # 4 lane counts x (persistent, persistent 2/SM, per-job)
+        # 4 lane counts x (persistent, persistent 2/SM, single, single 2/SM, per-job)
+        assert len(batch.tuning_ms) == 20
 
 
 def test_batch_argument_errors(pairs):
