@@ -529,8 +529,17 @@ int gbdic_fourier_shift_device(gbdic_fourier *f, const uint8_t *frame, int64_t r
         // The caller's stream orders everything: the transform buffers belong
         // to this handle, so calls on one handle must not overlap.
         cudaStream_t s = static_cast<cudaStream_t>(stream);
-        check_cuda(cudaEventRecord(f->fork, f->stream), "event");
-        check_cuda(cudaStreamWaitEvent(s, f->fork, 0), "event wait");
+        // Outside a stream capture the call is ordered after the handle's own
+        // stream (host-path estimates) and before its later work; inside a
+        // capture (a CUDA graph of the caller's frame) the graph's launches
+        // are ordered by the caller, and the handle's stream stays out of it.
+        cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+        check_cuda(cudaStreamIsCapturing(s, &capture), "capture query");
+        const bool capturing = capture != cudaStreamCaptureStatusNone;
+        if (!capturing) {
+            check_cuda(cudaEventRecord(f->fork, f->stream), "event");
+            check_cuda(cudaStreamWaitEvent(s, f->fork, 0), "event wait");
+        }
         check_cuda(cudaMemcpy2DAsync(f->window.get(), n, frame + (size_t)y * row_stride + x, (size_t)row_stride, n, n,
                                      cudaMemcpyDeviceToDevice, s), "window copy");
         f->spectrum_of(f->window.as<uint8_t>(), nullptr, f->cur_samples.as<double>(), nullptr, s);
@@ -554,8 +563,10 @@ int gbdic_fourier_shift_device(gbdic_fourier *f, const uint8_t *frame, int64_t r
             check_cuda(cudaGetLastError(), "shift rows");
         }
         // Later host-path estimates on the handle's own stream wait for this one.
-        check_cuda(cudaEventRecord(f->join, s), "event");
-        check_cuda(cudaStreamWaitEvent(f->stream, f->join, 0), "event wait");
+        if (!capturing) {
+            check_cuda(cudaEventRecord(f->join, s), "event");
+            check_cuda(cudaStreamWaitEvent(f->stream, f->join, 0), "event wait");
+        }
     });
 }
 

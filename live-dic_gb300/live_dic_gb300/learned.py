@@ -598,10 +598,12 @@ class LearnedSeeder:
     between them), IC-GN on the lattice nodes from those proposals (with
     `refine_nodes`), every subset seeded by interpolation of the node warps,
     seeded IC-GN, and ZNCC reseeding of failed or low-ZNCC subsets.  Every
-    step runs on the device in stream order, without host round trips."""
+    step runs on the device in stream order, without host round trips; with
+    `graph` (the default) register_device captures that sequence once as a
+    CUDA graph (frame read from a fixed buffer) and replays it per frame."""
 
     def __init__(self, engine, net: SeedNet, *, step: int = 4, reseed_radius: int = 10, passes: int = 2,
-                 global_alignment: bool = True, refine_nodes: bool = True) -> None:
+                 global_alignment: bool = True, refine_nodes: bool = True, graph: bool = True) -> None:
         torch = _torch()
         if not engine._reference_ready or engine.motion_model != "affine":
             raise ValueError("LearnedSeeder needs an affine engine with a prepared reference")
@@ -665,6 +667,10 @@ class LearnedSeeder:
         self._node_active = torch.from_numpy(node_active.ravel()).to(dev)
         self._shifted = False
         self.reseed_count = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.graph = bool(graph)
+        self._graph = None       # captured frame sequence, and what it was captured for
+        self._graph_key = None
+        self._graph_frame = None  # the fixed frame buffer the graph reads
 
     def set_reference_image(self, reference: np.ndarray) -> None:
         """Half-resolution reference for the network (the engine keeps its own),
@@ -674,6 +680,7 @@ class LearnedSeeder:
         is resolved to 4 frame pixels, well inside the network's range)."""
         torch = _torch()
 
+        self._drop_graph()
         self._ref_full.copy_(torch.from_numpy(np.ascontiguousarray(reference, dtype=np.uint8)))
         _call(self.lib, "gbdic_reduce_half", _ptr(self._ref_full), self.W, self.H, _ptr(self.ref_half), None)
         self.global_shift.close()
@@ -750,13 +757,47 @@ class LearnedSeeder:
         """Learned-seed registration of a device frame into self.state (on
         self.stream; callers synchronise or wait on it).  The number of
         reseeded subsets stays in self.reseed_count (device); with `counts`
-        it is also returned (one host synchronisation), else None."""
+        it is also returned (one host synchronisation), else None.
+
+        With `graph`, the first call for a given engine configuration runs
+        the sequence once directly, then captures it as a CUDA graph that
+        reads the frame from a fixed device buffer; later calls copy the
+        frame there and replay the graph.  The graph is captured again when
+        the reference, the engine's solver settings or `reseed` change."""
         torch = _torch()
         self.stream.wait_stream(torch.cuda.current_stream(self.net.device))
-        with torch.cuda.stream(self.stream):
-            self._register(frame, reseed, self._handle)
+        if self.graph:
+            key = (bool(reseed), tuple(sorted(self.engine._config.items())), self.engine.solver,
+                   tuple(frame.shape), frame.dtype)
+            if self._graph is None or self._graph_key != key:
+                self._capture(frame, bool(reseed), key)
+            with torch.cuda.stream(self.stream):
+                self._graph_frame.copy_(frame)
+                self._graph.replay()
+        else:
+            with torch.cuda.stream(self.stream):
+                self._register(frame, reseed, self._handle)
         torch.cuda.current_stream(self.net.device).wait_stream(self.stream)
         return {"reseeded": int(self.reseed_count.item()) if counts and reseed else (0 if counts else None)}
+
+    def _capture(self, frame, reseed: bool, key) -> None:
+        torch = _torch()
+        self._drop_graph()
+        self._graph_frame = torch.empty_like(frame)
+        with torch.cuda.stream(self.stream):
+            self._graph_frame.copy_(frame)
+            # one direct run: lazy set-up (kernel attributes, occupancy
+            # queries, tensor-map entry points) stays out of the capture
+            self._register(self._graph_frame, reseed, self._handle)
+        self.stream.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=self.stream):
+            self._register(self._graph_frame, reseed, self._handle)
+        self._graph, self._graph_key = graph, key
+
+    def _drop_graph(self) -> None:
+        self._graph = None
+        self._graph_key = None
 
     def _register(self, frame, reseed: bool, stream) -> None:
         eng = self.engine

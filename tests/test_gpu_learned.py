@@ -325,3 +325,33 @@ def test_learned_seeding_on_a_non_affine_field():
     gap = np.hypot(state[..., 0] - seeded.displacement[..., 0], state[..., 3] - seeded.displacement[..., 1])[both]
     assert np.percentile(gap, 99) < 0.01, np.percentile(gap, 99)
     assert stats["reseeded"] < 0.1 * inside.sum()
+
+
+def test_graph_replay_matches_the_direct_sequence():
+    """The learned frame captured as a CUDA graph (frame read from a fixed
+    buffer) gives the direct sequence's states and reseed counts bit for bit,
+    frame after frame, and again after the reference is replaced.  An
+    untrained network is enough: what is checked is the identity of the
+    two paths."""
+    net = learned.SeedNet(batch=128, seed=3)
+    W, H = 512, 384
+    ref, sp = synthetic.reference_image(W, H, seed=31, device="cuda")
+    moves = [(3.2, -1.4), (6.1, 2.2), (-4.5, 5.0)]
+    frames = [torch.from_numpy(synthetic.deformed_image(sp, synthetic.affine_field(dx, 2e-3, 0.0, dy, 0.0, -1e-3),
+                                                        noise_seed=40 + k, device="cuda")).cuda()
+              for k, (dx, dy) in enumerate(moves)]
+    with ICGNWGPU(subset_size=31, subset_stride=8) as engine:
+        engine.set_reference(ref, iterations=16, tolerance=5e-3)
+        seeders = {g: learned.LearnedSeeder(engine, net, step=4, graph=g) for g in (False, True)}
+        for rnd in range(2):
+            for s in seeders.values():
+                s.set_reference_image(ref if rnd == 0 else frames[0].cpu().numpy())
+            for f in frames:
+                out = {}
+                for g, s in seeders.items():
+                    stats = s.register_device(f)
+                    torch.cuda.synchronize()
+                    out[g] = (s.state.cpu().numpy().copy(), stats["reseeded"])
+                np.testing.assert_array_equal(out[True][0], out[False][0])
+                assert out[True][1] == out[False][1]
+        assert seeders[True]._graph is not None and seeders[False]._graph is None
