@@ -225,6 +225,30 @@ int gbdic_resolve_seeded_device(gbdic_engine *engine, const uint8_t *device_fram
 int gbdic_search_seeds_device(gbdic_engine *engine, const uint8_t *device_frame, float *device_seed,
                               uint32_t *device_active, const uint8_t *device_mask, int32_t radius, int32_t centered,
                               void *stream);
+/* The same search for the subsets device_list[0 .. *device_list_count)
+ * (device count, e.g. from gbdic_nn_reseed_select_list), on a fixed grid
+ * that strides over the list instead of one CTA per subset of the grid. */
+int gbdic_search_seeds_listed_device(gbdic_engine *engine, const uint8_t *device_frame, float *device_seed,
+                                     uint32_t *device_active, const int32_t *device_list,
+                                     const uint32_t *device_list_count, int32_t radius, int32_t centered,
+                                     void *stream);
+/* Seeded solve of the listed subsets only: device_list[0 .. list_length),
+ * or [0 .. min(list_length, *device_list_count)) when device_list_count is
+ * not NULL (then one persistent launch over the list), with
+ * threads_per_subset lanes per subset (16, 32, 64, 128; 0: the engine's).
+ * Equal, bit for bit, to gbdic_register_seeded_device (prefilter != 0) or
+ * gbdic_resolve_seeded_device (prefilter == 0) of an engine running the
+ * same lanes, with the same seed and activity, when the list holds exactly
+ * the active subsets (any order): every other row is written as those
+ * calls write a disabled subset, then the listed ones are solved with the
+ * exact pixel loop, then the outlier pass runs over the whole grid.
+ * Complete windows only (no partial-support reference).  Few listed
+ * subsets run latency-bound; more lanes per subset shorten each
+ * iteration. */
+int gbdic_solve_listed_device(gbdic_engine *engine, const uint8_t *device_frame, const float *device_seed,
+                              const uint32_t *device_active, const int32_t *device_list, int32_t list_length,
+                              const uint32_t *device_list_count, int32_t prefilter, int32_t threads_per_subset,
+                              const gbdic_solver_cfg *cfg, float *device_state, void *stream);
 
 /* Copies an internal buffer (GBDIC_EXPORT_*) to host memory. */
 int gbdic_export(gbdic_engine *engine, int32_t what, void *host_out, int64_t bytes);
@@ -624,6 +648,11 @@ int gbdic_nn_consensus(const float *pred, float *base, int32_t ldp, int32_t node
  * for those, 0 else; *counter (device, may be NULL) = their number. */
 int gbdic_nn_reseed_select(const float *state, int32_t row_floats, const uint8_t *usable, int32_t count,
                            uint8_t *mask, uint32_t *active, uint32_t *counter, void *stream);
+/* The same selection, also appending the selected subset indices to `list`
+ * (device, `count` entries of room; order arbitrary; *counter = their
+ * number), for gbdic_search_seeds_listed_device / gbdic_solve_listed_device. */
+int gbdic_nn_reseed_select_list(const float *state, int32_t row_floats, const uint8_t *usable, int32_t count,
+                                uint8_t *mask, uint32_t *active, uint32_t *counter, int32_t *list, void *stream);
 /* Lattice rows of `pred` (layout of gbdic_nn_lattice_seeds) from solved
  * node subsets: node (lx, ly) is grid subset (lx * step, ly * step) of the
  * affine state field `state` (8 floats per subset); where that subset

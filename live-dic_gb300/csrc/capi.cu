@@ -519,6 +519,62 @@ int gbdic_resolve_seeded_device(gbdic_engine *e, const uint8_t *device_frame, co
     });
 }
 
+int gbdic_solve_listed_device(gbdic_engine *e, const uint8_t *device_frame, const float *device_seed,
+                              const uint32_t *device_active, const int32_t *device_list, int32_t list_length,
+                              const uint32_t *device_list_count, int32_t prefilter, int32_t threads_per_subset,
+                              const gbdic_solver_cfg *cfg, float *device_state, void *stream) {
+    return guarded(e, [&] {
+        e->require_ready("solve_listed");
+        gbdic::validate_cfg(cfg);
+        if (!device_frame || !device_seed || !device_active || !device_state || (!device_list && list_length > 0))
+            fail(GBDIC_EINVAL, "device frame, seed, activity, list and state are required");
+        auto &rt = *e->rt;
+        auto &lvl = e->level;
+        auto &slot = *lvl.slots[0];
+        if (list_length < 0 || list_length > lvl.count) fail(GBDIC_EINVAL, "list_length must be in [0, subsets]");
+        cudaStream_t s = stream ? (cudaStream_t)stream : rt.stream();
+        const size_t sb = (size_t)lvl.count * gbdic::state_stride(rt.opts().o.motion_model) * sizeof(float);
+        check_cuda(cudaMemcpyAsync(slot.seed.get(), device_seed, sb, cudaMemcpyDeviceToDevice, s), "seed copy");
+        check_cuda(cudaMemcpyAsync(slot.active.get(), device_active, (size_t)lvl.count * sizeof(uint32_t),
+                                   cudaMemcpyDeviceToDevice, s), "activity copy");
+        if (prefilter) rt.enqueue_prefilter(lvl, slot, device_frame, s);
+        const bool disabled = rt.opts().o.outlier_policy == GBDIC_OUTLIER_DISABLED;
+        rt.enqueue_solve_list(lvl, slot, *cfg, reinterpret_cast<const int *>(device_list), list_length,
+                              reinterpret_cast<const unsigned *>(device_list_count), threads_per_subset,
+                              device_frame, disabled ? device_state : nullptr, s);
+        if (!disabled) rt.enqueue_uod(lvl, slot, false, device_state, s);
+    });
+}
+
+int gbdic_search_seeds_listed_device(gbdic_engine *e, const uint8_t *device_frame, float *device_seed,
+                                     uint32_t *device_active, const int32_t *device_list,
+                                     const uint32_t *device_list_count, int32_t radius, int32_t centered,
+                                     void *stream) {
+    return guarded(e, [&] {
+        e->require_ready("seed search");
+        auto &lvl = e->level;
+        if (!device_frame || !device_seed || !device_active || !device_list || !device_list_count)
+            fail(GBDIC_EINVAL, "device frame, seed, activity, list and list count are required");
+        if (!lvl.ref_image.get()) fail(GBDIC_ESTATE, "seed search needs a reference prepared by set_reference()");
+        const auto &o = e->rt->opts().o;
+        if (radius < 1 || gbdic::zncc_search_smem(o.subset_size, radius) > 48 * 1024)
+            fail(GBDIC_EINVAL, "radius must be >= 1 and its search tile must fit 48 KB of shared memory");
+        gbdic::SearchArgs q{};
+        q.ref = lvl.ref_image.as<uint8_t>();
+        q.tgt = device_frame;
+        q.seed = device_seed;
+        q.active = device_active;
+        q.selected = lvl.roi && lvl.selected.get() ? lvl.selected.as<uint8_t>() : nullptr;
+        q.W = lvl.W; q.H = lvl.H; q.grid_w = lvl.gw; q.count = lvl.count;
+        q.S = o.subset_size; q.stride = o.subset_stride; q.radius = radius; q.model = o.motion_model;
+        q.centered = centered ? 1 : 0;
+        q.subset_list = reinterpret_cast<const int *>(device_list);
+        q.list_count = reinterpret_cast<const unsigned *>(device_list_count);
+        cudaStream_t s = stream ? (cudaStream_t)stream : e->rt->stream();
+        check_cuda(gbdic::launch_zncc_search(q, s), "seed search launch");
+    });
+}
+
 int gbdic_search_seeds_device(gbdic_engine *e, const uint8_t *device_frame, float *device_seed,
                               uint32_t *device_active, const uint8_t *device_mask, int32_t radius, int32_t centered,
                               void *stream) {

@@ -140,6 +140,15 @@ class Runtime {
     // slot's queue head; the persistent flag of the current variant).
     SolveArgs solve_args(Level &level, LevelSlot &slot, const gbdic_solver_cfg &cfg, bool seeded,
                          bool preserve, const uint8_t *frame, float *state) const;
+    // Seeded solve of the listed subsets only (list[0 .. length), or
+    // list[0 .. min(length, *list_count)) when list_count is set): every row
+    // first as a disabled subset, then the exact loop over the list.  Equal
+    // to enqueue_solve(seeded) when the list holds exactly the active
+    // subsets and the same lanes per subset (`lanes`, 0: the engine's);
+    // complete windows only.
+    void enqueue_solve_list(Level &level, LevelSlot &slot, const gbdic_solver_cfg &cfg, const int *list,
+                            int length, const unsigned *list_count, int lanes, const uint8_t *frame, float *state,
+                            cudaStream_t stream);
     void enqueue_uod(Level &level, LevelSlot &slot, bool seed_mode, float *out, cudaStream_t stream);
     const float *output_state(LevelSlot &slot) const;
     void upload_frame(Level &level, LevelSlot &slot, const uint8_t *frame, int64_t row_stride,

@@ -166,6 +166,11 @@ struct SolveArgs {
     // Staged tiles (solver_staged.cu): 0 off, 1 compact (56 x 44 floats per
     // warp), 2 wide (72 x 56).
     int staged_tile;
+    // List mode (exact loop, complete windows): group g solves subset
+    // subset_list[g] for g < count, or g < min(count, *list_count) when
+    // list_count is set (a device count written by an earlier kernel).
+    const int *subset_list;
+    const unsigned *list_count;
 };
 
 }  // namespace gbdic

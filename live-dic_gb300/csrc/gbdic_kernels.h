@@ -23,6 +23,9 @@ int icgn_grid(int count, int lanes);
 int icgn_occupancy(int model, int interp, int lanes, bool gauss);
 cudaError_t launch_icgn(const SolveArgs &a, int model, int interp, int lanes, bool gauss,
                         int persistent_grid, cudaStream_t stream);
+// Rows 0 .. total-1 of a.state as the seeded solver writes disabled subsets
+// (from a.seed, a.active, a.meta); list-mode solves start from them.
+cudaError_t launch_disabled_rows(const SolveArgs &a, int model, int total, cudaStream_t stream);
 // Sliding-window ("fast") pixel loop: supported configurations, the row
 // segments per column that minimise its steps, its launcher (grid as for
 // launch_icgn; with occupancy_only set, the resident CTAs per SM instead).
@@ -147,6 +150,10 @@ struct SearchArgs {
     int only_missing;         // search only seeds whose status slot is -1
     int centered;             // shifts around the rounded seed translation
     const uint8_t *subset_mask;  // search only where non-zero, or nullptr
+    // List mode: search only the subsets subset_list[0 .. *list_count)
+    // (a device count, at most `count`), on a fixed grid.
+    const int *subset_list;
+    const unsigned *list_count;
 };
 size_t zncc_search_smem(int S, int radius);
 cudaError_t launch_zncc_search(const SearchArgs &a, cudaStream_t stream);
@@ -284,7 +291,7 @@ struct NnConv1Weights {
 cudaError_t launch_nn_conv_c2_direct(const NnConvShape &sh, const void *x, const NnConv1Weights &w, void *y,
                                      cudaStream_t s);
 cudaError_t launch_nn_reseed_select(const float *state, int row_floats, const uint8_t *usable, int count,
-                                    uint8_t *mask, uint32_t *active, unsigned *counter, cudaStream_t s);
+                                    uint8_t *mask, uint32_t *active, unsigned *counter, int *list, cudaStream_t s);
 cudaError_t launch_nn_node_rows(const float *state, int grid_w, int grid_h, int step, int lattice_w, int lattice_h,
                                 float *pred, const float *base, int ldp, float translation_scale, float gradient_scale,
                                 cudaStream_t s);

@@ -198,8 +198,17 @@ int gbdic_nn_consensus(const float *pred, float *base, int32_t ldp, int32_t node
 int gbdic_nn_reseed_select(const float *state, int32_t row_floats, const uint8_t *usable, int32_t count,
                            uint8_t *mask, uint32_t *active, uint32_t *counter, void *stream) {
     if (!state || !mask || !active || row_floats < 7 || count < 0) return invalid("invalid reseed selection arguments");
-    return rc(gbdic::launch_nn_reseed_select(state, row_floats, usable, count, mask, active, counter,
+    return rc(gbdic::launch_nn_reseed_select(state, row_floats, usable, count, mask, active, counter, nullptr,
                                              as_stream(stream)),
+              "reseed selection");
+}
+
+int gbdic_nn_reseed_select_list(const float *state, int32_t row_floats, const uint8_t *usable, int32_t count,
+                                uint8_t *mask, uint32_t *active, uint32_t *counter, int32_t *list, void *stream) {
+    if (!state || !mask || !active || !counter || !list || row_floats < 7 || count < 0)
+        return invalid("invalid reseed selection arguments");
+    return rc(gbdic::launch_nn_reseed_select(state, row_floats, usable, count, mask, active, counter,
+                                             reinterpret_cast<int *>(list), as_stream(stream)),
               "reseed selection");
 }
 

@@ -646,8 +646,10 @@ __global__ void __launch_bounds__(kConsensusThreads) consensus_kernel(NnConsensu
 // Subsets to reseed: not converged (status 0) or converged below the ZNCC
 // threshold (-2), among usable subsets; mask / activity 1 for those, 0 else,
 // and their count.
+// With `list`, the picked indices are also appended to it (one atomicAdd
+// per warp; the order across warps is arbitrary).
 __global__ void reseed_select_kernel(const float *state, int row_floats, const uint8_t *usable, int count,
-                                     uint8_t *mask, uint32_t *active, unsigned *counter) {
+                                     uint8_t *mask, uint32_t *active, unsigned *counter, int *list) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool pick = false;
     if (i < count) {
@@ -656,8 +658,13 @@ __global__ void reseed_select_kernel(const float *state, int row_floats, const u
         mask[i] = pick ? 1 : 0;
         active[i] = pick ? 1u : 0u;
     }
-    const unsigned votes = __popc(__ballot_sync(0xffffffffu, pick));
-    if ((threadIdx.x & 31) == 0 && votes && counter) atomicAdd(counter, votes);
+    const unsigned ballot = __ballot_sync(0xffffffffu, pick);
+    const unsigned votes = __popc(ballot);
+    const int lane = threadIdx.x & 31;
+    unsigned base = 0u;
+    if (lane == 0 && votes && counter) base = atomicAdd(counter, votes);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (list && pick) list[base + __popc(ballot & ((1u << lane) - 1u))] = i;
 }
 
 // dst row i = src row i where mask[i] (rows of row_floats floats).
@@ -876,13 +883,15 @@ cudaError_t launch_nn_consensus(const NnConsensusArgs &a, cudaStream_t s) {
 }
 
 cudaError_t launch_nn_reseed_select(const float *state, int row_floats, const uint8_t *usable, int count,
-                                    uint8_t *mask, uint32_t *active, unsigned *counter, cudaStream_t s) {
+                                    uint8_t *mask, uint32_t *active, unsigned *counter, int *list, cudaStream_t s) {
+    if (list && !counter) return cudaErrorInvalidValue;
     if (counter) {
         const cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
         if (e != cudaSuccess) return e;
     }
     if (count <= 0) return cudaSuccess;
-    reseed_select_kernel<<<blocks(count, 256), 256, 0, s>>>(state, row_floats, usable, count, mask, active, counter);
+    reseed_select_kernel<<<blocks(count, 256), 256, 0, s>>>(state, row_floats, usable, count, mask, active, counter,
+                                                            list);
     return cudaGetLastError();
 }
 

@@ -504,6 +504,36 @@ void Runtime::profile_read(double &solver_ms, long long &launches, long long &ti
                    "profile readback");
 }
 
+void Runtime::enqueue_solve_list(Level &level, LevelSlot &slot, const gbdic_solver_cfg &cfg, const int *list,
+                                 int length, const unsigned *list_count, int lanes, const uint8_t *frame, float *state,
+                                 cudaStream_t s) {
+    if (level.partial_count > 0) fail(GBDIC_EINVAL, "listed solves need a reference without partial-support windows");
+    if (lanes == 0) lanes = opt_.lanes;
+    if (lanes != 16 && lanes != 32 && lanes != 64 && lanes != 128)
+        fail(GBDIC_EINVAL, "threads_per_subset must be 16, 32, 64, or 128");
+    SolveArgs a = solve_args(level, slot, cfg, true, false, frame, state);
+    a.fast_segments = 0;
+    a.staged_tile = 0;
+    const int model = opt_.o.motion_model, interp = opt_.o.interpolation;
+    check_cuda(launch_disabled_rows(a, model, level.count, s), "disabled rows");
+    if (length <= 0) return;
+    a.subset_list = list;
+    a.list_count = list_count;
+    a.count = length;
+    int grid = 0;
+    const bool gauss = opt_.o.spatial_weighting == 1;
+    if (list_count != nullptr) {
+        // a device-side length: a persistent grid over the list
+        a.persistent = 1;
+        const int per_sm = icgn_occupancy(model, interp, lanes, gauss);
+        grid = std::max(1, per_sm) * sm_count_;
+        check_cuda(cudaMemsetAsync(slot.counter.get(), 0, sizeof(unsigned), s), "queue reset");
+    } else {
+        a.persistent = 0;
+    }
+    check_cuda(launch_icgn(a, model, interp, lanes, gauss, grid, s), "listed solver launch");
+}
+
 void Runtime::enqueue_uod(Level &level, LevelSlot &slot, bool seed_mode, float *out, cudaStream_t s) {
     if (opt_.o.outlier_policy == GBDIC_OUTLIER_DISABLED) return;
     UodArgs u{};

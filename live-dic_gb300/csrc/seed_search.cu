@@ -30,10 +30,9 @@ namespace {
 __host__ __device__ inline int ref_words(int S) { return (S + 3) / 4; }
 __host__ __device__ inline int tile_words(int S, int R) { return (S + 2 * R + 3) / 4 + 1; }
 
-__global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
-    extern __shared__ uint32_t smem_words[];
-    const int idx = blockIdx.x;
-    if (idx >= a.count) return;
+// The search of subset idx by the whole CTA (every return is CTA-uniform).
+__device__ void search_one(const SearchArgs &a, int idx, uint32_t *smem_words, double *s_best, int *s_cand) {
+    if (idx < 0 || idx >= a.count) return;
     const int ss = state_stride(a.model), sat = status_slot(a.model);
     float *seed = a.seed + (size_t)idx * ss;
     if (a.only_missing && seed[sat] != -1.0f) return;  // block-uniform
@@ -50,8 +49,6 @@ __global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
     const int px0 = (idx % a.grid_w) * a.stride + cx0, py0 = (idx / a.grid_w) * a.stride + cy0;
     const int rx0 = (idx % a.grid_w) * a.stride, ry0 = (idx / a.grid_w) * a.stride;
     const int tid = threadIdx.x;
-    __shared__ double s_best[128];
-    __shared__ int s_cand[128];
     if (!selected) {
         if (!a.only_missing && tid == 0) {
             for (int k = 0; k < ss; ++k) seed[k] = 0.0f;
@@ -152,6 +149,23 @@ __global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
     }
 }
 
+// One CTA per subset, or (list mode) a fixed grid striding over the first
+// *list_count entries of subset_list.
+__global__ void __launch_bounds__(128) zncc_search_kernel(SearchArgs a) {
+    extern __shared__ uint32_t smem_words[];
+    __shared__ double s_best[128];
+    __shared__ int s_cand[128];
+    if (a.subset_list == nullptr) {
+        search_one(a, blockIdx.x, smem_words, s_best, s_cand);
+        return;
+    }
+    const int live = min(a.count, (int)*a.list_count);
+    for (int i = blockIdx.x; i < live; i += gridDim.x) {
+        search_one(a, a.subset_list[i], smem_words, s_best, s_cand);
+        __syncthreads();  // the tiles and the candidate table are reused
+    }
+}
+
 }  // namespace
 
 size_t zncc_search_smem(int S, int radius) {
@@ -163,7 +177,9 @@ cudaError_t launch_zncc_search(const SearchArgs &a, cudaStream_t stream) {
     if (a.count <= 0) return cudaSuccess;
     const size_t smem = zncc_search_smem(a.S, a.radius);
     if (smem > 48 * 1024) return cudaErrorInvalidValue;
-    zncc_search_kernel<<<a.count, 128, smem, stream>>>(a);
+    if (a.subset_list != nullptr && a.list_count == nullptr) return cudaErrorInvalidValue;
+    const int grid = a.subset_list != nullptr ? (a.count < 1024 ? a.count : 1024) : a.count;
+    zncc_search_kernel<<<grid, 128, smem, stream>>>(a);
     return cudaGetLastError();
 }
 

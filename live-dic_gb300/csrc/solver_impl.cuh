@@ -643,9 +643,12 @@ __device__ __forceinline__ void solve_group(const SolveArgs &a, int group, int g
     // complete windows.
     constexpr bool kPair = GBDIC_SOLVER_PAIRS && INTERP == kInterpBspline && !PART &&
                            (MODEL != kModelQuadratic || GBDIC_QUAD_PAIRS);
-    const bool exists = group < a.count;
-    // Partial windows: group -> window index; support words and box.
-    const int idx = PART ? (exists ? __ldg(a.partial_index + group) : 0) : group;
+    const int live = (!PART && a.list_count != nullptr) ? min(a.count, (int)__ldg(a.list_count)) : a.count;
+    const bool exists = group < live;
+    // Partial windows: group -> window index; support words and box.  List
+    // mode: group -> listed subset.
+    const int idx = PART ? (exists ? __ldg(a.partial_index + group) : 0)
+                         : (a.subset_list != nullptr ? (exists ? __ldg(a.subset_list + group) : 0) : group);
     const uint32_t *support = PART ? a.support + (size_t)(exists ? group : 0) * a.support_words : nullptr;
     const float4 box = PART ? __ldg(a.support_box + (exists ? group : 0)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const int sidx = exists ? idx : 0;
@@ -834,6 +837,7 @@ __global__ void __launch_bounds__(128, MODEL == kModelQuadratic ? GBDIC_QUAD_MIN
     const int units_per_block = 128 / kUnitThreads;
     const long long unit = (long long)blockIdx.x * units_per_block + tid / kUnitThreads;
     float *red = red_smem + (kBlock ? group_in_unit * LANES * N : 0);
+    const int count = (!PART && a.list_count != nullptr) ? min(a.count, (int)__ldg(a.list_count)) : a.count;
     for (;;) {
         int base;
         if (a.persistent) {
@@ -848,9 +852,9 @@ __global__ void __launch_bounds__(128, MODEL == kModelQuadratic ? GBDIC_QUAD_MIN
                 base = __shfl_sync(kFullMask, v, 0);
             }
         } else {
-            base = unit * kGroups < (long long)a.count ? (int)(unit * kGroups) : a.count;
+            base = unit * kGroups < (long long)count ? (int)(unit * kGroups) : count;
         }
-        if (base >= a.count) break;
+        if (base >= count) break;
         solve_group<MODEL, INTERP, LANES, GAUSS, PART>(a, base + group_in_unit, glane, lane_in_warp, red);
         if (!a.persistent) break;
     }

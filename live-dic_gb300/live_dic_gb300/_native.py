@@ -224,11 +224,14 @@ _SIGNATURES = {
     "gbdic_nn_conv_c2_direct": (C.c_int, [C.POINTER(NnConvShape), P, P, P, P, P]),
     "gbdic_nn_consensus": (C.c_int, [P, P, I32, I32, P, P, I32, P, I32, P, I32, P, I32, C.c_float, P]),
     "gbdic_nn_reseed_select": (C.c_int, [P, I32, P, I32, P, P, P, P]),
+    "gbdic_nn_reseed_select_list": (C.c_int, [P, I32, P, I32, P, P, P, P, P]),
     "gbdic_nn_merge_rows": (C.c_int, [P, P, I32, I32, P, P]),
     "gbdic_nn_node_rows": (C.c_int, [P, I32, I32, I32, I32, I32, P, P, I32, C.c_float, C.c_float, P]),
     "gbdic_register_seeded_device": (C.c_int, [P, P, P, P, C.POINTER(SolverCfg), P, P]),
     "gbdic_resolve_seeded_device": (C.c_int, [P, P, P, P, C.POINTER(SolverCfg), P, P]),
     "gbdic_search_seeds_device": (C.c_int, [P, P, P, P, P, I32, I32, P]),
+    "gbdic_search_seeds_listed_device": (C.c_int, [P, P, P, P, P, P, I32, I32, P]),
+    "gbdic_solve_listed_device": (C.c_int, [P, P, P, P, P, I32, P, I32, I32, C.POINTER(SolverCfg), P, P]),
     "gbdic_pyramid_set_translation": (C.c_int, [P, I32, C.c_float, C.c_float]),
     "gbdic_set_partial_support": (C.c_int, [P, I32, P, P, I32, P, P, P]),
     "gbdic_field_summary": (C.c_int, [P, I64, I32, I32, P, P, P, C.POINTER(I64), C.POINTER(I64)]),

@@ -600,10 +600,17 @@ class LearnedSeeder:
     seeded IC-GN, and ZNCC reseeding of failed or low-ZNCC subsets.  Every
     step runs on the device in stream order, without host round trips; with
     `graph` (the default) register_device captures that sequence once as a
-    CUDA graph (frame read from a fixed buffer) and replays it per frame."""
+    CUDA graph (frame read from a fixed buffer) and replays it per frame.
+    With `listed` (the default) the node solve, the reseeding search and the
+    reseeding solve run over compact subset lists (the nodes; the subsets
+    the selection picked, counted on the device) instead of masked
+    full-grid launches, with `list_lanes` lanes per subset (these few
+    subsets run latency-bound: more lanes shorten each iteration; the fields
+    are those of masked full-grid solves at that lane count, bit for bit)."""
 
     def __init__(self, engine, net: SeedNet, *, step: int = 4, reseed_radius: int = 10, passes: int = 2,
-                 global_alignment: bool = True, refine_nodes: bool = True, graph: bool = True) -> None:
+                 global_alignment: bool = True, refine_nodes: bool = True, graph: bool = True,
+                 listed: bool = True, list_lanes: int = 128) -> None:
         torch = _torch()
         if not engine._reference_ready or engine.motion_model != "affine":
             raise ValueError("LearnedSeeder needs an affine engine with a prepared reference")
@@ -665,6 +672,12 @@ class LearnedSeeder:
         node_active = np.zeros((self.gh, self.gw), np.int32)
         node_active[::self.step, ::self.step] = 1
         self._node_active = torch.from_numpy(node_active.ravel()).to(dev)
+        self.listed = bool(listed)
+        if list_lanes not in (0, 16, 32, 64, 128):
+            raise ValueError("list_lanes must be 0 (the engine's), 16, 32, 64 or 128")
+        self.list_lanes = int(list_lanes)
+        self._node_list = torch.from_numpy(np.flatnonzero(node_active.ravel()).astype(np.int32)).to(dev)
+        self._reseed_list = torch.zeros(self.gh * self.gw, dtype=torch.int32, device=dev)
         self._shifted = False
         self.reseed_count = torch.zeros(1, dtype=torch.int32, device=dev)
         self.graph = bool(graph)
@@ -813,8 +826,13 @@ class LearnedSeeder:
             # keeps the network's warp.
             node_cfg = eng._cfg(eng._config)
             node_cfg.iterations = min(int(node_cfg.iterations), NODE_ITERATIONS)
-            _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self._node_active),
-                         C.byref(node_cfg), _ptr(self.state), stream)
+            if self.listed:
+                _call_engine(eng, "gbdic_solve_listed_device", _ptr(frame), _ptr(self.seeds), _ptr(self._node_active),
+                             _ptr(self._node_list), int(self._node_list.numel()), None, 1, self.list_lanes,
+                             C.byref(node_cfg), _ptr(self.state), stream)
+            else:
+                _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds),
+                             _ptr(self._node_active), C.byref(node_cfg), _ptr(self.state), stream)
             _call(self.lib, "gbdic_nn_node_rows", _ptr(self.state), self.gw, self.gh, self.step, self.lw, self.lh,
                   _ptr(self.pred), _ptr(self.base) if self._shifted else None, OUT_PAD, C.c_float(TRANSLATION_SCALE),
                   C.c_float(GRADIENT_SCALE), stream)
@@ -832,12 +850,21 @@ class LearnedSeeder:
         # cannot be rescued by a search.  No host round trip: an empty
         # selection costs three near-empty launches.
         count = self.gh * self.gw
-        _call(self.lib, "gbdic_nn_reseed_select", _ptr(self.state), 8, _ptr(self._usable8), count, _ptr(self.mask),
-              _ptr(self.active), _ptr(self.reseed_count), stream)
-        _call_engine(eng, "gbdic_search_seeds_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active),
-                     _ptr(self.mask), self.radius, 1, stream)
-        _call_engine(eng, "gbdic_resolve_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
-                     _ptr(self._retry), stream)
+        if self.listed:
+            _call(self.lib, "gbdic_nn_reseed_select_list", _ptr(self.state), 8, _ptr(self._usable8), count,
+                  _ptr(self.mask), _ptr(self.active), _ptr(self.reseed_count), _ptr(self._reseed_list), stream)
+            _call_engine(eng, "gbdic_search_seeds_listed_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active),
+                         _ptr(self._reseed_list), _ptr(self.reseed_count), self.radius, 1, stream)
+            _call_engine(eng, "gbdic_solve_listed_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active),
+                         _ptr(self._reseed_list), count, _ptr(self.reseed_count), 0, self.list_lanes, cfg,
+                         _ptr(self._retry), stream)
+        else:
+            _call(self.lib, "gbdic_nn_reseed_select", _ptr(self.state), 8, _ptr(self._usable8), count,
+                  _ptr(self.mask), _ptr(self.active), _ptr(self.reseed_count), stream)
+            _call_engine(eng, "gbdic_search_seeds_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active),
+                         _ptr(self.mask), self.radius, 1, stream)
+            _call_engine(eng, "gbdic_resolve_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
+                         _ptr(self._retry), stream)
         _call(self.lib, "gbdic_nn_merge_rows", _ptr(self._retry), _ptr(self.mask), count, 8, _ptr(self.state), stream)
 
 

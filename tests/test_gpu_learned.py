@@ -327,12 +327,13 @@ def test_learned_seeding_on_a_non_affine_field():
     assert stats["reseeded"] < 0.1 * inside.sum()
 
 
-def test_graph_replay_matches_the_direct_sequence():
+def test_graph_replay_and_listed_solves_match_the_direct_sequence():
     """The learned frame captured as a CUDA graph (frame read from a fixed
-    buffer) gives the direct sequence's states and reseed counts bit for bit,
-    frame after frame, and again after the reference is replaced.  An
-    untrained network is enough: what is checked is the identity of the
-    two paths."""
+    buffer), and the node solve / reseeding run over compact subset lists,
+    give the direct masked full-grid sequence's states and reseed counts bit
+    for bit, frame after frame, and again after the reference is replaced.
+    An untrained network is enough (it leaves many subsets to reseed): what
+    is checked is the identity of the paths."""
     net = learned.SeedNet(batch=128, seed=3)
     W, H = 512, 384
     ref, sp = synthetic.reference_image(W, H, seed=31, device="cuda")
@@ -340,9 +341,17 @@ def test_graph_replay_matches_the_direct_sequence():
     frames = [torch.from_numpy(synthetic.deformed_image(sp, synthetic.affine_field(dx, 2e-3, 0.0, dy, 0.0, -1e-3),
                                                         noise_seed=40 + k, device="cuda")).cuda()
               for k, (dx, dy) in enumerate(moves)]
-    with ICGNWGPU(subset_size=31, subset_stride=8) as engine:
+    for lanes in (16, 128):
+        _graph_and_list_identity(net, ref, frames, lanes)
+
+
+def _graph_and_list_identity(net, ref, frames, lanes):
+    # masked full-grid solves at the engine's lane count vs listed solves at
+    # the same lane count (list_lanes = lanes)
+    with ICGNWGPU(subset_size=31, subset_stride=8, solver_workgroup_size=lanes) as engine:
         engine.set_reference(ref, iterations=16, tolerance=5e-3)
-        seeders = {g: learned.LearnedSeeder(engine, net, step=4, graph=g) for g in (False, True)}
+        seeders = {(g, l): learned.LearnedSeeder(engine, net, step=4, graph=g, listed=l, list_lanes=lanes)
+                   for g, l in ((False, False), (True, True), (False, True))}
         for rnd in range(2):
             for s in seeders.values():
                 s.set_reference_image(ref if rnd == 0 else frames[0].cpu().numpy())
@@ -352,6 +361,9 @@ def test_graph_replay_matches_the_direct_sequence():
                     stats = s.register_device(f)
                     torch.cuda.synchronize()
                     out[g] = (s.state.cpu().numpy().copy(), stats["reseeded"])
-                np.testing.assert_array_equal(out[True][0], out[False][0])
-                assert out[True][1] == out[False][1]
-        assert seeders[True]._graph is not None and seeders[False]._graph is None
+                base = out[(False, False)]
+                assert base[1] > 0
+                for key in ((True, True), (False, True)):
+                    np.testing.assert_array_equal(out[key][0], base[0], err_msg=str(key))
+                    assert out[key][1] == base[1]
+        assert seeders[(True, True)]._graph is not None and seeders[(False, True)]._graph is None
