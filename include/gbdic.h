@@ -564,9 +564,9 @@ typedef struct {
  * mode 1, A[m][k] = the im2col row of the input, as gbdic_nn_im2col writes
  * it (M = B*OH*OW, K = Kp, C % 8 == 0); mode 2, A[m][k] = the data-gradient
  * gather of the output gradient, as gbdic_nn_dgrad_gather writes it
- * (M = B*H*W, K = 9*Cout, Cout % 8 == 0).  k_split must be 1.  Results are
- * those of gbdic_nn_gemm on the materialised matrix, which is never
- * written. */
+ * (M = B*H*W, K = 9*Cout, Cout % 8 == 0).  k_split may exceed 1 in mode 1
+ * only (partials as for gbdic_nn_gemm).  Results are those of
+ * gbdic_nn_gemm on the materialised matrix, which is never written. */
 int gbdic_nn_conv_gemm(const gbdic_nn_gemm_desc *desc, int32_t mode, const gbdic_nn_conv_shape *shape,
                        int32_t *device_error, void *stream);
 /* Forward GEMM operand A[(b, oy, ox)][(ky, kx, ci)] (zero beyond 9 C). */
@@ -596,6 +596,11 @@ int gbdic_nn_bias_grad(const float *dy, int32_t ld, const void *y, int64_t rows,
  * ld % 4 == 0, rows % 8 == 0 when dz_t != NULL. */
 int gbdic_nn_relu_bias_backward(const float *dy, int32_t ld, const void *y, int64_t rows, int32_t cols, void *dz,
                                 void *dz_t, float *partial, float *db, void *stream);
+/* y (BF16, rows x cols) = relu?(sum_s partial[s] + bias) over `splits` FP32
+ * partials rows x cols, split_stride floats apart (summed in split order):
+ * the epilogue of a split-K gbdic_nn_gemm / gbdic_nn_conv_gemm. */
+int gbdic_nn_splitk_bias_relu(const float *partial, int32_t splits, int64_t rows, int32_t cols, int64_t split_stride,
+                              const float *bias, int32_t relu, void *y, void *stream);
 /* a_t (rows_padded x B*OH*OW) = the im2col operand of x (gbdic_nn_im2col)
  * transposed, zero in rows >= 9 C, without writing the operand itself
  * (the weight-gradient GEMM's A); rows_padded % 64 == 0, B*OH*OW % 8 == 0. */

@@ -243,6 +243,9 @@ cudaError_t launch_nn_transpose(const void *src, int R, int C, int ld_src, void 
 // column sums; partial: C x ceil(rows / 64) FP32 scratch.
 cudaError_t launch_nn_relu_bias_backward(const float *dy, int ld, const void *y, long long rows, int C, void *dz,
                                         void *dzt, float *partial, float *db, cudaStream_t s);
+// y (BF16 rows x N) = relu(sum of `splits` FP32 partials + bias).
+cudaError_t launch_nn_splitk_bias_relu(const float *partial, int splits, long long rows, int N, long long split_stride,
+                                      const float *bias, int relu, void *y, cudaStream_t s);
 // At (Kt x M) = the im2col operand of x transposed, without writing it.
 cudaError_t launch_nn_im2col_t(const NnConvShape &sh, const void *x, void *At, int Kt, cudaStream_t s);
 cudaError_t launch_nn_relu_backward(const float *dy, int ld, const void *y, void *dz, long long rows, int C,

@@ -58,7 +58,7 @@ int gbdic_nn_conv_gemm(const gbdic_nn_gemm_desc *d, int32_t mode, const gbdic_nn
     a.gather = mode;
     a.conv = shape_of(s);
     return rc(gbdic::launch_tc_gemm(a, as_stream(stream)),
-              "implicit convolution GEMM (rows and K of the convolution, C or Cout % 8, k_split 1)");
+              "implicit convolution GEMM (rows and K of the convolution, C or Cout % 8, k_split 1 for mode 2)");
 }
 
 int gbdic_nn_patches(const uint8_t *const *refs, const uint8_t *const *tgts, const int32_t *image_index,
@@ -121,6 +121,13 @@ int gbdic_nn_relu_bias_backward(const float *dy, int32_t ld, const void *y, int6
         return invalid("invalid ReLU/bias backward arguments");
     return rc(gbdic::launch_nn_relu_bias_backward(dy, ld, y, rows, cols, dz, dz_t, partial, db, as_stream(stream)),
               "ReLU/bias backward (cols a power of two 4..256, ld % 4 == 0, rows % 8 == 0 with dz_t, aligned)");
+}
+
+int gbdic_nn_splitk_bias_relu(const float *partial, int32_t splits, int64_t rows, int32_t cols, int64_t split_stride,
+                              const float *bias, int32_t relu, void *y, void *stream) {
+    return rc(gbdic::launch_nn_splitk_bias_relu(partial, splits, rows, cols, split_stride, bias, relu, y,
+                                                as_stream(stream)),
+              "split-K epilogue (cols % 4 == 0, split_stride >= rows * cols, aligned)");
 }
 
 int gbdic_nn_im2col_t(const gbdic_nn_conv_shape *s, const void *x, void *a_t, int32_t rows_padded, void *stream) {

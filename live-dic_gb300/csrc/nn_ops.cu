@@ -285,6 +285,27 @@ __global__ void __launch_bounds__(256) relu_bias_backward_kernel(const float *dy
     }
 }
 
+// y[m][n] = BF16(relu(sum_s partial[s][m][n] + bias[n])) for split-K
+// convolution outputs (splits ascending), 4 columns per thread.
+__global__ void splitk_bias_relu_kernel(const float *partial, int splits, long long rows, int N,
+                                        long long split_stride, const float *bias, int relu, __nv_bfloat16 *y) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // float4 index
+    if (q >= rows * N / 4) return;
+    float4 acc = reinterpret_cast<const float4 *>(partial)[q];
+    for (int s = 1; s < splits; ++s) {
+        const float4 v = reinterpret_cast<const float4 *>(partial + s * split_stride)[q];
+        acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
+    }
+    const int n = (int)((4 * q) % N);
+    if (bias) { acc.x += bias[n]; acc.y += bias[n + 1]; acc.z += bias[n + 2]; acc.w += bias[n + 3]; }
+    if (relu) { acc.x = fmaxf(acc.x, 0.0f); acc.y = fmaxf(acc.y, 0.0f); acc.z = fmaxf(acc.z, 0.0f); acc.w = fmaxf(acc.w, 0.0f); }
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(acc.x, acc.y), hi = __floats2bfloat162_rn(acc.z, acc.w);
+    uint2 out;
+    out.x = *reinterpret_cast<const uint32_t *>(&lo);
+    out.y = *reinterpret_cast<const uint32_t *>(&hi);
+    reinterpret_cast<uint2 *>(y)[q] = out;
+}
+
 // db[c] = sum over tiles of partial[c * tiles + tile]: one CTA per column,
 // thread t the tiles t, t + 256, ... in order, then a fixed tree.
 __global__ void __launch_bounds__(256) bias_reduce_kernel(const float *partial, int tiles, float *db) {
@@ -830,6 +851,17 @@ cudaError_t launch_nn_relu_bias_backward(const float *dy, int ld, const void *y,
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     bias_reduce_kernel<<<C, 256, 0, s>>>(partial, (int)tiles, db);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_splitk_bias_relu(const float *partial, int splits, long long rows, int N, long long split_stride,
+                                      const float *bias, int relu, void *y, cudaStream_t s) {
+    if (!partial || !y || splits < 1 || rows <= 0 || N <= 0 || N % 4 || split_stride < rows * N ||
+        split_stride % 4 || ((reinterpret_cast<uintptr_t>(partial) & 15) | (reinterpret_cast<uintptr_t>(y) & 7)))
+        return cudaErrorInvalidValue;
+    const long long n = rows * N / 4;
+    splitk_bias_relu_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(partial, splits, rows, N, split_stride, bias,
+                                                                        relu, static_cast<__nv_bfloat16 *>(y));
     return cudaGetLastError();
 }
 

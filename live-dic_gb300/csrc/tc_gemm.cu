@@ -527,8 +527,11 @@ cudaError_t launch_tc_gemm(const TcGemmArgs &a, cudaStream_t stream) {
     if (a.gather != kGatherNone) {
         // The gathered operand's rows and reduction length must be the
         // convolution's exactly (every row and chunk maps into the tensor).
+        // k_split > 1 (partials per split, as for a plain GEMM) for the
+        // im2col gather only.
         const NnConvShape &s = a.conv;
-        if (a.k_split != 1 || s.B < 1 || s.H < 1 || s.W < 1 || s.OH != (s.H + 1) / 2 || s.OW != (s.W + 1) / 2)
+        if ((a.k_split != 1 && a.gather != kGatherIm2col) || s.B < 1 || s.H < 1 || s.W < 1 ||
+            s.OH != (s.H + 1) / 2 || s.OW != (s.W + 1) / 2)
             return cudaErrorInvalidValue;
         // chunk offsets are 32-bit in the kernel
         if (a.gather == kGatherIm2col) {

@@ -208,6 +208,7 @@ _SIGNATURES = {
     "gbdic_nn_gemm": (C.c_int, [C.POINTER(NnGemmDesc), P, P]),
     "gbdic_nn_conv_gemm": (C.c_int, [C.POINTER(NnGemmDesc), I32, C.POINTER(NnConvShape), P, P]),
     "gbdic_nn_relu_bias_backward": (C.c_int, [P, I32, P, I64, I32, P, P, P, P, P]),
+    "gbdic_nn_splitk_bias_relu": (C.c_int, [P, I32, I64, I32, I64, P, I32, P, P]),
     "gbdic_nn_im2col_t": (C.c_int, [C.POINTER(NnConvShape), P, P, I32, P]),
     "gbdic_nn_patches": (C.c_int, [P, P, P, P, I32, I32, I32, P, P, I32, C.c_float, P]),
     "gbdic_nn_im2col": (C.c_int, [C.POINTER(NnConvShape), P, P, P]),

@@ -94,9 +94,11 @@ class _Conv:
 
 class SeedNet:
     """The proposal network and its optimiser state on one CUDA device.
-    ``batch`` (a multiple of 128) fixes the buffer shapes."""
+    ``batch`` (a multiple of 128) fixes the buffer shapes.  ``split_forward``
+    (inference copies) runs the deep gathered layers split-K; it changes the
+    forward's summation order, so training keeps it off."""
 
-    def __init__(self, batch: int = 512, *, device: int = 0, seed: int = 0) -> None:
+    def __init__(self, batch: int = 512, *, device: int = 0, seed: int = 0, split_forward: bool = False) -> None:
         torch = _torch()
         if batch <= 0 or batch % 128:
             raise ValueError("batch must be a positive multiple of 128")
@@ -143,6 +145,12 @@ class SeedNet:
         # it inside the GEMM
         self.a = [torch.zeros(c.M, c.kp, dtype=bf16, device=dev) if c.cin % 8 else None for c in self.convs]
         self.y = [torch.zeros(c.M, c.cout, dtype=bf16, device=dev) for c in self.convs]
+        # Split-K forward for the gathered layers whose output tiles would not
+        # fill one wave of CTAs (the deep layers at small batches): FP32
+        # partials, then one fixed-order reduction with bias and ReLU.
+        self.fwd_splits = [self._forward_splits(c) if split_forward and c.cin % 8 == 0 else 1 for c in self.convs]
+        self.fwd_partial = [torch.zeros(s, c.M, c.cout, dtype=f32, device=dev) if s > 1 else None
+                            for s, c in zip(self.fwd_splits, self.convs, strict=True)]
         self.out = torch.zeros(batch, OUT_PAD, dtype=f32, device=dev)
         # backward buffers (allocated on first backward)
         self._bwd = None
@@ -202,7 +210,14 @@ class SeedNet:
                       stream)
                 x = self.y[0]
                 continue
-            if c.cin % 8 == 0:
+            if c.cin % 8 == 0 and self.fwd_splits[i] > 1:
+                # implicit GEMM, split K, then bias + ReLU over the partials
+                s, part = self.fwd_splits[i], self.fwd_partial[i]
+                self._gemm(x, self.wb[i], c.M, c.cout, c.kp, d_f32=part, k_split=s, split_stride=c.M * c.cout,
+                           stream=stream, gather=1, shape=self._shape(i))
+                _call(self.lib, "gbdic_nn_splitk_bias_relu", _ptr(part), s, c.M, c.cout, c.M * c.cout, _ptr(self.b[i]),
+                      1, _ptr(self.y[i]), stream)
+            elif c.cin % 8 == 0:
                 # implicit GEMM: the im2col rows are gathered in the kernel
                 self._gemm(x, self.wb[i], c.M, c.cout, c.kp, d_bf16=self.y[i], bias=self.b[i], relu=True,
                            stream=stream, gather=1, shape=self._shape(i))
@@ -235,6 +250,19 @@ class SeedNet:
         bufs["partial"] = [torch.zeros(s, c.kp_rows, c.cout, dtype=f32, device=dev)
                            for s, c in zip(bufs["splits"], self.convs, strict=True)]
         return bufs
+
+    @staticmethod
+    def _forward_splits(c: _Conv, sms: int = 152) -> int:
+        """Smallest divisor s of the K blocks with (output tiles) x s >= one
+        wave of CTAs (1 when the tiles already fill it)."""
+        tiles = (c.M // 128) * max(1, c.cout // min(128, c.cout))
+        blocks = c.kp // 64
+        if tiles >= sms:
+            return 1
+        for s in range(2, blocks + 1):
+            if blocks % s == 0 and tiles * s >= sms:
+                return s
+        return blocks
 
     @staticmethod
     def _splits(c: _Conv) -> int:
@@ -648,7 +676,7 @@ class LearnedSeeder:
         self.mask = torch.zeros(self.gh * self.gw, dtype=torch.uint8, device=dev)
         # Inference copy of the network sized to the whole lattice: one
         # forward per pass.
-        self.inet = SeedNet(batch=_pad(self.lattice, 128), device=net.device.index or 0)
+        self.inet = SeedNet(batch=_pad(self.lattice, 128), device=net.device.index or 0, split_forward=True)
         self.inet.load_state_dict(net.state_dict())
         self.inet.use_direct_first_layer()
         self.batches = 1

@@ -285,6 +285,27 @@ def test_direct_first_layer_matches_the_gemm_path():
     np.testing.assert_allclose(direct.out[:, :6].cpu().numpy(), gemm.out[:, :6].cpu().numpy(), rtol=2e-2, atol=2e-2)
 
 
+def test_split_k_forward_matches_the_single_pass_forward():
+    """The inference copies' split-K deep layers (FP32 partials, ordered sum,
+    bias and ReLU) against the single-pass tcgen05 epilogue on the same
+    weights and patches: identical up to the FP32 summation order before
+    BF16 rounding."""
+    plain = learned.SeedNet(batch=128, seed=3)
+    split = learned.SeedNet(batch=128, seed=3, split_forward=True)
+    assert max(split.fwd_splits) > 1 and max(plain.fwd_splits) == 1
+    rng = np.random.default_rng(10)
+    x = torch.from_numpy(rng.normal(size=(128, 64, 64, 2)).astype(np.float32)).to(torch.bfloat16).cuda()
+    plain.x0.copy_(x)
+    split.x0.copy_(x)
+    plain.forward()
+    split.forward()
+    torch.cuda.synchronize()
+    for a, b in zip(plain.y, split.y, strict=True):
+        a, b = a.float(), b.float()
+        assert ((a - b).abs() <= 1e-2 * a.abs() + 1e-3).float().mean().item() > 0.999
+    np.testing.assert_allclose(split.out[:, :6].cpu().numpy(), plain.out[:, :6].cpu().numpy(), rtol=2e-2, atol=2e-2)
+
+
 def test_learned_seeding_on_a_non_affine_field():
     """Large translation plus sinusoidal deformation (no global affine
     model fits it): the consensus only recentres the second pass, the lattice

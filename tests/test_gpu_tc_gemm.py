@@ -148,6 +148,41 @@ def test_implicit_dgrad_gemm_equals_materialised_operand(B, H, Cin, Cout):
     assert torch.equal(got, want)
 
 
+@pytest.mark.parametrize("B,H,Cin,Cout,splits", [(512, 8, 128, 128, 3), (512, 4, 128, 64, 18), (128, 8, 64, 128, 9)])
+def test_split_k_implicit_im2col_gemm(B, H, Cin, Cout, splits):
+    """Split-K implicit GEMM: every split's partial equals the materialised
+    split GEMM's bit for bit, and the split-K epilogue gives bias + ReLU of
+    their ordered sum in BF16."""
+    lib = _native.load()
+    shape, g = _conv_case(B, H, Cin, Cout, B + H + splits)
+    M = B * shape.OH * shape.OW
+    x = torch.randn(B, H, H, Cin, generator=g, device="cuda").to(torch.bfloat16)
+    w = torch.randn(Cout, shape.Kp, generator=g, device="cuda").to(torch.bfloat16)
+    bias = torch.randn(Cout, generator=g, device="cuda")
+    a = torch.empty(M, shape.Kp, dtype=torch.bfloat16, device="cuda")
+    _native.check(lib.gbdic_nn_im2col(C.byref(shape), C.c_void_p(x.data_ptr()), C.c_void_p(a.data_ptr()), None),
+                  lib.gbdic_last_error(None))
+    want = torch.empty(splits, M, Cout, device="cuda")
+    _gemm(a, w, d_f32=want, k_split=splits, split_stride=M * Cout)
+    got = torch.empty(splits, M, Cout, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    desc = _native.NnGemmDesc(x.data_ptr(), w.data_ptr(), M, Cout, shape.Kp, splits, got.data_ptr(), None, Cout,
+                              M * Cout, None, 0, 0)
+    _native.check(lib.gbdic_nn_conv_gemm(C.byref(desc), 1, C.byref(shape), C.c_void_p(err.data_ptr()), None),
+                  lib.gbdic_last_error(None))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    assert torch.equal(got, want)
+    y = torch.empty(M, Cout, dtype=torch.bfloat16, device="cuda")
+    _native.check(lib.gbdic_nn_splitk_bias_relu(C.c_void_p(got.data_ptr()), splits, M, Cout, M * Cout,
+                                                C.c_void_p(bias.data_ptr()), 1, C.c_void_p(y.data_ptr()), None),
+                  lib.gbdic_last_error(None))
+    total = got[0].clone()
+    for s in range(1, splits):
+        total += got[s]
+    assert torch.equal(y, torch.relu(total + bias).to(torch.bfloat16))
+
+
 def test_implicit_conv_gemm_rejects_mismatched_shapes():
     x = torch.zeros(2, 16, 16, 32, dtype=torch.bfloat16, device="cuda")
     w = torch.zeros(64, 320, dtype=torch.bfloat16, device="cuda")
