@@ -672,6 +672,9 @@ def measure_learned(args, local: int, *, steps: int, warmup: int) -> dict:
             reseeded.append(int(seeder.reseed_count.item()))
 
         learned_times, learned_acc = run(learned_step, engine.grid_height, engine.grid_width, learned_count)
+        # stage breakdown (CUDA events, the direct sequence) over the timed frames
+        stage_runs = [seeder.stage_times(frames[k]) for k in range(warmup, warmup + min(steps, 5))]
+        stages = {name: float(np.median([r[name] for r in stage_runs])) for name in stage_runs[0]}
         engine.close()
     lt, pt = float(np.mean(learned_times)), float(np.mean(plain_times))
     return {
@@ -701,6 +704,9 @@ def measure_learned(args, local: int, *, steps: int, warmup: int) -> dict:
                          "field, outliers = the accepted rest",
         "reseeded_per_frame": float(np.mean(reseeded)) if reseeded else None,
         "timing": "host clock around each synchronised frame (both methods include their host-side steps)",
+        "learned_stage_ms": stages,
+        "learned_stage_note": "median CUDA-event time per stage of the direct (not graph-replayed) sequence over "
+                              "up to 5 timed frames",
         "train_pairs": int(data.size), "train_images": args.train_images, "train_image_size": args.train_size,
         "train_steps": args.train_steps, "train_batch": 512, "pair_generation_s": gen_s, "training_s": train_s,
         "loss_first_last": [losses[0], losses[-1]],

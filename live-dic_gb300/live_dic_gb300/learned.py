@@ -712,6 +712,7 @@ class LearnedSeeder:
         self._graph = None       # captured frame sequence, and what it was captured for
         self._graph_key = None
         self._graph_frame = None  # the fixed frame buffer the graph reads
+        self._marks = None        # (stage, CUDA event) pairs while stage_times runs
 
     def set_reference_image(self, reference: np.ndarray) -> None:
         """Half-resolution reference for the network (the engine keeps its own),
@@ -778,16 +779,20 @@ class LearnedSeeder:
             self.global_shift.write(self.tgt_half.data_ptr(), self.base.data_ptr(), self.lattice, OUT_PAD,
                                     2.0 / TRANSLATION_SCALE, stream)
             shift = self.base
+        self._mark("half frame + shift")
         for p in range(self.passes):
             self._network_pass(self.pred, shift, stream)
+            self._mark(f"network pass {p + 1}")
             if p == self.passes - 1:
                 break
             if shift is None:
                 self.base.zero_()
             self._consensus_device(stream)
+            self._mark("consensus")
             shift = self.base
         self._shifted = shift is not None
         self._lattice_seeds(stream)
+        self._mark("lattice seeds")
 
     def _lattice_seeds(self, stream) -> None:
         _call(self.lib, "gbdic_nn_lattice_seeds", _ptr(self.pred), _ptr(self.base) if self._shifted else None,
@@ -820,6 +825,35 @@ class LearnedSeeder:
                 self._register(frame, reseed, self._handle)
         torch.cuda.current_stream(self.net.device).wait_stream(self.stream)
         return {"reseeded": int(self.reseed_count.item()) if counts and reseed else (0 if counts else None)}
+
+    def stage_times(self, frame, *, reseed: bool = True) -> dict[str, float]:
+        """One frame through the direct sequence with CUDA events between its
+        stages (on self.stream); returns milliseconds per stage (half-resolution
+        frame and global shift, each network pass, the consensus, the lattice
+        seeds, the node solve, the node rows and seeds, the full solve, the
+        reseeding) and their total.  Leaves self.state as register_device
+        would."""
+        torch = _torch()
+        self._marks = []
+        self.stream.wait_stream(torch.cuda.current_stream(self.net.device))
+        with torch.cuda.stream(self.stream):
+            self._mark("start")
+            self._register(frame, reseed, self._handle)
+        marks, self._marks = self._marks, None
+        self.stream.synchronize()
+        out: dict[str, float] = {}
+        for (_, a), (name, b) in zip(marks, marks[1:], strict=False):
+            out[name] = out.get(name, 0.0) + a.elapsed_time(b)
+        out["total"] = marks[0][1].elapsed_time(marks[-1][1])
+        return out
+
+    def _mark(self, name: str) -> None:
+        if self._marks is None:
+            return
+        torch = _torch()
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record(self.stream)
+        self._marks.append((name, ev))
 
     def _capture(self, frame, reseed: bool, key) -> None:
         torch = _torch()
@@ -861,15 +895,18 @@ class LearnedSeeder:
             else:
                 _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds),
                              _ptr(self._node_active), C.byref(node_cfg), _ptr(self.state), stream)
+            self._mark("node solve")
             _call(self.lib, "gbdic_nn_node_rows", _ptr(self.state), self.gw, self.gh, self.step, self.lw, self.lh,
                   _ptr(self.pred), _ptr(self.base) if self._shifted else None, OUT_PAD, C.c_float(TRANSLATION_SCALE),
                   C.c_float(GRADIENT_SCALE), stream)
             self._lattice_seeds(stream)
+            self._mark("node rows + seeds")
             _call_engine(eng, "gbdic_resolve_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
                          _ptr(self.state), stream)
         else:
             _call_engine(eng, "gbdic_register_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
                          _ptr(self.state), stream)
+        self._mark("full solve")
         if not reseed:
             return
         # Not converged (0) or converged below the ZNCC threshold (-2): ZNCC
@@ -894,6 +931,7 @@ class LearnedSeeder:
             _call_engine(eng, "gbdic_resolve_seeded_device", _ptr(frame), _ptr(self.seeds), _ptr(self.active), cfg,
                          _ptr(self._retry), stream)
         _call(self.lib, "gbdic_nn_merge_rows", _ptr(self._retry), _ptr(self.mask), count, 8, _ptr(self.state), stream)
+        self._mark("reseeding")
 
 
 def _native_copy(dst, row0: int, src, n: int) -> None:

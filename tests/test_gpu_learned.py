@@ -388,3 +388,14 @@ def _graph_and_list_identity(net, ref, frames, lanes):
                     np.testing.assert_array_equal(out[key][0], base[0], err_msg=str(key))
                     assert out[key][1] == base[1]
         assert seeders[(True, True)]._graph is not None and seeders[(False, True)]._graph is None
+        # the stage breakdown runs the direct sequence: same state again
+        seeder = seeders[(False, True)]
+        seeder.register_device(frames[-1])
+        torch.cuda.synchronize()
+        expected = seeder.state.cpu().numpy().copy()
+        stages = seeder.stage_times(frames[-1])
+        np.testing.assert_array_equal(seeder.state.cpu().numpy(), expected)
+        assert {"half frame + shift", "network pass 1", "consensus", "network pass 2", "node solve", "full solve",
+                "reseeding"} <= set(stages)
+        assert all(v >= 0.0 for v in stages.values())
+        assert abs(sum(v for k, v in stages.items() if k != "total") - stages["total"]) <= 1e-3 * stages["total"] + 1e-3
