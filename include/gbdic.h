@@ -511,7 +511,11 @@ int gbdic_fourier_estimate(gbdic_fourier *fourier, const uint8_t *frame, int64_t
  * dy * multiplier for i < count.  Accepted when the window's standard
  * deviation is >= 1, the peak score >= 8 and the overlap >= 0.25, else zero
  * (the sample-correlation test of gbdic_fourier_estimate is not applied).
- * Calls on one handle run in stream order and must not overlap. */
+ * Calls on one handle run in stream order and must not overlap.  Outside a
+ * stream capture the call is also ordered with the handle's own stream
+ * (gbdic_fourier_estimate); inside one (a CUDA graph of the caller's frame)
+ * it is not, so the graph's replays and host-path estimates must not use the
+ * same handle at the same time. */
 int gbdic_fourier_shift_device(gbdic_fourier *fourier, const uint8_t *frame, int64_t row_stride, int32_t height,
                                int32_t x, int32_t y, float multiplier, float *rows, int32_t count, int32_t pitch,
                                void *stream);

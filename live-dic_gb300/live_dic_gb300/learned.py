@@ -809,12 +809,13 @@ class LearnedSeeder:
         the sequence once directly, then captures it as a CUDA graph that
         reads the frame from a fixed device buffer; later calls copy the
         frame there and replay the graph.  The graph is captured again when
-        the reference, the engine's solver settings or `reseed` change."""
+        the reference (the seeder's or the engine's), the engine's solver
+        settings or `reseed` change."""
         torch = _torch()
         self.stream.wait_stream(torch.cuda.current_stream(self.net.device))
         if self.graph:
             key = (bool(reseed), tuple(sorted(self.engine._config.items())), self.engine.solver,
-                   tuple(frame.shape), frame.dtype)
+                   self.engine.reference_generation, tuple(frame.shape), frame.dtype)
             if self._graph is None or self._graph_key != key:
                 self._capture(frame, bool(reseed), key)
             with torch.cuda.stream(self.stream):

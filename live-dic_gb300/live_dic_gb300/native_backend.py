@@ -272,6 +272,9 @@ class ICGNWGPU:
         self.execution_device_type = "gpu"
         self.width = self.height = self.grid_width = self.grid_height = 0
         self._reference_ready = False
+        # incremented by every reference preparation (device-side users key
+        # captured work on it)
+        self.reference_generation = 0
         self._target_ready = False
         self._config: dict[str, float | int] = {"iterations": 30, "tolerance": 1e-3, "znccMin": 0.8}
         self.roi = None
@@ -433,6 +436,7 @@ class ICGNWGPU:
         admissible = self._export(_native.EXPORT_ADMISSIBLE, np.uint8, (gh, gw))
         self.reference_valid = immutable(admissible.astype(bool))
         self._reference_ready = True
+        self.reference_generation += 1
         if self.pyramid_levels > 1:
             self._prepare_pyramid(frame, zncc_min=config["znccMin"])
         usable = self.reference_valid if roi is None else self.reference_valid & roi.selected
@@ -494,6 +498,7 @@ class ICGNWGPU:
         admissible = self._export(_native.EXPORT_ADMISSIBLE, np.uint8, (gh, gw))
         self.reference_valid = immutable(admissible.astype(bool))
         self._reference_ready = True
+        self.reference_generation += 1
         return float(info.device_ms)
 
     def _prepare_partial(self, roi: RoiPlan) -> RoiPlan:
@@ -543,6 +548,7 @@ class ICGNWGPU:
         flags = metadata.reshape(-1, stride)[:, 1]
         self.reference_valid = immutable(((flags > 0.5) | (flags == -4)).reshape(gh, gw))
         self._reference_ready = True
+        self.reference_generation += 1
 
     # ------------------------------------------------------------ exports
     def _export(self, what: int, dtype, shape) -> np.ndarray:
