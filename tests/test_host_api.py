@@ -52,6 +52,8 @@ def test_library_exports_every_declared_symbol():
         ({"device_type": "tpu"}, "device_type"),
         ({"power_preference": "max"}, "power_preference"),
         ({"prefer_subgroups": True, "subset_size": 32}, "prefer_subgroups"),
+        ({"solver_mode": "tiled"}, "solver_mode"),
+        ({"solver_mode": 2}, "solver_mode"),
     ],
 )
 def test_engine_validation_before_device_work(kwargs, message):
@@ -348,3 +350,39 @@ def test_roi_planning_matches_reference_on_harder_masks(case):
                                                        stride=stride, reference_mask=mask), g[f"{k}_down"])
     np.testing.assert_array_equal(roi.seed_permissions(plan, coarse, source_scale=1, destination_scale=2, size=size,
                                                        stride=stride, reference_mask=mask), g[f"{k}_up"])
+
+
+def test_solver_modes_and_autotuner_axes():
+    """Pixel-loop modes accepted by the engines and the autotuner's axes:
+    lanes, work distribution, and the staging axis (L1, register window,
+    TMA-staged tile) with its two tile shapes."""
+    from live_dic_gb300 import autotune
+    from live_dic_gb300.native_backend import normalize_solver_mode
+
+    for mode in ("exact", "fast", "staged", "staged-wide"):
+        assert normalize_solver_mode(mode) == mode
+        assert _native.SOLVER_MODES[mode] in (0, 1, 2, 3)
+    modes = {m for _, _, m in autotune.CANDIDATES}
+    assert modes == {"exact", "fast", "staged", "staged-wide"}
+    assert len(autotune.CANDIDATES) == len(set(autotune.CANDIDATES)) == 18
+    assert {(lanes, persistent) for lanes, persistent, m in autotune.CANDIDATES if m == "staged"} == {
+        (16, False), (32, False), (16, True), (32, True)}
+    assert autotune.variant_name(16, False, "staged-wide") == "16-lane grid staged-wide"
+
+
+def test_batch_modes_and_split_k_choice():
+    """The batch step modes (single persistent launch by default) and the
+    inference network's split-K choice: the smallest divisor of the K
+    blocks that fills one wave of output tiles, 1 when the tiles do."""
+    from live_dic_gb300 import batch, learned
+
+    assert batch._MODES == {"persistent": _native.BATCH_PERSISTENT, "per-job": _native.BATCH_PER_JOB,
+                            "single": _native.BATCH_SINGLE}
+    C = learned._Conv
+    # (cin, cout, H, OH, kp, kp_rows, kt, M, Min) at batch 512: conv4 and conv5
+    conv4 = C(128, 128, 8, 4, 1152, 1152, 1152, 512 * 16, 512 * 64)
+    conv5 = C(128, 64, 4, 2, 1152, 1152, 576, 512 * 4, 512 * 16)
+    conv2 = C(32, 64, 32, 16, 320, 384, 576, 512 * 256, 512 * 1024)
+    assert learned.SeedNet._forward_splits(conv4) == 3   # 64 tiles -> 192
+    assert learned.SeedNet._forward_splits(conv5) == 18  # 16 tiles -> 288
+    assert learned.SeedNet._forward_splits(conv2) == 1   # 1024 tiles fill the GPU
