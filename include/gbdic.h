@@ -606,8 +606,10 @@ int gbdic_nn_relu_bias_backward(const float *dy, int32_t ld, const void *y, int6
 int gbdic_nn_splitk_bias_relu(const float *partial, int32_t splits, int64_t rows, int32_t cols, int64_t split_stride,
                               const float *bias, int32_t relu, void *y, void *stream);
 /* a_t (rows_padded x B*OH*OW) = the im2col operand of x (gbdic_nn_im2col)
- * transposed, zero in rows >= 9 C, without writing the operand itself
- * (the weight-gradient GEMM's A); rows_padded % 64 == 0, B*OH*OW % 8 == 0. */
+ * transposed, without writing the operand itself (the weight-gradient GEMM's
+ * A); rows_padded % 64 == 0, B*OH*OW % 8 == 0.  Rows 9 C up to the next
+ * multiple of 64 are written as zero; the rows beyond are not written (the
+ * caller keeps them zero). */
 int gbdic_nn_im2col_t(const gbdic_nn_conv_shape *shape, const void *x, void *a_t, int32_t rows_padded, void *stream);
 /* out[n][k] = sum_s partial[s][k][n] for k < Kp (partials Kp_rows x N). */
 int gbdic_nn_splitk_reduce(const float *partial, int32_t splits, int32_t kp_rows, int32_t n, int32_t kp, float *out,
@@ -616,6 +618,11 @@ int gbdic_nn_splitk_reduce(const float *partial, int32_t splits, int32_t kp_rows
  * 1 - beta1^t, 1 - beta2^t, weight_decay}. */
 int gbdic_nn_adam(float *param, const float *grad, float *m, float *v, int64_t count, const float *hyper,
                   void *stream);
+/* The same step over 1 to 16 tensors in one launch (host arrays of device
+ * pointers and element counts); per element the arithmetic of
+ * gbdic_nn_adam. */
+int gbdic_nn_adam_many(float *const *params, const float *const *grads, float *const *m, float *const *v,
+                       const int64_t *counts, int32_t tensors, const float *hyper, void *stream);
 /* BF16 copy of W [Cout][Kp] and, when wt != NULL, the data-gradient operand
  * Wt[ci][(ky, kx, co)] (row length kt). */
 int gbdic_nn_pack_weights(const float *w, int32_t cout, int32_t cin, int32_t kp, void *wb, void *wt, int32_t kt,

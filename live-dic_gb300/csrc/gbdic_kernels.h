@@ -235,6 +235,17 @@ struct NnAdamArgs {
     long long count;
     float lr, beta1, beta2, eps, bias1, bias2, weight_decay;
 };
+// Several tensors in one launch (passed by value with the launch).
+constexpr int kMaxAdamTensors = 16;
+struct NnAdamMany {
+    float *param[kMaxAdamTensors];
+    const float *grad[kMaxAdamTensors];
+    float *m[kMaxAdamTensors], *v[kMaxAdamTensors];
+    long long offset[kMaxAdamTensors + 1];  // element offsets of the tensors in the concatenation
+    int n;
+    float lr, beta1, beta2, eps, bias1, bias2, weight_decay;
+};
+cudaError_t launch_nn_adam_many(const NnAdamMany &a, cudaStream_t s);
 cudaError_t launch_nn_patches(const NnPatchArgs &a, cudaStream_t s);
 cudaError_t launch_nn_im2col(const NnConvShape &sh, const void *x, void *A, cudaStream_t s);
 cudaError_t launch_nn_dgrad_gather(const NnConvShape &sh, const void *dz, void *G, cudaStream_t s);

@@ -149,6 +149,23 @@ int gbdic_nn_adam(float *param, const float *grad, float *m, float *v, int64_t c
     return rc(gbdic::launch_nn_adam(a, as_stream(stream)), "Adam");
 }
 
+int gbdic_nn_adam_many(float *const *params, const float *const *grads, float *const *m, float *const *v,
+                       const int64_t *counts, int32_t tensors, const float *hyper, void *stream) {
+    if (!params || !grads || !m || !v || !counts || !hyper || tensors < 1 || tensors > gbdic::kMaxAdamTensors)
+        return invalid("invalid Adam arguments (1 to 16 tensors)");
+    gbdic::NnAdamMany a{};
+    a.n = tensors;
+    a.offset[0] = 0;
+    for (int t = 0; t < tensors; ++t) {
+        if (!params[t] || !grads[t] || !m[t] || !v[t] || counts[t] < 0) return invalid("invalid Adam tensor");
+        a.param[t] = params[t]; a.grad[t] = grads[t]; a.m[t] = m[t]; a.v[t] = v[t];
+        a.offset[t + 1] = a.offset[t] + counts[t];
+    }
+    a.lr = hyper[0]; a.beta1 = hyper[1]; a.beta2 = hyper[2]; a.eps = hyper[3];
+    a.bias1 = hyper[4]; a.bias2 = hyper[5]; a.weight_decay = hyper[6];
+    return rc(gbdic::launch_nn_adam_many(a, as_stream(stream)), "Adam");
+}
+
 int gbdic_nn_pack_weights(const float *w, int32_t cout, int32_t cin, int32_t kp, void *wb, void *wt, int32_t kt,
                           void *stream) {
     if (!w || !wb || cout <= 0 || cin <= 0 || kp < 9 * cin || (wt && kt < 9 * cout))

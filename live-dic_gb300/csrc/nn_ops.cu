@@ -11,6 +11,8 @@
 // [Cout][(ky, kx, ci)] with the reduction index padded to the GEMM tile.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include <cstdint>
 
 #include "gbdic_kernels.h"
@@ -347,6 +349,22 @@ __global__ void __launch_bounds__(256) im2col_t_kernel(NnConvShape s, const __nv
 #pragma unroll
             for (int q = 0; q < 8; ++q) tile[(8 * j + q) * 72 + ml] = e[q];
         }
+    } else if (s.C == 2 && k0 == 0) {
+        // 2 channels: one 4-byte load per (pixel, tap); rows 18 .. 63 zero
+        for (int i = t; i < 64 * 9; i += 256) {
+            const int ml = i & 63, tap = i >> 6, m = m0 + ml, ky = tap / 3, kx = tap - 3 * ky;
+            uint32_t v = 0u;
+            if (m < M) {
+                const int ox = m % s.OW, tt = m / s.OW, oy = tt % s.OH, b = tt / s.OH;
+                const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
+                if (iy >= 0 && iy < s.H && ix >= 0 && ix < s.W)
+                    v = __ldg(reinterpret_cast<const uint32_t *>(x + (((size_t)b * s.H + iy) * s.W + ix) * 2));
+            }
+            const __nv_bfloat162 pr = *reinterpret_cast<const __nv_bfloat162 *>(&v);
+            tile[(2 * tap) * 72 + ml] = pr.x;
+            tile[(2 * tap + 1) * 72 + ml] = pr.y;
+        }
+        for (int i = t; i < 64 * 46; i += 256) tile[(18 + (i >> 6)) * 72 + (i & 63)] = __float2bfloat16(0.0f);
     } else {
         for (int i = 0; i < 16; ++i) {
             const int kl = t & 63, ml = (t >> 6) + 4 * i, m = m0 + ml, k = k0 + kl;
@@ -369,24 +387,56 @@ __global__ void __launch_bounds__(256) im2col_t_kernel(NnConvShape s, const __nv
 }
 
 // out[n][k] = sum_s partial[s][k][n] (s ascending) for k < Kp, n < N.
+// Consecutive threads take consecutive n (contiguous partial reads); the
+// loads of four splits are issued before their ordered additions.
 __global__ void splitk_reduce_kernel(const float *partial, int splits, int Kp_rows, int N, int Kp, float *out) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= N * Kp) return;
-    const int n = idx / Kp, k = idx % Kp;
+    const int k = idx / N, n = idx - k * N;
+    const size_t stride = (size_t)Kp_rows * N;
+    const float *p = partial + (size_t)k * N + n;
     float acc = 0.0f;
-    for (int s = 0; s < splits; ++s) acc += partial[((size_t)s * Kp_rows + k) * N + n];
-    out[idx] = acc;
+    int s = 0;
+    for (; s + 4 <= splits; s += 4) {
+        const float v0 = __ldg(p + s * stride), v1 = __ldg(p + (s + 1) * stride);
+        const float v2 = __ldg(p + (s + 2) * stride), v3 = __ldg(p + (s + 3) * stride);
+        acc += v0;
+        acc += v1;
+        acc += v2;
+        acc += v3;
+    }
+    for (; s < splits; ++s) acc += __ldg(p + s * stride);
+    out[(size_t)n * Kp + k] = acc;
+}
+
+// One Adam element update (shared by both kernels so that they compile to
+// the same arithmetic).
+__device__ __forceinline__ void adam_element(float *param, const float *grad, float *m_, float *v_, long long j,
+                                             float lr, float beta1, float beta2, float eps, float bias1, float bias2,
+                                             float weight_decay) {
+    const float g = grad[j] + weight_decay * param[j];
+    const float m = beta1 * m_[j] + (1.0f - beta1) * g;
+    const float v = beta2 * v_[j] + (1.0f - beta2) * g * g;
+    m_[j] = m;
+    v_[j] = v;
+    param[j] -= lr * (m / bias1) / (sqrtf(v / bias2) + eps);
+}
+
+// Adam over up to kMaxAdamTensors tensors in one launch: element i of the
+// concatenation belongs to the tensor whose offset range holds it.
+__global__ void adam_many_kernel(NnAdamMany a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.offset[a.n]) return;
+    int t = 0;
+    while (i >= a.offset[t + 1]) ++t;
+    adam_element(a.param[t], a.grad[t], a.m[t], a.v[t], i - a.offset[t], a.lr, a.beta1, a.beta2, a.eps, a.bias1,
+                 a.bias2, a.weight_decay);
 }
 
 __global__ void adam_kernel(NnAdamArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.count) return;
-    const float g = a.grad[i] + a.weight_decay * a.param[i];
-    const float m = a.beta1 * a.m[i] + (1.0f - a.beta1) * g;
-    const float v = a.beta2 * a.v[i] + (1.0f - a.beta2) * g * g;
-    a.m[i] = m;
-    a.v[i] = v;
-    a.param[i] -= a.lr * (m / a.bias1) / (sqrtf(v / a.bias2) + a.eps);
+    adam_element(a.param, a.grad, a.m, a.v, i, a.lr, a.beta1, a.beta2, a.eps, a.bias1, a.bias2, a.weight_decay);
 }
 
 // W [Cout][Kp] FP32 -> BF16 copy, and the data-gradient operand
@@ -870,7 +920,10 @@ cudaError_t launch_nn_im2col_t(const NnConvShape &sh, const void *x, void *At, i
     if (M <= 0 || M % 8 || Kt <= 0 || Kt % 64 || M >= (1ll << 31) || (long long)Kt * M >= (1ll << 40) ||
         ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(At)) & 15))
         return cudaErrorInvalidValue;
-    dim3 grid((unsigned)((M + 63) / 64), (unsigned)(Kt / 64));
+    // Only the 64-row tiles that hold rows k < 9 C are written; the rows
+    // beyond stay as the caller keeps them (zero).
+    const int live = std::min(Kt, (9 * sh.C + 63) / 64 * 64);
+    dim3 grid((unsigned)((M + 63) / 64), (unsigned)(live / 64));
     im2col_t_kernel<<<grid, 256, 0, s>>>(sh, static_cast<const __nv_bfloat16 *>(x), static_cast<__nv_bfloat16 *>(At),
                                          Kt);
     return cudaGetLastError();
@@ -879,6 +932,14 @@ cudaError_t launch_nn_im2col_t(const NnConvShape &sh, const void *x, void *At, i
 cudaError_t launch_nn_splitk_reduce(const float *partial, int splits, int Kp_rows, int N, int Kp, float *out,
                                     cudaStream_t s) {
     splitk_reduce_kernel<<<blocks((long long)N * Kp, 256), 256, 0, s>>>(partial, splits, Kp_rows, N, Kp, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nn_adam_many(const NnAdamMany &a, cudaStream_t s) {
+    if (a.n < 1 || a.n > kMaxAdamTensors) return cudaErrorInvalidValue;
+    const long long total = a.offset[a.n];
+    if (total <= 0) return cudaSuccess;
+    adam_many_kernel<<<blocks(total, 256), 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

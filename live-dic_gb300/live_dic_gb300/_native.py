@@ -218,6 +218,7 @@ _SIGNATURES = {
     "gbdic_nn_bias_grad": (C.c_int, [P, I32, P, I64, I32, P, P]),
     "gbdic_nn_splitk_reduce": (C.c_int, [P, I32, I32, I32, I32, P, P]),
     "gbdic_nn_adam": (C.c_int, [P, P, P, P, I64, P, P]),
+    "gbdic_nn_adam_many": (C.c_int, [P, P, P, P, P, I32, P, P]),
     "gbdic_nn_pack_weights": (C.c_int, [P, I32, I32, I32, P, P, I32, P]),
     "gbdic_nn_regression_loss": (C.c_int, [P, I32, P, I32, I32, P, P, I32, P, P]),
     "gbdic_reduce_half": (C.c_int, [P, I32, I32, P, P]),

@@ -133,6 +133,7 @@ class SeedNet:
         self.m = [torch.zeros_like(p) for p in self.params]
         self.v = [torch.zeros_like(p) for p in self.params]
         self.steps = 0
+        self._adam_tables = None  # device pointers and sizes of params / grads / moments (fixed)
         # BF16 operands
         self.wb = [torch.zeros(c.cout, c.kp, dtype=bf16, device=dev) for c in self.convs]
         self.wt = [torch.zeros(c.cin, c.kt, dtype=bf16, device=dev) for c in self.convs]
@@ -321,8 +322,15 @@ class SeedNet:
         self.steps += 1
         t = self.steps
         hyper = (C.c_float * 7)(lr, beta1, beta2, eps, 1 - beta1 ** t, 1 - beta2 ** t, weight_decay)
-        for p, g, m, v in zip(self.params, self.grads, self.m, self.v, strict=True):
-            _call(self.lib, "gbdic_nn_adam", _ptr(p), _ptr(g), _ptr(m), _ptr(v), p.numel(), hyper, stream)
+        if self._adam_tables is None:
+            n = len(self.params)
+            ptrs = (C.c_void_p * n)
+            self._adam_tables = (ptrs(*[p.data_ptr() for p in self.params]), ptrs(*[g.data_ptr() for g in self.grads]),
+                                 ptrs(*[m.data_ptr() for m in self.m]), ptrs(*[v.data_ptr() for v in self.v]),
+                                 (C.c_int64 * n)(*[p.numel() for p in self.params]), n)
+        params, grads, ms, vs, counts, n = self._adam_tables
+        # every parameter tensor in one launch, per element gbdic_nn_adam's update
+        _call(self.lib, "gbdic_nn_adam_many", params, grads, ms, vs, counts, n, hyper, stream)
         self.pack(stream)
 
     def check_device_errors(self) -> None:

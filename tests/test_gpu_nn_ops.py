@@ -69,7 +69,33 @@ def test_transposed_im2col_equals_transpose_of_im2col(B, H, Cin, kp_rows):
     _native.check(lib.gbdic_nn_im2col(C.byref(shape), _p(x), _p(a), None), lib.gbdic_last_error(None))
     want = torch.full((kp_rows, M), 7.0, dtype=torch.bfloat16, device="cuda")
     _native.check(lib.gbdic_nn_transpose(_p(a), M, kp, kp, _p(want), M, kp_rows, None), lib.gbdic_last_error(None))
-    got = torch.full((kp_rows, M), 7.0, dtype=torch.bfloat16, device="cuda")
+    # rows beyond the last 64-row tile holding k < 9 C are the caller's (kept zero)
+    got = torch.zeros((kp_rows, M), dtype=torch.bfloat16, device="cuda")
+    live = min(kp_rows, -(-9 * Cin // 64) * 64)
+    got[live:] = 7.0
     _native.check(lib.gbdic_nn_im2col_t(C.byref(shape), _p(x), _p(got), kp_rows, None), lib.gbdic_last_error(None))
     torch.cuda.synchronize()
-    assert torch.equal(got, want)
+    assert torch.equal(got[:live], want[:live])
+    assert (got[live:] == 7.0).all() and (want[live:] == 0).all()
+
+
+def test_adam_many_equals_per_tensor_steps():
+    """One multi-tensor Adam launch against one launch per tensor: the same
+    parameters and moments bit for bit."""
+    lib = _native.load()
+    g = torch.Generator(device="cuda").manual_seed(5)
+    sizes = [32 * 64, 64 * 320, 128, 16 * 256, 7]
+    mk = lambda: [torch.randn(n, generator=g, device="cuda") for n in sizes]  # noqa: E731
+    params, grads, ms, vs = mk(), mk(), mk(), [t.abs() for t in mk()]
+    copies = [[t.clone() for t in group] for group in (params, grads, ms, vs)]
+    hyper = (ctypes_float7 := (C.c_float * 7)(2e-3, 0.9, 0.999, 1e-8, 0.1, 0.001, 1e-4))
+    for p, gr, m, v in zip(*copies, strict=True):
+        _native.check(lib.gbdic_nn_adam(_p(p), _p(gr), _p(m), _p(v), p.numel(), ctypes_float7, None),
+                      lib.gbdic_last_error(None))
+    n = len(sizes)
+    arr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])  # noqa: E731
+    _native.check(lib.gbdic_nn_adam_many(arr(params), arr(grads), arr(ms), arr(vs), (C.c_int64 * n)(*sizes), n, hyper,
+                                         None), lib.gbdic_last_error(None))
+    torch.cuda.synchronize()
+    for a, b in zip(params + ms + vs, copies[0] + copies[2] + copies[3], strict=True):
+        assert torch.equal(a, b)
