@@ -22,6 +22,7 @@ struct PyramidSlot {
     gbdic::HostBuffer shift_host;  // global translation seed (dx, dy), read at graph launch
     gbdic::DeviceBuffer shift_dev;
     cudaEvent_t begin = nullptr, end = nullptr;
+    cudaEvent_t uploaded = nullptr, computed = nullptr;  // copy-stream ordering
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // whole pyramid, finest level alone
     bool pending = false;
     std::chrono::steady_clock::time_point submitted;
@@ -29,6 +30,8 @@ struct PyramidSlot {
     void create() {
         check_cuda(cudaEventCreate(&begin), "event");
         check_cuda(cudaEventCreate(&end), "event");
+        check_cuda(cudaEventCreateWithFlags(&uploaded, cudaEventDisableTiming), "event");
+        check_cuda(cudaEventCreateWithFlags(&computed, cudaEventDisableTiming), "event");
         counters.ensure(4 * sizeof(uint32_t));
         counters_host.ensure(4 * sizeof(uint32_t));
         shift_host.ensure(2 * sizeof(float));
@@ -45,7 +48,9 @@ struct PyramidSlot {
         drop_graphs();
         if (begin) cudaEventDestroy(begin);
         if (end) cudaEventDestroy(end);
-        begin = end = nullptr;
+        if (uploaded) cudaEventDestroy(uploaded);
+        if (computed) cudaEventDestroy(computed);
+        begin = end = uploaded = computed = nullptr;
     }
 };
 
@@ -69,6 +74,10 @@ struct gbdic_pyramid {
     // B-spline prefilters run beside the reductions and coarse solves.
     cudaStream_t side = nullptr;
     cudaEvent_t fork_ev = nullptr, reduced_ev[4] = {}, filtered_ev[4] = {};
+    // Host-frame pipeline: uploads and readbacks on their own streams, so a
+    // slot's upload overlaps the previous frame's solve and its readback the
+    // next one's.
+    cudaStream_t upload = nullptr, readback = nullptr;
     std::vector<PyramidSlot> slots;
     bool ready = false;
     std::string error;
@@ -82,6 +91,12 @@ struct gbdic_pyramid {
         if (side) {
             cudaStreamSynchronize(side);
             cudaStreamDestroy(side);
+        }
+        for (cudaStream_t st : {upload, readback}) {
+            if (st) {
+                cudaStreamSynchronize(st);
+                cudaStreamDestroy(st);
+            }
         }
         if (fork_ev) cudaEventDestroy(fork_ev);
         for (auto &e : reduced_ev)
@@ -337,7 +352,10 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
                    "state copy");
 }
 
-// Upload + frame + readback into the slot's pinned buffers, as a graph.
+// Upload (upload stream) -> the frame as a graph (the engine's stream) ->
+// readback into the slot's pinned buffers (readback stream).  A slot is
+// reused only after its retire waited for its readback, so its buffers are
+// free when the next upload starts.
 void launch_slot(gbdic_pyramid *p, int k) {
     auto &rt = *p->rt;
     auto &ps = p->slots[k];
@@ -345,15 +363,7 @@ void launch_slot(gbdic_pyramid *p, int k) {
     cudaStream_t s = rt.stream();
     const size_t bytes = p->state_bytes(0);
     ps.out.ensure(bytes);
-    auto body = [&](cudaStream_t st) {
-        check_cuda(cudaMemcpyAsync(fine.slots[k]->frame.get(), ps.in.as<uint8_t>(), (size_t)fine.W * fine.H,
-                                   cudaMemcpyHostToDevice, st), "frame upload");
-        enqueue_pyramid(p, k, fine.slots[k]->frame.as<uint8_t>(), nullptr, st);
-        check_cuda(cudaMemcpyAsync(ps.out.as<float>(), rt.output_state(*fine.slots[k]), bytes, cudaMemcpyDeviceToHost, st),
-                   "state readback");
-        check_cuda(cudaMemcpyAsync(ps.counters_host.as<uint32_t>(), ps.counters.get(), 4 * sizeof(uint32_t),
-                                   cudaMemcpyDeviceToHost, st), "counter readback");
-    };
+    auto body = [&](cudaStream_t st) { enqueue_pyramid(p, k, fine.slots[k]->frame.as<uint8_t>(), nullptr, st); };
     cudaGraphExec_t &exec = ps.graph[p->active_levels == p->L() ? 0 : 1];
     if (exec == nullptr) {
         cudaGraph_t graph = nullptr;
@@ -370,9 +380,19 @@ void launch_slot(gbdic_pyramid *p, int k) {
         cudaGraphDestroy(graph);
         check_cuda(err, "graph instantiate");
     }
+    check_cuda(cudaMemcpyAsync(fine.slots[k]->frame.get(), ps.in.as<uint8_t>(), (size_t)fine.W * fine.H,
+                               cudaMemcpyHostToDevice, p->upload), "frame upload");
+    check_cuda(cudaEventRecord(ps.uploaded, p->upload), "event");
+    check_cuda(cudaStreamWaitEvent(s, ps.uploaded, 0), "upload wait");
     check_cuda(cudaEventRecord(ps.begin, s), "event");
     check_cuda(cudaGraphLaunch(exec, s), "graph launch");
-    check_cuda(cudaEventRecord(ps.end, s), "event");
+    check_cuda(cudaEventRecord(ps.computed, s), "event");
+    check_cuda(cudaStreamWaitEvent(p->readback, ps.computed, 0), "compute wait");
+    check_cuda(cudaMemcpyAsync(ps.out.as<float>(), rt.output_state(*fine.slots[k]), bytes, cudaMemcpyDeviceToHost,
+                               p->readback), "state readback");
+    check_cuda(cudaMemcpyAsync(ps.counters_host.as<uint32_t>(), ps.counters.get(), 4 * sizeof(uint32_t),
+                               cudaMemcpyDeviceToHost, p->readback), "counter readback");
+    check_cuda(cudaEventRecord(ps.end, p->readback), "event");
 }
 
 }  // namespace
@@ -413,6 +433,8 @@ int gbdic_pyramid_create(const gbdic_pyramid_options *options, gbdic_pyramid **o
         p->device = po.base.device;
         p->rt = std::make_unique<gbdic::Runtime>(po.base);
         check_cuda(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking), "stream");
+        check_cuda(cudaStreamCreateWithFlags(&p->upload, cudaStreamNonBlocking), "stream");
+        check_cuda(cudaStreamCreateWithFlags(&p->readback, cudaStreamNonBlocking), "stream");
         check_cuda(cudaEventCreateWithFlags(&p->fork_ev, cudaEventDisableTiming), "event");
         for (int l = 0; l < 4; ++l) {
             check_cuda(cudaEventCreateWithFlags(&p->reduced_ev[l], cudaEventDisableTiming), "event");
@@ -451,6 +473,9 @@ int gbdic_pyramid_set_reference(gbdic_pyramid *p, const uint8_t *image, int32_t 
             W /= 2;
             H /= 2;
         }
+        // in-flight frames (and their copies) end before the buffers go
+        for (cudaStream_t st : {p->rt->stream(), p->upload, p->readback})
+            check_cuda(cudaStreamSynchronize(st), "pending work");
         p->ready = false;
         for (auto &s : p->slots) {
             s.drop_graphs();
