@@ -352,17 +352,13 @@ void enqueue_pyramid(gbdic_pyramid *p, int k, const uint8_t *frame0, float *out_
                    "state copy");
 }
 
-// Upload (upload stream) -> the frame as a graph (the engine's stream) ->
-// readback into the slot's pinned buffers (readback stream).  A slot is
-// reused only after its retire waited for its readback, so its buffers are
-// free when the next upload starts.
-void launch_slot(gbdic_pyramid *p, int k) {
+// The frame's sequence for slot k (its resident target in the slot's frame
+// buffer) as a graph, captured on first use for the current level count.
+cudaGraphExec_t slot_graph(gbdic_pyramid *p, int k) {
     auto &rt = *p->rt;
     auto &ps = p->slots[k];
     auto &fine = *p->levels[0];
     cudaStream_t s = rt.stream();
-    const size_t bytes = p->state_bytes(0);
-    ps.out.ensure(bytes);
     auto body = [&](cudaStream_t st) { enqueue_pyramid(p, k, fine.slots[k]->frame.as<uint8_t>(), nullptr, st); };
     cudaGraphExec_t &exec = ps.graph[p->active_levels == p->L() ? 0 : 1];
     if (exec == nullptr) {
@@ -380,6 +376,21 @@ void launch_slot(gbdic_pyramid *p, int k) {
         cudaGraphDestroy(graph);
         check_cuda(err, "graph instantiate");
     }
+    return exec;
+}
+
+// Upload (upload stream) -> the frame as a graph (the engine's stream) ->
+// readback into the slot's pinned buffers (readback stream).  A slot is
+// reused only after its retire waited for its readback, so its buffers are
+// free when the next upload starts.
+void launch_slot(gbdic_pyramid *p, int k) {
+    auto &rt = *p->rt;
+    auto &ps = p->slots[k];
+    auto &fine = *p->levels[0];
+    cudaStream_t s = rt.stream();
+    const size_t bytes = p->state_bytes(0);
+    ps.out.ensure(bytes);
+    cudaGraphExec_t exec = slot_graph(p, k);
     check_cuda(cudaMemcpyAsync(fine.slots[k]->frame.get(), ps.in.as<uint8_t>(), (size_t)fine.W * fine.H,
                                cudaMemcpyHostToDevice, p->upload), "frame upload");
     check_cuda(cudaEventRecord(ps.uploaded, p->upload), "event");
@@ -621,7 +632,21 @@ int gbdic_pyramid_register_device(gbdic_pyramid *p, const uint8_t *device_frame,
         if (!p->ready) fail(GBDIC_ESTATE, "Call set_reference() before register().");
         if (!device_frame || !device_state) fail(GBDIC_EINVAL, "device_frame and device_state are required");
         cudaStream_t s = stream ? (cudaStream_t)stream : p->rt->stream();
-        enqueue_pyramid(p, 0, device_frame, device_state, s);
+        if (p->rt->profiling()) {
+            // per-launch solver events: the launches are issued directly
+            enqueue_pyramid(p, 0, device_frame, device_state, s);
+            return;
+        }
+        // Slot 0's graph between two device copies (the frame in, the
+        // output state out), in the order of `s`.
+        auto &fine = *p->levels[0];
+        auto &slot = *fine.slots[0];
+        cudaGraphExec_t exec = slot_graph(p, 0);
+        check_cuda(cudaMemcpyAsync(slot.frame.get(), device_frame, (size_t)fine.W * fine.H, cudaMemcpyDeviceToDevice, s),
+                   "frame copy");
+        check_cuda(cudaGraphLaunch(exec, s), "graph launch");
+        check_cuda(cudaMemcpyAsync(device_state, p->rt->output_state(slot), p->state_bytes(0), cudaMemcpyDeviceToDevice,
+                                   s), "state copy");
     });
 }
 

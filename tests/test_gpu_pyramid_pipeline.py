@@ -111,3 +111,29 @@ def test_fine_correction_keeps_fine_detail_over_frames():
         assert ok.mean() > 0.85
         np.testing.assert_allclose(np.median(r.displacement[ok], axis=0), [0.45 * k + 2e-4 * k * (W / 2),
                                                                           -0.3 * k - 1e-4 * k * (H / 2)], atol=0.05)
+
+
+def test_resident_graph_replay_equals_direct_launches():
+    """Resident registrations replay the slot's CUDA graph (between two
+    device copies) unless solver profiling is on, when the launches are
+    issued directly; over a temporal sequence both give the same states."""
+    torch = pytest.importorskip("torch")
+    ref, frames = _frames("ramp")
+    dev = [torch.from_numpy(np.ascontiguousarray(f)).cuda() for f in frames]
+    out = {}
+    for mode in ("graph", "direct"):
+        with ICGNWGPUFullPyramid(pyramid_levels=2, subset_size=21, subset_stride=10, initialization="temporal",
+                                 temporal_prediction="velocity") as engine:
+            info = engine.set_reference(ref)
+            gw, gh = info.grid
+            engine.set_profiling(mode == "direct")
+            state = torch.zeros(gw * gh * 8, dtype=torch.float32, device="cuda")
+            seq = []
+            for f in dev:
+                engine.register_device(f.data_ptr(), state.data_ptr())
+                torch.cuda.synchronize()
+                seq.append(state.view(gh, gw, 8).cpu().numpy().copy())
+            out[mode] = seq
+    assert len(out["graph"]) == len(frames)
+    for a, b in zip(out["graph"], out["direct"], strict=True):
+        np.testing.assert_array_equal(a, b)
