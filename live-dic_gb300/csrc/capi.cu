@@ -19,6 +19,7 @@ thread_local std::string g_create_error;
 struct SlotHost {
     gbdic::HostBuffer in, out;
     cudaEvent_t begin = nullptr, end = nullptr, done = nullptr;
+    cudaEvent_t uploaded = nullptr, computed = nullptr;  // stream pipeline ordering
     bool pending = false;
     std::chrono::steady_clock::time_point submitted;
     double upload_ms = 0.0;
@@ -27,14 +28,18 @@ struct SlotHost {
         check_cuda(cudaEventCreate(&begin), "event");
         check_cuda(cudaEventCreate(&end), "event");
         check_cuda(cudaEventCreateWithFlags(&done, cudaEventDisableTiming), "event");
+        check_cuda(cudaEventCreateWithFlags(&uploaded, cudaEventDisableTiming), "event");
+        check_cuda(cudaEventCreateWithFlags(&computed, cudaEventDisableTiming), "event");
     }
     void destroy() {
         if (graph) cudaGraphExecDestroy(graph);
         if (begin) cudaEventDestroy(begin);
         if (end) cudaEventDestroy(end);
         if (done) cudaEventDestroy(done);
+        if (uploaded) cudaEventDestroy(uploaded);
+        if (computed) cudaEventDestroy(computed);
         graph = nullptr;
-        begin = end = done = nullptr;
+        begin = end = done = uploaded = computed = nullptr;
     }
 };
 
@@ -78,13 +83,27 @@ struct gbdic_engine {
     bool ready = false;
     std::string error;
     int device = 0;
+    // Stream pipeline (submit / retire): uploads and readbacks on their own
+    // streams, so a slot's upload overlaps the previous frame's solve and its
+    // readback the next one's.
+    cudaStream_t upload = nullptr, readback = nullptr;
     ~gbdic_engine() {
         if (rt) {
             cudaSetDevice(device);
             cudaStreamSynchronize(rt->stream());
         }
+        for (cudaStream_t st : {upload, readback}) {
+            if (st) {
+                cudaStreamSynchronize(st);
+                cudaStreamDestroy(st);
+            }
+        }
         for (auto &h : host) h.destroy();
         level.slots.clear();
+    }
+    void sync_copies() const {
+        for (cudaStream_t st : {upload, readback})
+            if (st) check_cuda(cudaStreamSynchronize(st), "pending copies");
     }
     void require_ready(const char *what) const {
         if (!ready) fail(GBDIC_ESTATE, std::string("Call set_reference() before ") + what + "().");
@@ -121,6 +140,8 @@ int gbdic_create(const gbdic_options *options, gbdic_engine **out) {
         e->rt = std::make_unique<gbdic::Runtime>(*options);
         e->host = std::vector<SlotHost>(options->pipeline_slots);
         for (auto &h : e->host) h.create();
+        check_cuda(cudaStreamCreateWithFlags(&e->upload, cudaStreamNonBlocking), "stream");
+        check_cuda(cudaStreamCreateWithFlags(&e->readback, cudaStreamNonBlocking), "stream");
         e->slot_cfg.resize(options->pipeline_slots);
     } catch (const Failure &x) {
         g_create_error = x.message;
@@ -146,6 +167,7 @@ int set_reference_impl(gbdic_engine *e, const uint8_t *image, bool device, int32
         gbdic::grid_of(width, height, o.subset_size, o.subset_stride, gw, gh);
         if (gw < 1 || gh < 1)
             fail(GBDIC_EINVAL, "Reference dimensions must each be at least " + std::to_string(o.subset_size) + " pixels.");
+        e->sync_copies();
         e->ready = false;
         e->rt->configure_level(e->level, width, height, (int)e->host.size());
         auto &slot = *e->level.slots[0];
@@ -193,6 +215,7 @@ int gbdic_set_reference_arrays(gbdic_engine *e, int32_t width, int32_t height, c
         int gw, gh;
         gbdic::grid_of(width, height, o.subset_size, o.subset_stride, gw, gh);
         if (width < 16 || height < 16 || gw < 1 || gh < 1) fail(GBDIC_EINVAL, "invalid reference dimensions");
+        e->sync_copies();
         e->ready = false;
         e->rt->configure_level(e->level, width, height, (int)e->host.size());
         e->rt->upload_reference_arrays(e->level, plane, metadata, inverse, roi_links);
@@ -388,15 +411,22 @@ int gbdic_submit(gbdic_engine *e, int32_t slot_index, const uint8_t *frame, int6
         auto &h = e->host[slot_index];
         if (h.pending) fail(GBDIC_ESTATE, "slot is still in flight; retire it first");
         h.submitted = std::chrono::steady_clock::now();
-        e->rt->upload_frame(e->level, *e->level.slots[slot_index], frame, row_stride, h.in, e->rt->stream());
+        // upload stream -> the engine's stream -> readback stream; a slot is
+        // reused only after its retire waited for its readback
+        cudaStream_t s = e->rt->stream();
+        e->rt->upload_frame(e->level, *e->level.slots[slot_index], frame, row_stride, h.in, e->upload);
+        check_cuda(cudaEventRecord(h.uploaded, e->upload), "event");
+        check_cuda(cudaStreamWaitEvent(s, h.uploaded, 0), "upload wait");
         h.upload_ms = gbdic::ms_since(h.submitted);
         enqueue_frame(e, slot_index, *cfg, false, false, true);
+        check_cuda(cudaEventRecord(h.computed, s), "event");
         auto &lvl = e->level;
         const size_t bytes = (size_t)lvl.count * gbdic::state_stride(e->rt->opts().o.motion_model) * sizeof(float);
         h.out.ensure(bytes);
+        check_cuda(cudaStreamWaitEvent(e->readback, h.computed, 0), "compute wait");
         check_cuda(cudaMemcpyAsync(h.out.as<float>(), e->rt->output_state(*lvl.slots[slot_index]), bytes,
-                                   cudaMemcpyDeviceToHost, e->rt->stream()), "state readback");
-        check_cuda(cudaEventRecord(h.done, e->rt->stream()), "event");
+                                   cudaMemcpyDeviceToHost, e->readback), "state readback");
+        check_cuda(cudaEventRecord(h.done, e->readback), "event");
         h.pending = true;
     });
 }
