@@ -437,9 +437,10 @@ int gbdic_pyramid_set_partial_support(gbdic_pyramid *pyramid, int32_t level, int
  * call at a time, wgpu_backend.py:2893-2944).  Each job carries its own
  * GPU-prepared reference (B-spline interpolation, uniform weighting) and is
  * solved from a zero seed exactly like gbdic_register, followed by its own
- * outlier pass.  A step is one CUDA graph: prefilter of every target, one
- * persistent IC-GN launch per shape-function class over a device work queue
- * (affine/translation jobs, quadratic jobs), then the outlier passes. */
+ * outlier pass.  A step is one CUDA graph: prefilter of every target, the
+ * IC-GN launches of the step mode over a device work queue (by default one
+ * persistent launch over every job, heavy subsets first), then the outlier
+ * passes. */
 typedef struct gbdic_batch gbdic_batch;
 
 typedef struct {
@@ -450,8 +451,6 @@ typedef struct {
     gbdic_solver_cfg cfg;
 } gbdic_batch_job;
 
-/* Step modes: one persistent launch per class over the shared work queue, or
- * one grid launch per job in job order (the per-pair baseline). */
 /* Step modes: PERSISTENT, one persistent launch per shape-function class
  * (affine + translation, quadratic) on two graph branches; PER_JOB, one
  * grid launch per job; SINGLE, one persistent launch over every job. */
@@ -466,8 +465,9 @@ const char *gbdic_batch_last_error(const gbdic_batch *batch);
 int gbdic_batch_add(gbdic_batch *batch, const gbdic_batch_job *job, const uint8_t *reference, int32_t width,
                     int32_t height, int64_t row_stride, const uint8_t *roi_selected, const float *roi_links,
                     gbdic_ref_info *info, int32_t *job_index);
-/* Lanes per subset (32, 64, 128), step mode, and persistent CTAs per SM
- * (0 = as many as are resident). */
+/* Lanes per subset (16, 32, 64, 128; default 16), step mode (default
+ * GBDIC_BATCH_SINGLE), and persistent CTAs per SM (0 = as many as are
+ * resident). */
 int gbdic_batch_set_variant(gbdic_batch *batch, int32_t threads_per_subset, int32_t mode, int32_t ctas_per_sm);
 /* One step from host frames: frames[j] is job j's target (rows of its own
  * width, row_strides[j] bytes apart); out_states[j] receives its output
