@@ -92,6 +92,7 @@ struct Level {
     DeviceBuffer plane, meta, inv, links, selected;
     DeviceBuffer intensity, spline, scratch, valid;  // preparation scratch
     DeviceBuffer admissible;                         // u8 per subset, ROI ignored
+    DeviceBuffer moments;                            // quadratic row path: moments per subset
     DeviceBuffer ref_image;                          // reference bytes (seed search)
     DeviceBuffer partial_index, partial_words, partial_boxes;  // partial-support windows
     int partial_count = 0, support_words = 0;

@@ -94,8 +94,18 @@ struct PrepArgs {
     float *inv;             // count * n * n
     unsigned *valid_count;
     uint8_t *admissible;    // per subset numerical admissibility, ROI ignored
+    // quadratic row path: [71][count] binary32 moments and means, or nullptr
+    // (per-window path)
+    float *moments;
 };
 cudaError_t launch_reference_prep(const PrepArgs &a, cudaStream_t stream);
+// Quadratic preparation by window rows (column sums shared by the windows of
+// a grid row, one thread per 12x12 inverse): uniform weights, overlapping
+// windows (stride < S <= 256).  moments must hold
+// quadratic_row_prep_moment_floats(count) floats.
+bool quadratic_row_prep_supported(int model, int gaussian_weighting, int S, int stride, int grid_h);
+size_t quadratic_row_prep_moment_floats(int count);
+cudaError_t launch_quadratic_row_prep(const PrepArgs &a, cudaStream_t stream);
 
 // ------------------------------------------------------------ final ZNCC
 struct ZnccArgs {

@@ -252,7 +252,8 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
     s = t;
 }
 
-// Combine two compensated sums (s, c) with an exact TwoSum of the heads.
+// Combine two sums held as head + tail (s + c) with an exact TwoSum of the
+// heads.
 __device__ __forceinline__ void twosum_merge(float &s, float &c, float s2, float c2) {
     const float t = s + s2;
     const float bp = t - s;
@@ -261,7 +262,11 @@ __device__ __forceinline__ void twosum_merge(float &s, float &c, float s2, float
     c = (c + c2) + err;
 }
 
+// Warp total of per-lane Kahan sums.  On entry a lane's sum is s - c (c is
+// the compensation kahan_add carries: the excess of the last addition); on
+// return lane 0 holds the total as a head and an additive tail, s + c.
 __device__ __forceinline__ void warp_compensated_sum(float &s, float &c) {
+    c = -c;
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
         const float s2 = __shfl_down_sync(kFullMask, s, off);
@@ -586,7 +591,10 @@ cudaError_t launch_reference_prep(const PrepArgs &a, cudaStream_t stream) {
     gradient_kernel<<<dim3((W + 127) / 128, H), 128, 0, stream>>>(a.intensity, grad_src, W, H,
                                                                     bspline ? 1 : 0, a.plane);
     const int blocks = (a.count + 3) / 4;
-    if (blocks > 0) {
+    if (blocks > 0 && a.moments) {
+        const cudaError_t err = launch_quadratic_row_prep(a, stream);
+        if (err != cudaSuccess) return err;
+    } else if (blocks > 0) {
         switch (a.model) {
         case kModelTranslation: subset_prep_kernel<kModelTranslation><<<blocks, 128, 0, stream>>>(a); break;
         case kModelQuadratic: subset_prep_kernel<kModelQuadratic><<<blocks, 128, 0, stream>>>(a); break;

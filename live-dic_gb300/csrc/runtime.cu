@@ -300,6 +300,11 @@ double Runtime::prepare_reference(Level &level, const uint8_t *device_image, con
     a.inv = level.inv.as<float>();
     a.valid_count = level.valid.as<unsigned>();
     a.admissible = level.admissible.as<uint8_t>();
+    a.moments = nullptr;
+    if (quadratic_row_prep_supported(model, opt_.o.spatial_weighting, a.S, a.stride, a.grid_h)) {
+        level.moments.ensure(quadratic_row_prep_moment_floats(level.count) * sizeof(float));
+        a.moments = level.moments.as<float>();
+    }
     cudaEvent_t e0, e1;
     check_cuda(cudaEventCreate(&e0), "event");
     check_cuda(cudaEventCreate(&e1), "event");

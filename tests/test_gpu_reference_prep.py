@@ -15,6 +15,7 @@ import pytest
 
 from live_dic_gb300 import ICGNWGPU, synthetic
 from oracle import reference_prep as rp
+from quadratic_prep import check_quadratic_preparation
 
 pytestmark = pytest.mark.gpu
 
@@ -83,6 +84,22 @@ def test_gpu_preparation_matches_float64_oracle(model, interp, size, stride):
 @pytest.mark.parametrize("model", ["affine", "quadratic"])
 def test_gpu_preparation_on_speckle(model):
     _compare(_speckle(), model, "bspline", 21, 10)
+
+
+# Quadratic windows with uniform weights that overlap are prepared by window
+# rows (shared column sums); tiled grids and Gaussian weights by the
+# per-window sums.  Both against the float64 oracle, the second-order
+# moments stage by stage.
+@pytest.mark.parametrize("size,stride,weighting", [
+    (21, 10, "uniform"),    # row path, 8 windows in one row segment
+    (25, 4, "uniform"),     # row path, 16 windows per row segment
+    (21, 21, "uniform"),    # per-window path (tiled)
+    (21, 7, "gaussian"),    # per-window path (weighted)
+])
+def test_gpu_quadratic_preparation_paths(size, stride, weighting):
+    ok = check_quadratic_preparation(_speckle(), size, stride, weighting=weighting,
+                                     sigma=5.0 if weighting == "gaussian" else None)
+    assert ok.mean() > 0.9
 
 
 def test_gpu_preparation_gaussian_weights():
