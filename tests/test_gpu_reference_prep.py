@@ -93,6 +93,8 @@ def test_gpu_preparation_on_speckle(model):
 @pytest.mark.parametrize("size,stride,weighting", [
     (21, 10, "uniform"),    # row path, 8 windows in one row segment
     (25, 4, "uniform"),     # row path, 16 windows per row segment
+    (24, 6, "uniform"),     # row path, even size: half-integer window coordinates
+    (61, 15, "uniform"),    # row path, 256 columns per CTA (the widest segment)
     (21, 21, "uniform"),    # per-window path (tiled)
     (21, 7, "gaussian"),    # per-window path (weighted)
 ])
