@@ -12,8 +12,9 @@
 //      a. column sums V[Q, b](X) = sum_rows Q(X, Y) y^b, one thread per
 //         column, 29 Kahan sums over the S rows (packed FP32 pairs),
 //         into shared memory as head + tail;
-//      b. window sums sum_cols x^a V[Q, b], one (window, column sum) per
-//         thread, in double-float (exact products by FMA, TwoSum);
+//      b. window sums sum_cols x^a V[Q, b] for a = 0 .. 4 - b (or 2 - b),
+//         one (column sum, window) item per thread, Kahan sums in FP32
+//         pairs of powers of x, into shared memory as head + tail;
 //      c. per window: the moments of f = I - mean from those of I by
 //         expanding the mean (sum (I - m) Q = sum I Q - m sum Q, carried in
 //         double-float), rounded to binary32 in subset_prep_kernel's order
@@ -210,8 +211,7 @@ __device__ __forceinline__ void window_sums(const float2 *col, const float4 *xpo
 }
 
 // 96 registers: three 192-thread CTAs per SM (the shared-memory limit as well).
-__global__ void __maxnreg__(96) quadratic_row_moments_kernel(PrepArgs a, int windows_per_cta,
-                                                                               int pitch) {
+__global__ void __maxnreg__(96) quadratic_row_moments_kernel(PrepArgs a, int windows_per_cta, int pitch) {
     extern __shared__ float2 s_col[];  // [slot][pitch] column sums (head, tail)
     __shared__ float2 s_win[kRowWindows][kWindowSums];
     __shared__ float4 s_xpow[kRowMaxCols];  // (x, x^2, x^3, x^4) of window column j
