@@ -162,6 +162,7 @@ class Runtime {
     // The fast loop runs for this configuration.
     bool fast_active() const;
     const DeviceBuffer &weights() const { return weights_; }
+    const DeviceBuffer &axis_weights() const { return axis_weights_; }
     // Solver profiling: CUDA events around every solver launch (outside graph
     // capture) and a device counter of executed Gauss-Newton iterations.
     void set_profiling(bool enable);
@@ -173,6 +174,7 @@ class Runtime {
     Options opt_;
     cudaStream_t stream_ = nullptr;
     DeviceBuffer weights_;
+    DeviceBuffer axis_weights_;  // S factors; weights_ is their outer product (Gaussian) or ones
     int sm_count_ = 0;
     int device_ = 0;
     int persistent_grid_ = 0;

@@ -83,6 +83,7 @@ struct PrepArgs {
     int S, stride, grid_w, grid_h, count;
     int model, interp, gaussian_weighting;
     const float *weights;   // S*S integration weights (always provided)
+    const float *axis_weights;  // S factors along one axis: weights = outer product (row path)
     float weight_sum;
     const uint8_t *selected;  // ROI selection per subset, or nullptr
     // outputs / scratch
@@ -100,9 +101,10 @@ struct PrepArgs {
 };
 cudaError_t launch_reference_prep(const PrepArgs &a, cudaStream_t stream);
 // Quadratic preparation by window rows (column sums shared by the windows of
-// a grid row, one thread per 12x12 inverse): uniform weights, overlapping
-// windows (stride < S <= 256).  moments must hold
-// quadratic_row_prep_moment_floats(count) floats.
+// a grid row, one thread per 12x12 inverse): uniform or Gaussian weights (the
+// Gaussian as the outer product of axis_weights), overlapping windows
+// (stride < S <= 256).  moments must hold quadratic_row_prep_moment_floats(count)
+// floats.
 bool quadratic_row_prep_supported(int model, int gaussian_weighting, int S, int stride, int grid_h);
 size_t quadratic_row_prep_moment_floats(int count);
 cudaError_t launch_quadratic_row_prep(const PrepArgs &a, cudaStream_t stream);

@@ -3,16 +3,17 @@
 // per-window path for every other configuration is refprep.cu's
 // subset_prep_kernel, whose moment layout and finishing steps this follows).
 //
-// With uniform weights each moment of a window is a double sum
-//     sum_rows sum_cols Q(X, Y) x^a y^b
+// With uniform weights, or Gaussian weights w = wx(x) wy(y), each moment of
+// a window is a double sum
+//     sum_rows sum_cols w Q(X, Y) x^a y^b
 // of a pixel quantity Q (I, I^2, gx I, gy I, gx, gy, gx^2, gx gy, gy^2)
 // times window-local monomials.  The windows of one grid row share their
 // rows and overlapping windows share columns, so
 //   1. quadratic_row_moments_kernel, one CTA per segment of a window row:
-//      a. column sums V[Q, b](X) = sum_rows Q(X, Y) y^b, one thread per
+//      a. column sums V[Q, b](X) = sum_rows wy Q(X, Y) y^b, one thread per
 //         column, 29 Kahan sums over the S rows (packed FP32 pairs),
 //         into shared memory as head + tail;
-//      b. window sums sum_cols x^a V[Q, b] for a = 0 .. 4 - b (or 2 - b),
+//      b. window sums sum_cols wx x^a V[Q, b] for a = 0 .. 4 - b (or 2 - b),
 //         one (column sum, window) item per thread, Kahan sums in FP32
 //         pairs of powers of x, into shared memory as head + tail;
 //      c. per window: the moments of f = I - mean from those of I by
@@ -188,20 +189,24 @@ __device__ __forceinline__ void kahan_pair(float2 &s, float2 &c, float2 v) {
     s = t;
 }
 
-// Window sums of one column sum (head, tail) times x^0 .. x^D over the S
-// columns of a window: Kahan sums in FP32 pairs (x^0, x^1) (x^2, x^3)
-// (x^4, -), each term fl(head x^a + tail x^a).  Written as head s, tail -c.
+// Window sums of one column sum (head, tail) times wx x^0 .. wx x^D over the
+// S columns of a window: Kahan sums in FP32 pairs (x^0, x^1) (x^2, x^3)
+// (x^4, -), each term fl(head p + tail p) with p = wx x^a from the column's
+// power table (xpow03 = wx (1, x, x^2, x^3), xpow4 = wx x^4).  Written as
+// head s, tail -c.
 template <int D>
-__device__ __forceinline__ void window_sums(const float2 *col, const float4 *xpow, int S, float2 *out) {
+__device__ __forceinline__ void window_sums(const float2 *col, const float4 *xpow03, const float *xpow4, int S,
+                                            float2 *out) {
     constexpr int P = D / 2 + 1;
     float2 s[P], c[P];
 #pragma unroll
     for (int p = 0; p < P; ++p) { s[p] = make_float2(0.0f, 0.0f); c[p] = make_float2(0.0f, 0.0f); }
     for (int j = 0; j < S; ++j) {
         const float2 v = col[j];
-        const float4 x = xpow[j];  // (x, x^2, x^3, x^4)
+        const float4 x = xpow03[j];
         const float2 hi = make_float2(v.x, v.x), lo = make_float2(v.y, v.y);
-        const float2 pw[3] = {make_float2(1.0f, x.x), make_float2(x.y, x.z), make_float2(x.w, 0.0f)};
+        const float2 pw[3] = {make_float2(x.x, x.y), make_float2(x.z, x.w),
+                              make_float2(D >= 4 ? xpow4[j] : 0.0f, 0.0f)};
 #pragma unroll
         for (int p = 0; p < P; ++p) kahan_pair(s[p], c[p], __ffma2_rn(lo, pw[p], __fmul2_rn(hi, pw[p])));
     }
@@ -211,10 +216,13 @@ __device__ __forceinline__ void window_sums(const float2 *col, const float4 *xpo
 }
 
 // 96 registers: three 192-thread CTAs per SM (the shared-memory limit as well).
+template <bool GAUSS>
 __global__ void __maxnreg__(96) quadratic_row_moments_kernel(PrepArgs a, int windows_per_cta, int pitch) {
     extern __shared__ float2 s_col[];  // [slot][pitch] column sums (head, tail)
     __shared__ float2 s_win[kRowWindows][kWindowSums];
-    __shared__ float4 s_xpow[kRowMaxCols];  // (x, x^2, x^3, x^4) of window column j
+    __shared__ float4 s_xpow03[kRowMaxCols];  // wx (1, x, x^2, x^3) of window column j
+    __shared__ float s_xpow4[kRowMaxCols];    // wx x^4
+    __shared__ float s_wy[kRowMaxCols];       // wy of window row r
     const int tid = threadIdx.x;
     const int ix0 = blockIdx.x * windows_per_cta, iy = blockIdx.y;
     const int nw = min(windows_per_cta, a.grid_w - ix0);
@@ -222,6 +230,8 @@ __global__ void __maxnreg__(96) quadratic_row_moments_kernel(PrepArgs a, int win
     const int cols = (nw - 1) * st + S;
     const int gx0 = ix0 * st, gy0 = iy * st;
     const float half = 0.5f * ((float)S - 1.0f);
+    if (GAUSS && tid < S) s_wy[tid] = a.axis_weights[tid];
+    if (GAUSS) __syncthreads();
 
     // a. column sums over the window row's S image rows
     if (tid < cols) {
@@ -233,26 +243,39 @@ __global__ void __maxnreg__(96) quadratic_row_moments_kernel(PrepArgs a, int win
         for (int r = 0; r < S; ++r) {
             const float4 v = src[(size_t)r * a.W];
             const float y = (float)r - half, y2 = y * y;
-            const float2 y12 = make_float2(y, y2), y34 = make_float2(y2 * y, y2 * y2);
+            float2 y12 = make_float2(y, y2), y34 = make_float2(y2 * y, y2 * y2);
             const float I = v.x, gx = v.y, gy = v.z;
             const float2 gI = __fmul2_rn(make_float2(gx, gy), make_float2(I, I));
             const float2 G01 = __fmul2_rn(make_float2(gx, gx), make_float2(gx, gy));
             const float G2 = gy * gy;
-            kahan_pair(s[0], c[0], make_float2(I, I * I));
-            kahan_pair(s[1], c[1], gI);
+            // y^0 terms times wy; wy folded into the powers of y for the others
+            float2 t0 = make_float2(I, I * I), t1 = gI, t4 = make_float2(gx, gy), t7 = G01,
+                   t14 = make_float2(G2, 0.0f);
+            if (GAUSS) {
+                const float2 wy = make_float2(s_wy[r], s_wy[r]);
+                y12 = __fmul2_rn(y12, wy);
+                y34 = __fmul2_rn(y34, wy);
+                t0 = __fmul2_rn(t0, wy);
+                t1 = __fmul2_rn(t1, wy);
+                t4 = __fmul2_rn(t4, wy);
+                t7 = __fmul2_rn(t7, wy);
+                t14 = __fmul2_rn(t14, wy);
+            }
+            kahan_pair(s[0], c[0], t0);
+            kahan_pair(s[1], c[1], t1);
             kahan_pair(s[2], c[2], __fmul2_rn(make_float2(gI.x, gI.x), y12));
             kahan_pair(s[3], c[3], __fmul2_rn(make_float2(gI.y, gI.y), y12));
-            kahan_pair(s[4], c[4], make_float2(gx, gy));
+            kahan_pair(s[4], c[4], t4);
             kahan_pair(s[5], c[5], __fmul2_rn(make_float2(gx, gx), y12));
             kahan_pair(s[6], c[6], __fmul2_rn(make_float2(gy, gy), y12));
-            kahan_pair(s[7], c[7], G01);
+            kahan_pair(s[7], c[7], t7);
             kahan_pair(s[8], c[8], __fmul2_rn(make_float2(G01.x, G01.x), y12));
             kahan_pair(s[9], c[9], __fmul2_rn(make_float2(G01.x, G01.x), y34));
             kahan_pair(s[10], c[10], __fmul2_rn(make_float2(G01.y, G01.y), y12));
             kahan_pair(s[11], c[11], __fmul2_rn(make_float2(G01.y, G01.y), y34));
             kahan_pair(s[12], c[12], __fmul2_rn(make_float2(G2, G2), y12));
             kahan_pair(s[13], c[13], __fmul2_rn(make_float2(G2, G2), y34));
-            kahan_pair(s[14], c[14], make_float2(G2, 0.0f));
+            kahan_pair(s[14], c[14], t14);
         }
         // a Kahan sum is s - c: stored as head s, tail -c
 #pragma unroll
@@ -263,7 +286,14 @@ __global__ void __maxnreg__(96) quadratic_row_moments_kernel(PrepArgs a, int win
     }
     if (tid < S) {
         const float x = (float)tid - half, x2 = x * x;
-        s_xpow[tid] = make_float4(x, x2, x2 * x, x2 * x2);
+        if (GAUSS) {
+            const float wx = a.axis_weights[tid];
+            s_xpow03[tid] = make_float4(wx, wx * x, wx * x2, wx * (x2 * x));
+            s_xpow4[tid] = wx * (x2 * x2);
+        } else {
+            s_xpow03[tid] = make_float4(1.0f, x, x2, x2 * x);
+            s_xpow4[tid] = x2 * x2;
+        }
     }
     __syncthreads();
 
@@ -275,11 +305,11 @@ __global__ void __maxnreg__(96) quadratic_row_moments_kernel(PrepArgs a, int win
         const float2 *col = s_col + slot * pitch + w * st;
         float2 *out = &s_win[w][c_slot_base[slot]];
         switch (c_slot_degree[slot]) {
-        case 0: window_sums<0>(col, s_xpow, S, out); break;
-        case 1: window_sums<1>(col, s_xpow, S, out); break;
-        case 2: window_sums<2>(col, s_xpow, S, out); break;
-        case 3: window_sums<3>(col, s_xpow, S, out); break;
-        default: window_sums<4>(col, s_xpow, S, out); break;
+        case 0: window_sums<0>(col, s_xpow03, s_xpow4, S, out); break;
+        case 1: window_sums<1>(col, s_xpow03, s_xpow4, S, out); break;
+        case 2: window_sums<2>(col, s_xpow03, s_xpow4, S, out); break;
+        case 3: window_sums<3>(col, s_xpow03, s_xpow4, S, out); break;
+        default: window_sums<4>(col, s_xpow03, s_xpow4, S, out); break;
         }
     }
     __syncthreads();
@@ -442,8 +472,8 @@ __global__ void __maxnreg__(168) quadratic_finish_kernel(PrepArgs a) {
 #endif
 
 bool quadratic_row_prep_supported(int model, int gaussian_weighting, int S, int stride, int grid_h) {
-    return GBDIC_QUAD_ROW_PREP && model == kModelQuadratic && gaussian_weighting == 0 && stride < S && S <= kRowMaxCols &&
-           grid_h <= 65535;
+    return GBDIC_QUAD_ROW_PREP && model == kModelQuadratic && (gaussian_weighting == 0 || gaussian_weighting == 1) &&
+           stride < S && S <= kRowMaxCols && grid_h <= 65535;
 }
 
 size_t quadratic_row_prep_moment_floats(int count) { return (size_t)kMoments * (size_t)count; }
@@ -456,14 +486,16 @@ cudaError_t launch_quadratic_row_prep(const PrepArgs &a, cudaStream_t stream) {
     const int pitch = (wpc - 1) * a.stride + a.S;
     const int threads = (pitch + 31) / 32 * 32;
     const size_t shared = (size_t)kSlots * pitch * sizeof(float2);
-    cudaError_t err = cudaFuncSetAttribute(quadratic_row_moments_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)shared);
+    const bool gauss = a.gaussian_weighting == 1;
+    if (gauss && !a.axis_weights) return cudaErrorInvalidValue;
+    auto kernel = gauss ? quadratic_row_moments_kernel<true> : quadratic_row_moments_kernel<false>;
+    cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared);
     if (err == cudaSuccess)
-        err = cudaFuncSetAttribute(quadratic_row_moments_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+        err = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    (int)cudaSharedmemCarveoutMaxShared);
     if (err != cudaSuccess) return err;
     const dim3 grid((a.grid_w + wpc - 1) / wpc, a.grid_h);
-    quadratic_row_moments_kernel<<<grid, threads, shared, stream>>>(a, wpc, pitch);
+    kernel<<<grid, threads, shared, stream>>>(a, wpc, pitch);
     const size_t tri_shared = (size_t)kTri * (kFinishThreads + 1) * sizeof(double);
     quadratic_finish_kernel<<<(a.count + kFinishThreads - 1) / kFinishThreads, kFinishThreads, tri_shared, stream>>>(a);
     return cudaGetLastError();

@@ -159,6 +159,13 @@ Runtime::Runtime(const gbdic_options &options) {
     weights_.ensure(opt_.weights.size() * sizeof(float));
     check_cuda(cudaMemcpy(weights_.get(), opt_.weights.data(), opt_.weights.size() * sizeof(float),
                           cudaMemcpyHostToDevice), "weights upload");
+    // exp(-(x^2 + y^2) / 2 sigma^2) = exp(-x^2 / 2 sigma^2) exp(-y^2 / 2 sigma^2)
+    std::vector<float> axis((size_t)S, 1.0f);
+    if (options.spatial_weighting == 1)
+        for (int k = 0; k < S; ++k) axis[k] = (float)std::exp(-0.5 * (k - half) * (k - half) / (sigma * sigma));
+    axis_weights_.ensure(axis.size() * sizeof(float));
+    check_cuda(cudaMemcpy(axis_weights_.get(), axis.data(), axis.size() * sizeof(float), cudaMemcpyHostToDevice),
+               "axis weights upload");
     if (options.persistent) persistent_grid(opt_.lanes);
 }
 
@@ -290,6 +297,7 @@ double Runtime::prepare_reference(Level &level, const uint8_t *device_image, con
     a.grid_w = level.gw; a.grid_h = level.gh; a.count = level.count;
     a.model = model; a.interp = opt_.o.interpolation; a.gaussian_weighting = opt_.o.spatial_weighting;
     a.weights = weights_.as<float>();
+    a.axis_weights = axis_weights_.as<float>();
     a.weight_sum = opt_.weight_sum;
     a.selected = roi_selected ? level.selected.as<uint8_t>() : nullptr;
     a.intensity = level.intensity.as<float>();

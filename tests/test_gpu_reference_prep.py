@@ -86,17 +86,19 @@ def test_gpu_preparation_on_speckle(model):
     _compare(_speckle(), model, "bspline", 21, 10)
 
 
-# Quadratic windows with uniform weights that overlap are prepared by window
-# rows (shared column sums); tiled grids and Gaussian weights by the
-# per-window sums.  Both against the float64 oracle, the second-order
-# moments stage by stage.
+# Overlapping quadratic windows are prepared by window rows (shared column
+# sums; Gaussian weights as the outer product of their axis factors), tiled
+# grids by the per-window sums.  Both against the float64 oracle, the
+# second-order moments stage by stage.
 @pytest.mark.parametrize("size,stride,weighting", [
     (21, 10, "uniform"),    # row path, 8 windows in one row segment
     (25, 4, "uniform"),     # row path, 16 windows per row segment
     (24, 6, "uniform"),     # row path, even size: half-integer window coordinates
     (61, 15, "uniform"),    # row path, 256 columns per CTA (the widest segment)
+    (21, 7, "gaussian"),    # row path, weighted
+    (24, 6, "gaussian"),    # row path, weighted, even size
     (21, 21, "uniform"),    # per-window path (tiled)
-    (21, 7, "gaussian"),    # per-window path (weighted)
+    (21, 21, "gaussian"),   # per-window path (tiled, weighted)
 ])
 def test_gpu_quadratic_preparation_paths(size, stride, weighting):
     ok = check_quadratic_preparation(_speckle(), size, stride, weighting=weighting,
